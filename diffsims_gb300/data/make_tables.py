@@ -1,0 +1,45 @@
+"""Regenerate ``scattering_params.json`` from the reference's parameter modules.
+
+The two tables are published physical constants: the electron scattering
+factor fits of Lobato & Van Dyck, Acta Cryst. A70 (2014) 636, and the
+five-Gaussian fits of International Tables for Crystallography Vol. C,
+table 4.3.2.3.  diffsims ships them as ``ATOMIC_SCATTERING_PARAMS_LOBATO``
+(diffsims/utils/lobato_scattering_params.py:25) and
+``ATOMIC_SCATTERING_PARAMS`` (diffsims/utils/atomic_scattering_params.py:22),
+element symbol -> five (a_i, b_i) pairs.  This script copies the numbers
+verbatim into JSON so the library and the GPU host never need the reference.
+
+Usage (needs a checkout of the reference)::
+
+    python diffsims_gb300/data/make_tables.py /path/to/diffsims-checkout
+"""
+import importlib.util
+import json
+import pathlib
+import sys
+
+
+def _load_module(path, name):
+    spec = importlib.util.spec_from_file_location(name, path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def main(ref_root):
+    ref = pathlib.Path(ref_root) / "diffsims" / "utils"
+    lob = _load_module(ref / "lobato_scattering_params.py", "_lobato")
+    xt = _load_module(ref / "atomic_scattering_params.py", "_xtables")
+    out = {
+        "lobato": {k: [list(map(float, p)) for p in v]
+                   for k, v in lob.ATOMIC_SCATTERING_PARAMS_LOBATO.items()},
+        "xtables": {k: [list(map(float, p)) for p in v]
+                    for k, v in xt.ATOMIC_SCATTERING_PARAMS.items()},
+    }
+    dst = pathlib.Path(__file__).with_name("scattering_params.json")
+    dst.write_text(json.dumps(out, sort_keys=True, separators=(",", ":")))
+    print(f"wrote {dst} ({len(out['lobato'])} lobato, {len(out['xtables'])} xtables)")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
