@@ -1,0 +1,397 @@
+"""Benchmark of the kinematical spot-pattern path on one GB300.
+
+Workload (the large single-phase case): synthetic triclinic P1 cell, a, b, c
+uniform in [8, 15] Angstrom, alpha, beta, gamma uniform in [70, 110] deg, 200
+atoms with fractional coordinates uniform in [0, 1)^3, Z uniform in
+{6, 7, 8, 14, 26}, occupancy 1, B uniform in [0.3, 1.5] Angstrom^2;
+200 kV, reciprocal_radius 2.0 1/Angstrom, max_excitation_error 0.02,
+lorentzian shape factor, Lobato scattering factors; 100,000 orientations
+uniform on SO(3).  Seeded synthetic data (no dataset is involved).
+
+A step = one pass of the hot path over the batch: hkl enumeration, the
+structure-factor table, and the per-orientation kernel (rotation, excitation
+error, selection, shape factor, intensity, mask, ordered CSR output).
+
+Arms:
+  default           the CUDA path (mixed form).  value = patterns/s with the
+                    inputs resident in HBM; e2e = the same through the public
+                    API with host quaternions in and all spots copied back.
+  --impl reference  the reference's CPU path restated in numpy (the FP64
+                    oracle) on all host cores, a bounded sample per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(workload="triclinic P1, 200 atoms, 200 kV, r=2.0, s_max=0.02, lorentzian, lobato, 100k orientations",
+                cell_seed=1, orientation_seed=0, n_orientations=100_000, n_atoms=200, reciprocal_radius=2.0,
+                max_excitation_error=0.02, accelerating_voltage=200, shape_factor_model="lorentzian")
+METRIC = "orientation patterns/s"
+UNIT = "patterns/s"
+
+
+def make_crystal(seed=1, n_atoms=200):
+    rng = np.random.default_rng(seed)
+    lat = tuple(rng.uniform(8, 15, 3)) + tuple(rng.uniform(70, 110, 3))
+    els = list(rng.choice(["C", "N", "O", "Si", "Fe"], n_atoms))
+    xyz = rng.random((n_atoms, 3))
+    B = rng.uniform(0.3, 1.5, n_atoms)
+    return lat, els, xyz, B
+
+
+def uniform_quaternions(n, seed=0):
+    rng = np.random.default_rng(seed)
+    q = rng.standard_normal((n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    q[q[:, 0] < 0] *= -1
+    return q
+
+
+# --------------------------------------------------------------------- CPU
+def _cpu_worker(args):
+    """Reference CPU path (oracle restatement) on a slice of orientations."""
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    from oracle import kinematic as ok
+    lat, els, xyz, B, q, kv, r, eps, shape = args
+    cr = ok.Crystal(lat, els, xyz, B=B)
+    p = ok.SimParams(accelerating_voltage=kv, reciprocal_radius=r, max_excitation_error=eps, shape_factor_model=shape)
+    table = ok.phase_table(cr, p)
+    n = 0
+    for R in ok.quaternion_to_matrix(q):
+        n += ok.simulate_orientation(cr, p, table, R).hkl.shape[0]
+    return n
+
+
+def cpu_reference_rate(n_sample, cores, seed=0):
+    """patterns/s of the FP64 numpy restatement of the reference's path on
+    ``cores`` worker processes (spawned), OMP_NUM_THREADS=1 each."""
+    lat, els, xyz, B = make_crystal(WORKLOAD["cell_seed"], WORKLOAD["n_atoms"])
+    q = uniform_quaternions(n_sample, seed)
+    chunks = np.array_split(q, cores)
+    args = [(lat, els, xyz, B, c, WORKLOAD["accelerating_voltage"], WORKLOAD["reciprocal_radius"],
+             WORKLOAD["max_excitation_error"], WORKLOAD["shape_factor_model"]) for c in chunks if len(c)]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(len(args)) as pool:
+        pool.map(_cpu_worker, [(a[0], a[1], a[2], a[3], a[4][:1]) + a[5:] for a in args])  # warm the workers
+        t0 = time.perf_counter()
+        spots = sum(pool.map(_cpu_worker, args))
+        dt = time.perf_counter() - t0
+    return n_sample / dt, dt, spots
+
+
+# --------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, out_path=None):
+        self.out_path = out_path
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.f = open(self.out_path, "w") if self.out_path else subprocess.DEVNULL
+            self.tmp = self.out_path or os.path.join("/tmp", f"clocks_{os.getpid()}.csv")
+            if not self.out_path:
+                self.f = open(self.tmp, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.tmp) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax = float(parts[2])
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# ------------------------------------------------------------------ GPU
+def fp32_peak_tflops(torch, lib, N):
+    """Measured FP32 FMA throughput of this GPU (the screening kernel's
+    roofline denominator); best of 5."""
+    blocks = 152 * 8
+    iters = 4096
+    out = torch.empty(blocks * 256, dtype=torch.float32, device="cuda")
+    st = torch.cuda.current_stream()
+    best = 0.0
+    for _ in range(6):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        N.check(lib.ds_probe_fp32_fma(iters, blocks, N.ptr(out), N.stream_handle()), "probe")
+        e1.record(st)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = max(best, blocks * 256 * iters * 256 / (ms * 1e-3) / 1e12)
+    return best
+
+
+def run_gpu(args):
+    import torch
+    import diffsims_gb300 as ds
+    from diffsims_gb300 import _native as N
+    from diffsims_gb300.engine import PhaseTable, SpotBuffers, simulate_phase, estimate_spots
+
+    lib = N.load_library()
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    lat, els, xyz, B = make_crystal(WORKLOAD["cell_seed"], WORKLOAD["n_atoms"])
+    phase = ds.Phase("P1", ds.Structure([ds.Atom(e, x) for e, x in zip(els, xyz)], ds.Lattice(*lat)))
+    n_o = args.orientations
+    q_host = uniform_quaternions(n_o, WORKLOAD["orientation_seed"])
+    gen = ds.SimulationGenerator(WORKLOAD["accelerating_voltage"], "lobato",
+                                 shape_factor_model=WORKLOAD["shape_factor_model"])
+    r = WORKLOAD["reciprocal_radius"]
+    settings = gen.settings(WORKLOAD["max_excitation_error"], form="mixed")
+    q_dev = torch.from_numpy(q_host).to(dev)
+    table = PhaseTable(phase, r, True, "lobato", list(B), form="mixed", device=dev, build=True)
+    buffers = SpotBuffers(dev)
+    st = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > L2
+
+    def step():
+        table.build()
+        return simulate_phase(table, q_dev, settings, r, buffers)
+
+    for _ in range(args.warmup):
+        spots = step()
+    torch.cuda.synchronize()
+    step_ms, kern_ms = [], []
+    with ClockSampler(os.path.join(args.out_dir, "clocks.csv") if args.out_dir else None) as clk:
+        torch.cuda.synchronize()
+        t_all = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            spots = step()
+            e1.record(st)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t_all
+        # the dominant kernel alone (simulate), timed on its launch stream
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            simulate_phase(table, q_dev, settings, r, buffers, sync=False)
+            e1.record(st)
+            e1.synchronize()
+            kern_ms.append(e0.elapsed_time(e1))
+    clocks = clk.summary()
+    ms = statistics.mean(step_ms)
+    value = n_o / (ms * 1e-3)
+    total_spots = spots.total
+    n_h = table.n
+
+    # ---- end to end through the public API with host buffers
+    rot_host = ds.Rotation(q_host)
+    e2e_ms = []
+    h2d = q_host.nbytes
+    d2h = 0
+    for it in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim = gen.calculate_diffraction2d(phase, rot_host, reciprocal_radius=r,
+                                          max_excitation_error=WORKLOAD["max_excitation_error"],
+                                          debye_waller_factors=list(B))
+        sp = sim.spots(0)
+        sp.host(pinned=True)
+        dt = time.perf_counter() - t0
+        if it >= args.warmup:
+            e2e_ms.append(dt * 1e3)
+        d2h = sp.nbytes()
+    e2e_value = n_o / (statistics.mean(e2e_ms) * 1e-3)
+
+    # ---- roofline of the dominant kernel (FP32 issue-bound screen)
+    peak32 = fp32_peak_tflops(torch, lib, N)
+    kms = statistics.mean(kern_ms)
+    flops = 10.0 * n_o * n_h  # algorithmic FP32 FLOP per (orientation, row) pair
+    achieved = flops / (kms * 1e-3) / 1e12
+    bytes_alg = total_spots * 20 + (n_o + 1) * 8 + n_o * 32 + n_h * 32
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "simulate_kernel_traffic.json")
+    if os.path.exists(tpath):
+        tj = json.load(open(tpath))
+        traffic = tj.get("dram_bytes_per_pair", 0) * n_o * n_h + tj.get("dram_bytes_per_spot", 0) * total_spots or None
+
+    # ---- FP64 comparator form on a subset, and the error of the mixed form against it
+    n_cmp = min(args.fp64_orientations, n_o)
+    q_cmp = q_dev[:n_cmp].contiguous()
+    t64 = PhaseTable(phase, r, True, "lobato", list(B), form="fp64", device=dev)
+    s64 = gen.settings(WORKLOAD["max_excitation_error"], form="fp64")
+    b64 = SpotBuffers(dev, with_excitation_error=True)
+    simulate_phase(t64, q_cmp, s64, r, b64)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    t64.build()
+    ref64 = simulate_phase(t64, q_cmp, s64, r, b64)
+    e1.record(st)
+    e1.synchronize()
+    fp64_rate = n_cmp / (e0.elapsed_time(e1) * 1e-3)
+    mixed = simulate_phase(table, q_cmp, settings, r, SpotBuffers(dev, with_excitation_error=True))
+    err = compare_forms(mixed, ref64, table, q_host[:n_cmp], settings)
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        rate, dt, _ = cpu_reference_rate(args.cpu_sample, cores)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{args.cpu_sample} orientations of the same workload, FP64 numpy restatement of the "
+                         f"reference path, {cores} spawned processes, {dt:.1f} s"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded P1 cell and uniform SO(3) orientations)",
+        "config": dict(WORKLOAD, n_orientations=n_o, n_hkl=n_h, spots_per_step=total_spots,
+                       l2="256 MB buffer written between timed steps", form="mixed"),
+        "spots_per_s": total_spots / (ms * 1e-3),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "ms_per_step": statistics.mean(e2e_ms)},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
+                     "frac": achieved / peak32, "traffic": traffic, "kernel": "simulate_kernel",
+                     "kernel_ms": kms, "peak_source": "measured by bench.py FMA probe (ds_probe_fp32_fma)",
+                     "hbm": {"achieved_gbs": bytes_alg / (kms * 1e-3) / 1e9, "peak_gbs": hbm_peak,
+                             "frac": bytes_alg / (kms * 1e-3) / 1e9 / hbm_peak,
+                             "peak_source": "MEASURED_PEAKS.json" if peaks else "fallback"}},
+        "fp64_form": {"value": fp64_rate, "unit": UNIT, "orientations": n_cmp,
+                      "mixed_over_fp64": value / fp64_rate},
+        "error_vs_fp64_form": err,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "gpu_launches": 5 * args.steps,
+        "wall_s_timed_region": wall,
+    }
+    print(json.dumps(line))
+
+
+def compare_forms(mixed, ref, table, q_host, settings):
+    """Errors of the mixed form against the all-FP64 GPU form: max relative
+    intensity error, max |s| difference, selection flips (and how far from
+    the cutoff they sit, from an FP64 host evaluation of those pairs)."""
+    om, im, xm, sm = (mixed.offsets.cpu().numpy(), mixed.hkl_index.cpu().numpy(), mixed.xyzi.cpu().numpy(),
+                      mixed.excitation_error.cpu().numpy())
+    of, jf, xf, sf = (ref.offsets.cpu().numpy(), ref.hkl_index.cpu().numpy(), ref.xyzi.cpu().numpy(),
+                      ref.excitation_error.cpu().numpy())
+    hkl = table.hkl_host().astype(np.float64)
+    from diffsims_gb300.crystal import Rotation
+    Rs = Rotation(q_host).to_matrix()
+    k0, eps = settings.k0, settings.max_excitation_error
+    max_rel, max_ds, flips, max_fd = 0.0, 0.0, 0, 0.0
+    for i in range(len(q_host)):
+        a, b = im[om[i]:om[i + 1]], jf[of[i]:of[i + 1]]
+        common, ia, ib = np.intersect1d(a, b, return_indices=True)
+        I1, I2 = xm[om[i]:om[i + 1]][ia, 3].astype(np.float64), xf[of[i]:of[i + 1]][ib, 3].astype(np.float64)
+        nz = I2 != 0
+        if nz.any():
+            max_rel = max(max_rel, float(np.max(np.abs(I1[nz] - I2[nz]) / np.abs(I2[nz]))))
+        if common.size:
+            max_ds = max(max_ds, float(np.max(np.abs(sm[om[i]:om[i + 1]][ia] - sf[of[i]:of[i + 1]][ib]))))
+        for j in np.setxor1d(a, b):
+            g = hkl[j] @ table.recip
+            rot = g @ Rs[i]
+            rr = math.hypot(rot[0], rot[1])
+            s = (-math.sqrt(k0 * k0 - rr * rr) + k0) - rot[2]
+            flips += 1
+            max_fd = max(max_fd, abs(abs(s) - eps))
+    return {"max_rel_intensity": max_rel, "max_abs_excitation_error": max_ds, "flips": flips,
+            "max_flip_distance_from_cutoff": max_fd, "orientations": int(len(q_host))}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    n = args.cpu_sample
+    rates = []
+    for it in range(args.warmup + args.steps):
+        rate, dt, _ = cpu_reference_rate(n, cores, seed=it)
+        if it >= args.warmup:
+            rates.append(rate)
+    value = statistics.mean(rates)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": n / value * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded P1 cell and uniform SO(3) orientations)",
+        "config": dict(WORKLOAD, sample_orientations_per_step=n), "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{n} orientations per step of the same workload; FP64 numpy restatement of "
+                                   f"diffsims' calculate_diffraction2d loop, {cores} spawned processes"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--orientations", type=int, default=WORKLOAD["n_orientations"])
+    ap.add_argument("--fp64-orientations", type=int, default=4096)
+    ap.add_argument("--cpu-sample", type=int, default=1024)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--out-dir", default=None)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    # one process per GPU; the path shards by orientation with no exchange, so
+    # N > 1 runs independent replicas and only rank 0 reports
+    rank = int(os.environ.get("RANK", "0"))
+    if args.gpus > 1 and rank != 0:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("LOCAL_RANK", "0"))
+    run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,145 @@
+"""ctypes binding of libdiffsims_gb300.so (the C ABI in include/diffsims_gb300.h).
+
+There is no CPU fallback: if the library is missing or no CUDA device is
+present, every compute entry raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import pathlib
+import threading
+
+import torch
+
+_LIB_PATH = pathlib.Path(__file__).resolve().parent / "libdiffsims_gb300.so"
+_lock = threading.Lock()
+_lib = None
+
+# status codes / enums (mirror include/diffsims_gb300.h)
+DS_OK = 0
+DS_ERR_INVALID_ARGUMENT = 1
+DS_ERR_CUDA = 2
+DS_ERR_CAPACITY = 4
+DS_ERR_TIMEOUT = 8
+DS_ERR_UNSUPPORTED = 16
+DS_ERR_NONFINITE = 32
+
+DS_FORM_MIXED = 0
+DS_FORM_FP64 = 1
+
+DS_SCATTER = {"lobato": 0, "xtables": 1, None: 2}
+DS_SHAPE = {"linear": 0, "atanc": 1, "sinc": 2, "sin2c": 3, "lorentzian": 4, "binary": 5}
+DS_PRECESSION_NONE = 0
+DS_PRECESSION_LORENTZIAN = 1
+DS_PRECESSION_INTEGRAL = 2
+
+EXPORTED_SYMBOLS = (
+    "ds_box_extent", "ds_enumerate_scratch_bytes", "ds_enumerate_hkl",
+    "ds_structure_factor_scratch_bytes", "ds_structure_factors", "ds_kinematical_intensities",
+    "ds_simulate_scratch_bytes", "ds_simulate", "ds_probe_fp32_fma", "ds_last_error", "ds_version",
+)
+
+
+class ds_atom(C.Structure):
+    _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double), ("occupancy", C.c_double),
+                ("B", C.c_double), ("species", C.c_int32), ("_pad", C.c_int32)]
+
+
+class ds_atoms(C.Structure):
+    _fields_ = [("n_atoms", C.c_int32), ("n_species", C.c_int32), ("atoms", C.c_void_p),
+                ("coeffs", C.c_void_p), ("kind", C.c_int32), ("_pad", C.c_int32)]
+
+
+class ds_sim_params(C.Structure):
+    _fields_ = [("k0", C.c_double), ("max_excitation_error", C.c_double), ("shape_width", C.c_double),
+                ("precession_angle", C.c_double), ("minimum_intensity", C.c_double),
+                ("minima_number", C.c_double), ("shape_model", C.c_int32), ("precession_mode", C.c_int32),
+                ("form", C.c_int32), ("orient_tile", C.c_int32)]
+
+
+class ds_phase_table(C.Structure):
+    _fields_ = [("n_hkl", C.c_int64), ("hkl", C.c_void_p), ("g2", C.c_void_p), ("F2", C.c_void_p),
+                ("F2d", C.c_void_p), ("recip", C.c_double * 9), ("hmax", C.c_int32 * 3), ("_pad", C.c_int32)]
+
+
+class ds_spots(C.Structure):
+    _fields_ = [("offsets", C.c_void_p), ("hkl_index", C.c_void_p), ("xyzi", C.c_void_p),
+                ("capacity", C.c_int64), ("total", C.c_void_p), ("excitation_error", C.c_void_p)]
+
+
+assert C.sizeof(ds_atom) == 48
+
+
+class NativeError(RuntimeError):
+    """A C-ABI call returned an error status."""
+
+
+def library_path() -> pathlib.Path:
+    return _LIB_PATH
+
+
+def load_library(require_cuda: bool = True):
+    """Load the CUDA library once; raise if it is missing (no fallback)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not _LIB_PATH.exists():
+                raise NativeError(f"{_LIB_PATH.name} is not built: run `python -c \"import __graft_entry__ as g; "
+                                  f"g.build()\"` (the CUDA path has no CPU fallback)")
+            lib = C.CDLL(str(_LIB_PATH))
+            vp, i32, i64, sz, dp = C.c_void_p, C.c_int32, C.c_int64, C.c_size_t, C.c_double
+            lib.ds_box_extent.argtypes = [C.POINTER(C.c_double), dp, C.POINTER(C.c_int32)]
+            lib.ds_enumerate_scratch_bytes.argtypes = [C.POINTER(C.c_int32)]
+            lib.ds_enumerate_scratch_bytes.restype = sz
+            lib.ds_enumerate_hkl.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_int32), dp, i32, vp, vp, i64, vp,
+                                             vp, sz, vp, vp]
+            lib.ds_structure_factor_scratch_bytes.argtypes = [i64, i32]
+            lib.ds_structure_factor_scratch_bytes.restype = sz
+            lib.ds_structure_factors.argtypes = [C.POINTER(ds_atoms), vp, vp, vp, i64, i32, vp, vp, vp, vp, sz, vp, vp]
+            lib.ds_kinematical_intensities.argtypes = [C.POINTER(ds_atoms), vp, vp, vp, i64, vp, vp, sz, vp, vp]
+            lib.ds_simulate_scratch_bytes.argtypes = [C.POINTER(ds_sim_params), C.POINTER(ds_phase_table), i64]
+            lib.ds_simulate_scratch_bytes.restype = sz
+            lib.ds_simulate.argtypes = [C.POINTER(ds_sim_params), C.POINTER(ds_phase_table), vp, i64,
+                                        C.POINTER(ds_spots), vp, sz, vp, vp]
+            lib.ds_probe_fp32_fma.argtypes = [i64, i32, vp, vp]
+            lib.ds_last_error.restype = C.c_char_p
+            lib.ds_version.restype = C.c_char_p
+            for name in ("ds_box_extent", "ds_enumerate_hkl", "ds_structure_factors", "ds_kinematical_intensities",
+                         "ds_simulate", "ds_probe_fp32_fma"):
+                getattr(lib, name).restype = C.c_int32
+            _lib = lib
+    if require_cuda and not torch.cuda.is_available():
+        raise NativeError("diffsims_gb300 needs a CUDA device (GB300, sm_103a); none is visible")
+    return _lib
+
+
+def check(status: int, what: str):
+    if status != DS_OK:
+        msg = _lib.ds_last_error().decode() if _lib is not None else ""
+        if status == DS_ERR_INVALID_ARGUMENT:
+            raise ValueError(f"{what}: {msg}")
+        if status == DS_ERR_UNSUPPORTED:
+            raise NotImplementedError(f"{what}: {msg}")
+        raise NativeError(f"{what}: status {status}: {msg}")
+
+
+def check_device_status(status_tensor: torch.Tensor, what: str, allow=0) -> int:
+    """Read the device status word (synchronises) and raise on unexpected bits."""
+    v = int(status_tensor.item())
+    bad = v & ~allow
+    if bad & DS_ERR_TIMEOUT:
+        raise NativeError(f"{what}: a bounded device wait timed out (status {v})")
+    if bad & DS_ERR_NONFINITE:
+        raise ValueError(f"{what}: non-finite input (status {v})")
+    if bad:
+        raise NativeError(f"{what}: device status {v}")
+    return v
+
+
+def ptr(t: torch.Tensor | None):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def stream_handle(stream: torch.cuda.Stream | None = None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)

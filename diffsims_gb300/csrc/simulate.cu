@@ -1,0 +1,703 @@
+// A4-A7: per-orientation spot patterns of one phase.
+//
+// Replaces the orientation loop of SimulationGenerator.calculate_diffraction2d
+// (diffsims/generators/simulation_generator.py:211-241) and
+// get_intersecting_reflections (:319-412): rotation of the candidate table
+// into the beam frame (R(q)^T g, diffsims/crystallography/_diffracting_vector.py:160),
+// excitation error s = k0 - sqrt(k0^2 - r^2) - z, selection (|s| < s_max, or
+// the precession band), the rel-rod shape factor, I = sf |F|^2
+// (diffsims/utils/sim_utils.py:353), the mask I > max(I) * minimum_intensity
+// (:237-240) and ordered compaction of the survivors into CSR.
+//
+// One CTA owns a tile of O orientations and streams the whole candidate table
+// once for all of them:
+//   phase 1  FP32 screen.  z = m . hkl (m = R^T-column of the reciprocal basis)
+//            against the exact |s| < s_max interval of z for that |g|
+//            (precomputed per row) widened by a rounding guard.  One ballot per
+//            (32 rows, orientation) writes a word of a shared-memory bitmap.
+//   phase 2  refine every screened candidate: double-float (FP32 pair) z, r^2
+//            and s; FP64 only when s lies within 1e-9 of the cutoff (FP64
+//            step #2); shape factor, intensity, per-orientation max; rejected
+//            bits are cleared.  A mask pass runs only if some intensity is
+//            positive but <= max * minimum_intensity.
+//   phase 3  per-orientation counts, the tile's output offset by decoupled
+//            look-back on the tile ticket, then ordered, coalesced writes of
+//            (row index) and (x, y, z, I) records.
+// The plain all-FP64 form (FORM_FP64) shares phases 2-3 and evaluates every
+// (orientation, row) pair in FP64 in phase 1.
+#include <math.h>
+
+#include "common.cuh"
+
+namespace ds {
+
+constexpr int SIM_THREADS = 256;
+constexpr int SIM_WARPS = SIM_THREADS / 32;
+constexpr float SIM_TAU = 1e-9f;       // | |s| - s_max | below this -> FP64 decision
+constexpr float SIM_TAU_PREC = 2e-7f;  // precession band margin below this -> FP64 decision
+constexpr float SIM_U_MAX = 0.01f;     // (r / k0)^2 above this -> FP64 (series not used)
+constexpr int SIM_MAX_O = 32;
+
+struct SimConst {
+    double k0, eps, width, phi, thr, Pz, Pt, minima;
+    double recip[9];
+    dd eps_dd, c2k0_dd, width_dd, mw_dd;
+    float k0f, inv_k0sq, eps_f, width_f, sigma_f, mfac_f, phi_f, Pz_f, Pt_f, k0sq_f, guard;
+    int shape, prec, form, O;
+    int W, Ws;
+    long long n_hkl, n_orient, n_tiles, capacity;
+};
+
+struct __align__(16) OrientP {
+    float m[3][3];   // beam-frame coordinate c = sum_i m[c][i] * hkl_i   (FP32)
+    float mzlo[3];   // low words of m[2][i] (double-float z)
+    float _pad[4];
+    double M[3][3];  // FP64 copy
+};
+
+struct SimSmem {
+    size_t orient, bitmap, acc, total;
+};
+__host__ __device__ inline SimSmem sim_smem_layout(int O, int Ws) {
+    SimSmem L;
+    size_t o = 0;
+    L.orient = o; o += (size_t)O * sizeof(OrientP);
+    L.acc = o; o += (size_t)O * 8 * sizeof(unsigned long long) + 64;
+    o = (o + 15) & ~(size_t)15;
+    L.bitmap = o; o += (size_t)O * Ws * sizeof(uint32_t);
+    L.total = o;
+    return L;
+}
+
+// per-orientation accumulators in shared memory (8 words each)
+enum { ACC_MAXI = 0, ACC_MINPOS = 1, ACC_CNT = 2, ACC_OFF = 3, ACC_PART0 = 4 };  // PART0..PART0+3: part counts
+
+// ------------------------------------------------------------------ prep ----
+// Per row: (h, k, l, -z_mid) and z_half of the z-interval that holds every
+// selected (orientation, row) pair, plus |g|^2 as a float pair.
+// |s| < e  <=>  z_a < z < z_b with z_a = (g^2 + e^2 - 2 e k0) / (2 (k0 - e)),
+// z_b = (g^2 + e^2 + 2 e k0) / (2 (k0 + e))  (s is decreasing in z).
+// For precession e is widened by a bound on how far the precessing sphere
+// strays from the static one at this |g|:
+//   k0 (1 - cos phi) + Pt (2 |g| + Pt) / (2 sqrt(k0^2 - (|g| + Pt)^2)).
+__global__ void sim_prep_kernel(SimConst c, const int32_t *__restrict__ hkl, const double *__restrict__ g2,
+                                float4 *__restrict__ scr, float *__restrict__ zh, float2 *__restrict__ g2dd) {
+    long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= c.n_hkl) return;
+    double gsq = g2[j];
+    double e = c.eps;
+    if (c.prec != DS_PRECESSION_NONE) {
+        double g = sqrt(gsq);
+        double a = c.k0 * c.k0 - (g + c.Pt) * (g + c.Pt);
+        double wide = a > 0 ? c.k0 * (1.0 - cos(c.phi)) + c.Pt * (2.0 * g + c.Pt) / (2.0 * sqrt(a)) : 1e30;
+        e = c.eps + wide * 1.0001 + 1e-7;
+    }
+    double za = (gsq + e * e - 2.0 * e * c.k0) / (2.0 * (c.k0 - e));
+    double zb = (gsq + e * e + 2.0 * e * c.k0) / (2.0 * (c.k0 + e));
+    double zmid = 0.5 * (za + zb), zhalf = 0.5 * (zb - za);
+    scr[j] = make_float4((float)hkl[3 * j], (float)hkl[3 * j + 1], (float)hkl[3 * j + 2], (float)(-zmid));
+    zh[j] = (float)zhalf + c.guard;
+    float hi, lo;
+    split_double(gsq, hi, lo);
+    g2dd[j] = make_float2(hi, lo);
+}
+
+// --------------------------------------------------------- evaluation ----
+__device__ __forceinline__ dd z_dd(const OrientP &op, float h, float k, float l) {
+    dd p0 = two_prod(op.m[2][0], h), p1 = two_prod(op.m[2][1], k), p2 = two_prod(op.m[2][2], l);
+    dd s = two_sum(p0.hi, p1.hi);
+    dd t = two_sum(s.hi, p2.hi);
+    float lo = s.lo + t.lo + p0.lo + p1.lo + p2.lo;
+    lo = fmaf(op.mzlo[0], h, fmaf(op.mzlo[1], k, fmaf(op.mzlo[2], l, lo)));
+    return quick_two_sum(t.hi, lo);
+}
+
+// FP64 excitation error and selection in the reference's operation order
+// (simulation_generator.py:355-375): FP64 step #2.
+__device__ inline bool select_fp64(const SimConst &c, const OrientP &op, double h, double k, double l, double &s,
+                                   double &r, double &z) {
+    double x = op.M[0][0] * h + op.M[0][1] * k + op.M[0][2] * l;
+    double y = op.M[1][0] * h + op.M[1][1] * k + op.M[1][2] * l;
+    z = op.M[2][0] * h + op.M[2][1] * k + op.M[2][2] * l;
+    r = sqrt(x * x + y * y);
+    double zs = -sqrt(c.k0 * c.k0 - r * r) + c.k0;
+    s = zs - z;
+    if (c.prec == DS_PRECESSION_NONE) return fabs(s) < c.eps;
+    double zup = c.Pz - sqrt(c.k0 * c.k0 - (r + c.Pt) * (r + c.Pt));
+    double zdo = c.Pz - sqrt(c.k0 * c.k0 - (r - c.Pt) * (r - c.Pt));
+    return (z - c.eps <= zup) && (z + c.eps >= zdo);
+}
+
+// Mixed-form selection.  s and r returned for the shape factor.
+__device__ inline bool select_mixed(const SimConst &c, const OrientP &op, const float4 &e, float2 g2p, dd &s,
+                                    float &r, float &zf) {
+    dd z = z_dd(op, e.x, e.y, e.z);
+    dd r2 = dd_sub(dd{g2p.x, g2p.y}, dd_mul(z, z));
+    float u = r2.hi * c.inv_k0sq;
+    bool fallback = u > SIM_U_MAX;
+    bool sel = false;
+    r = sqrtf(fmaxf(r2.hi, 0.f));
+    if (!fallback) {
+        float corr = u * (0.25f + u * (0.125f + u * (0.078125f + u * (0.0546875f + u * 0.041015625f))));
+        dd w0 = dd_mul(r2, c.c2k0_dd);  // r^2 / (2 k0)
+        dd w = dd_add_f(w0, w0.hi * corr);  // k0 - sqrt(k0^2 - r^2)
+        s = dd_sub(w, z);
+        if (c.prec == DS_PRECESSION_NONE) {
+            dd d = dd_sub(dd_abs(s), c.eps_dd);
+            if (fabsf(d.hi) < SIM_TAU) fallback = true;
+            else sel = d.hi < 0.f;
+        } else {
+            float zz = z.hi + z.lo;
+            float rp = r + c.Pt_f, rm = r - c.Pt_f;
+            float a1 = c.k0sq_f - rp * rp, a2 = c.k0sq_f - rm * rm;
+            if (!(a1 > 0.f) || !(a2 > 0.f)) {
+                fallback = true;
+            } else {
+                float zup = r * (r + 2.f * c.Pt_f) / (c.Pz_f + sqrtf(a1));
+                float zdo = r * (r - 2.f * c.Pt_f) / (c.Pz_f + sqrtf(a2));
+                float d1 = zup - (zz - c.eps_f), d2 = (zz + c.eps_f) - zdo;
+                if (fabsf(d1) < SIM_TAU_PREC || fabsf(d2) < SIM_TAU_PREC) fallback = true;
+                else sel = (d1 >= 0.f) && (d2 >= 0.f);
+            }
+        }
+    }
+    if (fallback) {
+        double s64, r64, z64;
+        sel = select_fp64(c, op, (double)e.x, (double)e.y, (double)e.z, s64, r64, z64);
+        split_double(s64, s.hi, s.lo);
+        r = (float)r64;
+        zf = (float)z64;
+        return sel;
+    }
+    zf = z.hi + z.lo;
+    return sel;
+}
+
+// shape factors, mixed form (diffsims/utils/shape_factor_models.py)
+__device__ inline float shape_mixed(const SimConst &c, dd s, float r) {
+    if (c.prec == DS_PRECESSION_LORENTZIAN) {  // lorentzian_precession, :183-219
+        float sf = s.hi + s.lo;
+        float rphi = r * c.phi_f, as = fabsf(sf);
+        float A = (rphi - as) * (rphi + as);            // r^2 phi^2 - s^2 without cancellation
+        float sig = c.sigma_f;
+        float u = fmaf(sig * sig, A, 1.f);
+        float q = 2.f * sig * sf;
+        float z = sqrtf(fmaf(u, u, q * q));
+        float upz = u >= 0.f ? u + z : (q * q) / (z - u);  // u + z, stable for u < 0
+        return (sig / 3.14159265358979f) * sqrtf(2.f * upz) / z;
+    }
+    switch (c.shape) {
+        case DS_SHAPE_LINEAR: {  // :52-73
+            dd t = dd_sub(c.width_dd, dd_abs(s));
+            float v = __fdiv_rn(t.hi + t.lo, c.width_f);
+            return v > 0.f ? v : 0.f;
+        }
+        case DS_SHAPE_SINC:    // :76-101, s = 0 -> 0
+        case DS_SHAPE_SIN2C: { // :104-123
+            dd x = dd_mul(s, c.mw_dd);  // minima_number * s / width
+            float v = 0.f;
+            if (x.hi != 0.f) {
+                float n = rintf(x.hi);
+                float t = (x.hi - n) + x.lo;
+                float sp = sinpif(t);
+                v = fabsf(sp) / (3.14159265358979f * fabsf(x.hi + x.lo));
+            }
+            return c.shape == DS_SHAPE_SIN2C ? v * v : v;
+        }
+        case DS_SHAPE_ATANC: {  // :126-151, s = 0 -> 1
+            float y = c.mfac_f * (s.hi + s.lo);
+            return y == 0.f ? 1.f : atanf(y) / y;
+        }
+        case DS_SHAPE_LORENTZIAN: {  // :154-180 = 1 / (1 + (pi s / w)^2)
+            float x = c.sigma_f * (s.hi + s.lo);
+            return 1.f / fmaf(x, x, 1.f);
+        }
+        default:
+            return 1.f;  // binary, :33-49
+    }
+}
+
+// shape factors, FP64 form (direct transcription)
+__device__ inline double shape_fp64(const SimConst &c, double s, double r) {
+    const double PI = 3.14159265358979323846;
+    if (c.prec == DS_PRECESSION_LORENTZIAN) {
+        double sigma = PI / c.width;
+        double u = sigma * sigma * (r * r * c.phi * c.phi - s * s) + 1;
+        double z = sqrt(u * u + 4 * sigma * sigma * s * s);
+        return (sigma / PI) * sqrt(2 * (u + z) / (z * z));
+    }
+    switch (c.shape) {
+        case DS_SHAPE_LINEAR: {
+            double v = 1 - fabs(s) / c.width;
+            return v < 0 ? 0.0 : v;
+        }
+        case DS_SHAPE_SINC:
+        case DS_SHAPE_SIN2C: {
+            double fac = PI * c.minima / c.width;
+            double den = fac * s;
+            double v = den != 0 ? fabs(sin(fac * s) / den) : 0.0;
+            return c.shape == DS_SHAPE_SIN2C ? v * v : v;
+        }
+        case DS_SHAPE_ATANC: {
+            double fac = PI * c.minima / fabs(c.width);
+            double y = fac * s;
+            return y == 0 ? 1.0 : atan(y) / y;
+        }
+        case DS_SHAPE_LORENTZIAN: {
+            double sigma = PI / c.width;
+            return sigma / (PI * (sigma * sigma * s * s + 1)) * c.width;
+        }
+        default:
+            return 1.0;
+    }
+}
+
+struct TableP {
+    const float4 *scr;
+    const float *zh;
+    const float2 *g2dd;
+    const float *F2;
+    const double *F2d;
+};
+
+// Evaluate one screened candidate: selection, intensity, beam-frame z.
+template <int FORM>
+__device__ inline bool eval_spot(const SimConst &c, const OrientP &op, const TableP &T, long long j, float &I,
+                                 float &zout, double &sout) {
+    const float4 e = T.scr[j];
+    if (FORM == DS_FORM_FP64) {
+        double s, r, z;
+        bool sel = select_fp64(c, op, (double)e.x, (double)e.y, (double)e.z, s, r, z);
+        I = (float)(shape_fp64(c, s, r) * T.F2d[j]);
+        zout = (float)z;
+        sout = s;
+        return sel;
+    } else {
+        dd s;
+        float r, z;
+        bool sel = select_mixed(c, op, e, T.g2dd[j], s, r, z);
+        I = shape_mixed(c, s, r) * T.F2[j];
+        zout = z;
+        sout = (double)s.hi + (double)s.lo;
+        return sel;
+    }
+}
+
+__device__ __forceinline__ int owner_lane(int incl, int q) {
+    int lo = 0;
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1) {
+        int v = __shfl_sync(FULL_MASK, incl, lo + step - 1);
+        if (v <= q) lo += step;
+    }
+    return lo;
+}
+
+// Iterate the set bits of bitmap words [w0, w1) of one orientation in row
+// order, 32 at a time across the warp.  fn(j, rank, valid) is called by every
+// lane (valid = lane holds a bit); rank = bit position in the ordered list.
+template <typename Fn>
+__device__ __forceinline__ void for_each_bit(const uint32_t *row, int w0, int w1, int lane, Fn fn) {
+    int base_rank = 0;
+    for (int g0 = w0; g0 < w1; g0 += 32) {
+        int wi = g0 + lane;
+        uint32_t word = wi < w1 ? row[wi] : 0u;
+        int cnt = __popc(word);
+        int incl = warp_inclusive_scan(cnt, lane);
+        int total = __shfl_sync(FULL_MASK, incl, 31);
+        for (int q0 = 0; q0 < total; q0 += 32) {
+            int q = q0 + lane;
+            bool valid = q < total;
+            int own = owner_lane(incl, valid ? q : total - 1);
+            uint32_t ow = __shfl_sync(FULL_MASK, word, own);
+            int oin = __shfl_sync(FULL_MASK, incl, own);
+            int bit = 0;
+            if (valid) bit = (int)__fns(ow, 0, q - (oin - __popc(ow)) + 1);
+            long long j = (long long)(g0 + own) * 32 + bit;
+            fn(j, base_rank + q, valid, g0 + own, bit);
+        }
+        base_rank += total;
+    }
+}
+
+template <int O, int FORM>
+__global__ void __launch_bounds__(SIM_THREADS, 2)
+simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t *__restrict__ offsets,
+                int32_t *__restrict__ out_idx, float4 *__restrict__ out_xyzi, double *__restrict__ out_s,
+                int64_t *__restrict__ out_total, LookbackScratch lb, int32_t *status) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const SimSmem Ls = sim_smem_layout(O, c.Ws);
+    OrientP *sop = reinterpret_cast<OrientP *>(smem + Ls.orient);
+    unsigned long long *acc = reinterpret_cast<unsigned long long *>(smem + Ls.acc);
+    uint32_t *bitmap = reinterpret_cast<uint32_t *>(smem + Ls.bitmap);
+    __shared__ long long s_tile, s_prefix;
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) s_tile = (long long)atomicAdd(lb.ticket, 1ull);
+    for (int i = tid; i < O * 8; i += SIM_THREADS)
+        acc[i] = (i % 8 == ACC_MINPOS) ? (unsigned long long)__float_as_uint(INFINITY) : 0ull;
+    __syncthreads();
+    const long long tile = s_tile;
+    const long long o_base = tile * O;
+    const int n_valid = (int)min((long long)O, c.n_orient - o_base);
+
+    // per-orientation rotation: beam frame = g @ R, R the active matrix of q
+    if (tid < O) {
+        OrientP &op = sop[tid];
+        double R[3][3];
+        if (tid < n_valid) {
+            const double *q = quats + 4 * (o_base + tid);
+            double w = q[0], x = q[1], y = q[2], z = q[3];
+            double nrm = sqrt(w * w + x * x + y * y + z * z);
+            if (!(nrm > 0) || !isfinite(nrm)) { atomicOr(status, DS_ERR_NONFINITE); nrm = 1; w = 1; x = y = z = 0; }
+            w /= nrm; x /= nrm; y /= nrm; z /= nrm;
+            R[0][0] = 1 - 2 * (y * y + z * z); R[0][1] = 2 * (x * y - w * z); R[0][2] = 2 * (x * z + w * y);
+            R[1][0] = 2 * (x * y + w * z); R[1][1] = 1 - 2 * (x * x + z * z); R[1][2] = 2 * (y * z - w * x);
+            R[2][0] = 2 * (x * z - w * y); R[2][1] = 2 * (y * z + w * x); R[2][2] = 1 - 2 * (x * x + y * y);
+        } else {
+            for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) R[a][b] = 0.0;
+        }
+        for (int cc = 0; cc < 3; ++cc)
+            for (int i = 0; i < 3; ++i) {
+                double v = c.recip[3 * i + 0] * R[0][cc] + c.recip[3 * i + 1] * R[1][cc] + c.recip[3 * i + 2] * R[2][cc];
+                op.M[cc][i] = v;
+                float hi, lo;
+                split_double(v, hi, lo);
+                op.m[cc][i] = hi;
+                if (cc == 2) op.mzlo[i] = lo;
+            }
+    }
+    __syncthreads();
+
+    // ---------------- phase 1: screen every row against all O orientations
+    {
+        float m0[O], m1[O], m2[O];
+#pragma unroll
+        for (int o = 0; o < O; ++o) { m0[o] = sop[o].m[2][0]; m1[o] = sop[o].m[2][1]; m2[o] = sop[o].m[2][2]; }
+        for (int wc = warp; wc < c.W; wc += SIM_WARPS) {
+            long long j = (long long)wc * 32 + lane;
+            float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
+            float zh = -1.f;
+            if (j < c.n_hkl) { e = T.scr[j]; zh = T.zh[j]; }
+            uint32_t myword = 0;
+            if (FORM == DS_FORM_FP64) {
+                double hd = e.x, kd = e.y, ld = e.z;
+#pragma unroll 1
+                for (int o = 0; o < O; ++o) {
+                    double s, r, z;
+                    bool hit = (j < c.n_hkl) && (o < n_valid) && select_fp64(c, sop[o], hd, kd, ld, s, r, z);
+                    uint32_t b = __ballot_sync(FULL_MASK, hit);
+                    if (lane == o) myword = b;
+                }
+            } else {
+#pragma unroll
+                for (int o = 0; o < O; ++o) {
+                    float z = fmaf(m0[o], e.x, fmaf(m1[o], e.y, fmaf(m2[o], e.z, e.w)));
+                    uint32_t b = __ballot_sync(FULL_MASK, fabsf(z) < zh);
+                    if (lane == o) myword = b;
+                }
+            }
+            if (lane < O) bitmap[lane * c.Ws + wc] = myword;
+        }
+    }
+    __syncthreads();
+
+    // work split for phases 2-3: warps_per_o warps share one orientation's words
+    constexpr int WPO = O >= SIM_WARPS ? 1 : SIM_WARPS / O;
+    const int part = warp % WPO;
+    const int w0 = (int)(((long long)c.W * part) / WPO), w1 = (int)(((long long)c.W * (part + 1)) / WPO);
+    const bool all_zero_drop = c.thr >= 0.0;
+
+    // ---------------- phase 2: refine, intensities, per-orientation max
+    for (int o = warp / WPO; o < n_valid; o += SIM_WARPS / WPO) {
+        uint32_t *row = bitmap + o * c.Ws;
+        const OrientP &op = sop[o];
+        float lmax = 0.f, lminpos = INFINITY;
+        int lcnt = 0;
+        for_each_bit(row, w0, w1, lane, [&](long long j, int, bool valid, int wi, int bit) {
+            if (!valid) return;
+            float I, z;
+            double sv;
+            bool sel = eval_spot<FORM>(c, op, T, j, I, z, sv);
+            if (sel && I == 0.f && all_zero_drop) sel = false;
+            if (!sel) {
+                atomicAnd(&row[wi], ~(1u << bit));
+                return;
+            }
+            ++lcnt;
+            lmax = fmaxf(lmax, I);
+            if (I > 0.f) lminpos = fminf(lminpos, I);
+        });
+#pragma unroll
+        for (int d = 16; d >= 1; d >>= 1) {
+            lmax = fmaxf(lmax, __shfl_xor_sync(FULL_MASK, lmax, d));
+            lminpos = fminf(lminpos, __shfl_xor_sync(FULL_MASK, lminpos, d));
+            lcnt += __shfl_xor_sync(FULL_MASK, lcnt, d);
+        }
+        if (!(lmax > 0.f)) lmax = 0.f;  // no -0.0 or NaN in the bit-ordered max
+        if (lane == 0) {
+            // intensities are >= 0, so float bit patterns order like the values
+            atomicMax(&acc[o * 8 + ACC_MAXI], (unsigned long long)__float_as_uint(lmax));
+            atomicMin(&acc[o * 8 + ACC_MINPOS], (unsigned long long)__float_as_uint(lminpos));
+        }
+    }
+    __syncthreads();
+
+    // ---------------- mask pass (only where some I is positive but below max * thr)
+    for (int o = warp / WPO; o < n_valid; o += SIM_WARPS / WPO) {
+        float mx = __uint_as_float((unsigned)acc[o * 8 + ACC_MAXI]);
+        float mnp = __uint_as_float((unsigned)acc[o * 8 + ACC_MINPOS]);
+        if (!(c.thr > 0.0)) continue;
+        float cut = (float)((double)mx * c.thr);
+        if (!(mnp <= cut)) continue;
+        uint32_t *row = bitmap + o * c.Ws;
+        const OrientP &op = sop[o];
+        for_each_bit(row, w0, w1, lane, [&](long long j, int, bool valid, int wi, int bit) {
+            if (!valid) return;
+            float I, z;
+            double sv;
+            eval_spot<FORM>(c, op, T, j, I, z, sv);
+            if (!((double)I > (double)mx * c.thr)) atomicAnd(&row[wi], ~(1u << bit));
+        });
+    }
+    __syncthreads();
+
+    // ---------------- phase 3a: counts, offsets, look-back
+    for (int o = warp / WPO; o < n_valid; o += SIM_WARPS / WPO) {
+        const uint32_t *row = bitmap + o * c.Ws;
+        int cnt = 0;
+        for (int wi = w0 + lane; wi < w1; wi += 32) cnt += __popc(row[wi]);
+#pragma unroll
+        for (int d = 16; d >= 1; d >>= 1) cnt += __shfl_xor_sync(FULL_MASK, cnt, d);
+        if (lane == 0) acc[o * 8 + ACC_PART0 + part] = (unsigned long long)cnt;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        long long run = 0;
+        for (int o = 0; o < n_valid; ++o) {
+            acc[o * 8 + ACC_OFF] = (unsigned long long)run;
+            long long co = 0;
+            for (int p = 0; p < WPO; ++p) co += (long long)acc[o * 8 + ACC_PART0 + p];
+            acc[o * 8 + ACC_CNT] = (unsigned long long)co;
+            run += co;
+        }
+        long long prefix = lookback_exclusive(lb, tile, run, status);
+        s_prefix = prefix;
+        if (prefix >= 0 && tile == c.n_tiles - 1) {
+            offsets[c.n_orient] = prefix + run;
+            *out_total = prefix + run;
+        }
+    }
+    __syncthreads();
+    const long long prefix = s_prefix;
+    if (prefix < 0) return;
+    for (int o = tid; o < n_valid; o += SIM_THREADS) offsets[o_base + o] = prefix + (long long)acc[o * 8 + ACC_OFF];
+
+    // ---------------- phase 3b: ordered writes
+    for (int o = warp / WPO; o < n_valid; o += SIM_WARPS / WPO) {
+        const uint32_t *row = bitmap + o * c.Ws;
+        const OrientP &op = sop[o];
+        long long pos0 = prefix + (long long)acc[o * 8 + ACC_OFF];
+        for (int p = 0; p < part; ++p) pos0 += (long long)acc[o * 8 + ACC_PART0 + p];
+        bool overflow = false;
+        for_each_bit(row, w0, w1, lane, [&](long long j, int rank, bool valid, int, int) {
+            if (!valid) return;
+            float I, z;
+            double sv;
+            eval_spot<FORM>(c, op, T, j, I, z, sv);
+            const float4 e = T.scr[j];
+            float x, y;
+            if (FORM == DS_FORM_FP64) {
+                x = (float)(op.M[0][0] * (double)e.x + op.M[0][1] * (double)e.y + op.M[0][2] * (double)e.z);
+                y = (float)(op.M[1][0] * (double)e.x + op.M[1][1] * (double)e.y + op.M[1][2] * (double)e.z);
+            } else {
+                x = fmaf(op.m[0][0], e.x, fmaf(op.m[0][1], e.y, op.m[0][2] * e.z));
+                y = fmaf(op.m[1][0], e.x, fmaf(op.m[1][1], e.y, op.m[1][2] * e.z));
+            }
+            long long pos = pos0 + rank;
+            if (pos < c.capacity) {
+                out_idx[pos] = (int32_t)j;
+                out_xyzi[pos] = make_float4(x, y, z, I);
+                if (out_s) out_s[pos] = sv;
+            } else {
+                overflow = true;
+            }
+        });
+        if (__any_sync(FULL_MASK, overflow) && lane == 0) atomicOr(status, DS_ERR_CAPACITY);
+    }
+}
+
+// ------------------------------------------------------------- host side ----
+static inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+struct SimPlan {
+    int O, W, Ws;
+    long long n_tiles;
+    size_t off_lb, off_scr, off_zh, off_g2, total;
+    size_t smem;
+};
+
+static int pick_O(const ds_sim_params *p, long long n_hkl, long long n_orient) {
+    long long W = (n_hkl + 31) / 32;
+    long long Ws = W | 1;
+    const int o_cap = p->form == DS_FORM_FP64 ? 16 : SIM_MAX_O;
+    if (p->orient_tile > 0) return p->orient_tile < o_cap ? p->orient_tile : o_cap;
+    int O = o_cap;
+    const long long budget = 100 * 1024;  // two CTAs per SM
+    while (O > 4 && (long long)O * Ws * 4 + O * (long long)sizeof(OrientP) > budget) O >>= 1;
+    // keep at least ~2 tiles per SM when the orientation count allows it
+    while (O > 4 && (n_orient + O - 1) / O < 304) O >>= 1;
+    return O;
+}
+
+static SimPlan make_plan(const ds_sim_params *p, const ds_phase_table *t, long long n_orient) {
+    SimPlan P;
+    P.O = pick_O(p, t->n_hkl, n_orient);
+    P.W = (int)((t->n_hkl + 31) / 32);
+    P.Ws = P.W | 1;
+    P.n_tiles = (n_orient + P.O - 1) / P.O;
+    size_t o = 0;
+    P.off_lb = o; o += lookback_scratch_bytes(P.n_tiles);
+    o = align_up(o, 256);
+    P.off_scr = o; o += (size_t)t->n_hkl * sizeof(float4);
+    o = align_up(o, 256);
+    P.off_zh = o; o += (size_t)t->n_hkl * sizeof(float);
+    o = align_up(o, 256);
+    P.off_g2 = o; o += (size_t)t->n_hkl * sizeof(float2);
+    P.total = align_up(o, 256);
+    P.smem = sim_smem_layout(P.O, P.Ws).total;
+    return P;
+}
+
+template <int O, int FORM>
+static ds_status launch_sim(const SimConst &c, const TableP &T, const double *quats, ds_spots *out,
+                            LookbackScratch lb, size_t smem, int32_t *status, cudaStream_t s) {
+    auto kern = simulate_kernel<O, FORM>;
+    DS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<(unsigned)c.n_tiles, SIM_THREADS, smem, s>>>(c, T, quats, out->offsets, out->hkl_index,
+                                                        reinterpret_cast<float4 *>(out->xyzi), out->excitation_error, out->total,
+                                                        lb, status);
+    return check_launch("simulate_kernel");
+}
+
+}  // namespace ds
+
+using namespace ds;
+
+extern "C" size_t ds_simulate_scratch_bytes(const ds_sim_params *p, const ds_phase_table *t, int64_t n_orient) {
+    if (!p || !t || n_orient <= 0) return 0;
+    return make_plan(p, t, n_orient).total;
+}
+
+extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t, const double *quats,
+                                 int64_t n_orient, ds_spots *out, void *scratch, size_t scratch_bytes,
+                                 int32_t *status, void *stream) {
+    clear_error();
+    DS_REQUIRE(p && t && out && status, "ds_simulate: null pointer");
+    DS_REQUIRE(n_orient >= 0, "ds_simulate: n_orient < 0");
+    DS_REQUIRE(t->n_hkl >= 0 && t->n_hkl < (1ll << 31), "ds_simulate: n_hkl out of range");
+    DS_REQUIRE(p->k0 > 0 && isfinite(p->k0), "ds_simulate: k0 must be finite and > 0");
+    DS_REQUIRE(p->max_excitation_error > 0 && isfinite(p->max_excitation_error),
+               "ds_simulate: max_excitation_error must be > 0");
+    DS_REQUIRE(p->shape_width != 0 && isfinite(p->shape_width), "ds_simulate: shape width must be finite, non-zero");
+    DS_REQUIRE(p->shape_model >= DS_SHAPE_LINEAR && p->shape_model <= DS_SHAPE_BINARY, "ds_simulate: bad shape model");
+    DS_REQUIRE(p->precession_mode >= DS_PRECESSION_NONE && p->precession_mode <= DS_PRECESSION_INTEGRAL,
+               "ds_simulate: bad precession mode");
+    DS_REQUIRE(p->form == DS_FORM_MIXED || p->form == DS_FORM_FP64, "ds_simulate: bad form");
+    DS_REQUIRE(p->orient_tile == 0 || p->orient_tile == 4 || p->orient_tile == 8 || p->orient_tile == 16 ||
+                   p->orient_tile == 32, "ds_simulate: orient_tile must be 0, 4, 8, 16 or 32");
+    DS_REQUIRE(p->precession_mode == DS_PRECESSION_NONE || p->precession_angle > 0,
+               "ds_simulate: precession mode needs a positive angle");
+    if (p->precession_mode == DS_PRECESSION_INTEGRAL) {
+        set_error("ds_simulate: DS_PRECESSION_INTEGRAL is not available in this build");
+        return DS_ERR_UNSUPPORTED;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    if (n_orient == 0) {
+        DS_CUDA_TRY(cudaMemsetAsync(out->offsets, 0, sizeof(int64_t), s));
+        DS_CUDA_TRY(cudaMemsetAsync(out->total, 0, sizeof(int64_t), s));
+        return DS_OK;
+    }
+    DS_REQUIRE(quats && out->offsets && out->total, "ds_simulate: null quats / offsets / total");
+    DS_REQUIRE(t->n_hkl == 0 || (t->hkl && t->g2 && (p->form == DS_FORM_MIXED ? t->F2 != nullptr : t->F2d != nullptr)),
+               "ds_simulate: table arrays missing for this form");
+    DS_REQUIRE(out->capacity >= 0 && (out->capacity == 0 || (out->hkl_index && out->xyzi)),
+               "ds_simulate: output arrays missing");
+    DS_REQUIRE(((uintptr_t)out->xyzi & 15) == 0, "ds_simulate: xyzi must be 16-byte aligned");
+    SimPlan P = make_plan(p, t, n_orient);
+    DS_REQUIRE(scratch && scratch_bytes >= P.total, "ds_simulate: scratch too small");
+    DS_REQUIRE(P.smem <= 227 * 1024, "ds_simulate: candidate table too large for one orientation tile");
+
+    SimConst c;
+    c.k0 = p->k0;
+    c.eps = p->max_excitation_error;
+    c.width = p->shape_width;
+    c.phi = p->precession_angle;
+    c.thr = p->minimum_intensity;
+    c.minima = p->minima_number;
+    c.Pz = p->k0 * cos(p->precession_angle);
+    c.Pt = p->k0 * sin(p->precession_angle);
+    for (int i = 0; i < 9; ++i) c.recip[i] = t->recip[i];
+    split_double(c.eps, c.eps_dd.hi, c.eps_dd.lo);
+    split_double(1.0 / (2.0 * c.k0), c.c2k0_dd.hi, c.c2k0_dd.lo);
+    split_double(c.width, c.width_dd.hi, c.width_dd.lo);
+    split_double(c.minima / c.width, c.mw_dd.hi, c.mw_dd.lo);
+    const double PI = 3.14159265358979323846;
+    c.k0f = (float)c.k0;
+    c.inv_k0sq = (float)(1.0 / (c.k0 * c.k0));
+    c.eps_f = (float)c.eps;
+    c.width_f = (float)c.width;
+    c.sigma_f = (float)(PI / c.width);
+    c.mfac_f = (float)(PI * c.minima / fabs(c.width));
+    c.phi_f = (float)c.phi;
+    c.Pz_f = (float)c.Pz;
+    c.Pt_f = (float)c.Pt;
+    c.k0sq_f = (float)(c.k0 * c.k0);
+    // FP32 screen guard: bound on |z32 - z| from rounding m to FP32 and the FMA
+    // chain, 8 ulp of sum_i |row_i of recip| * max|hkl_i| (|R| = 1), plus the
+    // rounding of z_mid and z_half.
+    double zmax = 0;
+    for (int i = 0; i < 3; ++i)
+        zmax += sqrt(t->recip[3 * i] * t->recip[3 * i] + t->recip[3 * i + 1] * t->recip[3 * i + 1] +
+                     t->recip[3 * i + 2] * t->recip[3 * i + 2]) * (double)t->hmax[i];
+    c.guard = (float)(8.0 * 5.96e-8 * zmax + 4.0 * 5.96e-8 * (c.eps + zmax * zmax / (2 * c.k0)) + 1e-7);
+    c.shape = p->shape_model;
+    c.prec = p->precession_mode;
+    c.form = p->form;
+    c.O = P.O;
+    c.W = P.W;
+    c.Ws = P.Ws;
+    c.n_hkl = t->n_hkl;
+    c.n_orient = n_orient;
+    c.n_tiles = P.n_tiles;
+    c.capacity = out->capacity;
+
+    unsigned char *sb = reinterpret_cast<unsigned char *>(scratch);
+    TableP T;
+    T.scr = reinterpret_cast<float4 *>(sb + P.off_scr);
+    T.zh = reinterpret_cast<float *>(sb + P.off_zh);
+    T.g2dd = reinterpret_cast<float2 *>(sb + P.off_g2);
+    T.F2 = t->F2;
+    T.F2d = t->F2d;
+    DS_CUDA_TRY(cudaMemsetAsync(sb + P.off_lb, 0, lookback_scratch_bytes(P.n_tiles), s));
+    if (t->n_hkl > 0) {
+        sim_prep_kernel<<<(unsigned)((t->n_hkl + 255) / 256), 256, 0, s>>>(
+            c, t->hkl, t->g2, const_cast<float4 *>(T.scr), const_cast<float *>(T.zh), const_cast<float2 *>(T.g2dd));
+        ds_status st = check_launch("sim_prep_kernel");
+        if (st) return st;
+    }
+    LookbackScratch lb = lookback_scratch(sb + P.off_lb);
+    if (p->form == DS_FORM_FP64) {
+        switch (P.O) {
+            case 4: return launch_sim<4, DS_FORM_FP64>(c, T, quats, out, lb, P.smem, status, s);
+            case 8: return launch_sim<8, DS_FORM_FP64>(c, T, quats, out, lb, P.smem, status, s);
+            default: return launch_sim<16, DS_FORM_FP64>(c, T, quats, out, lb, P.smem, status, s);
+        }
+    }
+    switch (P.O) {
+        case 4: return launch_sim<4, DS_FORM_MIXED>(c, T, quats, out, lb, P.smem, status, s);
+        case 8: return launch_sim<8, DS_FORM_MIXED>(c, T, quats, out, lb, P.smem, status, s);
+        case 16: return launch_sim<16, DS_FORM_MIXED>(c, T, quats, out, lb, P.smem, status, s);
+        default: return launch_sim<32, DS_FORM_MIXED>(c, T, quats, out, lb, P.smem, status, s);
+    }
+}

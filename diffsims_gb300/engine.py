@@ -1,0 +1,246 @@
+"""Device-side engine: per-phase candidate tables and the batched
+orientation simulation, all through the C ABI.
+
+``PhaseTable`` = ReciprocalLatticeVector.from_min_dspacing + the structure
+factor table of one phase (diffsims/crystallography/reciprocal_lattice_vector.py:1077-1142,
+diffsims/utils/sim_utils.py:256-304).  ``simulate_phase`` = the orientation
+loop of SimulationGenerator.calculate_diffraction2d
+(diffsims/generators/simulation_generator.py:198-241) for one phase.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .crystal import lattice_params, lattice_base, sites_of, structure_of
+from .sim_utils import PackedAtoms, debye_waller_per_atom
+
+FORMS = {"mixed": N.DS_FORM_MIXED, "fp64": N.DS_FORM_FP64}
+
+
+def _device(device=None):
+    if device is None:
+        return torch.device("cuda", torch.cuda.current_device())
+    return torch.device(device)
+
+
+def reciprocal_basis(lattice) -> np.ndarray:
+    """Rows a*, b*, c* (1/Angstrom, no 2 pi) in the x || a, z || c* frame."""
+    return np.ascontiguousarray(np.linalg.inv(lattice_base(*lattice_params(lattice))).T)
+
+
+def box_extent(recip: np.ndarray, min_dspacing: float) -> np.ndarray:
+    lib = N.load_library(require_cuda=False)
+    r = (C.c_double * 9)(*recip.reshape(-1).tolist())
+    out = (C.c_int32 * 3)()
+    N.check(lib.ds_box_extent(r, float(min_dspacing), out), "box_extent")
+    return np.array(list(out), dtype=np.int64)
+
+
+class PhaseTable:
+    """Ordered candidate rows of one phase on the device: hkl (int32), |g|^2
+    (FP64) and |F|^2 (FP32 for the mixed form, FP64 for the FP64 form)."""
+
+    def __init__(self, phase, reciprocal_radius=1.0, with_direct_beam=True, scattering_params="lobato",
+                 debye_waller_factors=None, form="mixed", device=None, stream=None, build=True):
+        lib = N.load_library()
+        dev = _device(device)
+        self.device = dev
+        self.form = form
+        structure = structure_of(phase)
+        self.recip = reciprocal_basis(structure.lattice)
+        self.dmin = 1.0 / float(reciprocal_radius)
+        self.hmax = box_extent(self.recip, self.dmin)
+        self.n_zero = 2 if with_direct_beam else 0
+        box = int(np.prod(2 * self.hmax + 1))
+        self.cap = box + self.n_zero
+        self._hkl = torch.empty((self.cap, 3), dtype=torch.int32, device=dev)
+        self._g2 = torch.empty(self.cap, dtype=torch.float64, device=dev)
+        self._count = torch.zeros(1, dtype=torch.int64, device=dev)
+        self._status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self._hm = (C.c_int32 * 3)(*self.hmax.tolist())
+        self._rb = (C.c_double * 9)(*self.recip.reshape(-1).tolist())
+        self._enum_bytes = lib.ds_enumerate_scratch_bytes(self._hm)
+        els, xyz, occ = sites_of(structure)
+        B = debye_waller_per_atom(els, debye_waller_factors)
+        self.atoms = PackedAtoms(els, xyz, occ, B, scattering_params, dev)
+        self._sf_bytes = lib.ds_structure_factor_scratch_bytes(self.cap, self.atoms.n_atoms)
+        self._scratch = torch.empty(max(self._enum_bytes, self._sf_bytes), dtype=torch.uint8, device=dev)
+        self._F2 = torch.empty(self.cap, dtype=torch.float32, device=dev)
+        self._F2d = torch.empty(self.cap, dtype=torch.float64, device=dev) if form == "fp64" else None
+        self.n = 0
+        if build:
+            self.build(stream)
+
+    def build(self, stream=None):
+        """Enumerate the hkl rows and compute |F|^2 on the device (inputs
+        already resident).  Synchronises once to read the row count."""
+        lib = N.load_library()
+        st = N.stream_handle(stream)
+        self._status.zero_()
+        N.check(lib.ds_enumerate_hkl(self._rb, self._hm, self.dmin, self.n_zero, N.ptr(self._hkl), N.ptr(self._g2),
+                                     self.cap, N.ptr(self._count), N.ptr(self._scratch), self._enum_bytes,
+                                     N.ptr(self._status), st), "enumerate_hkl")
+        n = int(self._count.item())
+        N.check_device_status(self._status, "enumerate_hkl")
+        self.n = n
+        self.hkl = self._hkl[:n]
+        self.g2 = self._g2[:n]
+        self.F2 = self._F2[:max(n, 1)]
+        self.F2d = self._F2d[:max(n, 1)] if self._F2d is not None else None
+        if n:
+            a = self.atoms.cstruct()
+            N.check(lib.ds_structure_factors(a, N.ptr(self.hkl), None, N.ptr(self.g2), n, FORMS[self.form],
+                                             N.ptr(self.F2), N.ptr(self.F2d), None, N.ptr(self._scratch),
+                                             self._scratch.numel(), N.ptr(self._status), st), "structure_factors")
+        return self
+
+    def hkl_host(self) -> np.ndarray:
+        if getattr(self, "_hkl_host", None) is None or self._hkl_host.shape[0] != self.n:
+            self._hkl_host = self.hkl.cpu().numpy()
+        return self._hkl_host
+
+    def cstruct(self) -> N.ds_phase_table:
+        t = N.ds_phase_table()
+        t.n_hkl = self.n
+        t.hkl = self.hkl.data_ptr() if self.n else None
+        t.g2 = self.g2.data_ptr() if self.n else None
+        t.F2 = self.F2.data_ptr()
+        t.F2d = self.F2d.data_ptr() if self.F2d is not None else None
+        for i, v in enumerate(self.recip.reshape(-1)):
+            t.recip[i] = float(v)
+        for i, v in enumerate(self.hmax):
+            t.hmax[i] = int(v)
+        return t
+
+
+@dataclass
+class SimSettings:
+    """The per-call simulation constants (the generator's settings)."""
+    k0: float
+    max_excitation_error: float
+    shape_width: float
+    shape_model: str
+    precession_angle_rad: float = 0.0
+    precession_mode: int = N.DS_PRECESSION_NONE
+    minimum_intensity: float = 1e-20
+    minima_number: float = 5.0
+    form: str = "mixed"
+    orient_tile: int = 0
+
+    def cstruct(self) -> N.ds_sim_params:
+        return N.ds_sim_params(self.k0, self.max_excitation_error, self.shape_width, self.precession_angle_rad,
+                               self.minimum_intensity, self.minima_number, N.DS_SHAPE[self.shape_model],
+                               self.precession_mode, FORMS[self.form], self.orient_tile)
+
+
+class PhaseSpots:
+    """CSR spots of one phase on the device: ``offsets`` (n_orient + 1),
+    ``hkl_index`` (rows of the phase table), ``xyzi`` (x, y, z, intensity)."""
+
+    def __init__(self, table: PhaseTable, offsets, hkl_index, xyzi, total, excitation_error=None):
+        self.table = table
+        self.offsets = offsets
+        self.hkl_index = hkl_index[:total]
+        self.xyzi = xyzi[:total]
+        self.excitation_error = None if excitation_error is None else excitation_error[:total]
+        self.total = total
+        self._host = None
+
+    @property
+    def n_orient(self):
+        return self.offsets.shape[0] - 1
+
+    def host(self, pinned=False):
+        """numpy copies (offsets, hkl (total, 3) int, xyz (total, 3) float64,
+        intensity float64); with ``pinned`` the device arrays go through
+        page-locked buffers."""
+        if self._host is None:
+            def fetch(t):
+                if pinned:
+                    h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+                    h.copy_(t, non_blocking=True)
+                    return h
+                return t.cpu()
+            off, idx, xyzi = fetch(self.offsets), fetch(self.hkl_index), fetch(self.xyzi)
+            torch.cuda.current_stream().synchronize()
+            table_hkl = self.table.hkl_host()
+            idx = idx.numpy()
+            hkl = table_hkl[idx] if self.total else np.zeros((0, 3), np.int32)
+            xyzi = xyzi.numpy().astype(np.float64)
+            self._host = (off.numpy(), hkl, xyzi[:, :3], xyzi[:, 3])
+        return self._host
+
+    def nbytes(self):
+        return self.offsets.numel() * 8 + self.total * (4 + 16)
+
+
+class SpotBuffers:
+    """Reusable device buffers for ``simulate_phase`` (grown on demand)."""
+
+    def __init__(self, device, with_excitation_error=False):
+        self.device = device
+        self.capacity = 0
+        self.idx = self.xyzi = self.s = None
+        self.with_s = with_excitation_error
+        self.scratch = None
+        self.status = torch.zeros(1, dtype=torch.int32, device=device)
+        self.total = torch.zeros(1, dtype=torch.int64, device=device)
+
+    def ensure(self, capacity, scratch_bytes):
+        if capacity > self.capacity:
+            self.capacity = int(capacity)
+            self.idx = torch.empty(self.capacity, dtype=torch.int32, device=self.device)
+            self.xyzi = torch.empty((self.capacity, 4), dtype=torch.float32, device=self.device)
+            if self.with_s:
+                self.s = torch.empty(self.capacity, dtype=torch.float64, device=self.device)
+        if self.scratch is None or self.scratch.numel() < scratch_bytes:
+            self.scratch = torch.empty(int(scratch_bytes), dtype=torch.uint8, device=self.device)
+
+
+def estimate_spots(table: PhaseTable, settings: SimSettings, radius: float) -> int:
+    """Expected spots per orientation: rows inside the |s| < s_max shell (area
+    pi r^2 times thickness 2 s_max out of the 4/3 pi r^3 sphere), widened for
+    precession."""
+    band = 2 * settings.max_excitation_error + 2 * radius * np.sin(settings.precession_angle_rad)
+    frac = min(1.0, 1.5 * band / max(radius, 1e-9))
+    return int(table.n * frac) + 8
+
+
+def simulate_phase(table: PhaseTable, quats: torch.Tensor, settings: SimSettings, radius: float,
+                   buffers: SpotBuffers | None = None, stream=None, sync=True):
+    """Run ds_simulate for one phase; returns PhaseSpots (device CSR).
+
+    quats: (N, 4) float64 on the device.  On output-capacity overflow the call
+    is repeated once with the exact size the first run reported.
+    """
+    lib = N.load_library()
+    dev = table.device
+    n_orient = int(quats.shape[0])
+    buffers = buffers or SpotBuffers(dev)
+    p = settings.cstruct()
+    t = table.cstruct()
+    sbytes = lib.ds_simulate_scratch_bytes(p, t, n_orient)
+    cap = max(1024, n_orient * estimate_spots(table, settings, radius) * 5 // 4)
+    offsets = torch.empty(n_orient + 1, dtype=torch.int64, device=dev)
+    st = N.stream_handle(stream)
+    for attempt in range(2):
+        buffers.ensure(cap, sbytes)
+        buffers.status.zero_()
+        out = N.ds_spots(offsets.data_ptr(), buffers.idx.data_ptr(), buffers.xyzi.data_ptr(), buffers.capacity,
+                         buffers.total.data_ptr(), buffers.s.data_ptr() if buffers.s is not None else None)
+        N.check(lib.ds_simulate(p, t, N.ptr(quats), n_orient, out, N.ptr(buffers.scratch), sbytes,
+                                N.ptr(buffers.status), st), "simulate")
+        if not sync:
+            return None
+        v = N.check_device_status(buffers.status, "simulate", allow=N.DS_ERR_CAPACITY)
+        N.check_device_status(table._status, "structure_factors")
+        total = int(buffers.total.item())
+        if not (v & N.DS_ERR_CAPACITY):
+            return PhaseSpots(table, offsets, buffers.idx, buffers.xyzi, total, buffers.s)
+        cap = total + 1024
+    raise N.NativeError("simulate: output capacity still exceeded after resizing")

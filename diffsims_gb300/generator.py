@@ -1,0 +1,141 @@
+"""``SimulationGenerator``: drop-in for
+diffsims/generators/simulation_generator.py (``calculate_diffraction2d``)
+running on the CUDA library."""
+from __future__ import annotations
+
+from typing import Sequence, Union
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .crystal import Phase, Rotation, quaternions_of
+from .engine import PhaseTable, SimSettings, SpotBuffers, simulate_phase
+from .simulation2d import Simulation2D
+from .sim_utils import get_electron_wavelength
+
+_SHAPE_NAMES = ("linear", "atanc", "sinc", "sin2c", "lorentzian")
+
+
+def _shape_name(model):
+    """Name of a built-in shape model given by name or by function (the
+    reference's functions in diffsims.utils.shape_factor_models, or any
+    function with the same name and module tail)."""
+    if isinstance(model, str):
+        return model
+    name = getattr(model, "__name__", None)
+    mod = getattr(model, "__module__", "") or ""
+    if name in _SHAPE_NAMES + ("binary",) and mod.endswith("shape_factor_models"):
+        return name
+    return None
+
+
+class SimulationGenerator:
+    """Kinematic diffraction simulations on the GPU.
+
+    Constructor arguments as diffsims/generators/simulation_generator.py:74-128:
+    ``accelerating_voltage`` (kV), ``scattering_params`` ('lobato', 'xtables'
+    or None), ``precession_angle`` (degrees), ``shape_factor_model`` (one of
+    'linear', 'atanc', 'sinc', 'sin2c', 'lorentzian', or the reference's model
+    functions), ``approximate_precession``, ``minimum_intensity`` and keyword
+    arguments for the shape model (``minima_number``).
+    """
+
+    def __init__(self, accelerating_voltage: float = 200, scattering_params: str = "lobato",
+                 precession_angle: float = 0, shape_factor_model="lorentzian", approximate_precession: bool = True,
+                 minimum_intensity: float = 1e-20, **kwargs):
+        self.accelerating_voltage = accelerating_voltage
+        self.precession_angle = np.abs(precession_angle)
+        self.approximate_precession = approximate_precession
+        if isinstance(shape_factor_model, str):
+            if shape_factor_model not in _SHAPE_NAMES:
+                raise NotImplementedError(
+                    f"{shape_factor_model} is not a recognized shape factor model, choose from: "
+                    f"{_SHAPE_NAMES} or provide your own function.")
+            self.shape_factor_model = shape_factor_model
+        else:
+            if _shape_name(shape_factor_model) is None:
+                raise NotImplementedError(
+                    "custom shape factor callables cannot run inside the CUDA kernels; use one of "
+                    f"{_SHAPE_NAMES + ('binary',)} (by name or as diffsims.utils.shape_factor_models functions)")
+            self.shape_factor_model = shape_factor_model
+        self.minimum_intensity = minimum_intensity
+        self.shape_factor_kwargs = kwargs
+        unknown = set(kwargs) - {"minima_number"}
+        if unknown:
+            raise TypeError(f"unexpected shape factor keyword arguments: {sorted(unknown)}")
+        if scattering_params in ["lobato", "xtables", None]:
+            self.scattering_params = scattering_params
+        else:
+            raise NotImplementedError(
+                "The scattering parameters `{}` is not implemented. See documentation for available "
+                "implementations.".format(scattering_params))
+        self._buffers = {}
+
+    def __repr__(self):
+        return (f"SimulationGenerator(accelerating_voltage={self.accelerating_voltage}, "
+                f"scattering_params={self.scattering_params}, "
+                f"approximate_precession={self.approximate_precession})")
+
+    @property
+    def wavelength(self):
+        return get_electron_wavelength(self.accelerating_voltage)
+
+    def settings(self, max_excitation_error=1e-2, shape_factor_width=None, form="mixed",
+                 orient_tile=0) -> SimSettings:
+        """The kernel constants of one ``calculate_diffraction2d`` call."""
+        lam = self.wavelength
+        if not lam > 0:
+            raise ValueError("accelerating_voltage must be finite (wavelength > 0)")
+        phi = float(np.deg2rad(self.precession_angle))
+        if phi == 0:
+            mode = N.DS_PRECESSION_NONE
+        elif self.approximate_precession:
+            mode = N.DS_PRECESSION_LORENTZIAN
+        else:
+            mode = N.DS_PRECESSION_INTEGRAL
+        width = max_excitation_error if shape_factor_width is None else shape_factor_width
+        return SimSettings(k0=1.0 / lam, max_excitation_error=float(max_excitation_error), shape_width=float(width),
+                           shape_model=_shape_name(self.shape_factor_model), precession_angle_rad=phi,
+                           precession_mode=mode, minimum_intensity=float(self.minimum_intensity),
+                           minima_number=float(self.shape_factor_kwargs.get("minima_number", 5)), form=form,
+                           orient_tile=orient_tile)
+
+    def calculate_diffraction2d(self, phase: Union[Phase, Sequence[Phase]],
+                                rotation: Union[Rotation, Sequence[Rotation]] = None,
+                                reciprocal_radius: float = 1.0, with_direct_beam: bool = True,
+                                max_excitation_error: float = 1e-2, shape_factor_width: float = None,
+                                debye_waller_factors: dict = None, show_progressbar: bool = False,
+                                form: str = "mixed", orient_tile: int = 0):
+        """Spot patterns of one or more phases, each under its own rotations.
+
+        Arguments as diffsims/generators/simulation_generator.py:134-146;
+        ``form`` selects the arithmetic ('mixed': FP32 bulk with FP64 phase
+        reduction and FP64 excitation error near the cutoff; 'fp64': the plain
+        all-FP64 comparator).  ``show_progressbar`` is accepted and ignored
+        (each phase is one kernel launch).  Returns ``Simulation2D``.
+        """
+        if rotation is None:
+            rotation = Rotation.from_euler((0, 0, 0), degrees=True)
+        single_phase = not isinstance(phase, (list, tuple))
+        phases = [phase] if single_phase else list(phase)
+        rotations = [rotation] if not isinstance(rotation, (list, tuple)) else list(rotation)
+        if len(phases) != len(rotations):
+            raise ValueError("The number of phases and rotations must be equal. "
+                             f"Got {len(phases)} phases and {len(rotations)} rotations.")
+        if form not in ("mixed", "fp64"):
+            raise ValueError("form must be 'mixed' or 'fp64'")
+        N.load_library()
+        dev = torch.device("cuda", torch.cuda.current_device())
+        settings = self.settings(max_excitation_error, shape_factor_width, form, orient_tile)
+        rots, spots = [], []
+        for p, r in zip(phases, rotations):
+            rot = r if isinstance(r, Rotation) else Rotation(quaternions_of(r))
+            table = PhaseTable(p, reciprocal_radius, with_direct_beam, self.scattering_params,
+                               debye_waller_factors, form=form, device=dev)
+            q = torch.from_numpy(quaternions_of(rot)).to(dev)
+            spots.append(simulate_phase(table, q, settings, reciprocal_radius, buffers=SpotBuffers(dev)))
+            rots.append(rot)
+        if single_phase:
+            return Simulation2D(phases[0], rots[0], spots, self, reciprocal_radius)
+        return Simulation2D(phases, rots, spots, self, reciprocal_radius)

@@ -1,0 +1,237 @@
+"""Result containers: ``Simulation2D`` and ``DiffractingVector``.
+
+Mirror the parts of diffsims/simulations/simulation2d.py (``Simulation2D``,
+:109-764) and diffsims/crystallography/_diffracting_vector.py
+(``DiffractingVector``) that users of ``calculate_diffraction2d`` read: the
+phase x rotation nesting, iteration, per-pattern spot vectors with
+``data`` / ``intensity`` / ``hkl``, ``polar_flatten_simulations`` and
+``get_diffraction_pattern``.  Spots stay on the device in CSR form until a
+pattern is accessed; plotting is not provided.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .crystal import Rotation
+
+
+class DiffractingVector:
+    """Spots of one pattern: beam-frame ``data`` (n, 3) in 1/Angstrom,
+    ``intensity`` (n,), Miller indices ``hkl`` (n, 3)."""
+
+    def __init__(self, phase, xyz, intensity=None, hkl=None, rotation=None):
+        self.phase = phase
+        self.data = np.asarray(xyz, dtype=np.float64).reshape(-1, 3)
+        n = self.data.shape[0]
+        self._intensity = np.full(n, np.nan) if intensity is None else np.asarray(intensity, dtype=np.float64)
+        if self._intensity.shape[0] != n:
+            raise ValueError("Length of intensity array must match number of vectors")
+        self._hkl = None if hkl is None else np.asarray(hkl, dtype=np.float64).reshape(-1, 3)
+        self.rotation = rotation
+
+    @property
+    def size(self):
+        return self.data.shape[0]
+
+    @property
+    def shape(self):
+        return (self.size,)
+
+    def __len__(self):
+        return self.size
+
+    @property
+    def x(self):
+        return self.data[:, 0]
+
+    @property
+    def y(self):
+        return self.data[:, 1]
+
+    @property
+    def z(self):
+        return self.data[:, 2]
+
+    @property
+    def intensity(self):
+        return self._intensity
+
+    @intensity.setter
+    def intensity(self, value):
+        if not hasattr(value, "__len__"):
+            value = np.array([value] * self.size)
+        if len(value) != self.size:
+            raise ValueError("Length of intensity array must match number of vectors")
+        self._intensity = np.array(value, dtype=np.float64)
+
+    @property
+    def hkl(self):
+        return self._hkl
+
+    @property
+    def gspacing(self):
+        return np.linalg.norm(self.data, axis=1)
+
+    def __getitem__(self, key):
+        if isinstance(key, (int, np.integer)):
+            key = slice(key, key + 1 if key != -1 else None)
+        return DiffractingVector(self.phase, self.data[key], self._intensity[key],
+                                 None if self._hkl is None else self._hkl[key], self.rotation)
+
+    def flatten(self):
+        return self
+
+    def to_flat_polar(self):
+        """(r, theta) of the spots projected on the x, y plane
+        (diffsims/crystallography/_diffracting_vector.py:186-194)."""
+        r = np.linalg.norm(self.data[:, :2], axis=1)
+        return r, np.arctan2(self.data[:, 1], self.data[:, 0])
+
+    def __repr__(self):
+        name = getattr(self.phase, "name", "")
+        return f"DiffractingVector ({self.size},), {name}"
+
+
+class _PhaseCoordinates:
+    """Lazy sequence of one phase's patterns (CSR on the device)."""
+
+    def __init__(self, phase, spots, rotation):
+        self.phase = phase
+        self.spots = spots
+        self.rotation = rotation
+
+    def __len__(self):
+        return self.spots.n_orient
+
+    @property
+    def size(self):
+        return len(self)
+
+    def __getitem__(self, i):
+        if isinstance(i, slice):
+            return [self[k] for k in range(*i.indices(len(self)))]
+        n = len(self)
+        if i < 0:
+            i += n
+        if not 0 <= i < n:
+            raise IndexError(i)
+        off, hkl, xyz, inten = self.spots.host()
+        a, b = off[i], off[i + 1]
+        return DiffractingVector(self.phase, xyz[a:b], inten[a:b], hkl[a:b], self.rotation[i])
+
+    def __iter__(self):
+        for i in range(len(self)):
+            yield self[i]
+
+
+class Simulation2D:
+    """Result of ``SimulationGenerator.calculate_diffraction2d``.
+
+    ``phases``, ``rotations`` and ``coordinates`` nest as in the reference
+    (diffsims/generators/simulation_generator.py:244-258): one phase and one
+    rotation -> ``coordinates`` is a ``DiffractingVector``; one phase and N
+    rotations -> a sequence of N; P phases -> a list of P sequences.
+    """
+
+    def __init__(self, phases, rotations, phase_spots, simulation_generator, reciprocal_radius=1.0):
+        self._multi_phase = isinstance(phases, (list, tuple))
+        self.phases = phases
+        self.rotations = rotations
+        self.simulation_generator = simulation_generator
+        self.reciporical_radius = reciprocal_radius
+        self.reciprocal_radius = reciprocal_radius
+        self._spots = phase_spots  # list of PhaseSpots, one per phase
+        plist = phases if self._multi_phase else [phases]
+        rlist = rotations if self._multi_phase else [rotations]
+        self._coords = [_PhaseCoordinates(p, s, r) for p, s, r in zip(plist, phase_spots, rlist)]
+        self.phase_index = 0
+        self.rotation_index = 0
+
+    # --- nesting as in the reference
+    @property
+    def coordinates(self):
+        if self._multi_phase:
+            return [c for c in self._coords]
+        c = self._coords[0]
+        if self.rotations.size == 1:
+            return c[0]
+        return c
+
+    @property
+    def has_multiple_phases(self):
+        return self._multi_phase and len(self._coords) > 1
+
+    @property
+    def has_multiple_rotations(self):
+        if self._multi_phase:
+            return [r.size > 1 for r in self.rotations]
+        return self.rotations.size > 1
+
+    @property
+    def num_phases(self):
+        return len(self._coords) if self._multi_phase else 1
+
+    @property
+    def current_size(self):
+        return len(self._coords[self.phase_index])
+
+    def get_simulation(self, item):
+        """(rotation, phase index, DiffractingVector) of flat index ``item``."""
+        counts = np.cumsum([len(c) for c in self._coords])
+        ind = int(np.searchsorted(counts, item, side="right"))
+        start = 0 if ind == 0 else counts[ind - 1]
+        c = self._coords[ind]
+        return c.rotation[item - start], ind, c[item - start]
+
+    def get_current_coordinates(self):
+        return self._coords[self.phase_index][self.rotation_index]
+
+    def __iter__(self):
+        for c in self._coords:
+            for v in c:
+                yield v
+
+    def __len__(self):
+        return sum(len(c) for c in self._coords)
+
+    def spots(self, phase_index=0):
+        """Device CSR arrays of one phase (``PhaseSpots``)."""
+        return self._spots[phase_index]
+
+    def polar_flatten_simulations(self, radial_axes=None, azimuthal_axes=None):
+        """(r, theta, intensity) templates padded to the largest pattern
+        (diffsims/simulations/simulation2d.py:313-355)."""
+        vecs = list(self)
+        max_n = max([v.size for v in vecs]) if vecs else 0
+        r_t = np.zeros((len(vecs), max_n))
+        t_t = np.zeros((len(vecs), max_n))
+        i_t = np.zeros((len(vecs), max_n))
+        for i, v in enumerate(vecs):
+            r, t = v.to_flat_polar()
+            inten = v.intensity
+            if radial_axes is not None and azimuthal_axes is not None:
+                r = _get_closest(radial_axes, r)
+                t = _get_closest(azimuthal_axes, t)
+                mask = (r < len(radial_axes) - 1) & (t < len(azimuthal_axes) - 1)
+                r, t, inten = r[mask], t[mask], inten[mask]
+            r_t[i, :len(r)] = r
+            t_t[i, :len(r)] = t
+            i_t[i, :len(inten)] = inten
+        if radial_axes is not None and azimuthal_axes is not None:
+            r_t = np.array(r_t, dtype=int)
+            t_t = np.array(t_t, dtype=int)
+        return r_t, t_t, i_t
+
+    def __repr__(self):
+        return f"Simulation2D({self.num_phases} phase(s), {len(self)} pattern(s))"
+
+
+def _get_closest(array, values):
+    """Index of the closest entry of the sorted ``array`` for each value, the
+    upper one on ties (diffsims/simulations/simulation2d.py:767-781)."""
+    array = np.asarray(array)
+    idxs = np.searchsorted(array, values, side="left")
+    prev_closer = (idxs == len(array)) | (
+        np.fabs(values - array[np.maximum(idxs - 1, 0)]) < np.fabs(values - array[np.minimum(idxs, len(array) - 1)]))
+    idxs[prev_closer] -= 1
+    return idxs

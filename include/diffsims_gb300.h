@@ -1,0 +1,185 @@
+/*
+ * diffsims_gb300 -- C ABI of the GB300 (sm_103a) kinematical spot-pattern path.
+ *
+ * Every device buffer is owned by the caller (plain device pointers and
+ * sizes; no torch types).  Every compute call is asynchronous on the given
+ * CUDA stream; a host-side status (ds_status) reports argument and launch
+ * errors immediately, a device status word (int32, caller-owned) reports
+ * data-dependent conditions (output capacity, bounded-wait timeouts) once the
+ * stream is synchronised.  The library never allocates device memory: the
+ * callers size scratch with the *_scratch_bytes queries.
+ *
+ * The reference (diffsims 0.7.x) is pure Python; the entries below replace
+ * the numpy arithmetic behind its public calls.  Citations are paths inside
+ * that project.
+ */
+#ifndef DIFFSIMS_GB300_H
+#define DIFFSIMS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t ds_status;
+enum {
+    DS_OK = 0,
+    DS_ERR_INVALID_ARGUMENT = 1,
+    DS_ERR_CUDA = 2,
+    DS_ERR_CAPACITY = 4,      /* device word bit: output capacity exceeded   */
+    DS_ERR_TIMEOUT = 8,       /* device word bit: a bounded wait gave up     */
+    DS_ERR_UNSUPPORTED = 16,
+    DS_ERR_NONFINITE = 32     /* device word bit: non-finite input met       */
+};
+
+/* arithmetic form of a call */
+enum { DS_FORM_MIXED = 0, /* FP32 bulk, FP64 phase reduction + FP64 s near the cutoff */
+       DS_FORM_FP64 = 1   /* plain all-FP64 comparator                              */ };
+
+/* scattering factor parameterisation (diffsims/utils/sim_utils.py:139-162,227-253) */
+enum { DS_SCATTER_LOBATO = 0, DS_SCATTER_XTABLES = 1, DS_SCATTER_NONE = 2 };
+
+/* rel-rod shape models (diffsims/utils/shape_factor_models.py) */
+enum { DS_SHAPE_LINEAR = 0, DS_SHAPE_ATANC = 1, DS_SHAPE_SINC = 2, DS_SHAPE_SIN2C = 3,
+       DS_SHAPE_LORENTZIAN = 4, DS_SHAPE_BINARY = 5 };
+
+/* precession handling (diffsims/generators/simulation_generator.py:363-411) */
+enum { DS_PRECESSION_NONE = 0,
+       DS_PRECESSION_LORENTZIAN = 1, /* approximate_precession=True: lorentzian_precession */
+       DS_PRECESSION_INTEGRAL = 2    /* approximate_precession=False: rotation average     */ };
+
+/* ---------------------------------------------------------------- A1 ---- */
+/* Per-axis hkl box half-widths: first n with 1/|n e_i| <= min_dspacing.
+ * Replaces orix _get_highest_hkl as called at
+ * diffsims/crystallography/reciprocal_lattice_vector.py:1131-1133 (rule stated at
+ * diffsims/crystallography/get_hkl.py:49-57).  Host only.
+ * recip: rows a*, b*, c* (1/Angstrom, no 2 pi) in the x||a, z||c* frame. */
+ds_status ds_box_extent(const double recip[9], double min_dspacing, int32_t hmax_out[3]);
+
+/* Scratch bytes for ds_enumerate_hkl with this box. */
+size_t ds_enumerate_scratch_bytes(const int32_t hmax[3]);
+
+/* Ordered hkl set of ReciprocalLatticeVector.from_min_dspacing
+ * (diffsims/crystallography/reciprocal_lattice_vector.py:1131-1141): the box
+ * in descending (h,k,l) order without 000, kept where 1/|g| >= min_dspacing,
+ * followed by n_zero rows of 000 (from_min_dspacing's include_zero_vector and
+ * the second 000 of generators/simulation_generator.py:351-353).
+ * hkl_out: capacity x 3 int32; g2_out: capacity doubles (|g|^2); count_out:
+ * one int64 (device) = rows written.  capacity must be >= box size + n_zero. */
+ds_status ds_enumerate_hkl(const double recip[9], const int32_t hmax[3], double min_dspacing,
+                           int32_t n_zero, int32_t *hkl_out, double *g2_out, int64_t capacity,
+                           int64_t *count_out, void *scratch, size_t scratch_bytes,
+                           int32_t *status, void *stream);
+
+/* ---------------------------------------------------------------- A3 ---- */
+/* One atom of a phase: 48-byte record (a multiple of 16 so the atom table can
+ * be staged into shared memory with 1-D TMA bulk copies). */
+typedef struct {
+    double x, y, z;           /* fractional coordinates                        */
+    double occupancy;
+    double B;                 /* Debye-Waller B (Angstrom^2)                   */
+    int32_t species;          /* row of ds_atoms.coeffs                        */
+    int32_t _pad;
+} ds_atom;
+
+/* One phase's atoms (device arrays; both 16-byte aligned). */
+typedef struct {
+    int32_t n_atoms;
+    int32_t n_species;
+    const ds_atom *atoms;     /* n_atoms records                                 */
+    const double *coeffs;     /* n_species x 10: a1,b1,...,a5,b5 (zeros = unknown element) */
+    int32_t kind;             /* DS_SCATTER_*                                    */
+    int32_t _pad;
+} ds_atoms;
+
+size_t ds_structure_factor_scratch_bytes(int64_t n_hkl, int32_t n_atoms);
+
+/* Structure factors of n reflections: F = sum_j f_j occ_j exp(2 pi i h.x_j - B_j g^2/4)
+ * (diffsims/utils/sim_utils.py:256-304).  Exactly one of hkl_i (int32 n x 3) and
+ * hkl_d (double n x 3, non-integer indices allowed) is non-null.  g2: |g|^2 per
+ * reflection.  Outputs (any may be null): F2 (float |F|^2), F2d (double |F|^2),
+ * F (double re, im pairs).  form DS_FORM_MIXED: FP64 phase reduction frac(h.x),
+ * FP32 sincospi / scattering factors / Debye-Waller with compensated sums, and
+ * an FP64 re-evaluation of the reflections whose |F|^2 is small against
+ * sum_j |amplitude_j|^2; DS_FORM_FP64: all FP64. */
+ds_status ds_structure_factors(const ds_atoms *atoms, const int32_t *hkl_i, const double *hkl_d,
+                               const double *g2, int64_t n, int32_t form, float *F2, double *F2d,
+                               double *F, void *scratch, size_t scratch_bytes, int32_t *status,
+                               void *stream);
+
+/* get_kinematical_intensities (diffsims/utils/sim_utils.py:307-354):
+ * out[i] = prefactor[i] * |F_i|^2 with |g| given (not derived from the lattice).
+ * prefactor may be null (1).  Computed in FP64. */
+ds_status ds_kinematical_intensities(const ds_atoms *atoms, const double *hkl_d, const double *g_spacing,
+                                     const double *prefactor, int64_t n, double *out, void *scratch,
+                                     size_t scratch_bytes, int32_t *status, void *stream);
+
+/* ------------------------------------------------------------- A4-A7 ---- */
+typedef struct {
+    double k0;                   /* 1 / wavelength (1/Angstrom)                     */
+    double max_excitation_error; /* selection cut-off                               */
+    double shape_width;          /* shape_factor_width or max_excitation_error      */
+    double precession_angle;     /* radians (>= 0)                                  */
+    double minimum_intensity;    /* mask: keep I > max_pattern(I) * this            */
+    double minima_number;        /* sinc / sin2c / atanc parameter (default 5)      */
+    int32_t shape_model;         /* DS_SHAPE_*                                      */
+    int32_t precession_mode;     /* DS_PRECESSION_*                                 */
+    int32_t form;                /* DS_FORM_*                                       */
+    int32_t orient_tile;         /* orientations per CTA (0 = library choice)       */
+} ds_sim_params;
+
+/* One phase's candidate table (device arrays of n_hkl rows, in reference order). */
+typedef struct {
+    int64_t n_hkl;
+    const int32_t *hkl;          /* n_hkl x 3                                      */
+    const double *g2;            /* n_hkl |g|^2                                    */
+    const float *F2;             /* n_hkl |F|^2 (mixed form)                       */
+    const double *F2d;           /* n_hkl |F|^2 (FP64 form; may be null for mixed) */
+    double recip[9];             /* rows a*, b*, c*: g = hkl @ recip               */
+    int32_t hmax[3];             /* max |h|, |k|, |l| in the table                 */
+    int32_t _pad;
+} ds_phase_table;
+
+/* Output spots in CSR form (device arrays). */
+typedef struct {
+    int64_t *offsets;            /* n_orient + 1                                   */
+    int32_t *hkl_index;          /* capacity: row of the candidate table           */
+    float *xyzi;                 /* capacity x 4: beam-frame x, y, z, intensity    */
+    int64_t capacity;
+    int64_t *total;              /* one int64: spots of the call (may exceed capacity) */
+    double *excitation_error;    /* capacity, optional (null): s of every spot      */
+} ds_spots;
+
+size_t ds_simulate_scratch_bytes(const ds_sim_params *p, const ds_phase_table *t, int64_t n_orient);
+
+/* The per-orientation loop of SimulationGenerator.calculate_diffraction2d
+ * (diffsims/generators/simulation_generator.py:211-241) with
+ * get_intersecting_reflections (:319-412): rotate the table into the beam frame
+ * (R(q)^T g), excitation error, selection, shape factor, I = sf |F|^2, the
+ * minimum-intensity mask, ordered compaction into CSR.
+ * quats: n_orient x 4 doubles (w, x, y, z) -- active rotation of the crystal.
+ * On capacity overflow *total still gets the exact size, offsets are exact,
+ * rows beyond capacity are not written and DS_ERR_CAPACITY is or-ed into
+ * *status: re-run with capacity >= *total. */
+ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t, const double *quats,
+                      int64_t n_orient, ds_spots *out, void *scratch, size_t scratch_bytes,
+                      int32_t *status, void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* FP32 FMA throughput probe (no counterpart in the reference): blocks x 256
+ * threads, each 8 chains x 16 x iters fused multiply-adds; out holds
+ * blocks*256 floats.  FLOPs = blocks * 256 * iters * 256.  Used to measure the
+ * FP32 roofline denominator. */
+ds_status ds_probe_fp32_fma(int64_t iters, int32_t blocks, float *out, void *stream);
+
+/* Last host-side error message of the calling thread ("" if none). */
+const char *ds_last_error(void);
+/* Library version string. */
+const char *ds_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DIFFSIMS_GB300_H */

@@ -1,0 +1,125 @@
+"""CPU tests of the host side: the C-ABI library loads and exports every
+declared entry, the host-only box rule matches the oracle, the conventions
+of the drop-in types, and the reference's error behaviour."""
+import ctypes
+import pathlib
+import re
+
+import numpy as np
+import pytest
+
+from oracle import kinematic as ok
+
+ROOT = pathlib.Path(__file__).resolve().parents[1]
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from diffsims_gb300 import _build, _native
+    _build.build()
+    return _native.load_library(require_cuda=False)
+
+
+def declared_functions():
+    names = []
+    for h in (ROOT / "include").glob("*.h"):
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names += re.findall(r"\b(ds_[a-z0-9_]+)\s*\(", text)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = declared_functions()
+    assert "ds_simulate" in names and "ds_enumerate_hkl" in names
+    for name in names:
+        assert hasattr(lib, name), f"{name} declared in include/ but not exported"
+    from diffsims_gb300 import _native
+    assert set(_native.EXPORTED_SYMBOLS) <= set(names)
+    assert lib.ds_version().decode().startswith("diffsims_gb300")
+
+
+@pytest.mark.parametrize("lat, r", [
+    ((4.05, 4.05, 4.05, 90, 90, 90), 1.0),
+    ((4.04, 4.04, 4.04, 90, 90, 90), 1 / 0.7),
+    ((2.464, 2.464, 6.711, 90, 90, 120), 1.6768),
+    ((9.1, 11.3, 12.7, 81.0, 97.0, 104.0), 2.0),
+    ((7.1, 9.3, 12.4, 90, 90, 90), 1.5),
+    ((3.0, 20.0, 7.5, 85.0, 95.0, 100.0), 1.5),
+])
+def test_box_extent_matches_oracle(lib, lat, r):
+    from diffsims_gb300.engine import box_extent, reciprocal_basis
+    from diffsims_gb300.crystal import Lattice
+    recip = reciprocal_basis(Lattice(*lat))
+    np.testing.assert_allclose(recip, ok.reciprocal_base(ok.lattice_base(*lat)), rtol=0, atol=0)
+    np.testing.assert_array_equal(box_extent(recip, 1 / r), ok.highest_hkl(ok.reciprocal_base(ok.lattice_base(*lat)), 1 / r))
+
+
+def test_box_extent_rejects_bad_arguments(lib):
+    r = (ctypes.c_double * 9)(*([0.0] * 9))
+    out = (ctypes.c_int32 * 3)()
+    assert lib.ds_box_extent(r, -1.0, out) == 1
+    assert "min_dspacing" in lib.ds_last_error().decode()
+
+
+def test_euler_and_rotation_conventions():
+    import diffsims_gb300 as ds
+    e = np.array([[0, 90, 90], [10, 20, 30], [123, 45, 300]], dtype=float)
+    np.testing.assert_allclose(ds.Rotation.from_euler(e, degrees=True).data, ok.euler_to_quaternion(e, True),
+                               atol=1e-15)
+    q = ok.random_quaternions(5, seed=3)
+    np.testing.assert_allclose(ds.Rotation(q).to_matrix(), ok.quaternion_to_matrix(q), atol=1e-15)
+    np.testing.assert_allclose(ds.Rotation.random(7, seed=0).data, ok.random_quaternions(7, seed=0))
+
+
+def test_wavelength_matches_oracle():
+    import diffsims_gb300 as ds
+    for kv in (100, 200, 300, 80.5):
+        assert ds.get_electron_wavelength(kv) == ok.electron_wavelength(kv)
+    assert ds.get_electron_wavelength("inf") == 0
+
+
+def test_generator_errors_and_repr():
+    # diffsims/tests/generators/test_simulation_generator.py:122-135,268-280
+    import diffsims_gb300 as ds
+    g = ds.SimulationGenerator(300)
+    assert repr(g) == "SimulationGenerator(accelerating_voltage=300, scattering_params=lobato, approximate_precession=True)"
+    assert g.scattering_params == "lobato" and g.precession_angle == 0 and g.minimum_intensity == 1e-20
+    with pytest.raises(NotImplementedError):
+        ds.SimulationGenerator(300, scattering_params="_empty")
+    with pytest.raises(NotImplementedError):
+        ds.SimulationGenerator(300, shape_factor_model="dracula")
+    for sp in ("lobato", "xtables", None):
+        ds.SimulationGenerator(300, scattering_params=sp)
+
+
+def test_settings_mapping():
+    import diffsims_gb300 as ds
+    from diffsims_gb300 import _native as N
+    s = ds.SimulationGenerator(200, precession_angle=-0.5).settings(0.02)
+    assert s.precession_mode == N.DS_PRECESSION_LORENTZIAN and np.isclose(s.precession_angle_rad, np.deg2rad(0.5))
+    s = ds.SimulationGenerator(200, precession_angle=1, approximate_precession=False).settings(0.02, 0.03)
+    assert s.precession_mode == N.DS_PRECESSION_INTEGRAL and s.shape_width == 0.03
+    s = ds.SimulationGenerator(300, shape_factor_model="sinc", minima_number=3).settings()
+    assert s.shape_model == "sinc" and s.minima_number == 3 and np.isclose(s.k0, 1 / ok.electron_wavelength(300))
+
+
+def test_packed_atoms_layout():
+    from diffsims_gb300 import _native as N
+    assert ctypes.sizeof(N.ds_atom) == 48
+    assert ctypes.sizeof(N.ds_sim_params) == 6 * 8 + 4 * 4
+    assert N.ds_phase_table.recip.offset % 8 == 0
+
+
+def test_debye_waller_rules():
+    from diffsims_gb300.sim_utils import debye_waller_per_atom
+    np.testing.assert_array_equal(debye_waller_per_atom(["Al", "Fe2+", "O"], {"Al": 0.5, "Fe": 0.3}), [0.5, 0.3, 0])
+    np.testing.assert_array_equal(debye_waller_per_atom(["Al", "O"], [0.1, 0.2]), [0.1, 0.2])
+    with pytest.raises(ValueError):
+        debye_waller_per_atom(["Al", "O"], [0.1])
+
+
+def test_get_closest_matches_reference_rule():
+    from diffsims_gb300.simulation2d import _get_closest
+    a = np.array([0.0, 1.0, 2.0, 3.0])
+    np.testing.assert_array_equal(_get_closest(a, np.array([-1, 0.4, 0.5, 0.6, 2.9, 7.0])), [0, 0, 1, 1, 3, 3])
