@@ -219,6 +219,10 @@ def run_gpu(args):
             kern_ms.append(e0.elapsed_time(e1))
     clocks = clk.summary()
     ms = statistics.mean(step_ms)
+    if args.device_only:
+        print(json.dumps({"device_only": True, "ms_per_step": ms, "kernel_ms": statistics.mean(kern_ms),
+                          "patterns_per_s": n_o / (ms * 1e-3), "n_hkl": table.n, "spots": spots.total}))
+        return
     value = n_o / (ms * 1e-3)
     total_spots = spots.total
     n_h = table.n
@@ -381,6 +385,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=1024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--out-dir", default=None)
+    ap.add_argument("--device-only", action="store_true",
+                    help="time only the device-resident step (for profiling); no e2e, FP64 form or CPU legs")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

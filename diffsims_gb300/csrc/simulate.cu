@@ -55,6 +55,10 @@ struct __align__(16) OrientP {
     double M[3][3];  // FP64 copy
 };
 
+// per-orientation accumulators in shared memory (ACC_WORDS words each):
+// max I, min positive I, count, offset, then one count per warp part
+enum { ACC_MAXI = 0, ACC_MINPOS = 1, ACC_CNT = 2, ACC_OFF = 3, ACC_PART0 = 4, ACC_WORDS = 12 };
+
 struct SimSmem {
     size_t orient, bitmap, acc, total;
 };
@@ -62,15 +66,13 @@ __host__ __device__ inline SimSmem sim_smem_layout(int O, int Ws) {
     SimSmem L;
     size_t o = 0;
     L.orient = o; o += (size_t)O * sizeof(OrientP);
-    L.acc = o; o += (size_t)O * 8 * sizeof(unsigned long long) + 64;
+    L.acc = o; o += (size_t)O * ACC_WORDS * sizeof(unsigned long long) + 64;
     o = (o + 15) & ~(size_t)15;
     L.bitmap = o; o += (size_t)O * Ws * sizeof(uint32_t);
     L.total = o;
     return L;
 }
 
-// per-orientation accumulators in shared memory (8 words each)
-enum { ACC_MAXI = 0, ACC_MINPOS = 1, ACC_CNT = 2, ACC_OFF = 3, ACC_PART0 = 4 };  // PART0..PART0+3: part counts
 
 // ------------------------------------------------------------------ prep ----
 // Per row: (h, k, l, -z_mid) and z_half of the z-interval that holds every
@@ -334,8 +336,8 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0) s_tile = (long long)atomicAdd(lb.ticket, 1ull);
-    for (int i = tid; i < O * 8; i += SIM_THREADS)
-        acc[i] = (i % 8 == ACC_MINPOS) ? (unsigned long long)__float_as_uint(INFINITY) : 0ull;
+    for (int i = tid; i < O * ACC_WORDS; i += SIM_THREADS)
+        acc[i] = (i % ACC_WORDS == ACC_MINPOS) ? (unsigned long long)__float_as_uint(INFINITY) : 0ull;
     __syncthreads();
     const long long tile = s_tile;
     const long long o_base = tile * O;
@@ -437,16 +439,16 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
         if (!(lmax > 0.f)) lmax = 0.f;  // no -0.0 or NaN in the bit-ordered max
         if (lane == 0) {
             // intensities are >= 0, so float bit patterns order like the values
-            atomicMax(&acc[o * 8 + ACC_MAXI], (unsigned long long)__float_as_uint(lmax));
-            atomicMin(&acc[o * 8 + ACC_MINPOS], (unsigned long long)__float_as_uint(lminpos));
+            atomicMax(&acc[o * ACC_WORDS + ACC_MAXI], (unsigned long long)__float_as_uint(lmax));
+            atomicMin(&acc[o * ACC_WORDS + ACC_MINPOS], (unsigned long long)__float_as_uint(lminpos));
         }
     }
     __syncthreads();
 
     // ---------------- mask pass (only where some I is positive but below max * thr)
     for (int o = warp / WPO; o < n_valid; o += SIM_WARPS / WPO) {
-        float mx = __uint_as_float((unsigned)acc[o * 8 + ACC_MAXI]);
-        float mnp = __uint_as_float((unsigned)acc[o * 8 + ACC_MINPOS]);
+        float mx = __uint_as_float((unsigned)acc[o * ACC_WORDS + ACC_MAXI]);
+        float mnp = __uint_as_float((unsigned)acc[o * ACC_WORDS + ACC_MINPOS]);
         if (!(c.thr > 0.0)) continue;
         float cut = (float)((double)mx * c.thr);
         if (!(mnp <= cut)) continue;
@@ -469,16 +471,16 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
         for (int wi = w0 + lane; wi < w1; wi += 32) cnt += __popc(row[wi]);
 #pragma unroll
         for (int d = 16; d >= 1; d >>= 1) cnt += __shfl_xor_sync(FULL_MASK, cnt, d);
-        if (lane == 0) acc[o * 8 + ACC_PART0 + part] = (unsigned long long)cnt;
+        if (lane == 0) acc[o * ACC_WORDS + ACC_PART0 + part] = (unsigned long long)cnt;
     }
     __syncthreads();
     if (tid == 0) {
         long long run = 0;
         for (int o = 0; o < n_valid; ++o) {
-            acc[o * 8 + ACC_OFF] = (unsigned long long)run;
+            acc[o * ACC_WORDS + ACC_OFF] = (unsigned long long)run;
             long long co = 0;
-            for (int p = 0; p < WPO; ++p) co += (long long)acc[o * 8 + ACC_PART0 + p];
-            acc[o * 8 + ACC_CNT] = (unsigned long long)co;
+            for (int p = 0; p < WPO; ++p) co += (long long)acc[o * ACC_WORDS + ACC_PART0 + p];
+            acc[o * ACC_WORDS + ACC_CNT] = (unsigned long long)co;
             run += co;
         }
         long long prefix = lookback_exclusive(lb, tile, run, status);
@@ -491,14 +493,14 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
     __syncthreads();
     const long long prefix = s_prefix;
     if (prefix < 0) return;
-    for (int o = tid; o < n_valid; o += SIM_THREADS) offsets[o_base + o] = prefix + (long long)acc[o * 8 + ACC_OFF];
+    for (int o = tid; o < n_valid; o += SIM_THREADS) offsets[o_base + o] = prefix + (long long)acc[o * ACC_WORDS + ACC_OFF];
 
     // ---------------- phase 3b: ordered writes
     for (int o = warp / WPO; o < n_valid; o += SIM_WARPS / WPO) {
         const uint32_t *row = bitmap + o * c.Ws;
         const OrientP &op = sop[o];
-        long long pos0 = prefix + (long long)acc[o * 8 + ACC_OFF];
-        for (int p = 0; p < part; ++p) pos0 += (long long)acc[o * 8 + ACC_PART0 + p];
+        long long pos0 = prefix + (long long)acc[o * ACC_WORDS + ACC_OFF];
+        for (int p = 0; p < part; ++p) pos0 += (long long)acc[o * ACC_WORDS + ACC_PART0 + p];
         bool overflow = false;
         for_each_bit(row, w0, w1, lane, [&](long long j, int rank, bool valid, int, int) {
             if (!valid) return;
@@ -544,7 +546,7 @@ static int pick_O(const ds_sim_params *p, long long n_hkl, long long n_orient) {
     if (p->orient_tile > 0) return p->orient_tile < o_cap ? p->orient_tile : o_cap;
     int O = o_cap;
     const long long budget = 100 * 1024;  // two CTAs per SM
-    while (O > 4 && (long long)O * Ws * 4 + O * (long long)sizeof(OrientP) > budget) O >>= 1;
+    while (O > 1 && (long long)O * Ws * 4 + O * (long long)sizeof(OrientP) > budget) O >>= 1;
     // keep at least ~2 tiles per SM when the orientation count allows it
     while (O > 4 && (n_orient + O - 1) / O < 304) O >>= 1;
     return O;
@@ -604,8 +606,9 @@ extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t
     DS_REQUIRE(p->precession_mode >= DS_PRECESSION_NONE && p->precession_mode <= DS_PRECESSION_INTEGRAL,
                "ds_simulate: bad precession mode");
     DS_REQUIRE(p->form == DS_FORM_MIXED || p->form == DS_FORM_FP64, "ds_simulate: bad form");
-    DS_REQUIRE(p->orient_tile == 0 || p->orient_tile == 4 || p->orient_tile == 8 || p->orient_tile == 16 ||
-                   p->orient_tile == 32, "ds_simulate: orient_tile must be 0, 4, 8, 16 or 32");
+    DS_REQUIRE(p->orient_tile == 0 || p->orient_tile == 1 || p->orient_tile == 2 || p->orient_tile == 4 ||
+                   p->orient_tile == 8 || p->orient_tile == 16 || p->orient_tile == 32,
+               "ds_simulate: orient_tile must be 0, 1, 2, 4, 8, 16 or 32");
     DS_REQUIRE(p->precession_mode == DS_PRECESSION_NONE || p->precession_angle > 0,
                "ds_simulate: precession mode needs a positive angle");
     if (p->precession_mode == DS_PRECESSION_INTEGRAL) {
@@ -689,12 +692,16 @@ extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t
     LookbackScratch lb = lookback_scratch(sb + P.off_lb);
     if (p->form == DS_FORM_FP64) {
         switch (P.O) {
+            case 1: return launch_sim<1, DS_FORM_FP64>(c, T, quats, out, lb, P.smem, status, s);
+            case 2: return launch_sim<2, DS_FORM_FP64>(c, T, quats, out, lb, P.smem, status, s);
             case 4: return launch_sim<4, DS_FORM_FP64>(c, T, quats, out, lb, P.smem, status, s);
             case 8: return launch_sim<8, DS_FORM_FP64>(c, T, quats, out, lb, P.smem, status, s);
             default: return launch_sim<16, DS_FORM_FP64>(c, T, quats, out, lb, P.smem, status, s);
         }
     }
     switch (P.O) {
+        case 1: return launch_sim<1, DS_FORM_MIXED>(c, T, quats, out, lb, P.smem, status, s);
+        case 2: return launch_sim<2, DS_FORM_MIXED>(c, T, quats, out, lb, P.smem, status, s);
         case 4: return launch_sim<4, DS_FORM_MIXED>(c, T, quats, out, lb, P.smem, status, s);
         case 8: return launch_sim<8, DS_FORM_MIXED>(c, T, quats, out, lb, P.smem, status, s);
         case 16: return launch_sim<16, DS_FORM_MIXED>(c, T, quats, out, lb, P.smem, status, s);

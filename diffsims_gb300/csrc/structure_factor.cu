@@ -64,23 +64,7 @@ __device__ __forceinline__ void load_hkl(const SfConst &c, const int32_t *hkl_i,
     }
 }
 
-// f_s(g^2) for FP32 (mixed) -- same formulas as sim_utils.py:249-253
-__device__ __forceinline__ float scatter_f32(const float *cf, int kind, float g2) {
-    if (kind == DS_SCATTER_NONE) return 1.f;
-    float f = 0.f;
-#pragma unroll
-    for (int i = 0; i < 5; ++i) {
-        float a = cf[2 * i], b = cf[2 * i + 1];
-        float gb = g2 * b;
-        if (kind == DS_SCATTER_LOBATO) {
-            float d = 1.f + gb;
-            f = fmaf(a, (2.f + gb) / (d * d), f);
-        } else {
-            f = fmaf(a, expf(-0.25f * gb), f);
-        }
-    }
-    return f;
-}
+// f_s(g^2) -- the formulas of diffsims/utils/sim_utils.py:249-253
 __device__ __forceinline__ double scatter_f64(const double *cf, int kind, double g2) {
     if (kind == DS_SCATTER_NONE) return 1.0;
     double f = 0.0;
@@ -142,7 +126,6 @@ sf_mixed_kernel(SfConst c, ds_atoms A, const int32_t *__restrict__ hkl_i, const 
     const int chunk_cap = c.n_atoms < SF_ATOM_CHUNK ? c.n_atoms : SF_ATOM_CHUNK;
     const SfSmem Ls = sf_smem_layout(c.n_species, chunk_cap);
     sf_prologue(c, A, smem, Ls);
-    const float *cf = reinterpret_cast<const float *>(smem + Ls.coeff_f);
     const ds_atom *sa = reinterpret_cast<const ds_atom *>(smem + Ls.atoms);
     const float *occf = reinterpret_cast<const float *>(smem + Ls.occf);
     const float *bqf = reinterpret_cast<const float *>(smem + Ls.bqf);
@@ -158,7 +141,12 @@ sf_mixed_kernel(SfConst c, ds_atoms A, const int32_t *__restrict__ hkl_i, const 
         if (c.g_is_spacing) g2 = g2 * g2;
     }
     const float g2f = (float)g2;
-    for (int s = 0; s < c.n_species; ++s) fs[s * SF_THREADS + threadIdx.x] = scatter_f32(cf + 10 * s, c.kind, g2f);
+    // f_s(g) in FP64: the Lobato fits sum terms of mixed sign and size, whose
+    // cancellation costs FP32 up to ~1e-4 relative; one evaluation per
+    // (reflection, species) is cheap next to the per-atom phase work.
+    const double *cd = reinterpret_cast<const double *>(smem + Ls.coeff_d);
+    for (int s = 0; s < c.n_species; ++s)
+        fs[s * SF_THREADS + threadIdx.x] = (float)scatter_f64(cd + 10 * s, c.kind, g2);
 
     dd re = {0.f, 0.f}, im = {0.f, 0.f};
     float sumsq = 0.f;

@@ -156,27 +156,35 @@ class PhaseSpots:
         return self.offsets.shape[0] - 1
 
     def host(self, pinned=False):
-        """numpy copies (offsets, hkl (total, 3) int, xyz (total, 3) float64,
-        intensity float64); with ``pinned`` the device arrays go through
-        page-locked buffers."""
+        """Host copies (offsets int64, hkl (total, 3) int32, xyz (total, 3)
+        float32, intensity float32).  With ``pinned`` the device arrays land in
+        page-locked staging buffers reused across calls."""
         if self._host is None:
-            def fetch(t):
-                if pinned:
-                    h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
-                    h.copy_(t, non_blocking=True)
-                    return h
-                return t.cpu()
-            off, idx, xyzi = fetch(self.offsets), fetch(self.hkl_index), fetch(self.xyzi)
+            if pinned:
+                off, idx, xyzi = _fetch_pinned((self.offsets, self.hkl_index, self.xyzi))
+            else:
+                off, idx, xyzi = self.offsets.cpu(), self.hkl_index.cpu(), self.xyzi.cpu()
             torch.cuda.current_stream().synchronize()
             table_hkl = self.table.hkl_host()
             idx = idx.numpy()
             hkl = table_hkl[idx] if self.total else np.zeros((0, 3), np.int32)
-            xyzi = xyzi.numpy().astype(np.float64)
+            xyzi = xyzi.numpy()
             self._host = (off.numpy(), hkl, xyzi[:, :3], xyzi[:, 3])
         return self._host
 
     def nbytes(self):
         return self.offsets.numel() * 8 + self.total * (4 + 16)
+
+
+def _fetch_pinned(tensors):
+    """Device -> page-locked host copies (torch's caching host allocator
+    reuses freed pinned blocks, so repeated calls do not pay for pinning)."""
+    out = []
+    for t in tensors:
+        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+        h.copy_(t, non_blocking=True)
+        out.append(h)
+    return out
 
 
 class SpotBuffers:

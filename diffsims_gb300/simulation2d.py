@@ -117,7 +117,8 @@ class _PhaseCoordinates:
             raise IndexError(i)
         off, hkl, xyz, inten = self.spots.host()
         a, b = off[i], off[i + 1]
-        return DiffractingVector(self.phase, xyz[a:b], inten[a:b], hkl[a:b], self.rotation[i])
+        return DiffractingVector(self.phase, xyz[a:b].astype(np.float64), inten[a:b].astype(np.float64), hkl[a:b],
+                                 self.rotation[i])
 
     def __iter__(self):
         for i in range(len(self)):
