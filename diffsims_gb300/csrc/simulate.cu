@@ -55,9 +55,11 @@ struct __align__(16) OrientP {
     double M[3][3];  // FP64 copy
 };
 
-// per-orientation accumulators in shared memory (ACC_WORDS words each):
-// max I, min positive I, count, offset, then one count per warp part
-enum { ACC_MAXI = 0, ACC_MINPOS = 1, ACC_CNT = 2, ACC_OFF = 3, ACC_PART0 = 4, ACC_WORDS = 12 };
+// per-orientation accumulators in shared memory (ACC_WORDS words each): max I,
+// min positive I, count, output offset, then per warp part (up to 8 parts):
+// kept count, staging base, candidate count
+enum { ACC_MAXI = 0, ACC_MINPOS = 1, ACC_CNT = 2, ACC_OFF = 3, ACC_PART0 = 4, ACC_CBASE0 = 12, ACC_CCNT0 = 20,
+       ACC_WORDS = 28 };
 
 struct SimSmem {
     size_t orient, bitmap, acc, total;
@@ -322,11 +324,23 @@ __device__ __forceinline__ void for_each_bit(const uint32_t *row, int w0, int w1
     }
 }
 
+// Per-CTA staging in global scratch (L2-resident): the screened candidate
+// rows of the tile in (orientation, row) order and their intensities, so the
+// refine pass evaluates full warps of candidates once and the write pass
+// only gathers.  Orientation parts that do not fit fall back to walking the
+// bitmap and re-evaluating.
+struct StageP {
+    int32_t *idx;
+    float *inten;
+    long long cap;  // entries per CTA
+};
+constexpr unsigned long long NO_STAGE = ~0ull;
+
 template <int O, int FORM>
 __global__ void __launch_bounds__(SIM_THREADS, 2)
 simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t *__restrict__ offsets,
                 int32_t *__restrict__ out_idx, float4 *__restrict__ out_xyzi, double *__restrict__ out_s,
-                int64_t *__restrict__ out_total, LookbackScratch lb, int32_t *status) {
+                int64_t *__restrict__ out_total, LookbackScratch lb, StageP stg, int32_t *status) {
     extern __shared__ __align__(16) unsigned char smem[];
     const SimSmem Ls = sim_smem_layout(O, c.Ws);
     OrientP *sop = reinterpret_cast<OrientP *>(smem + Ls.orient);
@@ -335,207 +349,328 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
     __shared__ long long s_tile, s_prefix;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) s_tile = (long long)atomicAdd(lb.ticket, 1ull);
-    for (int i = tid; i < O * ACC_WORDS; i += SIM_THREADS)
-        acc[i] = (i % ACC_WORDS == ACC_MINPOS) ? (unsigned long long)__float_as_uint(INFINITY) : 0ull;
-    __syncthreads();
-    const long long tile = s_tile;
-    const long long o_base = tile * O;
-    const int n_valid = (int)min((long long)O, c.n_orient - o_base);
-
-    // per-orientation rotation: beam frame = g @ R, R the active matrix of q
-    if (tid < O) {
-        OrientP &op = sop[tid];
-        double R[3][3];
-        if (tid < n_valid) {
-            const double *q = quats + 4 * (o_base + tid);
-            double w = q[0], x = q[1], y = q[2], z = q[3];
-            double nrm = sqrt(w * w + x * x + y * y + z * z);
-            if (!(nrm > 0) || !isfinite(nrm)) { atomicOr(status, DS_ERR_NONFINITE); nrm = 1; w = 1; x = y = z = 0; }
-            w /= nrm; x /= nrm; y /= nrm; z /= nrm;
-            R[0][0] = 1 - 2 * (y * y + z * z); R[0][1] = 2 * (x * y - w * z); R[0][2] = 2 * (x * z + w * y);
-            R[1][0] = 2 * (x * y + w * z); R[1][1] = 1 - 2 * (x * x + z * z); R[1][2] = 2 * (y * z - w * x);
-            R[2][0] = 2 * (x * z - w * y); R[2][1] = 2 * (y * z + w * x); R[2][2] = 1 - 2 * (x * x + y * y);
-        } else {
-            for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) R[a][b] = 0.0;
-        }
-        for (int cc = 0; cc < 3; ++cc)
-            for (int i = 0; i < 3; ++i) {
-                double v = c.recip[3 * i + 0] * R[0][cc] + c.recip[3 * i + 1] * R[1][cc] + c.recip[3 * i + 2] * R[2][cc];
-                op.M[cc][i] = v;
-                float hi, lo;
-                split_double(v, hi, lo);
-                op.m[cc][i] = hi;
-                if (cc == 2) op.mzlo[i] = lo;
-            }
-    }
-    __syncthreads();
-
-    // ---------------- phase 1: screen every row against all O orientations
-    {
-        float m0[O], m1[O], m2[O];
-#pragma unroll
-        for (int o = 0; o < O; ++o) { m0[o] = sop[o].m[2][0]; m1[o] = sop[o].m[2][1]; m2[o] = sop[o].m[2][2]; }
-        for (int wc = warp; wc < c.W; wc += SIM_WARPS) {
-            long long j = (long long)wc * 32 + lane;
-            float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
-            float zh = -1.f;
-            if (j < c.n_hkl) { e = T.scr[j]; zh = T.zh[j]; }
-            uint32_t myword = 0;
-            if (FORM == DS_FORM_FP64) {
-                double hd = e.x, kd = e.y, ld = e.z;
-#pragma unroll 1
-                for (int o = 0; o < O; ++o) {
-                    double s, r, z;
-                    bool hit = (j < c.n_hkl) && (o < n_valid) && select_fp64(c, sop[o], hd, kd, ld, s, r, z);
-                    uint32_t b = __ballot_sync(FULL_MASK, hit);
-                    if (lane == o) myword = b;
-                }
-            } else {
-#pragma unroll
-                for (int o = 0; o < O; ++o) {
-                    float z = fmaf(m0[o], e.x, fmaf(m1[o], e.y, fmaf(m2[o], e.z, e.w)));
-                    uint32_t b = __ballot_sync(FULL_MASK, fabsf(z) < zh);
-                    if (lane == o) myword = b;
-                }
-            }
-            if (lane < O) bitmap[lane * c.Ws + wc] = myword;
-        }
-    }
-    __syncthreads();
-
-    // work split for phases 2-3: warps_per_o warps share one orientation's words
+    int32_t *my_idx = stg.idx + (long long)blockIdx.x * stg.cap;
+    float *my_I = stg.inten + (long long)blockIdx.x * stg.cap;
+    // work split for phases 2-3: WPO warps share one orientation's words
     constexpr int WPO = O >= SIM_WARPS ? 1 : SIM_WARPS / O;
     const int part = warp % WPO;
     const int w0 = (int)(((long long)c.W * part) / WPO), w1 = (int)(((long long)c.W * (part + 1)) / WPO);
     const bool all_zero_drop = c.thr >= 0.0;
+    const unsigned lanemask_lt = (1u << lane) - 1u;
 
-    // ---------------- phase 2: refine, intensities, per-orientation max
-    for (int o = warp / WPO; o < n_valid; o += SIM_WARPS / WPO) {
-        uint32_t *row = bitmap + o * c.Ws;
-        const OrientP &op = sop[o];
-        float lmax = 0.f, lminpos = INFINITY;
-        int lcnt = 0;
-        for_each_bit(row, w0, w1, lane, [&](long long j, int, bool valid, int wi, int bit) {
-            if (!valid) return;
-            float I, z;
-            double sv;
-            bool sel = eval_spot<FORM>(c, op, T, j, I, z, sv);
-            if (sel && I == 0.f && all_zero_drop) sel = false;
-            if (!sel) {
-                atomicAnd(&row[wi], ~(1u << bit));
-                return;
-            }
-            ++lcnt;
-            lmax = fmaxf(lmax, I);
-            if (I > 0.f) lminpos = fminf(lminpos, I);
-        });
-#pragma unroll
-        for (int d = 16; d >= 1; d >>= 1) {
-            lmax = fmaxf(lmax, __shfl_xor_sync(FULL_MASK, lmax, d));
-            lminpos = fminf(lminpos, __shfl_xor_sync(FULL_MASK, lminpos, d));
-            lcnt += __shfl_xor_sync(FULL_MASK, lcnt, d);
-        }
-        if (!(lmax > 0.f)) lmax = 0.f;  // no -0.0 or NaN in the bit-ordered max
-        if (lane == 0) {
-            // intensities are >= 0, so float bit patterns order like the values
-            atomicMax(&acc[o * ACC_WORDS + ACC_MAXI], (unsigned long long)__float_as_uint(lmax));
-            atomicMin(&acc[o * ACC_WORDS + ACC_MINPOS], (unsigned long long)__float_as_uint(lminpos));
-        }
-    }
-    __syncthreads();
+    for (;;) {  // persistent: one tile of O orientations per ticket
+        if (tid == 0) s_tile = (long long)atomicAdd(lb.ticket, 1ull);
+        for (int i = tid; i < O * ACC_WORDS; i += SIM_THREADS)
+            acc[i] = (i % ACC_WORDS == ACC_MINPOS) ? (unsigned long long)__float_as_uint(INFINITY) : 0ull;
+        __syncthreads();
+        const long long tile = s_tile;
+        if (tile >= c.n_tiles) break;
+        const long long o_base = tile * O;
+        const int n_valid = (int)min((long long)O, c.n_orient - o_base);
 
-    // ---------------- mask pass (only where some I is positive but below max * thr)
-    for (int o = warp / WPO; o < n_valid; o += SIM_WARPS / WPO) {
-        float mx = __uint_as_float((unsigned)acc[o * ACC_WORDS + ACC_MAXI]);
-        float mnp = __uint_as_float((unsigned)acc[o * ACC_WORDS + ACC_MINPOS]);
-        if (!(c.thr > 0.0)) continue;
-        float cut = (float)((double)mx * c.thr);
-        if (!(mnp <= cut)) continue;
-        uint32_t *row = bitmap + o * c.Ws;
-        const OrientP &op = sop[o];
-        for_each_bit(row, w0, w1, lane, [&](long long j, int, bool valid, int wi, int bit) {
-            if (!valid) return;
-            float I, z;
-            double sv;
-            eval_spot<FORM>(c, op, T, j, I, z, sv);
-            if (!((double)I > (double)mx * c.thr)) atomicAnd(&row[wi], ~(1u << bit));
-        });
-    }
-    __syncthreads();
-
-    // ---------------- phase 3a: counts, offsets, look-back
-    for (int o = warp / WPO; o < n_valid; o += SIM_WARPS / WPO) {
-        const uint32_t *row = bitmap + o * c.Ws;
-        int cnt = 0;
-        for (int wi = w0 + lane; wi < w1; wi += 32) cnt += __popc(row[wi]);
-#pragma unroll
-        for (int d = 16; d >= 1; d >>= 1) cnt += __shfl_xor_sync(FULL_MASK, cnt, d);
-        if (lane == 0) acc[o * ACC_WORDS + ACC_PART0 + part] = (unsigned long long)cnt;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        long long run = 0;
-        for (int o = 0; o < n_valid; ++o) {
-            acc[o * ACC_WORDS + ACC_OFF] = (unsigned long long)run;
-            long long co = 0;
-            for (int p = 0; p < WPO; ++p) co += (long long)acc[o * ACC_WORDS + ACC_PART0 + p];
-            acc[o * ACC_WORDS + ACC_CNT] = (unsigned long long)co;
-            run += co;
-        }
-        long long prefix = lookback_exclusive(lb, tile, run, status);
-        s_prefix = prefix;
-        if (prefix >= 0 && tile == c.n_tiles - 1) {
-            offsets[c.n_orient] = prefix + run;
-            *out_total = prefix + run;
-        }
-    }
-    __syncthreads();
-    const long long prefix = s_prefix;
-    if (prefix < 0) return;
-    for (int o = tid; o < n_valid; o += SIM_THREADS) offsets[o_base + o] = prefix + (long long)acc[o * ACC_WORDS + ACC_OFF];
-
-    // ---------------- phase 3b: ordered writes
-    for (int o = warp / WPO; o < n_valid; o += SIM_WARPS / WPO) {
-        const uint32_t *row = bitmap + o * c.Ws;
-        const OrientP &op = sop[o];
-        long long pos0 = prefix + (long long)acc[o * ACC_WORDS + ACC_OFF];
-        for (int p = 0; p < part; ++p) pos0 += (long long)acc[o * ACC_WORDS + ACC_PART0 + p];
-        bool overflow = false;
-        for_each_bit(row, w0, w1, lane, [&](long long j, int rank, bool valid, int, int) {
-            if (!valid) return;
-            float I, z;
-            double sv;
-            eval_spot<FORM>(c, op, T, j, I, z, sv);
-            const float4 e = T.scr[j];
-            float x, y;
-            if (FORM == DS_FORM_FP64) {
-                x = (float)(op.M[0][0] * (double)e.x + op.M[0][1] * (double)e.y + op.M[0][2] * (double)e.z);
-                y = (float)(op.M[1][0] * (double)e.x + op.M[1][1] * (double)e.y + op.M[1][2] * (double)e.z);
+        // per-orientation rotation: beam frame = g @ R, R the active matrix of q
+        if (tid < O) {
+            OrientP &op = sop[tid];
+            double R[3][3];
+            if (tid < n_valid) {
+                const double *q = quats + 4 * (o_base + tid);
+                double w = q[0], x = q[1], y = q[2], z = q[3];
+                double nrm = sqrt(w * w + x * x + y * y + z * z);
+                if (!(nrm > 0) || !isfinite(nrm)) { atomicOr(status, DS_ERR_NONFINITE); nrm = 1; w = 1; x = y = z = 0; }
+                w /= nrm; x /= nrm; y /= nrm; z /= nrm;
+                R[0][0] = 1 - 2 * (y * y + z * z); R[0][1] = 2 * (x * y - w * z); R[0][2] = 2 * (x * z + w * y);
+                R[1][0] = 2 * (x * y + w * z); R[1][1] = 1 - 2 * (x * x + z * z); R[1][2] = 2 * (y * z - w * x);
+                R[2][0] = 2 * (x * z - w * y); R[2][1] = 2 * (y * z + w * x); R[2][2] = 1 - 2 * (x * x + y * y);
             } else {
-                x = fmaf(op.m[0][0], e.x, fmaf(op.m[0][1], e.y, op.m[0][2] * e.z));
-                y = fmaf(op.m[1][0], e.x, fmaf(op.m[1][1], e.y, op.m[1][2] * e.z));
+                for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) R[a][b] = 0.0;
             }
-            long long pos = pos0 + rank;
-            if (pos < c.capacity) {
-                out_idx[pos] = (int32_t)j;
-                out_xyzi[pos] = make_float4(x, y, z, I);
-                if (out_s) out_s[pos] = sv;
+            for (int cc = 0; cc < 3; ++cc)
+                for (int i = 0; i < 3; ++i) {
+                    double v = c.recip[3 * i + 0] * R[0][cc] + c.recip[3 * i + 1] * R[1][cc] + c.recip[3 * i + 2] * R[2][cc];
+                    op.M[cc][i] = v;
+                    float hi, lo;
+                    split_double(v, hi, lo);
+                    op.m[cc][i] = hi;
+                    if (cc == 2) op.mzlo[i] = lo;
+                }
+        }
+        __syncthreads();
+
+        // ---------------- phase 1: screen every row against all O orientations
+        {
+            float m0[O], m1[O], m2[O];
+#pragma unroll
+            for (int o = 0; o < O; ++o) { m0[o] = sop[o].m[2][0]; m1[o] = sop[o].m[2][1]; m2[o] = sop[o].m[2][2]; }
+            float4 en = make_float4(0.f, 0.f, 0.f, 0.f);
+            float zn = -1.f;
+            {
+                long long j = (long long)warp * 32 + lane;
+                if (warp < c.W && j < c.n_hkl) { en = T.scr[j]; zn = T.zh[j]; }
+            }
+            for (int wc = warp; wc < c.W; wc += SIM_WARPS) {
+                const long long j = (long long)wc * 32 + lane;
+                const float4 e = en;
+                const float zh = zn;
+                {  // prefetch the next chunk of this warp
+                    const long long jn = j + 32 * SIM_WARPS;
+                    en = make_float4(0.f, 0.f, 0.f, 0.f);
+                    zn = -1.f;
+                    if (jn < c.n_hkl) { en = T.scr[jn]; zn = T.zh[jn]; }
+                }
+                uint32_t myword = 0;
+                if (FORM == DS_FORM_FP64) {
+                    double hd = e.x, kd = e.y, ld = e.z;
+#pragma unroll 1
+                    for (int o = 0; o < O; ++o) {
+                        double s, r, z;
+                        bool hit = (j < c.n_hkl) && (o < n_valid) && select_fp64(c, sop[o], hd, kd, ld, s, r, z);
+                        uint32_t b = __ballot_sync(FULL_MASK, hit);
+                        if (lane == o) myword = b;
+                    }
+                } else {
+#pragma unroll
+                    for (int o = 0; o < O; ++o) {
+                        float z = fmaf(m0[o], e.x, fmaf(m1[o], e.y, fmaf(m2[o], e.z, e.w)));
+                        uint32_t b = __ballot_sync(FULL_MASK, fabsf(z) < zh);
+                        if (lane == o) myword = b;
+                    }
+                }
+                if (lane < O) bitmap[lane * c.Ws + wc] = myword;
+            }
+        }
+        __syncthreads();
+
+        // ---------------- candidate counts per (orientation, part) and staging bases
+        for (int o = warp / WPO; o < n_valid; o += SIM_WARPS / WPO) {
+            const uint32_t *row = bitmap + o * c.Ws;
+            int cnt = 0;
+            for (int wi = w0 + lane; wi < w1; wi += 32) cnt += __popc(row[wi]);
+#pragma unroll
+            for (int d = 16; d >= 1; d >>= 1) cnt += __shfl_xor_sync(FULL_MASK, cnt, d);
+            if (lane == 0) acc[o * ACC_WORDS + ACC_CCNT0 + part] = (unsigned long long)cnt;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            long long run = 0;
+            for (int o = 0; o < n_valid; ++o)
+                for (int p = 0; p < WPO; ++p) {
+                    long long cc = (long long)acc[o * ACC_WORDS + ACC_CCNT0 + p];
+                    if (run + cc <= stg.cap) {
+                        acc[o * ACC_WORDS + ACC_CBASE0 + p] = (unsigned long long)run;
+                        run += cc;
+                    } else {
+                        acc[o * ACC_WORDS + ACC_CBASE0 + p] = NO_STAGE;
+                    }
+                }
+        }
+        __syncthreads();
+
+        // ---------------- phase 2: refine, intensities, per-orientation max
+        for (int o = warp / WPO; o < n_valid; o += SIM_WARPS / WPO) {
+            uint32_t *row = bitmap + o * c.Ws;
+            const OrientP &op = sop[o];
+            const unsigned long long base = acc[o * ACC_WORDS + ACC_CBASE0 + part];
+            const int cc = (int)acc[o * ACC_WORDS + ACC_CCNT0 + part];
+            float lmax = 0.f, lminpos = INFINITY;
+            int lcnt = 0;
+            if (base != NO_STAGE) {
+                for_each_bit(row, w0, w1, lane, [&](long long j, int rank, bool valid, int, int) {
+                    if (valid) my_idx[base + rank] = (int32_t)j;
+                });
+                __syncwarp();
+                for (int r0 = 0; r0 < cc; r0 += 32) {
+                    const int r = r0 + lane;
+                    if (r < cc) {
+                        const long long j = my_idx[base + r];
+                        float I, z;
+                        double sv;
+                        bool sel = eval_spot<FORM>(c, op, T, j, I, z, sv);
+                        if (sel && I == 0.f && all_zero_drop) sel = false;
+                        my_I[base + r] = sel ? I : -1.f;
+                        if (sel) {
+                            ++lcnt;
+                            lmax = fmaxf(lmax, I);
+                            if (I > 0.f) lminpos = fminf(lminpos, I);
+                        }
+                    }
+                }
             } else {
-                overflow = true;
+                for_each_bit(row, w0, w1, lane, [&](long long j, int, bool valid, int wi, int bit) {
+                    if (!valid) return;
+                    float I, z;
+                    double sv;
+                    bool sel = eval_spot<FORM>(c, op, T, j, I, z, sv);
+                    if (sel && I == 0.f && all_zero_drop) sel = false;
+                    if (!sel) {
+                        atomicAnd(&row[wi], ~(1u << bit));
+                        return;
+                    }
+                    ++lcnt;
+                    lmax = fmaxf(lmax, I);
+                    if (I > 0.f) lminpos = fminf(lminpos, I);
+                });
             }
-        });
-        if (__any_sync(FULL_MASK, overflow) && lane == 0) atomicOr(status, DS_ERR_CAPACITY);
+#pragma unroll
+            for (int d = 16; d >= 1; d >>= 1) {
+                lmax = fmaxf(lmax, __shfl_xor_sync(FULL_MASK, lmax, d));
+                lminpos = fminf(lminpos, __shfl_xor_sync(FULL_MASK, lminpos, d));
+                lcnt += __shfl_xor_sync(FULL_MASK, lcnt, d);
+            }
+            if (!(lmax > 0.f)) lmax = 0.f;  // no -0.0 or NaN in the bit-ordered max
+            if (lane == 0) {
+                // intensities are >= 0, so float bit patterns order like the values
+                atomicMax(&acc[o * ACC_WORDS + ACC_MAXI], (unsigned long long)__float_as_uint(lmax));
+                atomicMin(&acc[o * ACC_WORDS + ACC_MINPOS], (unsigned long long)__float_as_uint(lminpos));
+                acc[o * ACC_WORDS + ACC_PART0 + part] = (unsigned long long)lcnt;
+            }
+        }
+        __syncthreads();
+
+        // ---------------- mask pass (only where some I is positive but <= max * thr)
+        for (int o = warp / WPO; o < n_valid; o += SIM_WARPS / WPO) {
+            if (!(c.thr > 0.0)) break;
+            const float mx = __uint_as_float((unsigned)acc[o * ACC_WORDS + ACC_MAXI]);
+            const float mnp = __uint_as_float((unsigned)acc[o * ACC_WORDS + ACC_MINPOS]);
+            if (!((double)mnp <= (double)mx * c.thr)) continue;
+            uint32_t *row = bitmap + o * c.Ws;
+            const OrientP &op = sop[o];
+            const unsigned long long base = acc[o * ACC_WORDS + ACC_CBASE0 + part];
+            const int cc = (int)acc[o * ACC_WORDS + ACC_CCNT0 + part];
+            int dropped = 0;
+            if (base != NO_STAGE) {
+                for (int r = lane; r < cc; r += 32) {
+                    const float I = my_I[base + r];
+                    if (!(I < 0.f) && !((double)I > (double)mx * c.thr)) {
+                        my_I[base + r] = -1.f;
+                        ++dropped;
+                    }
+                }
+            } else {
+                for_each_bit(row, w0, w1, lane, [&](long long j, int, bool valid, int wi, int bit) {
+                    if (!valid) return;
+                    float I, z;
+                    double sv;
+                    eval_spot<FORM>(c, op, T, j, I, z, sv);
+                    if (!((double)I > (double)mx * c.thr)) {
+                        atomicAnd(&row[wi], ~(1u << bit));
+                        ++dropped;
+                    }
+                });
+            }
+#pragma unroll
+            for (int d = 16; d >= 1; d >>= 1) dropped += __shfl_xor_sync(FULL_MASK, dropped, d);
+            if (lane == 0) acc[o * ACC_WORDS + ACC_PART0 + part] -= (unsigned long long)dropped;
+        }
+        __syncthreads();
+
+        // ---------------- counts, offsets, look-back
+        if (tid == 0) {
+            long long run = 0;
+            for (int o = 0; o < n_valid; ++o) {
+                acc[o * ACC_WORDS + ACC_OFF] = (unsigned long long)run;
+                long long co = 0;
+                for (int p = 0; p < WPO; ++p) co += (long long)acc[o * ACC_WORDS + ACC_PART0 + p];
+                acc[o * ACC_WORDS + ACC_CNT] = (unsigned long long)co;
+                run += co;
+            }
+            long long prefix = lookback_exclusive(lb, tile, run, status);
+            s_prefix = prefix;
+            if (prefix >= 0 && tile == c.n_tiles - 1) {
+                offsets[c.n_orient] = prefix + run;
+                *out_total = prefix + run;
+            }
+        }
+        __syncthreads();
+        const long long prefix = s_prefix;
+        if (prefix < 0) break;  // bounded wait gave up: DS_ERR_TIMEOUT is set
+        for (int o = tid; o < n_valid; o += SIM_THREADS)
+            offsets[o_base + o] = prefix + (long long)acc[o * ACC_WORDS + ACC_OFF];
+
+        // ---------------- phase 3: ordered, coalesced writes
+        for (int o = warp / WPO; o < n_valid; o += SIM_WARPS / WPO) {
+            const uint32_t *row = bitmap + o * c.Ws;
+            const OrientP &op = sop[o];
+            long long pos0 = prefix + (long long)acc[o * ACC_WORDS + ACC_OFF];
+            for (int p = 0; p < part; ++p) pos0 += (long long)acc[o * ACC_WORDS + ACC_PART0 + p];
+            const unsigned long long base = acc[o * ACC_WORDS + ACC_CBASE0 + part];
+            const int cc = (int)acc[o * ACC_WORDS + ACC_CCNT0 + part];
+            bool overflow = false;
+            if (base != NO_STAGE) {
+                long long out_r = 0;
+                for (int r0 = 0; r0 < cc; r0 += 32) {
+                    const int r = r0 + lane;
+                    const float I = r < cc ? my_I[base + r] : -1.f;
+                    const bool keep = !(I < 0.f);
+                    const unsigned bal = __ballot_sync(FULL_MASK, keep);
+                    if (keep) {
+                        const long long j = my_idx[base + r];
+                        const float4 e = T.scr[j];
+                        float x, y, z;
+                        if (FORM == DS_FORM_FP64) {
+                            x = (float)(op.M[0][0] * (double)e.x + op.M[0][1] * (double)e.y + op.M[0][2] * (double)e.z);
+                            y = (float)(op.M[1][0] * (double)e.x + op.M[1][1] * (double)e.y + op.M[1][2] * (double)e.z);
+                            z = (float)(op.M[2][0] * (double)e.x + op.M[2][1] * (double)e.y + op.M[2][2] * (double)e.z);
+                        } else {
+                            x = fmaf(op.m[0][0], e.x, fmaf(op.m[0][1], e.y, op.m[0][2] * e.z));
+                            y = fmaf(op.m[1][0], e.x, fmaf(op.m[1][1], e.y, op.m[1][2] * e.z));
+                            z = fmaf(op.m[2][0], e.x, fmaf(op.m[2][1], e.y, op.m[2][2] * e.z));
+                        }
+                        const long long pos = pos0 + out_r + __popc(bal & lanemask_lt);
+                        if (pos < c.capacity) {
+                            out_idx[pos] = (int32_t)j;
+                            out_xyzi[pos] = make_float4(x, y, z, I);
+                            if (out_s) {
+                                float I2, z2;
+                                double sv;
+                                eval_spot<FORM>(c, op, T, j, I2, z2, sv);
+                                out_s[pos] = sv;
+                            }
+                        } else {
+                            overflow = true;
+                        }
+                    }
+                    out_r += __popc(bal);
+                }
+            } else {
+                for_each_bit(row, w0, w1, lane, [&](long long j, int rank, bool valid, int, int) {
+                    if (!valid) return;
+                    float I, z;
+                    double sv;
+                    eval_spot<FORM>(c, op, T, j, I, z, sv);
+                    const float4 e = T.scr[j];
+                    float x, y;
+                    if (FORM == DS_FORM_FP64) {
+                        x = (float)(op.M[0][0] * (double)e.x + op.M[0][1] * (double)e.y + op.M[0][2] * (double)e.z);
+                        y = (float)(op.M[1][0] * (double)e.x + op.M[1][1] * (double)e.y + op.M[1][2] * (double)e.z);
+                    } else {
+                        x = fmaf(op.m[0][0], e.x, fmaf(op.m[0][1], e.y, op.m[0][2] * e.z));
+                        y = fmaf(op.m[1][0], e.x, fmaf(op.m[1][1], e.y, op.m[1][2] * e.z));
+                    }
+                    long long pos = pos0 + rank;
+                    if (pos < c.capacity) {
+                        out_idx[pos] = (int32_t)j;
+                        out_xyzi[pos] = make_float4(x, y, z, I);
+                        if (out_s) out_s[pos] = sv;
+                    } else {
+                        overflow = true;
+                    }
+                });
+            }
+            if (__any_sync(FULL_MASK, overflow) && lane == 0) atomicOr(status, DS_ERR_CAPACITY);
+        }
+        __syncthreads();  // smem and staging are reused by the next tile
     }
 }
 
 // ------------------------------------------------------------- host side ----
 static inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+constexpr long long STAGE_CAP = 32768;  // staged candidates per CTA (8 bytes each)
+
 struct SimPlan {
     int O, W, Ws;
-    long long n_tiles;
-    size_t off_lb, off_scr, off_zh, off_g2, total;
+    long long n_tiles, grid, stage_cap;
+    size_t off_lb, off_scr, off_zh, off_g2, off_sidx, off_sI, total;
     size_t smem;
 };
 
@@ -552,12 +687,50 @@ static int pick_O(const ds_sim_params *p, long long n_hkl, long long n_orient) {
     return O;
 }
 
-static SimPlan make_plan(const ds_sim_params *p, const ds_phase_table *t, long long n_orient) {
-    SimPlan P;
+static const void *kernel_ptr(int O, int form) {
+    if (form == DS_FORM_FP64) {
+        switch (O) {
+            case 1: return (const void *)simulate_kernel<1, DS_FORM_FP64>;
+            case 2: return (const void *)simulate_kernel<2, DS_FORM_FP64>;
+            case 4: return (const void *)simulate_kernel<4, DS_FORM_FP64>;
+            case 8: return (const void *)simulate_kernel<8, DS_FORM_FP64>;
+            default: return (const void *)simulate_kernel<16, DS_FORM_FP64>;
+        }
+    }
+    switch (O) {
+        case 1: return (const void *)simulate_kernel<1, DS_FORM_MIXED>;
+        case 2: return (const void *)simulate_kernel<2, DS_FORM_MIXED>;
+        case 4: return (const void *)simulate_kernel<4, DS_FORM_MIXED>;
+        case 8: return (const void *)simulate_kernel<8, DS_FORM_MIXED>;
+        case 16: return (const void *)simulate_kernel<16, DS_FORM_MIXED>;
+        default: return (const void *)simulate_kernel<32, DS_FORM_MIXED>;
+    }
+}
+
+// Launch plan: tile size, persistent grid (resident CTAs, at most one per
+// tile) and the scratch layout.
+static ds_status make_plan(const ds_sim_params *p, const ds_phase_table *t, long long n_orient, SimPlan &P) {
     P.O = pick_O(p, t->n_hkl, n_orient);
+    if (p->form == DS_FORM_FP64 && P.O > 16) P.O = 16;
     P.W = (int)((t->n_hkl + 31) / 32);
     P.Ws = P.W | 1;
     P.n_tiles = (n_orient + P.O - 1) / P.O;
+    P.smem = sim_smem_layout(P.O, P.Ws).total;
+    DS_REQUIRE(P.smem <= 227 * 1024, "ds_simulate: candidate table too large for one orientation tile");
+    const void *kern = kernel_ptr(P.O, p->form);
+    DS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem));
+    int dev = 0, n_sm = 0, per_sm = 0;
+    DS_CUDA_TRY(cudaGetDevice(&dev));
+    DS_CUDA_TRY(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+    DS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, SIM_THREADS, P.smem));
+    if (per_sm < 1) per_sm = 1;
+    long long resident = (long long)n_sm * per_sm;
+    P.grid = P.n_tiles < resident ? P.n_tiles : resident;
+    if (P.grid < 1) P.grid = 1;
+    long long most = (long long)P.O * t->n_hkl;
+    const long long cap = p->stage_cap > 0 ? p->stage_cap : STAGE_CAP;
+    P.stage_cap = most < cap ? most : cap;
+    if (P.stage_cap < 1) P.stage_cap = 1;
     size_t o = 0;
     P.off_lb = o; o += lookback_scratch_bytes(P.n_tiles);
     o = align_up(o, 256);
@@ -566,19 +739,20 @@ static SimPlan make_plan(const ds_sim_params *p, const ds_phase_table *t, long l
     P.off_zh = o; o += (size_t)t->n_hkl * sizeof(float);
     o = align_up(o, 256);
     P.off_g2 = o; o += (size_t)t->n_hkl * sizeof(float2);
+    o = align_up(o, 256);
+    P.off_sidx = o; o += (size_t)(P.grid * P.stage_cap) * sizeof(int32_t);
+    o = align_up(o, 256);
+    P.off_sI = o; o += (size_t)(P.grid * P.stage_cap) * sizeof(float);
     P.total = align_up(o, 256);
-    P.smem = sim_smem_layout(P.O, P.Ws).total;
-    return P;
+    return DS_OK;
 }
 
 template <int O, int FORM>
 static ds_status launch_sim(const SimConst &c, const TableP &T, const double *quats, ds_spots *out,
-                            LookbackScratch lb, size_t smem, int32_t *status, cudaStream_t s) {
-    auto kern = simulate_kernel<O, FORM>;
-    DS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<(unsigned)c.n_tiles, SIM_THREADS, smem, s>>>(c, T, quats, out->offsets, out->hkl_index,
-                                                        reinterpret_cast<float4 *>(out->xyzi), out->excitation_error, out->total,
-                                                        lb, status);
+                            LookbackScratch lb, StageP stg, const SimPlan &P, int32_t *status, cudaStream_t s) {
+    simulate_kernel<O, FORM><<<(unsigned)P.grid, SIM_THREADS, P.smem, s>>>(
+        c, T, quats, out->offsets, out->hkl_index, reinterpret_cast<float4 *>(out->xyzi), out->excitation_error,
+        out->total, lb, stg, status);
     return check_launch("simulate_kernel");
 }
 
@@ -588,7 +762,9 @@ using namespace ds;
 
 extern "C" size_t ds_simulate_scratch_bytes(const ds_sim_params *p, const ds_phase_table *t, int64_t n_orient) {
     if (!p || !t || n_orient <= 0) return 0;
-    return make_plan(p, t, n_orient).total;
+    SimPlan P;
+    if (make_plan(p, t, n_orient, P) != DS_OK) return 0;
+    return P.total;
 }
 
 extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t, const double *quats,
@@ -609,6 +785,7 @@ extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t
     DS_REQUIRE(p->orient_tile == 0 || p->orient_tile == 1 || p->orient_tile == 2 || p->orient_tile == 4 ||
                    p->orient_tile == 8 || p->orient_tile == 16 || p->orient_tile == 32,
                "ds_simulate: orient_tile must be 0, 1, 2, 4, 8, 16 or 32");
+    DS_REQUIRE(p->stage_cap >= 0, "ds_simulate: stage_cap < 0");
     DS_REQUIRE(p->precession_mode == DS_PRECESSION_NONE || p->precession_angle > 0,
                "ds_simulate: precession mode needs a positive angle");
     if (p->precession_mode == DS_PRECESSION_INTEGRAL) {
@@ -627,9 +804,10 @@ extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t
     DS_REQUIRE(out->capacity >= 0 && (out->capacity == 0 || (out->hkl_index && out->xyzi)),
                "ds_simulate: output arrays missing");
     DS_REQUIRE(((uintptr_t)out->xyzi & 15) == 0, "ds_simulate: xyzi must be 16-byte aligned");
-    SimPlan P = make_plan(p, t, n_orient);
+    SimPlan P;
+    ds_status pst = make_plan(p, t, n_orient, P);
+    if (pst != DS_OK) return pst;
     DS_REQUIRE(scratch && scratch_bytes >= P.total, "ds_simulate: scratch too small");
-    DS_REQUIRE(P.smem <= 227 * 1024, "ds_simulate: candidate table too large for one orientation tile");
 
     SimConst c;
     c.k0 = p->k0;
@@ -690,21 +868,25 @@ extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t
         if (st) return st;
     }
     LookbackScratch lb = lookback_scratch(sb + P.off_lb);
+    StageP stg;
+    stg.idx = reinterpret_cast<int32_t *>(sb + P.off_sidx);
+    stg.inten = reinterpret_cast<float *>(sb + P.off_sI);
+    stg.cap = P.stage_cap;
     if (p->form == DS_FORM_FP64) {
         switch (P.O) {
-            case 1: return launch_sim<1, DS_FORM_FP64>(c, T, quats, out, lb, P.smem, status, s);
-            case 2: return launch_sim<2, DS_FORM_FP64>(c, T, quats, out, lb, P.smem, status, s);
-            case 4: return launch_sim<4, DS_FORM_FP64>(c, T, quats, out, lb, P.smem, status, s);
-            case 8: return launch_sim<8, DS_FORM_FP64>(c, T, quats, out, lb, P.smem, status, s);
-            default: return launch_sim<16, DS_FORM_FP64>(c, T, quats, out, lb, P.smem, status, s);
+            case 1: return launch_sim<1, DS_FORM_FP64>(c, T, quats, out, lb, stg, P, status, s);
+            case 2: return launch_sim<2, DS_FORM_FP64>(c, T, quats, out, lb, stg, P, status, s);
+            case 4: return launch_sim<4, DS_FORM_FP64>(c, T, quats, out, lb, stg, P, status, s);
+            case 8: return launch_sim<8, DS_FORM_FP64>(c, T, quats, out, lb, stg, P, status, s);
+            default: return launch_sim<16, DS_FORM_FP64>(c, T, quats, out, lb, stg, P, status, s);
         }
     }
     switch (P.O) {
-        case 1: return launch_sim<1, DS_FORM_MIXED>(c, T, quats, out, lb, P.smem, status, s);
-        case 2: return launch_sim<2, DS_FORM_MIXED>(c, T, quats, out, lb, P.smem, status, s);
-        case 4: return launch_sim<4, DS_FORM_MIXED>(c, T, quats, out, lb, P.smem, status, s);
-        case 8: return launch_sim<8, DS_FORM_MIXED>(c, T, quats, out, lb, P.smem, status, s);
-        case 16: return launch_sim<16, DS_FORM_MIXED>(c, T, quats, out, lb, P.smem, status, s);
-        default: return launch_sim<32, DS_FORM_MIXED>(c, T, quats, out, lb, P.smem, status, s);
+        case 1: return launch_sim<1, DS_FORM_MIXED>(c, T, quats, out, lb, stg, P, status, s);
+        case 2: return launch_sim<2, DS_FORM_MIXED>(c, T, quats, out, lb, stg, P, status, s);
+        case 4: return launch_sim<4, DS_FORM_MIXED>(c, T, quats, out, lb, stg, P, status, s);
+        case 8: return launch_sim<8, DS_FORM_MIXED>(c, T, quats, out, lb, stg, P, status, s);
+        case 16: return launch_sim<16, DS_FORM_MIXED>(c, T, quats, out, lb, stg, P, status, s);
+        default: return launch_sim<32, DS_FORM_MIXED>(c, T, quats, out, lb, stg, P, status, s);
     }
 }

@@ -197,23 +197,28 @@ sf_mixed_kernel(SfConst c, ds_atoms A, const int32_t *__restrict__ hkl_i, const 
 // All-FP64 evaluation of the reflections listed in queue[0 .. *queue_len) (or of
 // every reflection when queue is null).  Used for the FP64 form, for the
 // get_kinematical_intensities entry and for the mixed form's re-evaluations.
+// L lanes share one reflection's atom sum (partial sums meet by shuffles), so
+// a short queue still spreads over many SMs' FP64 units.
+template <int L>
 __global__ void __launch_bounds__(SF_THREADS)
 sf_fp64_kernel(SfConst c, ds_atoms A, const int32_t *__restrict__ hkl_i, const double *__restrict__ hkl_d,
                const double *__restrict__ g2in, const double *__restrict__ prefactor, float *__restrict__ F2,
                double *__restrict__ F2d, double *__restrict__ Fout, const int32_t *__restrict__ queue,
                const int32_t *__restrict__ queue_len, int32_t *status) {
     extern __shared__ __align__(16) unsigned char smem[];
+    constexpr int PER_BLOCK = SF_THREADS / L;
     const int chunk_cap = c.n_atoms < SF_ATOM_CHUNK ? c.n_atoms : SF_ATOM_CHUNK;
     const SfSmem Ls = sf_smem_layout(c.n_species, chunk_cap);
     const long long n_work = queue ? (long long)(*queue_len) : c.n;
-    if ((long long)blockIdx.x * SF_THREADS >= n_work) return;  // uniform per block
+    if ((long long)blockIdx.x * PER_BLOCK >= n_work) return;  // uniform per block
     sf_prologue(c, A, smem, Ls);
     const double *cd = reinterpret_cast<const double *>(smem + Ls.coeff_d);
     const ds_atom *sa = reinterpret_cast<const ds_atom *>(smem + Ls.atoms);
+    const int sub = threadIdx.x % L;
     uint32_t parity = 0;  // mbarrier phase, carried across the grid-stride loop
 
-    for (long long base = (long long)blockIdx.x * SF_THREADS; base < n_work; base += (long long)gridDim.x * SF_THREADS) {
-        const long long w = base + threadIdx.x;
+    for (long long base = (long long)blockIdx.x * PER_BLOCK; base < n_work; base += (long long)gridDim.x * PER_BLOCK) {
+        const long long w = base + threadIdx.x / L;
         const bool active = w < n_work;
         const long long j = active ? (queue ? (long long)queue[w] : w) : 0;
         double h = 0, k = 0, l = 0, g2 = 0;
@@ -229,7 +234,7 @@ sf_fp64_kernel(SfConst c, ds_atoms A, const int32_t *__restrict__ hkl_i, const d
             int cnt = min(chunk_cap, c.n_atoms - start);
             if (!sf_stage_chunk(A, smem, Ls, start, cnt, parity, status, false)) return;
             if (active) {
-                for (int i = 0; i < cnt; ++i) {
+                for (int i = sub; i < cnt; i += L) {
                     const ds_atom &a = sa[i];
                     double t = h * a.x + k * a.y + l * a.z;
                     double r = t - rint(t);
@@ -242,7 +247,12 @@ sf_fp64_kernel(SfConst c, ds_atoms A, const int32_t *__restrict__ hkl_i, const d
             }
             __syncthreads();
         }
-        if (active) {
+#pragma unroll
+        for (int d = L / 2; d >= 1; d >>= 1) {
+            re += __shfl_xor_sync(FULL_MASK, re, d);
+            im += __shfl_xor_sync(FULL_MASK, im, d);
+        }
+        if (active && sub == 0) {
             double f2 = re * re + im * im;
             if (prefactor) f2 *= prefactor[j];
             if (F2) F2[j] = (float)f2;
@@ -262,19 +272,38 @@ static ds_status validate_atoms(const ds_atoms *A) {
     return DS_OK;
 }
 
+template <int L>
+static ds_status launch_fp64_l(const SfConst &c, const ds_atoms &A, const int32_t *hkl_i, const double *hkl_d,
+                               const double *g2, const double *pref, float *F2, double *F2d, double *F,
+                               const int32_t *queue, const int32_t *queue_len, long long max_work,
+                               int32_t *status, cudaStream_t s) {
+    int chunk = c.n_atoms < SF_ATOM_CHUNK ? c.n_atoms : SF_ATOM_CHUNK;
+    SfSmem Ls = sf_smem_layout(c.n_species, chunk);
+    DS_CUDA_TRY(cudaFuncSetAttribute(sf_fp64_kernel<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Ls.total));
+    long long blocks = (max_work * L + SF_THREADS - 1) / SF_THREADS;
+    if (blocks > 8192) blocks = 8192;
+    sf_fp64_kernel<L><<<(unsigned)blocks, SF_THREADS, Ls.total, s>>>(c, A, hkl_i, hkl_d, g2, pref, F2, F2d, F, queue,
+                                                                    queue_len, status);
+    return check_launch("sf_fp64_kernel");
+}
+
+// L lanes per reflection: whole warps for short lists and many atoms, one lane
+// per reflection when the reflections alone fill the GPU.
 static ds_status launch_fp64(const SfConst &c, const ds_atoms &A, const int32_t *hkl_i, const double *hkl_d,
                              const double *g2, const double *pref, float *F2, double *F2d, double *F,
                              const int32_t *queue, const int32_t *queue_len, long long max_work,
                              int32_t *status, cudaStream_t s) {
     if (max_work <= 0) return DS_OK;
-    int chunk = c.n_atoms < SF_ATOM_CHUNK ? c.n_atoms : SF_ATOM_CHUNK;
-    SfSmem L = sf_smem_layout(c.n_species, chunk);
-    DS_CUDA_TRY(cudaFuncSetAttribute(sf_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total));
-    long long blocks = (max_work + SF_THREADS - 1) / SF_THREADS;
-    if (blocks > 4096) blocks = 4096;
-    sf_fp64_kernel<<<(unsigned)blocks, SF_THREADS, L.total, s>>>(c, A, hkl_i, hkl_d, g2, pref, F2, F2d, F,
-                                                                 queue, queue_len, status);
-    return check_launch("sf_fp64_kernel");
+    const long long want = 152ll * 2048;
+    if (queue) {  // typically ~1% of the table: a warp per reflection
+        if (c.n_atoms >= 32) return launch_fp64_l<32>(c, A, hkl_i, hkl_d, g2, pref, F2, F2d, F, queue, queue_len, max_work, status, s);
+        return launch_fp64_l<8>(c, A, hkl_i, hkl_d, g2, pref, F2, F2d, F, queue, queue_len, max_work, status, s);
+    }
+    if (max_work >= want || c.n_atoms < 8)
+        return launch_fp64_l<1>(c, A, hkl_i, hkl_d, g2, pref, F2, F2d, F, queue, queue_len, max_work, status, s);
+    if (max_work * 4 >= want || c.n_atoms < 32)
+        return launch_fp64_l<4>(c, A, hkl_i, hkl_d, g2, pref, F2, F2d, F, queue, queue_len, max_work, status, s);
+    return launch_fp64_l<32>(c, A, hkl_i, hkl_d, g2, pref, F2, F2d, F, queue, queue_len, max_work, status, s);
 }
 
 template <int L>

@@ -128,6 +128,8 @@ typedef struct {
     int32_t precession_mode;     /* DS_PRECESSION_*                                 */
     int32_t form;                /* DS_FORM_*                                       */
     int32_t orient_tile;         /* orientations per CTA (0 = library choice)       */
+    int32_t stage_cap;           /* staged candidates per CTA (0 = library choice)  */
+    int32_t _pad;
 } ds_sim_params;
 
 /* One phase's candidate table (device arrays of n_hkl rows, in reference order). */

@@ -250,6 +250,34 @@ def test_orientation_tiles_agree(tile):
     assert np.array_equal(a.xyzi.cpu().numpy(), b.xyzi.cpu().numpy())  # deterministic, bit for bit
 
 
+@pytest.mark.parametrize("stage_cap", [1, 64, 700])
+def test_staging_fallback_agrees(stage_cap):
+    """Orientation parts whose candidates do not fit the per-CTA staging walk
+    the bitmap and re-evaluate: same spots, bit for bit."""
+    import torch
+    from diffsims_gb300.engine import PhaseTable, SpotBuffers, simulate_phase
+    dev = torch.device("cuda", 0)
+    crystal = random_p1(20, 13)
+    q = ok.random_quaternions(100, seed=5)
+    p = ok.SimParams(accelerating_voltage=200, shape_factor_model="sinc", reciprocal_radius=1.4,
+                     max_excitation_error=0.02, minimum_intensity=1e-3)
+    gen = pu.generator_for(p)
+    table = PhaseTable(pu.to_phase(crystal), 1.4, True, "lobato", list(crystal.B), device=dev)
+    qd = torch.as_tensor(q).to(dev)
+    s0 = gen.settings(0.02)
+    s1 = gen.settings(0.02)
+    s1.stage_cap = stage_cap
+    a = simulate_phase(table, qd, s0, 1.4, SpotBuffers(dev))
+    b = simulate_phase(table, qd, s1, 1.4, SpotBuffers(dev))
+    assert a.total == b.total
+    assert np.array_equal(a.offsets.cpu().numpy(), b.offsets.cpu().numpy())
+    assert np.array_equal(a.hkl_index.cpu().numpy(), b.hkl_index.cpu().numpy())
+    xa, xb = a.xyzi.cpu().numpy(), b.xyzi.cpu().numpy()
+    assert np.array_equal(xa[:, 3], xb[:, 3])
+    np.testing.assert_allclose(xa[:, :3], xb[:, :3], atol=1e-6)  # z: FP32 in the staged path, double-float otherwise
+    pu.compare(b, crystal, q, p)
+
+
 def test_capacity_overflow_is_retried():
     import torch
     from diffsims_gb300 import engine
