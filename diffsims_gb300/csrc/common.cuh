@@ -7,7 +7,7 @@
 
 #include <string>
 
-#include "../../include/diffsims_gb300.h"
+#include "diffsims_gb300.h"
 
 namespace ds {
 
@@ -131,15 +131,16 @@ __device__ __forceinline__ void lb_store(unsigned long long *p, unsigned long lo
     asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-// Called by ONE thread of the tile.  Returns the exclusive prefix of the tile's
-// count; on timeout returns -1 and sets DS_ERR_TIMEOUT in *status.
-__device__ inline long long lookback_exclusive(LookbackScratch lb, long long tile, long long count,
-                                               int32_t *status) {
-    if (tile == 0) {
-        lb_store(lb.state, LB_FLAG_INC | ((unsigned long long)count & LB_VALUE_MASK));
-        return 0;
-    }
-    lb_store(lb.state + tile, LB_FLAG_AGG | ((unsigned long long)count & LB_VALUE_MASK));
+// Publish a tile's count (its inclusive prefix directly for tile 0).  ONE thread.
+__device__ inline void lookback_publish(LookbackScratch lb, long long tile, long long count) {
+    lb_store(lb.state + tile, (tile == 0 ? LB_FLAG_INC : LB_FLAG_AGG) | ((unsigned long long)count & LB_VALUE_MASK));
+}
+
+// Exclusive prefix of a tile whose count was published; publishes its
+// inclusive prefix.  ONE thread.  On timeout returns -1 and sets
+// DS_ERR_TIMEOUT in *status.
+__device__ inline long long lookback_resolve(LookbackScratch lb, long long tile, long long count, int32_t *status) {
+    if (tile == 0) return 0;
     long long excl = 0;
     long long idx = tile - 1;
     long long spins = 0;
@@ -162,6 +163,13 @@ __device__ inline long long lookback_exclusive(LookbackScratch lb, long long til
     }
     lb_store(lb.state + tile, LB_FLAG_INC | ((unsigned long long)(excl + count) & LB_VALUE_MASK));
     return excl;
+}
+
+// Publish and resolve in one go.  ONE thread.
+__device__ inline long long lookback_exclusive(LookbackScratch lb, long long tile, long long count,
+                                               int32_t *status) {
+    lookback_publish(lb, tile, count);
+    return lookback_resolve(lb, tile, count, status);
 }
 
 // ----------------------------------------------------------------------------

@@ -45,13 +45,15 @@ struct SimConst {
     float k0f, inv_k0sq, eps_f, width_f, sigma_f, mfac_f, phi_f, Pz_f, Pt_f, k0sq_f, guard;
     int shape, prec, form, O;
     int W, Ws;
+    int hmax[3];
     long long n_hkl, n_orient, n_tiles, capacity;
 };
 
 struct __align__(16) OrientP {
     float m[3][3];   // beam-frame coordinate c = sum_i m[c][i] * hkl_i   (FP32)
-    float mzlo[3];   // low words of m[2][i] (double-float z)
-    float _pad[4];
+    float za[3];     // z column split: za on a power-of-two grid coarse enough that
+    float zb[3];     //   sum_i za_i hkl_i is exact in FP32; zb = m - za (small)
+    float _pad;
     double M[3][3];  // FP64 copy
 };
 
@@ -60,6 +62,8 @@ struct __align__(16) OrientP {
 // kept count, staging base, candidate count
 enum { ACC_MAXI = 0, ACC_MINPOS = 1, ACC_CNT = 2, ACC_OFF = 3, ACC_PART0 = 4, ACC_CBASE0 = 12, ACC_CCNT0 = 20,
        ACC_WORDS = 28 };
+// one accumulator block = O orientation slots + 8 words (word 0: tile total)
+__host__ __device__ constexpr int acc_stride(int O) { return O * ACC_WORDS + 8; }
 
 struct SimSmem {
     size_t orient, bitmap, acc, total;
@@ -67,8 +71,8 @@ struct SimSmem {
 __host__ __device__ inline SimSmem sim_smem_layout(int O, int Ws) {
     SimSmem L;
     size_t o = 0;
-    L.orient = o; o += (size_t)O * sizeof(OrientP);
-    L.acc = o; o += (size_t)O * ACC_WORDS * sizeof(unsigned long long) + 64;
+    L.orient = o; o += (size_t)2 * O * sizeof(OrientP);  // two pipeline buffers
+    L.acc = o; o += (size_t)2 * acc_stride(O) * sizeof(unsigned long long);
     o = (o + 15) & ~(size_t)15;
     L.bitmap = o; o += (size_t)O * Ws * sizeof(uint32_t);
     L.total = o;
@@ -107,15 +111,6 @@ __global__ void sim_prep_kernel(SimConst c, const int32_t *__restrict__ hkl, con
 }
 
 // --------------------------------------------------------- evaluation ----
-__device__ __forceinline__ dd z_dd(const OrientP &op, float h, float k, float l) {
-    dd p0 = two_prod(op.m[2][0], h), p1 = two_prod(op.m[2][1], k), p2 = two_prod(op.m[2][2], l);
-    dd s = two_sum(p0.hi, p1.hi);
-    dd t = two_sum(s.hi, p2.hi);
-    float lo = s.lo + t.lo + p0.lo + p1.lo + p2.lo;
-    lo = fmaf(op.mzlo[0], h, fmaf(op.mzlo[1], k, fmaf(op.mzlo[2], l, lo)));
-    return quick_two_sum(t.hi, lo);
-}
-
 // FP64 excitation error and selection in the reference's operation order
 // (simulation_generator.py:355-375): FP64 step #2.
 __device__ inline bool select_fp64(const SimConst &c, const OrientP &op, double h, double k, double l, double &s,
@@ -133,33 +128,46 @@ __device__ inline bool select_fp64(const SimConst &c, const OrientP &op, double 
 }
 
 // Mixed-form selection.  s and r returned for the shape factor.
+//  z     = Sa + Sb: Sa = za . hkl is exact in FP32 (za on a coarse power-of-two
+//          grid), Sb = zb . hkl is a ~2^-16 relative correction: z to ~1e-12.
+//  r^2   = g^2 - z^2 as an FP32 pair (no cancellation: z^2 << g^2 near the sphere).
+//  w     = k0 - sqrt(k0^2 - r^2) = (r^2 / 2k0)(1 + u/4 + u^2/8 + 5u^3/64 + ...),
+//          u = r^2/k0^2 <= 0.01 (series error < 1e-14 relative).
+//  s     = w - z as an FP32 pair, error < ~5e-11.  Pairs within 1e-9 of the
+//          cutoff are decided in FP64 (FP64 step #2).
 __device__ inline bool select_mixed(const SimConst &c, const OrientP &op, const float4 &e, float2 g2p, dd &s,
                                     float &r, float &zf) {
-    dd z = z_dd(op, e.x, e.y, e.z);
-    dd r2 = dd_sub(dd{g2p.x, g2p.y}, dd_mul(z, z));
-    float u = r2.hi * c.inv_k0sq;
+    const float Sa = fmaf(op.za[0], e.x, fmaf(op.za[1], e.y, op.za[2] * e.z));
+    const float Sb = fmaf(op.zb[0], e.x, fmaf(op.zb[1], e.y, op.zb[2] * e.z));
+    const float zz = fmaf(Sa, Sa, (2.f * Sa + Sb) * Sb);
+    dd r2 = two_sum(g2p.x, -zz);
+    r2.lo += g2p.y;
+    const float u = r2.hi * c.inv_k0sq;
     bool fallback = u > SIM_U_MAX;
     bool sel = false;
     r = sqrtf(fmaxf(r2.hi, 0.f));
     if (!fallback) {
-        float corr = u * (0.25f + u * (0.125f + u * (0.078125f + u * (0.0546875f + u * 0.041015625f))));
-        dd w0 = dd_mul(r2, c.c2k0_dd);  // r^2 / (2 k0)
-        dd w = dd_add_f(w0, w0.hi * corr);  // k0 - sqrt(k0^2 - r^2)
-        s = dd_sub(w, z);
+        const float corr = u * (0.25f + u * (0.125f + u * (0.078125f + u * (0.0546875f + u * 0.041015625f))));
+        const float w0h = r2.hi * c.c2k0_dd.hi;
+        const float w0l = fmaf(r2.hi, c.c2k0_dd.hi, -w0h) + fmaf(r2.hi, c.c2k0_dd.lo, r2.lo * c.c2k0_dd.hi);
+        const dd t = two_sum(w0h, -Sa);
+        s = two_sum(t.hi, t.lo + (w0l - Sb) + w0h * corr);
         if (c.prec == DS_PRECESSION_NONE) {
-            dd d = dd_sub(dd_abs(s), c.eps_dd);
-            if (fabsf(d.hi) < SIM_TAU) fallback = true;
-            else sel = d.hi < 0.f;
+            // |s| - eps: the leading difference is exact (Sterbenz) whenever it matters
+            const float sg = s.hi < 0.f ? -1.f : 1.f;
+            const float d = (fabsf(s.hi) - c.eps_dd.hi) + (sg * s.lo - c.eps_dd.lo);
+            if (fabsf(d) < SIM_TAU) fallback = true;
+            else sel = d < 0.f;
         } else {
-            float zz = z.hi + z.lo;
-            float rp = r + c.Pt_f, rm = r - c.Pt_f;
-            float a1 = c.k0sq_f - rp * rp, a2 = c.k0sq_f - rm * rm;
+            const float zs = Sa + Sb;
+            const float rp = r + c.Pt_f, rm = r - c.Pt_f;
+            const float a1 = c.k0sq_f - rp * rp, a2 = c.k0sq_f - rm * rm;
             if (!(a1 > 0.f) || !(a2 > 0.f)) {
                 fallback = true;
             } else {
-                float zup = r * (r + 2.f * c.Pt_f) / (c.Pz_f + sqrtf(a1));
-                float zdo = r * (r - 2.f * c.Pt_f) / (c.Pz_f + sqrtf(a2));
-                float d1 = zup - (zz - c.eps_f), d2 = (zz + c.eps_f) - zdo;
+                const float zup = r * (r + 2.f * c.Pt_f) / (c.Pz_f + sqrtf(a1));
+                const float zdo = r * (r - 2.f * c.Pt_f) / (c.Pz_f + sqrtf(a2));
+                const float d1 = zup - (zs - c.eps_f), d2 = (zs + c.eps_f) - zdo;
                 if (fabsf(d1) < SIM_TAU_PREC || fabsf(d2) < SIM_TAU_PREC) fallback = true;
                 else sel = (d1 >= 0.f) && (d2 >= 0.f);
             }
@@ -173,7 +181,7 @@ __device__ inline bool select_mixed(const SimConst &c, const OrientP &op, const 
         zf = (float)z64;
         return sel;
     }
-    zf = z.hi + z.lo;
+    zf = Sa + Sb;
     return sel;
 }
 
@@ -324,6 +332,45 @@ __device__ __forceinline__ void for_each_bit(const uint32_t *row, int w0, int w1
     }
 }
 
+// As for_each_bit, with K consecutive words per lane (groups of 32 K words),
+// so that sparse bitmaps still fill most lanes of each 32-candidate batch.
+template <int K, typename Fn>
+__device__ __forceinline__ void for_each_bit_k(const uint32_t *row, int w0, int w1, int lane, Fn fn) {
+    int base_rank = 0;
+    for (int g0 = w0; g0 < w1; g0 += 32 * K) {
+        uint32_t wd[K];
+        int cnt = 0;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int wi = g0 + lane * K + k;
+            wd[k] = wi < w1 ? row[wi] : 0u;
+            cnt += __popc(wd[k]);
+        }
+        const int incl = warp_inclusive_scan(cnt, lane);
+        const int total = __shfl_sync(FULL_MASK, incl, 31);
+        for (int q0 = 0; q0 < total; q0 += 32) {
+            const int q = q0 + lane;
+            const bool valid = q < total;
+            const int own = owner_lane(incl, valid ? q : total - 1);
+            const int n = q - (__shfl_sync(FULL_MASK, incl, own) - __shfl_sync(FULL_MASK, cnt, own));
+            uint32_t word = 0;
+            int wsel = 0, before = 0, run = 0;
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const uint32_t ow = __shfl_sync(FULL_MASK, wd[k], own);
+                const int pc = __popc(ow);
+                if (n >= run && n < run + pc) { word = ow; wsel = k; before = run; }
+                run += pc;
+            }
+            int bit = 0;
+            if (valid) bit = (int)__fns(word, 0, n - before + 1);
+            const int wi = g0 + own * K + wsel;
+            fn((long long)wi * 32 + bit, base_rank + q, valid, wi, bit);
+        }
+        base_rank += total;
+    }
+}
+
 // Per-CTA staging in global scratch (L2-resident): the screened candidate
 // rows of the tile in (orientation, row) order and their intensities, so the
 // refine pass evaluates full warps of candidates once and the write pass
@@ -343,14 +390,15 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
                 int64_t *__restrict__ out_total, LookbackScratch lb, StageP stg, int32_t *status) {
     extern __shared__ __align__(16) unsigned char smem[];
     const SimSmem Ls = sim_smem_layout(O, c.Ws);
-    OrientP *sop = reinterpret_cast<OrientP *>(smem + Ls.orient);
-    unsigned long long *acc = reinterpret_cast<unsigned long long *>(smem + Ls.acc);
+    OrientP *sop_buf = reinterpret_cast<OrientP *>(smem + Ls.orient);  // [2][O]
+    unsigned long long *acc_buf = reinterpret_cast<unsigned long long *>(smem + Ls.acc);  // [2][O * ACC_WORDS]
     uint32_t *bitmap = reinterpret_cast<uint32_t *>(smem + Ls.bitmap);
     __shared__ long long s_tile, s_prefix;
+    __shared__ int s_defer;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    int32_t *my_idx = stg.idx + (long long)blockIdx.x * stg.cap;
-    float *my_I = stg.inten + (long long)blockIdx.x * stg.cap;
+    constexpr int ACC_STRIDE = acc_stride(O);
+    constexpr int ACC_TILE_TOTAL = O * ACC_WORDS;
     // work split for phases 2-3: WPO warps share one orientation's words
     constexpr int WPO = O >= SIM_WARPS ? 1 : SIM_WARPS / O;
     const int part = warp % WPO;
@@ -358,15 +406,30 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
     const bool all_zero_drop = c.thr >= 0.0;
     const unsigned lanemask_lt = (1u << lane) - 1u;
 
-    for (;;) {  // persistent: one tile of O orientations per ticket
+    // Two-stage software pipeline over tiles: a tile is screened and refined
+    // (front), its count published, and its look-back and writes (back) run
+    // after the NEXT tile's front, by when its predecessors have long
+    // published: the look-back rarely waits.  Tiles whose candidates did not
+    // all fit the staging need their bitmap in the back and are finished at
+    // once.  Buffers (orientations, accumulators, staging) alternate.
+    int cur = 0;
+    long long pend_tile = -1;
+    bool aborted = false;
+    for (;;) {
         if (tid == 0) s_tile = (long long)atomicAdd(lb.ticket, 1ull);
-        for (int i = tid; i < O * ACC_WORDS; i += SIM_THREADS)
-            acc[i] = (i % ACC_WORDS == ACC_MINPOS) ? (unsigned long long)__float_as_uint(INFINITY) : 0ull;
+        OrientP *sop = sop_buf + cur * O;
+        unsigned long long *acc = acc_buf + cur * ACC_STRIDE;
+        int32_t *my_idx = stg.idx + (2 * (long long)blockIdx.x + cur) * stg.cap;
+        float *my_I = stg.inten + (2 * (long long)blockIdx.x + cur) * stg.cap;
+        for (int i = tid; i < ACC_STRIDE; i += SIM_THREADS)
+            acc[i] = (i < ACC_TILE_TOTAL && i % ACC_WORDS == ACC_MINPOS) ? (unsigned long long)__float_as_uint(INFINITY)
+                                                                          : 0ull;
         __syncthreads();
         const long long tile = s_tile;
-        if (tile >= c.n_tiles) break;
+        const bool have_new = tile < c.n_tiles;
         const long long o_base = tile * O;
-        const int n_valid = (int)min((long long)O, c.n_orient - o_base);
+        const int n_valid = have_new ? (int)min((long long)O, c.n_orient - o_base) : 0;
+        if (have_new) {
 
         // per-orientation rotation: beam frame = g @ R, R the active matrix of q
         if (tid < O) {
@@ -388,11 +451,17 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
                 for (int i = 0; i < 3; ++i) {
                     double v = c.recip[3 * i + 0] * R[0][cc] + c.recip[3 * i + 1] * R[1][cc] + c.recip[3 * i + 2] * R[2][cc];
                     op.M[cc][i] = v;
-                    float hi, lo;
-                    split_double(v, hi, lo);
-                    op.m[cc][i] = hi;
-                    if (cc == 2) op.mzlo[i] = lo;
+                    op.m[cc][i] = (float)v;
                 }
+            // exact-product split of the z column: grid 2^q with 2^(q+24) >= 2 sum_i |M_zi| hmax_i
+            double Z = 0.0;
+            for (int i = 0; i < 3; ++i) Z += fabs(op.M[2][i]) * (double)c.hmax[i];
+            const int q = (Z > 0.0 ? ilogb(Z) : -100) + 2 - 24;
+            for (int i = 0; i < 3; ++i) {
+                const double a = ldexp(rint(ldexp(op.M[2][i], -q)), q);
+                op.za[i] = (float)a;
+                op.zb[i] = (float)(op.M[2][i] - a);
+            }
         }
         __syncthreads();
 
@@ -401,21 +470,25 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
             float m0[O], m1[O], m2[O];
 #pragma unroll
             for (int o = 0; o < O; ++o) { m0[o] = sop[o].m[2][0]; m1[o] = sop[o].m[2][1]; m2[o] = sop[o].m[2][2]; }
-            float4 en = make_float4(0.f, 0.f, 0.f, 0.f);
-            float zn = -1.f;
+            // rows of chunks wc + 8 and wc + 16 are in flight while chunk wc is screened
+            float4 e1 = make_float4(0.f, 0.f, 0.f, 0.f), e2 = e1;
+            float z1 = -1.f, z2 = -1.f;
             {
-                long long j = (long long)warp * 32 + lane;
-                if (warp < c.W && j < c.n_hkl) { en = T.scr[j]; zn = T.zh[j]; }
+                const long long j1 = (long long)warp * 32 + lane, j2 = j1 + 32 * SIM_WARPS;
+                if (j1 < c.n_hkl) { e1 = T.scr[j1]; z1 = T.zh[j1]; }
+                if (j2 < c.n_hkl) { e2 = T.scr[j2]; z2 = T.zh[j2]; }
             }
             for (int wc = warp; wc < c.W; wc += SIM_WARPS) {
                 const long long j = (long long)wc * 32 + lane;
-                const float4 e = en;
-                const float zh = zn;
-                {  // prefetch the next chunk of this warp
-                    const long long jn = j + 32 * SIM_WARPS;
-                    en = make_float4(0.f, 0.f, 0.f, 0.f);
-                    zn = -1.f;
-                    if (jn < c.n_hkl) { en = T.scr[jn]; zn = T.zh[jn]; }
+                const float4 e = e1;
+                const float zh = z1;
+                e1 = e2;
+                z1 = z2;
+                {
+                    const long long jn = j + 64 * SIM_WARPS;
+                    e2 = make_float4(0.f, 0.f, 0.f, 0.f);
+                    z2 = -1.f;
+                    if (jn < c.n_hkl) { e2 = T.scr[jn]; z2 = T.zh[jn]; }
                 }
                 uint32_t myword = 0;
                 if (FORM == DS_FORM_FP64) {
@@ -474,26 +547,22 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
             float lmax = 0.f, lminpos = INFINITY;
             int lcnt = 0;
             if (base != NO_STAGE) {
-                for_each_bit(row, w0, w1, lane, [&](long long j, int rank, bool valid, int, int) {
-                    if (valid) my_idx[base + rank] = (int32_t)j;
-                });
-                __syncwarp();
-                for (int r0 = 0; r0 < cc; r0 += 32) {
-                    const int r = r0 + lane;
-                    if (r < cc) {
-                        const long long j = my_idx[base + r];
-                        float I, z;
-                        double sv;
-                        bool sel = eval_spot<FORM>(c, op, T, j, I, z, sv);
-                        if (sel && I == 0.f && all_zero_drop) sel = false;
-                        my_I[base + r] = sel ? I : -1.f;
-                        if (sel) {
-                            ++lcnt;
-                            lmax = fmaxf(lmax, I);
-                            if (I > 0.f) lminpos = fminf(lminpos, I);
-                        }
+                // evaluate each screened candidate once; keep (row, I or -1) in
+                // candidate order for the write pass
+                for_each_bit_k<4>(row, w0, w1, lane, [&](long long j, int rank, bool valid, int, int) {
+                    if (!valid) return;
+                    float I, z;
+                    double sv;
+                    bool sel = eval_spot<FORM>(c, op, T, j, I, z, sv);
+                    if (sel && I == 0.f && all_zero_drop) sel = false;
+                    my_idx[base + rank] = (int32_t)j;
+                    my_I[base + rank] = sel ? I : -1.f;
+                    if (sel) {
+                        ++lcnt;
+                        lmax = fmaxf(lmax, I);
+                        if (I > 0.f) lminpos = fminf(lminpos, I);
                     }
-                }
+                });
             } else {
                 for_each_bit(row, w0, w1, lane, [&](long long j, int, bool valid, int wi, int bit) {
                     if (!valid) return;
@@ -563,103 +632,139 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
         }
         __syncthreads();
 
-        // ---------------- counts, offsets, look-back
+        // ---------------- tile count, published for the look-back of later tiles
         if (tid == 0) {
             long long run = 0;
+            int defer = 1;
             for (int o = 0; o < n_valid; ++o) {
                 acc[o * ACC_WORDS + ACC_OFF] = (unsigned long long)run;
                 long long co = 0;
-                for (int p = 0; p < WPO; ++p) co += (long long)acc[o * ACC_WORDS + ACC_PART0 + p];
+                for (int p = 0; p < WPO; ++p) {
+                    co += (long long)acc[o * ACC_WORDS + ACC_PART0 + p];
+                    if (acc[o * ACC_WORDS + ACC_CBASE0 + p] == NO_STAGE) defer = 0;
+                }
                 acc[o * ACC_WORDS + ACC_CNT] = (unsigned long long)co;
                 run += co;
             }
-            long long prefix = lookback_exclusive(lb, tile, run, status);
-            s_prefix = prefix;
-            if (prefix >= 0 && tile == c.n_tiles - 1) {
-                offsets[c.n_orient] = prefix + run;
-                *out_total = prefix + run;
-            }
+            acc[ACC_TILE_TOTAL] = (unsigned long long)run;
+            lookback_publish(lb, tile, run);
+            s_defer = defer;
         }
         __syncthreads();
-        const long long prefix = s_prefix;
-        if (prefix < 0) break;  // bounded wait gave up: DS_ERR_TIMEOUT is set
-        for (int o = tid; o < n_valid; o += SIM_THREADS)
-            offsets[o_base + o] = prefix + (long long)acc[o * ACC_WORDS + ACC_OFF];
+        }  // have_new
 
-        // ---------------- phase 3: ordered, coalesced writes
-        for (int o = warp / WPO; o < n_valid; o += SIM_WARPS / WPO) {
-            const uint32_t *row = bitmap + o * c.Ws;
-            const OrientP &op = sop[o];
-            long long pos0 = prefix + (long long)acc[o * ACC_WORDS + ACC_OFF];
-            for (int p = 0; p < part; ++p) pos0 += (long long)acc[o * ACC_WORDS + ACC_PART0 + p];
-            const unsigned long long base = acc[o * ACC_WORDS + ACC_CBASE0 + part];
-            const int cc = (int)acc[o * ACC_WORDS + ACC_CCNT0 + part];
-            bool overflow = false;
-            if (base != NO_STAGE) {
-                long long out_r = 0;
-                for (int r0 = 0; r0 < cc; r0 += 32) {
-                    const int r = r0 + lane;
-                    const float I = r < cc ? my_I[base + r] : -1.f;
-                    const bool keep = !(I < 0.f);
-                    const unsigned bal = __ballot_sync(FULL_MASK, keep);
-                    if (keep) {
-                        const long long j = my_idx[base + r];
+        // ---------------- back: look-back and ordered writes of a finished tile
+        auto back = [&](long long btile, int bbuf) -> bool {
+            const OrientP *bsop = sop_buf + bbuf * O;
+            const unsigned long long *bacc = acc_buf + bbuf * ACC_STRIDE;
+            const int32_t *b_idx = stg.idx + (2 * (long long)blockIdx.x + bbuf) * stg.cap;
+            const float *b_I = stg.inten + (2 * (long long)blockIdx.x + bbuf) * stg.cap;
+            const long long bo_base = btile * O;
+            const int bn_valid = (int)min((long long)O, c.n_orient - bo_base);
+            if (tid == 0) {
+                const long long run = (long long)bacc[ACC_TILE_TOTAL];
+                const long long prefix = lookback_resolve(lb, btile, run, status);
+                s_prefix = prefix;
+                if (prefix >= 0 && btile == c.n_tiles - 1) {
+                    offsets[c.n_orient] = prefix + run;
+                    *out_total = prefix + run;
+                }
+            }
+            __syncthreads();
+            const long long prefix = s_prefix;
+            if (prefix < 0) return false;  // bounded wait gave up: DS_ERR_TIMEOUT is set
+            for (int o = tid; o < bn_valid; o += SIM_THREADS)
+                offsets[bo_base + o] = prefix + (long long)bacc[o * ACC_WORDS + ACC_OFF];
+            for (int o = warp / WPO; o < bn_valid; o += SIM_WARPS / WPO) {
+                const uint32_t *row = bitmap + o * c.Ws;
+                const OrientP &op = bsop[o];
+                long long pos0 = prefix + (long long)bacc[o * ACC_WORDS + ACC_OFF];
+                for (int p = 0; p < part; ++p) pos0 += (long long)bacc[o * ACC_WORDS + ACC_PART0 + p];
+                const unsigned long long base = bacc[o * ACC_WORDS + ACC_CBASE0 + part];
+                const int cc = (int)bacc[o * ACC_WORDS + ACC_CCNT0 + part];
+                bool overflow = false;
+                if (base != NO_STAGE) {
+                    long long out_r = 0;
+                    for (int r0 = 0; r0 < cc; r0 += 32) {
+                        const int r = r0 + lane;
+                        const float I = r < cc ? b_I[base + r] : -1.f;
+                        const bool keep = !(I < 0.f);
+                        const unsigned bal = __ballot_sync(FULL_MASK, keep);
+                        if (keep) {
+                            const long long j = b_idx[base + r];
+                            const float4 e = T.scr[j];
+                            float x, y, z;
+                            if (FORM == DS_FORM_FP64) {
+                                x = (float)(op.M[0][0] * (double)e.x + op.M[0][1] * (double)e.y + op.M[0][2] * (double)e.z);
+                                y = (float)(op.M[1][0] * (double)e.x + op.M[1][1] * (double)e.y + op.M[1][2] * (double)e.z);
+                                z = (float)(op.M[2][0] * (double)e.x + op.M[2][1] * (double)e.y + op.M[2][2] * (double)e.z);
+                            } else {
+                                x = fmaf(op.m[0][0], e.x, fmaf(op.m[0][1], e.y, op.m[0][2] * e.z));
+                                y = fmaf(op.m[1][0], e.x, fmaf(op.m[1][1], e.y, op.m[1][2] * e.z));
+                                z = fmaf(op.za[0], e.x, fmaf(op.za[1], e.y, op.za[2] * e.z)) +
+                                    fmaf(op.zb[0], e.x, fmaf(op.zb[1], e.y, op.zb[2] * e.z));
+                            }
+                            const long long pos = pos0 + out_r + __popc(bal & lanemask_lt);
+                            if (pos < c.capacity) {
+                                out_idx[pos] = (int32_t)j;
+                                out_xyzi[pos] = make_float4(x, y, z, I);
+                                if (out_s) {
+                                    float I2, z2;
+                                    double sv;
+                                    eval_spot<FORM>(c, op, T, j, I2, z2, sv);
+                                    out_s[pos] = sv;
+                                }
+                            } else {
+                                overflow = true;
+                            }
+                        }
+                        out_r += __popc(bal);
+                    }
+                } else {
+                    for_each_bit(row, w0, w1, lane, [&](long long j, int rank, bool valid, int, int) {
+                        if (!valid) return;
+                        float I, z;
+                        double sv;
+                        eval_spot<FORM>(c, op, T, j, I, z, sv);
                         const float4 e = T.scr[j];
-                        float x, y, z;
+                        float x, y;
                         if (FORM == DS_FORM_FP64) {
                             x = (float)(op.M[0][0] * (double)e.x + op.M[0][1] * (double)e.y + op.M[0][2] * (double)e.z);
                             y = (float)(op.M[1][0] * (double)e.x + op.M[1][1] * (double)e.y + op.M[1][2] * (double)e.z);
-                            z = (float)(op.M[2][0] * (double)e.x + op.M[2][1] * (double)e.y + op.M[2][2] * (double)e.z);
                         } else {
                             x = fmaf(op.m[0][0], e.x, fmaf(op.m[0][1], e.y, op.m[0][2] * e.z));
                             y = fmaf(op.m[1][0], e.x, fmaf(op.m[1][1], e.y, op.m[1][2] * e.z));
-                            z = fmaf(op.m[2][0], e.x, fmaf(op.m[2][1], e.y, op.m[2][2] * e.z));
                         }
-                        const long long pos = pos0 + out_r + __popc(bal & lanemask_lt);
+                        const long long pos = pos0 + rank;
                         if (pos < c.capacity) {
                             out_idx[pos] = (int32_t)j;
                             out_xyzi[pos] = make_float4(x, y, z, I);
-                            if (out_s) {
-                                float I2, z2;
-                                double sv;
-                                eval_spot<FORM>(c, op, T, j, I2, z2, sv);
-                                out_s[pos] = sv;
-                            }
+                            if (out_s) out_s[pos] = sv;
                         } else {
                             overflow = true;
                         }
-                    }
-                    out_r += __popc(bal);
+                    });
                 }
-            } else {
-                for_each_bit(row, w0, w1, lane, [&](long long j, int rank, bool valid, int, int) {
-                    if (!valid) return;
-                    float I, z;
-                    double sv;
-                    eval_spot<FORM>(c, op, T, j, I, z, sv);
-                    const float4 e = T.scr[j];
-                    float x, y;
-                    if (FORM == DS_FORM_FP64) {
-                        x = (float)(op.M[0][0] * (double)e.x + op.M[0][1] * (double)e.y + op.M[0][2] * (double)e.z);
-                        y = (float)(op.M[1][0] * (double)e.x + op.M[1][1] * (double)e.y + op.M[1][2] * (double)e.z);
-                    } else {
-                        x = fmaf(op.m[0][0], e.x, fmaf(op.m[0][1], e.y, op.m[0][2] * e.z));
-                        y = fmaf(op.m[1][0], e.x, fmaf(op.m[1][1], e.y, op.m[1][2] * e.z));
-                    }
-                    long long pos = pos0 + rank;
-                    if (pos < c.capacity) {
-                        out_idx[pos] = (int32_t)j;
-                        out_xyzi[pos] = make_float4(x, y, z, I);
-                        if (out_s) out_s[pos] = sv;
-                    } else {
-                        overflow = true;
-                    }
-                });
+                if (__any_sync(FULL_MASK, overflow) && lane == 0) atomicOr(status, DS_ERR_CAPACITY);
             }
-            if (__any_sync(FULL_MASK, overflow) && lane == 0) atomicOr(status, DS_ERR_CAPACITY);
+            __syncthreads();  // staging / bitmap reused afterwards
+            return true;
+        };
+
+        if (pend_tile >= 0) {
+            if (!back(pend_tile, cur ^ 1)) { aborted = true; break; }
+            pend_tile = -1;
         }
-        __syncthreads();  // smem and staging are reused by the next tile
+        if (!have_new) break;
+        if (s_defer) {
+            pend_tile = tile;
+            cur ^= 1;
+        } else if (!back(tile, cur)) {
+            aborted = true;
+            break;
+        }
     }
+    (void)aborted;
 }
 
 // ------------------------------------------------------------- host side ----
@@ -740,9 +845,9 @@ static ds_status make_plan(const ds_sim_params *p, const ds_phase_table *t, long
     o = align_up(o, 256);
     P.off_g2 = o; o += (size_t)t->n_hkl * sizeof(float2);
     o = align_up(o, 256);
-    P.off_sidx = o; o += (size_t)(P.grid * P.stage_cap) * sizeof(int32_t);
+    P.off_sidx = o; o += (size_t)(2 * P.grid * P.stage_cap) * sizeof(int32_t);  // two pipeline slots per CTA
     o = align_up(o, 256);
-    P.off_sI = o; o += (size_t)(P.grid * P.stage_cap) * sizeof(float);
+    P.off_sI = o; o += (size_t)(2 * P.grid * P.stage_cap) * sizeof(float);
     P.total = align_up(o, 256);
     return DS_OK;
 }
@@ -848,6 +953,7 @@ extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t
     c.O = P.O;
     c.W = P.W;
     c.Ws = P.Ws;
+    for (int i = 0; i < 3; ++i) c.hmax[i] = t->hmax[i] > 0 ? t->hmax[i] : 1;
     c.n_hkl = t->n_hkl;
     c.n_orient = n_orient;
     c.n_tiles = P.n_tiles;
