@@ -272,27 +272,78 @@ struct TableP {
     const double *F2d;
 };
 
+// One candidate's table data, loaded ahead of its evaluation.
+struct SpotIn {
+    float4 e;    // h, k, l, -z_mid
+    float2 g2;   // |g|^2 as an FP32 pair
+    float F2;    // |F|^2 (mixed)
+    double F2d;  // |F|^2 (FP64 form)
+};
+template <int FORM>
+__device__ __forceinline__ SpotIn load_spot(const TableP &T, long long j) {
+    SpotIn in;
+    in.e = T.scr[j];
+    if (FORM == DS_FORM_FP64) {
+        in.F2d = T.F2d[j];
+    } else {
+        in.g2 = T.g2dd[j];
+        in.F2 = T.F2[j];
+    }
+    return in;
+}
+
 // Evaluate one screened candidate: selection, intensity, beam-frame z.
 template <int FORM>
-__device__ inline bool eval_spot(const SimConst &c, const OrientP &op, const TableP &T, long long j, float &I,
-                                 float &zout, double &sout) {
-    const float4 e = T.scr[j];
+__device__ inline bool eval_in(const SimConst &c, const OrientP &op, const SpotIn &in, float &I, float &zout,
+                               double &sout) {
+    const float4 &e = in.e;
     if (FORM == DS_FORM_FP64) {
         double s, r, z;
         bool sel = select_fp64(c, op, (double)e.x, (double)e.y, (double)e.z, s, r, z);
-        I = (float)(shape_fp64(c, s, r) * T.F2d[j]);
+        I = (float)(shape_fp64(c, s, r) * in.F2d);
         zout = (float)z;
         sout = s;
         return sel;
     } else {
         dd s;
         float r, z;
-        bool sel = select_mixed(c, op, e, T.g2dd[j], s, r, z);
-        I = shape_mixed(c, s, r) * T.F2[j];
+        bool sel = select_mixed(c, op, e, in.g2, s, r, z);
+        I = shape_mixed(c, s, r) * in.F2;
         zout = z;
         sout = (double)s.hi + (double)s.lo;
         return sel;
     }
+}
+
+template <int FORM>
+__device__ inline bool eval_spot(const SimConst &c, const OrientP &op, const TableP &T, long long j, float &I,
+                                 float &zout, double &sout) {
+    return eval_in<FORM>(c, op, load_spot<FORM>(T, j), I, zout, sout);
+}
+
+template <int FORM>
+__device__ __forceinline__ void spot_xy(const OrientP &op, const float4 &e, float &x, float &y) {
+    if (FORM == DS_FORM_FP64) {
+        x = (float)(op.M[0][0] * (double)e.x + op.M[0][1] * (double)e.y + op.M[0][2] * (double)e.z);
+        y = (float)(op.M[1][0] * (double)e.x + op.M[1][1] * (double)e.y + op.M[1][2] * (double)e.z);
+    } else {
+        x = fmaf(op.m[0][0], e.x, fmaf(op.m[0][1], e.y, op.m[0][2] * e.z));
+        y = fmaf(op.m[1][0], e.x, fmaf(op.m[1][1], e.y, op.m[1][2] * e.z));
+    }
+}
+
+// 32x32 bit-matrix transpose across a warp: on return bit r of lane c is
+// bit c of lane r on entry (recursive block swap, 5 butterfly stages).
+__device__ __forceinline__ uint32_t transpose32(uint32_t x, int lane) {
+    const uint32_t masks[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+    for (int st = 0; st < 5; ++st) {
+        const int w = 16 >> st;
+        const uint32_t m = masks[st];
+        const uint32_t y = __shfl_xor_sync(FULL_MASK, x, w);
+        x = (lane & w) ? ((x & ~m) | ((y >> w) & m)) : ((x & m) | ((y << w) & ~m));
+    }
+    return x;
 }
 
 __device__ __forceinline__ int owner_lane(int incl, int q) {
@@ -332,10 +383,33 @@ __device__ __forceinline__ void for_each_bit(const uint32_t *row, int w0, int w1
     }
 }
 
-// As for_each_bit, with K consecutive words per lane (groups of 32 K words),
-// so that sparse bitmaps still fill most lanes of each 32-candidate batch.
+// Set bits of bitmap words [w0, w1) of one orientation in row order, with K
+// consecutive words per lane (groups of 32 K words) so sparse bitmaps still
+// fill the lanes, and two candidates per lane per step (q and q + 32) so the
+// table loads of both are in flight together.  fn(j0, rank0, valid0, j1,
+// rank1, valid1) is called by every lane.
+template <int K>
+__device__ __forceinline__ void locate_bit(const uint32_t (&wd)[K], int incl, int cnt, int total, int q, int g0,
+                                           long long &j, bool &valid) {
+    valid = q < total;
+    const int own = owner_lane(incl, valid ? q : total - 1);
+    const int n = q - (__shfl_sync(FULL_MASK, incl, own) - __shfl_sync(FULL_MASK, cnt, own));
+    uint32_t word = 0;
+    int wsel = 0, before = 0, run = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const uint32_t ow = __shfl_sync(FULL_MASK, wd[k], own);
+        const int pc = __popc(ow);
+        if (n >= run && n < run + pc) { word = ow; wsel = k; before = run; }
+        run += pc;
+    }
+    int bit = 0;
+    if (valid) bit = (int)__fns(word, 0, n - before + 1);
+    j = (long long)(g0 + own * K + wsel) * 32 + bit;
+}
+
 template <int K, typename Fn>
-__device__ __forceinline__ void for_each_bit_k(const uint32_t *row, int w0, int w1, int lane, Fn fn) {
+__device__ __forceinline__ void for_each_bit_pair(const uint32_t *row, int w0, int w1, int lane, Fn fn) {
     int base_rank = 0;
     for (int g0 = w0; g0 < w1; g0 += 32 * K) {
         uint32_t wd[K];
@@ -348,24 +422,12 @@ __device__ __forceinline__ void for_each_bit_k(const uint32_t *row, int w0, int 
         }
         const int incl = warp_inclusive_scan(cnt, lane);
         const int total = __shfl_sync(FULL_MASK, incl, 31);
-        for (int q0 = 0; q0 < total; q0 += 32) {
-            const int q = q0 + lane;
-            const bool valid = q < total;
-            const int own = owner_lane(incl, valid ? q : total - 1);
-            const int n = q - (__shfl_sync(FULL_MASK, incl, own) - __shfl_sync(FULL_MASK, cnt, own));
-            uint32_t word = 0;
-            int wsel = 0, before = 0, run = 0;
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
-                const uint32_t ow = __shfl_sync(FULL_MASK, wd[k], own);
-                const int pc = __popc(ow);
-                if (n >= run && n < run + pc) { word = ow; wsel = k; before = run; }
-                run += pc;
-            }
-            int bit = 0;
-            if (valid) bit = (int)__fns(word, 0, n - before + 1);
-            const int wi = g0 + own * K + wsel;
-            fn((long long)wi * 32 + bit, base_rank + q, valid, wi, bit);
+        for (int q0 = 0; q0 < total; q0 += 64) {
+            long long ja, jb;
+            bool va, vb;
+            locate_bit<K>(wd, incl, cnt, total, q0 + lane, g0, ja, va);
+            locate_bit<K>(wd, incl, cnt, total, q0 + 32 + lane, g0, jb, vb);
+            fn(ja, base_rank + q0 + lane, va, jb, base_rank + q0 + 32 + lane, vb);
         }
         base_rank += total;
     }
@@ -377,9 +439,9 @@ __device__ __forceinline__ void for_each_bit_k(const uint32_t *row, int w0, int 
 // only gathers.  Orientation parts that do not fit fall back to walking the
 // bitmap and re-evaluating.
 struct StageP {
-    int32_t *idx;
-    float *inten;
-    long long cap;  // entries per CTA
+    int32_t *idx;    // table row
+    float4 *rec;     // x, y, z, I (I = -1: not a spot)
+    long long cap;   // entries per pipeline slot
 };
 constexpr unsigned long long NO_STAGE = ~0ull;
 
@@ -420,7 +482,7 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
         OrientP *sop = sop_buf + cur * O;
         unsigned long long *acc = acc_buf + cur * ACC_STRIDE;
         int32_t *my_idx = stg.idx + (2 * (long long)blockIdx.x + cur) * stg.cap;
-        float *my_I = stg.inten + (2 * (long long)blockIdx.x + cur) * stg.cap;
+        float4 *my_rec = stg.rec + (2 * (long long)blockIdx.x + cur) * stg.cap;
         for (int i = tid; i < ACC_STRIDE; i += SIM_THREADS)
             acc[i] = (i < ACC_TILE_TOTAL && i % ACC_WORDS == ACC_MINPOS) ? (unsigned long long)__float_as_uint(INFINITY)
                                                                           : 0ull;
@@ -500,15 +562,20 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
                         uint32_t b = __ballot_sync(FULL_MASK, hit);
                         if (lane == o) myword = b;
                     }
+                    if (lane < O) bitmap[lane * c.Ws + wc] = myword;
                 } else {
+                    // sign bit of |z - z_mid| - z_half per orientation, collected
+                    // into one word per lane (bit O-1-o), then a 32x32 bit
+                    // transpose hands lane O-1-o the word of orientation o
+                    uint32_t bits = 0;
 #pragma unroll
                     for (int o = 0; o < O; ++o) {
-                        float z = fmaf(m0[o], e.x, fmaf(m1[o], e.y, fmaf(m2[o], e.z, e.w)));
-                        uint32_t b = __ballot_sync(FULL_MASK, fabsf(z) < zh);
-                        if (lane == o) myword = b;
+                        const float z = fmaf(m0[o], e.x, fmaf(m1[o], e.y, fmaf(m2[o], e.z, e.w)));
+                        bits = __funnelshift_l(__float_as_uint(fabsf(z) - zh), bits, 1);
                     }
+                    bits = transpose32(bits, lane);
+                    if (lane < O) bitmap[(O - 1 - lane) * c.Ws + wc] = bits;
                 }
-                if (lane < O) bitmap[lane * c.Ws + wc] = myword;
             }
         }
         __syncthreads();
@@ -547,20 +614,32 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
             float lmax = 0.f, lminpos = INFINITY;
             int lcnt = 0;
             if (base != NO_STAGE) {
-                // evaluate each screened candidate once; keep (row, I or -1) in
-                // candidate order for the write pass
-                for_each_bit_k<4>(row, w0, w1, lane, [&](long long j, int rank, bool valid, int, int) {
-                    if (!valid) return;
-                    float I, z;
-                    double sv;
-                    bool sel = eval_spot<FORM>(c, op, T, j, I, z, sv);
-                    if (sel && I == 0.f && all_zero_drop) sel = false;
-                    my_idx[base + rank] = (int32_t)j;
-                    my_I[base + rank] = sel ? I : -1.f;
-                    if (sel) {
-                        ++lcnt;
-                        lmax = fmaxf(lmax, I);
-                        if (I > 0.f) lminpos = fminf(lminpos, I);
+                // evaluate each screened candidate once; stage (row, x, y, z, I)
+                // in candidate order, I = -1 for rejected candidates
+                for_each_bit_pair<4>(row, w0, w1, lane,
+                                     [&](long long ja, int ra, bool va, long long jb, int rb, bool vb) {
+                    SpotIn ia, ib;
+                    if (va) ia = load_spot<FORM>(T, ja);
+                    if (vb) ib = load_spot<FORM>(T, jb);
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const bool v = h ? vb : va;
+                        if (!v) continue;
+                        const SpotIn &in = h ? ib : ia;
+                        float I, z;
+                        double sv;
+                        bool sel = eval_in<FORM>(c, op, in, I, z, sv);
+                        if (sel && I == 0.f && all_zero_drop) sel = false;
+                        float x, y;
+                        spot_xy<FORM>(op, in.e, x, y);
+                        const int rk = h ? rb : ra;
+                        my_idx[base + rk] = (int32_t)(h ? jb : ja);
+                        my_rec[base + rk] = make_float4(x, y, z, sel ? I : -1.f);
+                        if (sel) {
+                            ++lcnt;
+                            lmax = fmaxf(lmax, I);
+                            if (I > 0.f) lminpos = fminf(lminpos, I);
+                        }
                     }
                 });
             } else {
@@ -608,9 +687,9 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
             int dropped = 0;
             if (base != NO_STAGE) {
                 for (int r = lane; r < cc; r += 32) {
-                    const float I = my_I[base + r];
+                    const float I = my_rec[base + r].w;
                     if (!(I < 0.f) && !((double)I > (double)mx * c.thr)) {
-                        my_I[base + r] = -1.f;
+                        my_rec[base + r].w = -1.f;
                         ++dropped;
                     }
                 }
@@ -658,7 +737,7 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
             const OrientP *bsop = sop_buf + bbuf * O;
             const unsigned long long *bacc = acc_buf + bbuf * ACC_STRIDE;
             const int32_t *b_idx = stg.idx + (2 * (long long)blockIdx.x + bbuf) * stg.cap;
-            const float *b_I = stg.inten + (2 * (long long)blockIdx.x + bbuf) * stg.cap;
+            const float4 *b_rec = stg.rec + (2 * (long long)blockIdx.x + bbuf) * stg.cap;
             const long long bo_base = btile * O;
             const int bn_valid = (int)min((long long)O, c.n_orient - bo_base);
             if (tid == 0) {
@@ -684,41 +763,42 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
                 const int cc = (int)bacc[o * ACC_WORDS + ACC_CCNT0 + part];
                 bool overflow = false;
                 if (base != NO_STAGE) {
+                    // compaction copy of the staged records, four batches in flight
                     long long out_r = 0;
-                    for (int r0 = 0; r0 < cc; r0 += 32) {
-                        const int r = r0 + lane;
-                        const float I = r < cc ? b_I[base + r] : -1.f;
-                        const bool keep = !(I < 0.f);
-                        const unsigned bal = __ballot_sync(FULL_MASK, keep);
-                        if (keep) {
-                            const long long j = b_idx[base + r];
-                            const float4 e = T.scr[j];
-                            float x, y, z;
-                            if (FORM == DS_FORM_FP64) {
-                                x = (float)(op.M[0][0] * (double)e.x + op.M[0][1] * (double)e.y + op.M[0][2] * (double)e.z);
-                                y = (float)(op.M[1][0] * (double)e.x + op.M[1][1] * (double)e.y + op.M[1][2] * (double)e.z);
-                                z = (float)(op.M[2][0] * (double)e.x + op.M[2][1] * (double)e.y + op.M[2][2] * (double)e.z);
-                            } else {
-                                x = fmaf(op.m[0][0], e.x, fmaf(op.m[0][1], e.y, op.m[0][2] * e.z));
-                                y = fmaf(op.m[1][0], e.x, fmaf(op.m[1][1], e.y, op.m[1][2] * e.z));
-                                z = fmaf(op.za[0], e.x, fmaf(op.za[1], e.y, op.za[2] * e.z)) +
-                                    fmaf(op.zb[0], e.x, fmaf(op.zb[1], e.y, op.zb[2] * e.z));
-                            }
-                            const long long pos = pos0 + out_r + __popc(bal & lanemask_lt);
-                            if (pos < c.capacity) {
-                                out_idx[pos] = (int32_t)j;
-                                out_xyzi[pos] = make_float4(x, y, z, I);
-                                if (out_s) {
-                                    float I2, z2;
-                                    double sv;
-                                    eval_spot<FORM>(c, op, T, j, I2, z2, sv);
-                                    out_s[pos] = sv;
-                                }
-                            } else {
-                                overflow = true;
+                    for (int r0 = 0; r0 < cc; r0 += 128) {
+                        float4 rec[4];
+                        int32_t jj[4];
+#pragma unroll
+                        for (int b = 0; b < 4; ++b) {
+                            const int r = r0 + 32 * b + lane;
+                            rec[b] = make_float4(0.f, 0.f, 0.f, -1.f);
+                            jj[b] = 0;
+                            if (r < cc) {
+                                rec[b] = b_rec[base + r];
+                                jj[b] = b_idx[base + r];
                             }
                         }
-                        out_r += __popc(bal);
+#pragma unroll
+                        for (int b = 0; b < 4; ++b) {
+                            const bool keep = !(rec[b].w < 0.f);
+                            const unsigned bal = __ballot_sync(FULL_MASK, keep);
+                            if (keep) {
+                                const long long pos = pos0 + out_r + __popc(bal & lanemask_lt);
+                                if (pos < c.capacity) {
+                                    out_idx[pos] = jj[b];
+                                    out_xyzi[pos] = rec[b];
+                                    if (out_s) {
+                                        float I2, z2;
+                                        double sv;
+                                        eval_spot<FORM>(c, op, T, jj[b], I2, z2, sv);
+                                        out_s[pos] = sv;
+                                    }
+                                } else {
+                                    overflow = true;
+                                }
+                            }
+                            out_r += __popc(bal);
+                        }
                     }
                 } else {
                     for_each_bit(row, w0, w1, lane, [&](long long j, int rank, bool valid, int, int) {
@@ -770,7 +850,7 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
 // ------------------------------------------------------------- host side ----
 static inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
-constexpr long long STAGE_CAP = 32768;  // staged candidates per CTA (8 bytes each)
+constexpr long long STAGE_CAP = 24576;  // staged candidates per pipeline slot (20 bytes each)
 
 struct SimPlan {
     int O, W, Ws;
@@ -847,7 +927,7 @@ static ds_status make_plan(const ds_sim_params *p, const ds_phase_table *t, long
     o = align_up(o, 256);
     P.off_sidx = o; o += (size_t)(2 * P.grid * P.stage_cap) * sizeof(int32_t);  // two pipeline slots per CTA
     o = align_up(o, 256);
-    P.off_sI = o; o += (size_t)(2 * P.grid * P.stage_cap) * sizeof(float);
+    P.off_sI = o; o += (size_t)(2 * P.grid * P.stage_cap) * sizeof(float4);
     P.total = align_up(o, 256);
     return DS_OK;
 }
@@ -976,7 +1056,7 @@ extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t
     LookbackScratch lb = lookback_scratch(sb + P.off_lb);
     StageP stg;
     stg.idx = reinterpret_cast<int32_t *>(sb + P.off_sidx);
-    stg.inten = reinterpret_cast<float *>(sb + P.off_sI);
+    stg.rec = reinterpret_cast<float4 *>(sb + P.off_sI);
     stg.cap = P.stage_cap;
     if (p->form == DS_FORM_FP64) {
         switch (P.O) {
