@@ -346,6 +346,18 @@ __device__ __forceinline__ uint32_t transpose32(uint32_t x, int lane) {
     return x;
 }
 
+// Position of the n-th (0-based) set bit of w, n < popc(w): a popcount
+// bisection over halves, quarters, ... (branch-free selects).
+__device__ __forceinline__ int nth_set_bit(uint32_t w, int n) {
+    int pos = 0, c;
+    c = __popc(w & 0xFFFFu); if (n >= c) { n -= c; w >>= 16; pos += 16; }
+    c = __popc(w & 0xFFu);   if (n >= c) { n -= c; w >>= 8;  pos += 8; }
+    c = __popc(w & 0xFu);    if (n >= c) { n -= c; w >>= 4;  pos += 4; }
+    c = __popc(w & 0x3u);    if (n >= c) { n -= c; w >>= 2;  pos += 2; }
+    c = (int)(w & 1u);       if (n >= c) { pos += 1; }
+    return pos;
+}
+
 __device__ __forceinline__ int owner_lane(int incl, int q) {
     int lo = 0;
 #pragma unroll
@@ -375,7 +387,7 @@ __device__ __forceinline__ void for_each_bit(const uint32_t *row, int w0, int w1
             uint32_t ow = __shfl_sync(FULL_MASK, word, own);
             int oin = __shfl_sync(FULL_MASK, incl, own);
             int bit = 0;
-            if (valid) bit = (int)__fns(ow, 0, q - (oin - __popc(ow)) + 1);
+            if (valid) bit = nth_set_bit(ow, q - (oin - __popc(ow)));
             long long j = (long long)(g0 + own) * 32 + bit;
             fn(j, base_rank + q, valid, g0 + own, bit);
         }
@@ -404,7 +416,7 @@ __device__ __forceinline__ void locate_bit(const uint32_t (&wd)[K], int incl, in
         run += pc;
     }
     int bit = 0;
-    if (valid) bit = (int)__fns(word, 0, n - before + 1);
+    if (valid) bit = nth_set_bit(word, n - before);
     j = (long long)(g0 + own * K + wsel) * 32 + bit;
 }
 
@@ -452,21 +464,30 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
                 int64_t *__restrict__ out_total, LookbackScratch lb, StageP stg, int32_t *status) {
     extern __shared__ __align__(16) unsigned char smem[];
     const SimSmem Ls = sim_smem_layout(O, c.Ws);
-    OrientP *sop_buf = reinterpret_cast<OrientP *>(smem + Ls.orient);  // [2][O]
-    unsigned long long *acc_buf = reinterpret_cast<unsigned long long *>(smem + Ls.acc);  // [2][O * ACC_WORDS]
-    uint32_t *bitmap = reinterpret_cast<uint32_t *>(smem + Ls.bitmap);
+    OrientP *sop_buf = reinterpret_cast<OrientP *>(smem + Ls.orient);                  // [2][O]
+    unsigned long long *acc_buf = reinterpret_cast<unsigned long long *>(smem + Ls.acc);  // [2][ACC_STRIDE]
+    uint32_t *bitmap = reinterpret_cast<uint32_t *>(smem + Ls.bitmap);                   // [O][Ws]
     __shared__ long long s_tile, s_prefix;
     __shared__ int s_defer;
+    __shared__ int s_unit[4];  // work-unit counters of the dynamic phases
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     constexpr int ACC_STRIDE = acc_stride(O);
     constexpr int ACC_TILE_TOTAL = O * ACC_WORDS;
-    // work split for phases 2-3: WPO warps share one orientation's words
-    constexpr int WPO = O >= SIM_WARPS ? 1 : SIM_WARPS / O;
-    const int part = warp % WPO;
-    const int w0 = (int)(((long long)c.W * part) / WPO), w1 = (int)(((long long)c.W * (part + 1)) / WPO);
+    // phases 2-3 run over units (orientation, part): NP word ranges per
+    // orientation, taken by warps from a shared counter for load balance
+    constexpr int NP = O >= 2 ? 4 : 8;
     const bool all_zero_drop = c.thr >= 0.0;
     const unsigned lanemask_lt = (1u << lane) - 1u;
+    auto part_range = [&](int p, int &w0, int &w1) {
+        w0 = (int)(((long long)c.W * p) / NP);
+        w1 = (int)(((long long)c.W * (p + 1)) / NP);
+    };
+    auto next_unit = [&](int k) -> int {
+        int u = 0;
+        if (lane == 0) u = atomicAdd(&s_unit[k], 1);
+        return __shfl_sync(FULL_MASK, u, 0);
+    };
 
     // Two-stage software pipeline over tiles: a tile is screened and refined
     // (front), its count published, and its look-back and writes (back) run
@@ -476,9 +497,9 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
     // once.  Buffers (orientations, accumulators, staging) alternate.
     int cur = 0;
     long long pend_tile = -1;
-    bool aborted = false;
     for (;;) {
         if (tid == 0) s_tile = (long long)atomicAdd(lb.ticket, 1ull);
+        if (tid < 4) s_unit[tid] = 0;
         OrientP *sop = sop_buf + cur * O;
         unsigned long long *acc = acc_buf + cur * ACC_STRIDE;
         int32_t *my_idx = stg.idx + (2 * (long long)blockIdx.x + cur) * stg.cap;
@@ -491,110 +512,119 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
         const bool have_new = tile < c.n_tiles;
         const long long o_base = tile * O;
         const int n_valid = have_new ? (int)min((long long)O, c.n_orient - o_base) : 0;
+        const int n_units = n_valid * NP;
         if (have_new) {
-
-        // per-orientation rotation: beam frame = g @ R, R the active matrix of q
-        if (tid < O) {
-            OrientP &op = sop[tid];
-            double R[3][3];
-            if (tid < n_valid) {
-                const double *q = quats + 4 * (o_base + tid);
-                double w = q[0], x = q[1], y = q[2], z = q[3];
-                double nrm = sqrt(w * w + x * x + y * y + z * z);
-                if (!(nrm > 0) || !isfinite(nrm)) { atomicOr(status, DS_ERR_NONFINITE); nrm = 1; w = 1; x = y = z = 0; }
-                w /= nrm; x /= nrm; y /= nrm; z /= nrm;
-                R[0][0] = 1 - 2 * (y * y + z * z); R[0][1] = 2 * (x * y - w * z); R[0][2] = 2 * (x * z + w * y);
-                R[1][0] = 2 * (x * y + w * z); R[1][1] = 1 - 2 * (x * x + z * z); R[1][2] = 2 * (y * z - w * x);
-                R[2][0] = 2 * (x * z - w * y); R[2][1] = 2 * (y * z + w * x); R[2][2] = 1 - 2 * (x * x + y * y);
-            } else {
-                for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) R[a][b] = 0.0;
-            }
-            for (int cc = 0; cc < 3; ++cc)
-                for (int i = 0; i < 3; ++i) {
-                    double v = c.recip[3 * i + 0] * R[0][cc] + c.recip[3 * i + 1] * R[1][cc] + c.recip[3 * i + 2] * R[2][cc];
-                    op.M[cc][i] = v;
-                    op.m[cc][i] = (float)v;
-                }
-            // exact-product split of the z column: grid 2^q with 2^(q+24) >= 2 sum_i |M_zi| hmax_i
-            double Z = 0.0;
-            for (int i = 0; i < 3; ++i) Z += fabs(op.M[2][i]) * (double)c.hmax[i];
-            const int q = (Z > 0.0 ? ilogb(Z) : -100) + 2 - 24;
-            for (int i = 0; i < 3; ++i) {
-                const double a = ldexp(rint(ldexp(op.M[2][i], -q)), q);
-                op.za[i] = (float)a;
-                op.zb[i] = (float)(op.M[2][i] - a);
-            }
-        }
-        __syncthreads();
-
-        // ---------------- phase 1: screen every row against all O orientations
-        {
-            float m0[O], m1[O], m2[O];
-#pragma unroll
-            for (int o = 0; o < O; ++o) { m0[o] = sop[o].m[2][0]; m1[o] = sop[o].m[2][1]; m2[o] = sop[o].m[2][2]; }
-            // rows of chunks wc + 8 and wc + 16 are in flight while chunk wc is screened
-            float4 e1 = make_float4(0.f, 0.f, 0.f, 0.f), e2 = e1;
-            float z1 = -1.f, z2 = -1.f;
-            {
-                const long long j1 = (long long)warp * 32 + lane, j2 = j1 + 32 * SIM_WARPS;
-                if (j1 < c.n_hkl) { e1 = T.scr[j1]; z1 = T.zh[j1]; }
-                if (j2 < c.n_hkl) { e2 = T.scr[j2]; z2 = T.zh[j2]; }
-            }
-            for (int wc = warp; wc < c.W; wc += SIM_WARPS) {
-                const long long j = (long long)wc * 32 + lane;
-                const float4 e = e1;
-                const float zh = z1;
-                e1 = e2;
-                z1 = z2;
-                {
-                    const long long jn = j + 64 * SIM_WARPS;
-                    e2 = make_float4(0.f, 0.f, 0.f, 0.f);
-                    z2 = -1.f;
-                    if (jn < c.n_hkl) { e2 = T.scr[jn]; z2 = T.zh[jn]; }
-                }
-                uint32_t myword = 0;
-                if (FORM == DS_FORM_FP64) {
-                    double hd = e.x, kd = e.y, ld = e.z;
-#pragma unroll 1
-                    for (int o = 0; o < O; ++o) {
-                        double s, r, z;
-                        bool hit = (j < c.n_hkl) && (o < n_valid) && select_fp64(c, sop[o], hd, kd, ld, s, r, z);
-                        uint32_t b = __ballot_sync(FULL_MASK, hit);
-                        if (lane == o) myword = b;
+            // ---------------- per-orientation rotation: beam frame = g @ R, R the active matrix of q
+            if (tid < O) {
+                OrientP &op = sop[tid];
+                double R[3][3];
+                if (tid < n_valid) {
+                    const double *q = quats + 4 * (o_base + tid);
+                    double w = q[0], x = q[1], y = q[2], z = q[3];
+                    double nrm = sqrt(w * w + x * x + y * y + z * z);
+                    if (!(nrm > 0) || !isfinite(nrm)) {
+                        atomicOr(status, DS_ERR_NONFINITE);
+                        nrm = 1; w = 1; x = y = z = 0;
                     }
-                    if (lane < O) bitmap[lane * c.Ws + wc] = myword;
+                    w /= nrm; x /= nrm; y /= nrm; z /= nrm;
+                    R[0][0] = 1 - 2 * (y * y + z * z); R[0][1] = 2 * (x * y - w * z); R[0][2] = 2 * (x * z + w * y);
+                    R[1][0] = 2 * (x * y + w * z); R[1][1] = 1 - 2 * (x * x + z * z); R[1][2] = 2 * (y * z - w * x);
+                    R[2][0] = 2 * (x * z - w * y); R[2][1] = 2 * (y * z + w * x); R[2][2] = 1 - 2 * (x * x + y * y);
                 } else {
-                    // sign bit of |z - z_mid| - z_half per orientation, collected
-                    // into one word per lane (bit O-1-o), then a 32x32 bit
-                    // transpose hands lane O-1-o the word of orientation o
-                    uint32_t bits = 0;
-#pragma unroll
-                    for (int o = 0; o < O; ++o) {
-                        const float z = fmaf(m0[o], e.x, fmaf(m1[o], e.y, fmaf(m2[o], e.z, e.w)));
-                        bits = __funnelshift_l(__float_as_uint(fabsf(z) - zh), bits, 1);
+                    for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) R[a][b] = 0.0;
+                }
+                for (int cc = 0; cc < 3; ++cc)
+                    for (int i = 0; i < 3; ++i) {
+                        double v = c.recip[3 * i] * R[0][cc] + c.recip[3 * i + 1] * R[1][cc] + c.recip[3 * i + 2] * R[2][cc];
+                        op.M[cc][i] = v;
+                        op.m[cc][i] = (float)v;
                     }
-                    bits = transpose32(bits, lane);
-                    if (lane < O) bitmap[(O - 1 - lane) * c.Ws + wc] = bits;
+                // exact-product split of the z column: grid 2^q with 2^(q+24) >= 2 sum_i |M_zi| hmax_i
+                double Z = 0.0;
+                for (int i = 0; i < 3; ++i) Z += fabs(op.M[2][i]) * (double)c.hmax[i];
+                const int q = (Z > 0.0 ? ilogb(Z) : -100) + 2 - 24;
+                for (int i = 0; i < 3; ++i) {
+                    const double a = ldexp(rint(ldexp(op.M[2][i], -q)), q);
+                    op.za[i] = (float)a;
+                    op.zb[i] = (float)(op.M[2][i] - a);
                 }
             }
-        }
-        __syncthreads();
+            __syncthreads();
 
-        // ---------------- candidate counts per (orientation, part) and staging bases
-        for (int o = warp / WPO; o < n_valid; o += SIM_WARPS / WPO) {
-            const uint32_t *row = bitmap + o * c.Ws;
-            int cnt = 0;
-            for (int wi = w0 + lane; wi < w1; wi += 32) cnt += __popc(row[wi]);
+            // ---------------- phase 1: screen every row against all O orientations
+            {
+                float m0[O], m1[O], m2[O];
 #pragma unroll
-            for (int d = 16; d >= 1; d >>= 1) cnt += __shfl_xor_sync(FULL_MASK, cnt, d);
-            if (lane == 0) acc[o * ACC_WORDS + ACC_CCNT0 + part] = (unsigned long long)cnt;
-        }
-        __syncthreads();
-        if (tid == 0) {
-            long long run = 0;
-            for (int o = 0; o < n_valid; ++o)
-                for (int p = 0; p < WPO; ++p) {
-                    long long cc = (long long)acc[o * ACC_WORDS + ACC_CCNT0 + p];
+                for (int o = 0; o < O; ++o) { m0[o] = sop[o].m[2][0]; m1[o] = sop[o].m[2][1]; m2[o] = sop[o].m[2][2]; }
+                // rows of chunks wc + 8, wc + 16 and wc + 24 are in flight while chunk wc is screened
+                constexpr int PF = 3;
+                float4 ep[PF];
+                float zp[PF];
+#pragma unroll
+                for (int k = 0; k < PF; ++k) {
+                    const long long jk = ((long long)warp + k * SIM_WARPS) * 32 + lane;
+                    ep[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    zp[k] = -1.f;
+                    if (jk < c.n_hkl) { ep[k] = T.scr[jk]; zp[k] = T.zh[jk]; }
+                }
+                for (int wc = warp; wc < c.W; wc += SIM_WARPS) {
+                    const long long j = (long long)wc * 32 + lane;
+                    const float4 e = ep[0];
+                    const float zh = zp[0];
+#pragma unroll
+                    for (int k = 0; k + 1 < PF; ++k) { ep[k] = ep[k + 1]; zp[k] = zp[k + 1]; }
+                    {
+                        const long long jn = j + 32LL * SIM_WARPS * PF;
+                        ep[PF - 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+                        zp[PF - 1] = -1.f;
+                        if (jn < c.n_hkl) { ep[PF - 1] = T.scr[jn]; zp[PF - 1] = T.zh[jn]; }
+                    }
+                    if (FORM == DS_FORM_FP64) {
+                        uint32_t myword = 0;
+                        const double hd = e.x, kd = e.y, ld = e.z;
+#pragma unroll 1
+                        for (int o = 0; o < O; ++o) {
+                            double sx, rx, zx;
+                            const bool hit = (j < c.n_hkl) && (o < n_valid) && select_fp64(c, sop[o], hd, kd, ld, sx, rx, zx);
+                            const uint32_t b = __ballot_sync(FULL_MASK, hit);
+                            if (lane == o) myword = b;
+                        }
+                        if (lane < O) bitmap[lane * c.Ws + wc] = myword;
+                    } else {
+                        // sign bit of |z - z_mid| - z_half per orientation, collected
+                        // into one word per lane (bit O-1-o), then a 32x32 bit
+                        // transpose hands lane O-1-o the word of orientation o
+                        uint32_t bits = 0;
+#pragma unroll
+                        for (int o = 0; o < O; ++o) {
+                            const float z = fmaf(m0[o], e.x, fmaf(m1[o], e.y, fmaf(m2[o], e.z, e.w)));
+                            bits = __funnelshift_l(__float_as_uint(fabsf(z) - zh), bits, 1);
+                        }
+                        bits = transpose32(bits, lane);
+                        if (lane < O) bitmap[(O - 1 - lane) * c.Ws + wc] = bits;
+                    }
+                }
+            }
+            __syncthreads();
+
+            // ---------------- candidate counts per unit and staging bases
+            for (int u = warp; u < n_units; u += SIM_WARPS) {
+                const int o = u / NP, p = u % NP;
+                int w0, w1;
+                part_range(p, w0, w1);
+                const uint32_t *row = bitmap + o * c.Ws;
+                int cnt = 0;
+                for (int wi = w0 + lane; wi < w1; wi += 32) cnt += __popc(row[wi]);
+#pragma unroll
+                for (int d = 16; d >= 1; d >>= 1) cnt += __shfl_xor_sync(FULL_MASK, cnt, d);
+                if (lane == 0) acc[o * ACC_WORDS + ACC_CCNT0 + p] = (unsigned long long)cnt;
+            }
+            __syncthreads();
+            if (tid == 0) {
+                long long run = 0;
+                for (int u = 0; u < n_units; ++u) {
+                    const int o = u / NP, p = u % NP;
+                    const long long cc = (long long)acc[o * ACC_WORDS + ACC_CCNT0 + p];
                     if (run + cc <= stg.cap) {
                         acc[o * ACC_WORDS + ACC_CBASE0 + p] = (unsigned long long)run;
                         run += cc;
@@ -602,138 +632,144 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
                         acc[o * ACC_WORDS + ACC_CBASE0 + p] = NO_STAGE;
                     }
                 }
-        }
-        __syncthreads();
+            }
+            __syncthreads();
 
-        // ---------------- phase 2: refine, intensities, per-orientation max
-        for (int o = warp / WPO; o < n_valid; o += SIM_WARPS / WPO) {
-            uint32_t *row = bitmap + o * c.Ws;
-            const OrientP &op = sop[o];
-            const unsigned long long base = acc[o * ACC_WORDS + ACC_CBASE0 + part];
-            const int cc = (int)acc[o * ACC_WORDS + ACC_CCNT0 + part];
-            float lmax = 0.f, lminpos = INFINITY;
-            int lcnt = 0;
-            if (base != NO_STAGE) {
-                // evaluate each screened candidate once; stage (row, x, y, z, I)
-                // in candidate order, I = -1 for rejected candidates
-                for_each_bit_pair<4>(row, w0, w1, lane,
-                                     [&](long long ja, int ra, bool va, long long jb, int rb, bool vb) {
-                    SpotIn ia, ib;
-                    if (va) ia = load_spot<FORM>(T, ja);
-                    if (vb) ib = load_spot<FORM>(T, jb);
+            // ---------------- phase 2: refine, intensities, per-orientation max
+            for (int u = next_unit(0); u < n_units; u = next_unit(0)) {
+                const int o = u / NP, p = u % NP;
+                int w0, w1;
+                part_range(p, w0, w1);
+                uint32_t *row = bitmap + o * c.Ws;
+                const OrientP &op = sop[o];
+                const unsigned long long base = acc[o * ACC_WORDS + ACC_CBASE0 + p];
+                float lmax = 0.f, lminpos = INFINITY;
+                int lcnt = 0;
+                if (base != NO_STAGE) {
+                    // evaluate each screened candidate once; stage (row, x, y, z, I)
+                    // in candidate order, I = -1 for rejected candidates
+                    for_each_bit_pair<4>(row, w0, w1, lane,
+                                         [&](long long ja, int ra, bool va, long long jb, int rb, bool vb) {
+                        SpotIn ia, ib;
+                        if (va) ia = load_spot<FORM>(T, ja);
+                        if (vb) ib = load_spot<FORM>(T, jb);
 #pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        const bool v = h ? vb : va;
-                        if (!v) continue;
-                        const SpotIn &in = h ? ib : ia;
+                        for (int h = 0; h < 2; ++h) {
+                            const bool v = h ? vb : va;
+                            if (!v) continue;
+                            const SpotIn &in = h ? ib : ia;
+                            float I, z;
+                            double sv;
+                            bool sel = eval_in<FORM>(c, op, in, I, z, sv);
+                            if (sel && I == 0.f && all_zero_drop) sel = false;
+                            float x, y;
+                            spot_xy<FORM>(op, in.e, x, y);
+                            const int rk = h ? rb : ra;
+                            my_idx[base + rk] = (int32_t)(h ? jb : ja);
+                            my_rec[base + rk] = make_float4(x, y, z, sel ? I : -1.f);
+                            if (sel) {
+                                ++lcnt;
+                                lmax = fmaxf(lmax, I);
+                                if (I > 0.f) lminpos = fminf(lminpos, I);
+                            }
+                        }
+                    });
+                } else {
+                    for_each_bit(row, w0, w1, lane, [&](long long j, int, bool valid, int wi, int bit) {
+                        if (!valid) return;
                         float I, z;
                         double sv;
-                        bool sel = eval_in<FORM>(c, op, in, I, z, sv);
+                        bool sel = eval_spot<FORM>(c, op, T, j, I, z, sv);
                         if (sel && I == 0.f && all_zero_drop) sel = false;
-                        float x, y;
-                        spot_xy<FORM>(op, in.e, x, y);
-                        const int rk = h ? rb : ra;
-                        my_idx[base + rk] = (int32_t)(h ? jb : ja);
-                        my_rec[base + rk] = make_float4(x, y, z, sel ? I : -1.f);
-                        if (sel) {
-                            ++lcnt;
-                            lmax = fmaxf(lmax, I);
-                            if (I > 0.f) lminpos = fminf(lminpos, I);
+                        if (!sel) {
+                            atomicAnd(&row[wi], ~(1u << bit));
+                            return;
                         }
-                    }
-                });
-            } else {
-                for_each_bit(row, w0, w1, lane, [&](long long j, int, bool valid, int wi, int bit) {
-                    if (!valid) return;
-                    float I, z;
-                    double sv;
-                    bool sel = eval_spot<FORM>(c, op, T, j, I, z, sv);
-                    if (sel && I == 0.f && all_zero_drop) sel = false;
-                    if (!sel) {
-                        atomicAnd(&row[wi], ~(1u << bit));
-                        return;
-                    }
-                    ++lcnt;
-                    lmax = fmaxf(lmax, I);
-                    if (I > 0.f) lminpos = fminf(lminpos, I);
-                });
-            }
-#pragma unroll
-            for (int d = 16; d >= 1; d >>= 1) {
-                lmax = fmaxf(lmax, __shfl_xor_sync(FULL_MASK, lmax, d));
-                lminpos = fminf(lminpos, __shfl_xor_sync(FULL_MASK, lminpos, d));
-                lcnt += __shfl_xor_sync(FULL_MASK, lcnt, d);
-            }
-            if (!(lmax > 0.f)) lmax = 0.f;  // no -0.0 or NaN in the bit-ordered max
-            if (lane == 0) {
-                // intensities are >= 0, so float bit patterns order like the values
-                atomicMax(&acc[o * ACC_WORDS + ACC_MAXI], (unsigned long long)__float_as_uint(lmax));
-                atomicMin(&acc[o * ACC_WORDS + ACC_MINPOS], (unsigned long long)__float_as_uint(lminpos));
-                acc[o * ACC_WORDS + ACC_PART0 + part] = (unsigned long long)lcnt;
-            }
-        }
-        __syncthreads();
-
-        // ---------------- mask pass (only where some I is positive but <= max * thr)
-        for (int o = warp / WPO; o < n_valid; o += SIM_WARPS / WPO) {
-            if (!(c.thr > 0.0)) break;
-            const float mx = __uint_as_float((unsigned)acc[o * ACC_WORDS + ACC_MAXI]);
-            const float mnp = __uint_as_float((unsigned)acc[o * ACC_WORDS + ACC_MINPOS]);
-            if (!((double)mnp <= (double)mx * c.thr)) continue;
-            uint32_t *row = bitmap + o * c.Ws;
-            const OrientP &op = sop[o];
-            const unsigned long long base = acc[o * ACC_WORDS + ACC_CBASE0 + part];
-            const int cc = (int)acc[o * ACC_WORDS + ACC_CCNT0 + part];
-            int dropped = 0;
-            if (base != NO_STAGE) {
-                for (int r = lane; r < cc; r += 32) {
-                    const float I = my_rec[base + r].w;
-                    if (!(I < 0.f) && !((double)I > (double)mx * c.thr)) {
-                        my_rec[base + r].w = -1.f;
-                        ++dropped;
-                    }
+                        ++lcnt;
+                        lmax = fmaxf(lmax, I);
+                        if (I > 0.f) lminpos = fminf(lminpos, I);
+                    });
                 }
-            } else {
-                for_each_bit(row, w0, w1, lane, [&](long long j, int, bool valid, int wi, int bit) {
-                    if (!valid) return;
-                    float I, z;
-                    double sv;
-                    eval_spot<FORM>(c, op, T, j, I, z, sv);
-                    if (!((double)I > (double)mx * c.thr)) {
-                        atomicAnd(&row[wi], ~(1u << bit));
-                        ++dropped;
-                    }
-                });
-            }
 #pragma unroll
-            for (int d = 16; d >= 1; d >>= 1) dropped += __shfl_xor_sync(FULL_MASK, dropped, d);
-            if (lane == 0) acc[o * ACC_WORDS + ACC_PART0 + part] -= (unsigned long long)dropped;
-        }
-        __syncthreads();
-
-        // ---------------- tile count, published for the look-back of later tiles
-        if (tid == 0) {
-            long long run = 0;
-            int defer = 1;
-            for (int o = 0; o < n_valid; ++o) {
-                acc[o * ACC_WORDS + ACC_OFF] = (unsigned long long)run;
-                long long co = 0;
-                for (int p = 0; p < WPO; ++p) {
-                    co += (long long)acc[o * ACC_WORDS + ACC_PART0 + p];
-                    if (acc[o * ACC_WORDS + ACC_CBASE0 + p] == NO_STAGE) defer = 0;
+                for (int d = 16; d >= 1; d >>= 1) {
+                    lmax = fmaxf(lmax, __shfl_xor_sync(FULL_MASK, lmax, d));
+                    lminpos = fminf(lminpos, __shfl_xor_sync(FULL_MASK, lminpos, d));
+                    lcnt += __shfl_xor_sync(FULL_MASK, lcnt, d);
                 }
-                acc[o * ACC_WORDS + ACC_CNT] = (unsigned long long)co;
-                run += co;
+                if (!(lmax > 0.f)) lmax = 0.f;  // no -0.0 or NaN in the bit-ordered max
+                if (lane == 0) {
+                    // intensities are >= 0, so float bit patterns order like the values
+                    atomicMax(&acc[o * ACC_WORDS + ACC_MAXI], (unsigned long long)__float_as_uint(lmax));
+                    atomicMin(&acc[o * ACC_WORDS + ACC_MINPOS], (unsigned long long)__float_as_uint(lminpos));
+                    acc[o * ACC_WORDS + ACC_PART0 + p] = (unsigned long long)lcnt;
+                }
             }
-            acc[ACC_TILE_TOTAL] = (unsigned long long)run;
-            lookback_publish(lb, tile, run);
-            s_defer = defer;
-        }
-        __syncthreads();
+            __syncthreads();
+
+            // ---------------- mask pass (only where some I is positive but <= max * thr)
+            if (c.thr > 0.0) {
+                for (int u = next_unit(1); u < n_units; u = next_unit(1)) {
+                    const int o = u / NP, p = u % NP;
+                    const float mx = __uint_as_float((unsigned)acc[o * ACC_WORDS + ACC_MAXI]);
+                    const float mnp = __uint_as_float((unsigned)acc[o * ACC_WORDS + ACC_MINPOS]);
+                    if (!((double)mnp <= (double)mx * c.thr)) continue;
+                    int w0, w1;
+                    part_range(p, w0, w1);
+                    uint32_t *row = bitmap + o * c.Ws;
+                    const OrientP &op = sop[o];
+                    const unsigned long long base = acc[o * ACC_WORDS + ACC_CBASE0 + p];
+                    const int cc = (int)acc[o * ACC_WORDS + ACC_CCNT0 + p];
+                    int dropped = 0;
+                    if (base != NO_STAGE) {
+                        for (int r = lane; r < cc; r += 32) {
+                            const float I = my_rec[base + r].w;
+                            if (!(I < 0.f) && !((double)I > (double)mx * c.thr)) {
+                                my_rec[base + r].w = -1.f;
+                                ++dropped;
+                            }
+                        }
+                    } else {
+                        for_each_bit(row, w0, w1, lane, [&](long long j, int, bool valid, int wi, int bit) {
+                            if (!valid) return;
+                            float I, z;
+                            double sv;
+                            eval_spot<FORM>(c, op, T, j, I, z, sv);
+                            if (!((double)I > (double)mx * c.thr)) {
+                                atomicAnd(&row[wi], ~(1u << bit));
+                                ++dropped;
+                            }
+                        });
+                    }
+#pragma unroll
+                    for (int d = 16; d >= 1; d >>= 1) dropped += __shfl_xor_sync(FULL_MASK, dropped, d);
+                    if (lane == 0) acc[o * ACC_WORDS + ACC_PART0 + p] -= (unsigned long long)dropped;
+                }
+                __syncthreads();
+            }
+
+            // ---------------- tile count, published for the look-back of later tiles
+            if (tid == 0) {
+                long long run = 0;
+                int defer = 1;
+                for (int o = 0; o < n_valid; ++o) {
+                    acc[o * ACC_WORDS + ACC_OFF] = (unsigned long long)run;
+                    long long co = 0;
+                    for (int p = 0; p < NP; ++p) {
+                        co += (long long)acc[o * ACC_WORDS + ACC_PART0 + p];
+                        if (acc[o * ACC_WORDS + ACC_CBASE0 + p] == NO_STAGE) defer = 0;
+                    }
+                    acc[o * ACC_WORDS + ACC_CNT] = (unsigned long long)co;
+                    run += co;
+                }
+                acc[ACC_TILE_TOTAL] = (unsigned long long)run;
+                lookback_publish(lb, tile, run);
+                s_defer = defer;
+            }
+            __syncthreads();
         }  // have_new
 
         // ---------------- back: look-back and ordered writes of a finished tile
-        auto back = [&](long long btile, int bbuf) -> bool {
+        auto back = [&](long long btile, int bbuf, int counter) -> bool {
             const OrientP *bsop = sop_buf + bbuf * O;
             const unsigned long long *bacc = acc_buf + bbuf * ACC_STRIDE;
             const int32_t *b_idx = stg.idx + (2 * (long long)blockIdx.x + bbuf) * stg.cap;
@@ -754,13 +790,16 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
             if (prefix < 0) return false;  // bounded wait gave up: DS_ERR_TIMEOUT is set
             for (int o = tid; o < bn_valid; o += SIM_THREADS)
                 offsets[bo_base + o] = prefix + (long long)bacc[o * ACC_WORDS + ACC_OFF];
-            for (int o = warp / WPO; o < bn_valid; o += SIM_WARPS / WPO) {
+            for (int u = next_unit(counter); u < bn_valid * NP; u = next_unit(counter)) {
+                const int o = u / NP, p = u % NP;
+                int w0, w1;
+                part_range(p, w0, w1);
                 const uint32_t *row = bitmap + o * c.Ws;
                 const OrientP &op = bsop[o];
                 long long pos0 = prefix + (long long)bacc[o * ACC_WORDS + ACC_OFF];
-                for (int p = 0; p < part; ++p) pos0 += (long long)bacc[o * ACC_WORDS + ACC_PART0 + p];
-                const unsigned long long base = bacc[o * ACC_WORDS + ACC_CBASE0 + part];
-                const int cc = (int)bacc[o * ACC_WORDS + ACC_CCNT0 + part];
+                for (int pp = 0; pp < p; ++pp) pos0 += (long long)bacc[o * ACC_WORDS + ACC_PART0 + pp];
+                const unsigned long long base = bacc[o * ACC_WORDS + ACC_CBASE0 + p];
+                const int cc = (int)bacc[o * ACC_WORDS + ACC_CCNT0 + p];
                 bool overflow = false;
                 if (base != NO_STAGE) {
                     // compaction copy of the staged records, four batches in flight
@@ -808,13 +847,7 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
                         eval_spot<FORM>(c, op, T, j, I, z, sv);
                         const float4 e = T.scr[j];
                         float x, y;
-                        if (FORM == DS_FORM_FP64) {
-                            x = (float)(op.M[0][0] * (double)e.x + op.M[0][1] * (double)e.y + op.M[0][2] * (double)e.z);
-                            y = (float)(op.M[1][0] * (double)e.x + op.M[1][1] * (double)e.y + op.M[1][2] * (double)e.z);
-                        } else {
-                            x = fmaf(op.m[0][0], e.x, fmaf(op.m[0][1], e.y, op.m[0][2] * e.z));
-                            y = fmaf(op.m[1][0], e.x, fmaf(op.m[1][1], e.y, op.m[1][2] * e.z));
-                        }
+                        spot_xy<FORM>(op, e, x, y);
                         const long long pos = pos0 + rank;
                         if (pos < c.capacity) {
                             out_idx[pos] = (int32_t)j;
@@ -832,19 +865,17 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
         };
 
         if (pend_tile >= 0) {
-            if (!back(pend_tile, cur ^ 1)) { aborted = true; break; }
+            if (!back(pend_tile, cur ^ 1, 2)) break;
             pend_tile = -1;
         }
         if (!have_new) break;
         if (s_defer) {
             pend_tile = tile;
             cur ^= 1;
-        } else if (!back(tile, cur)) {
-            aborted = true;
+        } else if (!back(tile, cur, 3)) {
             break;
         }
     }
-    (void)aborted;
 }
 
 // ------------------------------------------------------------- host side ----
