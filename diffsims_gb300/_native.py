@@ -29,6 +29,7 @@ DS_FORM_FP64 = 1
 
 DS_SCATTER = {"lobato": 0, "xtables": 1, None: 2}
 DS_SHAPE = {"linear": 0, "atanc": 1, "sinc": 2, "sin2c": 3, "lorentzian": 4, "binary": 5}
+DS_SCREEN = {"auto": 0, "rows": 1, "lines": 2}
 DS_PRECESSION_NONE = 0
 DS_PRECESSION_LORENTZIAN = 1
 DS_PRECESSION_INTEGRAL = 2
@@ -54,7 +55,7 @@ class ds_sim_params(C.Structure):
     _fields_ = [("k0", C.c_double), ("max_excitation_error", C.c_double), ("shape_width", C.c_double),
                 ("precession_angle", C.c_double), ("minimum_intensity", C.c_double),
                 ("minima_number", C.c_double), ("shape_model", C.c_int32), ("precession_mode", C.c_int32),
-                ("form", C.c_int32), ("orient_tile", C.c_int32), ("stage_cap", C.c_int32), ("_pad", C.c_int32)]
+                ("form", C.c_int32), ("orient_tile", C.c_int32), ("stage_cap", C.c_int32), ("screen", C.c_int32)]
 
 
 class ds_phase_table(C.Structure):

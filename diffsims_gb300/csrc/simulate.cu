@@ -37,6 +37,14 @@ constexpr float SIM_TAU = 1e-9f;       // | |s| - s_max | below this -> FP64 dec
 constexpr float SIM_TAU_PREC = 2e-7f;  // precession band margin below this -> FP64 decision
 constexpr float SIM_U_MAX = 0.01f;     // (r / k0)^2 above this -> FP64 (series not used)
 constexpr int SIM_MAX_O = 32;
+// tuning knobs (compile time): word ranges per orientation in the refine and
+// write passes, and chunks screened per step in phase 1
+#ifndef DS_SIM_PARTS
+#define DS_SIM_PARTS 4
+#endif
+#ifndef DS_SIM_SCREEN_CHUNKS
+#define DS_SIM_SCREEN_CHUNKS 2
+#endif
 
 struct SimConst {
     double k0, eps, width, phi, thr, Pz, Pt, minima;
@@ -46,6 +54,9 @@ struct SimConst {
     int shape, prec, form, O;
     int W, Ws;
     int hmax[3];
+    int line_mode;                  // phase 1 by per-(orientation, line) intervals
+    double alpha0, alpha1, beta0, beta1, csq;  // z_a = alpha0 + alpha1 g^2, z_b = beta0 + beta1 g^2, |c*|^2
+    float a2f, b2f;                 // -alpha1 |c*|^2, -beta1 |c*|^2
     long long n_hkl, n_orient, n_tiles, capacity;
 };
 
@@ -74,7 +85,7 @@ __host__ __device__ inline SimSmem sim_smem_layout(int O, int Ws) {
     L.orient = o; o += (size_t)2 * O * sizeof(OrientP);  // two pipeline buffers
     L.acc = o; o += (size_t)2 * acc_stride(O) * sizeof(unsigned long long);
     o = (o + 15) & ~(size_t)15;
-    L.bitmap = o; o += (size_t)O * Ws * sizeof(uint32_t);
+    L.bitmap = o; o += (((size_t)O * Ws + 3) & ~(size_t)3) * sizeof(uint32_t);  // whole uint4s (zeroing)
     L.total = o;
     return L;
 }
@@ -108,6 +119,167 @@ __global__ void sim_prep_kernel(SimConst c, const int32_t *__restrict__ hkl, con
     float hi, lo;
     split_double(gsq, hi, lo);
     g2dd[j] = make_float2(hi, lo);
+}
+
+// ------------------------------------------------------------ hkl lines ----
+// Rows come in descending (h, k, l) order, so rows sharing (h, k) form a run
+// of consecutive l values (|g|^2 is convex in l: the d-spacing filter keeps a
+// contiguous range) -- a "line".  Along a line z = A + m_z l and
+// |g|^2 = P + 2 Q l + C l^2 (A = m_x h + m_y k, P = |h a* + k b*|^2,
+// Q = (h a* + k b*).c*, C = |c*|^2), so the screen z_a - G < z < z_b + G
+// becomes two quadratic inequalities in l whose roots bound the candidate
+// rows of the line: a few per (orientation, line) instead of a test per row.
+struct LineP {
+    float h, k;    // line indices
+    float pa, qa;  // alpha0 - G + alpha1 P, 2 alpha1 Q
+    float pb, qb;  // beta0 + G + beta1 P, 2 beta1 Q
+    int row0, n, l_top, _pad0, _pad1, _pad2;
+};
+
+constexpr int LN_THREADS = 256;
+constexpr int LN_ITEMS = 4;
+constexpr int LN_TILE = LN_THREADS * LN_ITEMS;
+
+__device__ __forceinline__ bool row_is_zero(const int32_t *hkl, long long j) {
+    return hkl[3 * j] == 0 && hkl[3 * j + 1] == 0 && hkl[3 * j + 2] == 0;
+}
+
+__global__ void __launch_bounds__(LN_THREADS)
+lines_kernel(SimConst c, const int32_t *__restrict__ hkl, LineP *__restrict__ lines, int *__restrict__ meta,
+             LookbackScratch lb, long long n_tiles, int32_t *status) {
+    // meta[0] = number of lines, meta[1] = first trailing 000 row
+    __shared__ long long s_tile, s_prefix;
+    __shared__ int s_warp[LN_THREADS / 32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) s_tile = (long long)atomicAdd(lb.ticket, 1ull);
+    __syncthreads();
+    const long long tile = s_tile;
+    const long long base = tile * LN_TILE + (long long)tid * LN_ITEMS;
+    bool start[LN_ITEMS];
+    int cnt = 0;
+#pragma unroll
+    for (int it = 0; it < LN_ITEMS; ++it) {
+        const long long j = base + it;
+        start[it] = false;
+        if (j < c.n_hkl) {
+            if (row_is_zero(hkl, j)) {
+                atomicMin(&meta[1], (int)j);
+            } else {
+                start[it] = j == 0 || hkl[3 * j - 3] != hkl[3 * j] || hkl[3 * j - 2] != hkl[3 * j + 1];
+            }
+        }
+        cnt += start[it] ? 1 : 0;
+    }
+    const int incl = warp_inclusive_scan(cnt, lane);
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        const int v = lane < LN_THREADS / 32 ? s_warp[lane] : 0;
+        const int w = warp_inclusive_scan(v, lane);
+        if (lane < LN_THREADS / 32) s_warp[lane] = w - v;
+        if (lane == LN_THREADS / 32 - 1) {
+            const long long prefix = lookback_exclusive(lb, tile, (long long)w, status);
+            s_prefix = prefix;
+            if (prefix >= 0 && tile == n_tiles - 1) meta[0] = (int)(prefix + w);
+        }
+    }
+    __syncthreads();
+    if (s_prefix < 0) return;
+    long long pos = s_prefix + s_warp[warp] + (incl - cnt);
+#pragma unroll
+    for (int it = 0; it < LN_ITEMS; ++it) {
+        if (!start[it]) continue;
+        const long long j = base + it;
+        const int h = hkl[3 * j], k = hkl[3 * j + 1];
+        long long e = j + 1;
+        while (e < c.n_hkl && hkl[3 * e] == h && hkl[3 * e + 1] == k && !row_is_zero(hkl, e)) ++e;
+        // P, Q in FP64 from the reciprocal basis (rows a*, b*, c*)
+        double v[3];
+        for (int t = 0; t < 3; ++t) v[t] = (double)h * c.recip[t] + (double)k * c.recip[3 + t];
+        const double P = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+        const double Q = v[0] * c.recip[6] + v[1] * c.recip[7] + v[2] * c.recip[8];
+        LineP L;
+        L.h = (float)h;
+        L.k = (float)k;
+        L.pa = (float)(c.alpha0 - (double)c.guard + c.alpha1 * P);
+        L.qa = (float)(2.0 * c.alpha1 * Q);
+        L.pb = (float)(c.beta0 + (double)c.guard + c.beta1 * P);
+        L.qb = (float)(2.0 * c.beta1 * Q);
+        L.row0 = (int)j;
+        L.n = (int)(e - j);
+        L.l_top = hkl[3 * j + 2];
+        L._pad0 = L._pad1 = L._pad2 = 0;
+        lines[pos] = L;
+        ++pos;
+    }
+}
+
+// Set bits [j1, j2] of one bitmap row (shared memory).
+__device__ __forceinline__ void set_bit_range(uint32_t *row, int j1, int j2) {
+    const int wa = j1 >> 5, wb = j2 >> 5;
+    for (int w = wa; w <= wb; ++w) {
+        const int lo = w == wa ? (j1 & 31) : 0;
+        const int hi = w == wb ? (j2 & 31) : 31;
+        const uint32_t m = (hi == 31 ? 0xFFFFFFFFu : ((1u << (hi + 1)) - 1u)) & ~((1u << lo) - 1u);
+        atomicOr(&row[w], m);
+    }
+}
+
+// Candidate rows of one (orientation, line): the l where
+//   qa(l) = a2 l^2 + (m_z - qa) l + (A - pa) > 0    (z > z_a - G; a2 < 0: between roots)
+//   qb(l) = b2 l^2 + (m_z - qb) l + (A - pb) < 0    (z < z_b + G; b2 < 0: outside roots)
+// Roots by the stable quadratic formula; every root is pushed outward (the
+// kept set only grows) by its FP32 error bound, so the rows marked are a
+// superset of the rows the exact screen keeps.
+__device__ __forceinline__ void line_candidates(const SimConst &c, const LineP &L, float mx, float my, float mz,
+                                                uint32_t *row) {
+    const float A = fmaf(mx, L.h, my * L.k);
+    const float ca1 = mz - L.qa, ca0 = A - L.pa;
+    const float cb1 = mz - L.qb, cb0 = A - L.pb;
+    // FP32 error of the constant terms (|A| and |p| are O(1)): a few ulps
+    const float lmax = (float)max(abs(L.l_top), abs(L.l_top - L.n + 1));
+    const float dc = 8.f * 5.96e-8f *
+                         (fabsf(mx * L.h) + fabsf(my * L.k) + fabsf(L.pa) + fabsf(L.pb) +
+                          (fabsf(mz) + fabsf(L.qa) + fabsf(L.qb)) * lmax) + 1e-12f;
+    const float fa = -4.f * c.a2f * ca0;
+    float Da = fmaf(ca1, ca1, fa);
+    Da += 1e-5f * (ca1 * ca1 + fabsf(fa)) + 4.f * fabsf(c.a2f) * dc;
+    if (!(Da > 0.f)) return;  // qa <= 0 on the whole line
+    const float sa = sqrtf(Da);
+    const float ta = -0.5f * (ca1 + copysignf(sa, ca1));
+    const float r1 = ca0 / ta, r2 = ta / c.a2f;
+    const float ma = 2.f * dc / sa + 1e-3f;
+    const float a_lo = fminf(r1, r2) - ma, a_hi = fmaxf(r1, r2) + ma;
+    const float fb = -4.f * c.b2f * cb0;
+    float Db = fmaf(cb1, cb1, fb);
+    Db -= 1e-5f * (cb1 * cb1 + fabsf(fb)) + 4.f * fabsf(c.b2f) * dc;
+    float b_lo = INFINITY, b_hi = -INFINITY;  // excluded open interval (b_lo, b_hi)
+    if (Db > 0.f) {
+        const float sb = sqrtf(Db);
+        const float tb = -0.5f * (cb1 + copysignf(sb, cb1));
+        const float s1 = cb0 / tb, s2 = tb / c.b2f;
+        const float mb = 2.f * dc / sb + 1e-3f;
+        b_lo = fminf(s1, s2) + mb;
+        b_hi = fmaxf(s1, s2) - mb;
+    }
+    const int l_bot = L.l_top - L.n + 1;
+    float x1[2], x2[2];
+    int ni;
+    if (!(b_lo < b_hi)) {
+        x1[0] = a_lo; x2[0] = a_hi; ni = 1;
+    } else {
+        x1[0] = a_lo; x2[0] = fminf(a_hi, b_lo);
+        x1[1] = fmaxf(a_lo, b_hi); x2[1] = a_hi;
+        ni = 2;
+    }
+    for (int q = 0; q < ni; ++q) {
+        if (!(x1[q] <= x2[q])) continue;
+        const float flo = fmaxf(ceilf(x1[q]), (float)l_bot);
+        const float fhi = fminf(floorf(x2[q]), (float)L.l_top);
+        if (!(flo <= fhi)) continue;
+        const int lo = (int)flo, hi = (int)fhi;
+        set_bit_range(row, L.row0 + (L.l_top - hi), L.row0 + (L.l_top - lo));
+    }
 }
 
 // --------------------------------------------------------- evaluation ----
@@ -270,6 +442,8 @@ struct TableP {
     const float2 *g2dd;
     const float *F2;
     const double *F2d;
+    const LineP *lines;   // line screen: per-line constants
+    const int *line_meta; // [0] lines, [1] first trailing 000 row
 };
 
 // One candidate's table data, loaded ahead of its evaluation.
@@ -452,7 +626,7 @@ __device__ __forceinline__ void for_each_bit_pair(const uint32_t *row, int w0, i
 // bitmap and re-evaluating.
 struct StageP {
     int32_t *idx;    // table row
-    float4 *rec;     // x, y, z, I (I = -1: not a spot)
+    float *inten;    // I (-1: not a spot)
     long long cap;   // entries per pipeline slot
 };
 constexpr unsigned long long NO_STAGE = ~0ull;
@@ -476,7 +650,7 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
     constexpr int ACC_TILE_TOTAL = O * ACC_WORDS;
     // phases 2-3 run over units (orientation, part): NP word ranges per
     // orientation, taken by warps from a shared counter for load balance
-    constexpr int NP = O >= 2 ? 4 : 8;
+    constexpr int NP = O >= 2 ? DS_SIM_PARTS : 8;
     const bool all_zero_drop = c.thr >= 0.0;
     const unsigned lanemask_lt = (1u << lane) - 1u;
     auto part_range = [&](int p, int &w0, int &w1) {
@@ -503,7 +677,7 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
         OrientP *sop = sop_buf + cur * O;
         unsigned long long *acc = acc_buf + cur * ACC_STRIDE;
         int32_t *my_idx = stg.idx + (2 * (long long)blockIdx.x + cur) * stg.cap;
-        float4 *my_rec = stg.rec + (2 * (long long)blockIdx.x + cur) * stg.cap;
+        float *my_I = stg.inten + (2 * (long long)blockIdx.x + cur) * stg.cap;
         for (int i = tid; i < ACC_STRIDE; i += SIM_THREADS)
             acc[i] = (i < ACC_TILE_TOTAL && i % ACC_WORDS == ACC_MINPOS) ? (unsigned long long)__float_as_uint(INFINITY)
                                                                           : 0ull;
@@ -552,56 +726,91 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
             __syncthreads();
 
             // ---------------- phase 1: screen every row against all O orientations
-            {
+            if (FORM == DS_FORM_MIXED && c.line_mode) {
+                // per-(orientation, line) candidate intervals, OR-ed into a zeroed bitmap
+                uint4 *bm4 = reinterpret_cast<uint4 *>(bitmap);
+                for (int i = tid; i < (O * c.Ws + 3) / 4; i += SIM_THREADS) bm4[i] = make_uint4(0u, 0u, 0u, 0u);
+                __syncthreads();
+                const int n_lines = T.line_meta[0];
+                const int zero_start = T.line_meta[1];
+                float mx[O], my[O], mz[O];
+#pragma unroll
+                for (int o = 0; o < O; ++o) { mx[o] = sop[o].m[2][0]; my[o] = sop[o].m[2][1]; mz[o] = sop[o].m[2][2]; }
+                for (int li = tid; li < n_lines; li += SIM_THREADS) {
+                    const LineP L = T.lines[li];
+#pragma unroll
+                    for (int o = 0; o < O; ++o)
+                        if (o < n_valid) line_candidates(c, L, mx[o], my[o], mz[o], bitmap + o * c.Ws);
+                }
+                // the trailing 000 rows (direct beam) are always candidates
+                for (int i = tid; i < n_valid * (int)(c.n_hkl - zero_start); i += SIM_THREADS) {
+                    const int o = i / (int)(c.n_hkl - zero_start), j = zero_start + i % (int)(c.n_hkl - zero_start);
+                    atomicOr(&bitmap[o * c.Ws + (j >> 5)], 1u << (j & 31));
+                }
+            } else if (FORM == DS_FORM_FP64) {
+                for (int wc = warp; wc < c.W; wc += SIM_WARPS) {
+                    const long long j = (long long)wc * 32 + lane;
+                    float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (j < c.n_hkl) e = T.scr[j];
+                    uint32_t myword = 0;
+                    const double hd = e.x, kd = e.y, ld = e.z;
+#pragma unroll 1
+                    for (int o = 0; o < O; ++o) {
+                        double sx, rx, zx;
+                        const bool hit = (j < c.n_hkl) && (o < n_valid) && select_fp64(c, sop[o], hd, kd, ld, sx, rx, zx);
+                        const uint32_t b = __ballot_sync(FULL_MASK, hit);
+                        if (lane == o) myword = b;
+                    }
+                    if (lane < O) bitmap[lane * c.Ws + wc] = myword;
+                }
+            } else {
                 float m0[O], m1[O], m2[O];
 #pragma unroll
                 for (int o = 0; o < O; ++o) { m0[o] = sop[o].m[2][0]; m1[o] = sop[o].m[2][1]; m2[o] = sop[o].m[2][2]; }
-                // rows of chunks wc + 8, wc + 16 and wc + 24 are in flight while chunk wc is screened
-                constexpr int PF = 3;
-                float4 ep[PF];
-                float zp[PF];
+                // Each step screens two chunks (wc, wc + 8) with independent
+                // dependency chains; the rows of the next step are in flight.
+                // Per orientation: the sign bit of |z - z_mid| - z_half, collected
+                // into one word per lane (bit O-1-o); a 32x32 bit transpose then
+                // hands lane O-1-o the word of orientation o.
+                constexpr int CH = DS_SIM_SCREEN_CHUNKS;
+                float4 en[CH];
+                float zn[CH];
 #pragma unroll
-                for (int k = 0; k < PF; ++k) {
+                for (int k = 0; k < CH; ++k) {
                     const long long jk = ((long long)warp + k * SIM_WARPS) * 32 + lane;
-                    ep[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-                    zp[k] = -1.f;
-                    if (jk < c.n_hkl) { ep[k] = T.scr[jk]; zp[k] = T.zh[jk]; }
+                    en[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    zn[k] = -1.f;
+                    if (jk < c.n_hkl) { en[k] = T.scr[jk]; zn[k] = T.zh[jk]; }
                 }
-                for (int wc = warp; wc < c.W; wc += SIM_WARPS) {
-                    const long long j = (long long)wc * 32 + lane;
-                    const float4 e = ep[0];
-                    const float zh = zp[0];
+                for (int wc = warp; wc < c.W; wc += CH * SIM_WARPS) {
+                    float4 e[CH];
+                    float zh[CH];
 #pragma unroll
-                    for (int k = 0; k + 1 < PF; ++k) { ep[k] = ep[k + 1]; zp[k] = zp[k + 1]; }
-                    {
-                        const long long jn = j + 32LL * SIM_WARPS * PF;
-                        ep[PF - 1] = make_float4(0.f, 0.f, 0.f, 0.f);
-                        zp[PF - 1] = -1.f;
-                        if (jn < c.n_hkl) { ep[PF - 1] = T.scr[jn]; zp[PF - 1] = T.zh[jn]; }
+                    for (int k = 0; k < CH; ++k) {
+                        e[k] = en[k];
+                        zh[k] = zn[k];
+                        const long long jn = ((long long)wc + (CH + k) * SIM_WARPS) * 32 + lane;
+                        en[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                        zn[k] = -1.f;
+                        if (jn < c.n_hkl) { en[k] = T.scr[jn]; zn[k] = T.zh[jn]; }
                     }
-                    if (FORM == DS_FORM_FP64) {
-                        uint32_t myword = 0;
-                        const double hd = e.x, kd = e.y, ld = e.z;
-#pragma unroll 1
-                        for (int o = 0; o < O; ++o) {
-                            double sx, rx, zx;
-                            const bool hit = (j < c.n_hkl) && (o < n_valid) && select_fp64(c, sop[o], hd, kd, ld, sx, rx, zx);
-                            const uint32_t b = __ballot_sync(FULL_MASK, hit);
-                            if (lane == o) myword = b;
-                        }
-                        if (lane < O) bitmap[lane * c.Ws + wc] = myword;
-                    } else {
-                        // sign bit of |z - z_mid| - z_half per orientation, collected
-                        // into one word per lane (bit O-1-o), then a 32x32 bit
-                        // transpose hands lane O-1-o the word of orientation o
-                        uint32_t bits = 0;
+                    uint32_t bits[CH];
 #pragma unroll
-                        for (int o = 0; o < O; ++o) {
-                            const float z = fmaf(m0[o], e.x, fmaf(m1[o], e.y, fmaf(m2[o], e.z, e.w)));
-                            bits = __funnelshift_l(__float_as_uint(fabsf(z) - zh), bits, 1);
+                    for (int k = 0; k < CH; ++k) bits[k] = 0;
+#pragma unroll
+                    for (int o = 0; o < O; ++o) {
+#pragma unroll
+                        for (int k = 0; k < CH; ++k) {
+                            const float z = fmaf(m0[o], e[k].x, fmaf(m1[o], e[k].y, fmaf(m2[o], e[k].z, e[k].w)));
+                            bits[k] = __funnelshift_l(__float_as_uint(fabsf(z) - zh[k]), bits[k], 1);
                         }
-                        bits = transpose32(bits, lane);
-                        if (lane < O) bitmap[(O - 1 - lane) * c.Ws + wc] = bits;
+                    }
+#pragma unroll
+                    for (int k = 0; k < CH; ++k) bits[k] = transpose32(bits[k], lane);
+#pragma unroll
+                    for (int k = 0; k < CH; ++k) {
+                        const int wck = wc + k * SIM_WARPS;
+                        if (lane < O && wck < c.W) bitmap[(O - 1 - lane) * c.Ws + wck] = bits[k];
                     }
                 }
             }
@@ -658,15 +867,13 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
                             const bool v = h ? vb : va;
                             if (!v) continue;
                             const SpotIn &in = h ? ib : ia;
-                            float I, z;
+                                float I, z;
                             double sv;
                             bool sel = eval_in<FORM>(c, op, in, I, z, sv);
                             if (sel && I == 0.f && all_zero_drop) sel = false;
-                            float x, y;
-                            spot_xy<FORM>(op, in.e, x, y);
                             const int rk = h ? rb : ra;
                             my_idx[base + rk] = (int32_t)(h ? jb : ja);
-                            my_rec[base + rk] = make_float4(x, y, z, sel ? I : -1.f);
+                            my_I[base + rk] = sel ? I : -1.f;
                             if (sel) {
                                 ++lcnt;
                                 lmax = fmaxf(lmax, I);
@@ -722,9 +929,9 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
                     int dropped = 0;
                     if (base != NO_STAGE) {
                         for (int r = lane; r < cc; r += 32) {
-                            const float I = my_rec[base + r].w;
+                            const float I = my_I[base + r];
                             if (!(I < 0.f) && !((double)I > (double)mx * c.thr)) {
-                                my_rec[base + r].w = -1.f;
+                                my_I[base + r] = -1.f;
                                 ++dropped;
                             }
                         }
@@ -773,7 +980,7 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
             const OrientP *bsop = sop_buf + bbuf * O;
             const unsigned long long *bacc = acc_buf + bbuf * ACC_STRIDE;
             const int32_t *b_idx = stg.idx + (2 * (long long)blockIdx.x + bbuf) * stg.cap;
-            const float4 *b_rec = stg.rec + (2 * (long long)blockIdx.x + bbuf) * stg.cap;
+            const float *b_I = stg.inten + (2 * (long long)blockIdx.x + bbuf) * stg.cap;
             const long long bo_base = btile * O;
             const int bn_valid = (int)min((long long)O, c.n_orient - bo_base);
             if (tid == 0) {
@@ -802,30 +1009,45 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
                 const int cc = (int)bacc[o * ACC_WORDS + ACC_CCNT0 + p];
                 bool overflow = false;
                 if (base != NO_STAGE) {
-                    // compaction copy of the staged records, four batches in flight
+                    // compaction of the staged (row, I) pairs, four batches in flight;
+                    // beam-frame x, y, z recomputed from the row's hkl
                     long long out_r = 0;
                     for (int r0 = 0; r0 < cc; r0 += 128) {
-                        float4 rec[4];
+                        float II[4];
                         int32_t jj[4];
 #pragma unroll
                         for (int b = 0; b < 4; ++b) {
                             const int r = r0 + 32 * b + lane;
-                            rec[b] = make_float4(0.f, 0.f, 0.f, -1.f);
+                            II[b] = -1.f;
                             jj[b] = 0;
                             if (r < cc) {
-                                rec[b] = b_rec[base + r];
+                                II[b] = b_I[base + r];
                                 jj[b] = b_idx[base + r];
                             }
                         }
+                        float4 ee[4];
 #pragma unroll
                         for (int b = 0; b < 4; ++b) {
-                            const bool keep = !(rec[b].w < 0.f);
+                            ee[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+                            if (!(II[b] < 0.f)) ee[b] = T.scr[jj[b]];
+                        }
+#pragma unroll
+                        for (int b = 0; b < 4; ++b) {
+                            const bool keep = !(II[b] < 0.f);
                             const unsigned bal = __ballot_sync(FULL_MASK, keep);
                             if (keep) {
+                                const float4 e = ee[b];
+                                float x, y, z;
+                                spot_xy<FORM>(op, e, x, y);
+                                if (FORM == DS_FORM_FP64)
+                                    z = (float)(op.M[2][0] * (double)e.x + op.M[2][1] * (double)e.y + op.M[2][2] * (double)e.z);
+                                else
+                                    z = fmaf(op.za[0], e.x, fmaf(op.za[1], e.y, op.za[2] * e.z)) +
+                                        fmaf(op.zb[0], e.x, fmaf(op.zb[1], e.y, op.zb[2] * e.z));
                                 const long long pos = pos0 + out_r + __popc(bal & lanemask_lt);
                                 if (pos < c.capacity) {
                                     out_idx[pos] = jj[b];
-                                    out_xyzi[pos] = rec[b];
+                                    out_xyzi[pos] = make_float4(x, y, z, II[b]);
                                     if (out_s) {
                                         float I2, z2;
                                         double sv;
@@ -886,7 +1108,9 @@ constexpr long long STAGE_CAP = 24576;  // staged candidates per pipeline slot (
 struct SimPlan {
     int O, W, Ws;
     long long n_tiles, grid, stage_cap;
-    size_t off_lb, off_scr, off_zh, off_g2, off_sidx, off_sI, total;
+    int line_mode;
+    long long line_tiles;
+    size_t off_lb, off_scr, off_zh, off_g2, off_sidx, off_sI, off_lines, off_lmeta, off_llb, total;
     size_t smem;
 };
 
@@ -926,6 +1150,12 @@ static const void *kernel_ptr(int O, int form) {
 // Launch plan: tile size, persistent grid (resident CTAs, at most one per
 // tile) and the scratch layout.
 static ds_status make_plan(const ds_sim_params *p, const ds_phase_table *t, long long n_orient, SimPlan &P) {
+    // screen: per-(orientation, line) intervals for the mixed form without
+    // precession (the band of the precessing sphere is not quadratic in l),
+    // per-row tests otherwise or on request
+    P.line_mode = (p->form == DS_FORM_MIXED && p->precession_mode == DS_PRECESSION_NONE && p->screen != DS_SCREEN_ROWS)
+                      ? 1 : 0;
+    P.line_tiles = (t->n_hkl + LN_TILE - 1) / LN_TILE;
     P.O = pick_O(p, t->n_hkl, n_orient);
     if (p->form == DS_FORM_FP64 && P.O > 16) P.O = 16;
     P.W = (int)((t->n_hkl + 31) / 32);
@@ -958,7 +1188,12 @@ static ds_status make_plan(const ds_sim_params *p, const ds_phase_table *t, long
     o = align_up(o, 256);
     P.off_sidx = o; o += (size_t)(2 * P.grid * P.stage_cap) * sizeof(int32_t);  // two pipeline slots per CTA
     o = align_up(o, 256);
-    P.off_sI = o; o += (size_t)(2 * P.grid * P.stage_cap) * sizeof(float4);
+    P.off_sI = o; o += (size_t)(2 * P.grid * P.stage_cap) * sizeof(float);
+    o = align_up(o, 256);
+    P.off_lines = o; o += P.line_mode ? (size_t)t->n_hkl * sizeof(LineP) : 0;
+    o = align_up(o, 256);
+    P.off_lmeta = o; o += 256;
+    P.off_llb = o; o += P.line_mode ? lookback_scratch_bytes(P.line_tiles) : 0;
     P.total = align_up(o, 256);
     return DS_OK;
 }
@@ -1067,6 +1302,17 @@ extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t
     for (int i = 0; i < 3; ++i) c.hmax[i] = t->hmax[i] > 0 ? t->hmax[i] : 1;
     c.n_hkl = t->n_hkl;
     c.n_orient = n_orient;
+    c.line_mode = P.line_mode;
+    {
+        const double e = c.eps, k0 = c.k0;
+        c.alpha1 = 1.0 / (2.0 * (k0 - e));
+        c.alpha0 = (e * e - 2.0 * e * k0) * c.alpha1;
+        c.beta1 = 1.0 / (2.0 * (k0 + e));
+        c.beta0 = (e * e + 2.0 * e * k0) * c.beta1;
+        c.csq = t->recip[6] * t->recip[6] + t->recip[7] * t->recip[7] + t->recip[8] * t->recip[8];
+        c.a2f = (float)(-c.alpha1 * c.csq);
+        c.b2f = (float)(-c.beta1 * c.csq);
+    }
     c.n_tiles = P.n_tiles;
     c.capacity = out->capacity;
 
@@ -1084,10 +1330,21 @@ extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t
         ds_status st = check_launch("sim_prep_kernel");
         if (st) return st;
     }
+    T.lines = reinterpret_cast<const LineP *>(sb + P.off_lines);
+    T.line_meta = reinterpret_cast<const int *>(sb + P.off_lmeta);
+    if (P.line_mode && t->n_hkl > 0) {
+        DS_CUDA_TRY(cudaMemsetAsync(sb + P.off_lmeta, 0x7f, 256, s));  // [1] = no 000 row yet
+        DS_CUDA_TRY(cudaMemsetAsync(sb + P.off_llb, 0, lookback_scratch_bytes(P.line_tiles), s));
+        lines_kernel<<<(unsigned)P.line_tiles, LN_THREADS, 0, s>>>(
+            c, t->hkl, reinterpret_cast<LineP *>(sb + P.off_lines), reinterpret_cast<int *>(sb + P.off_lmeta),
+            lookback_scratch(sb + P.off_llb), P.line_tiles, status);
+        ds_status st = check_launch("lines_kernel");
+        if (st) return st;
+    }
     LookbackScratch lb = lookback_scratch(sb + P.off_lb);
     StageP stg;
     stg.idx = reinterpret_cast<int32_t *>(sb + P.off_sidx);
-    stg.rec = reinterpret_cast<float4 *>(sb + P.off_sI);
+    stg.inten = reinterpret_cast<float *>(sb + P.off_sI);
     stg.cap = P.stage_cap;
     if (p->form == DS_FORM_FP64) {
         switch (P.O) {

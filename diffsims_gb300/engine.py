@@ -132,11 +132,13 @@ class SimSettings:
     form: str = "mixed"
     orient_tile: int = 0
     stage_cap: int = 0
+    screen: str = "auto"
 
     def cstruct(self) -> N.ds_sim_params:
         return N.ds_sim_params(self.k0, self.max_excitation_error, self.shape_width, self.precession_angle_rad,
                                self.minimum_intensity, self.minima_number, N.DS_SHAPE[self.shape_model],
-                               self.precession_mode, FORMS[self.form], self.orient_tile, self.stage_cap, 0)
+                               self.precession_mode, FORMS[self.form], self.orient_tile, self.stage_cap,
+                               N.DS_SCREEN[self.screen])
 
 
 class PhaseSpots:

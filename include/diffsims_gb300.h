@@ -45,6 +45,11 @@ enum { DS_SCATTER_LOBATO = 0, DS_SCATTER_XTABLES = 1, DS_SCATTER_NONE = 2 };
 enum { DS_SHAPE_LINEAR = 0, DS_SHAPE_ATANC = 1, DS_SHAPE_SINC = 2, DS_SHAPE_SIN2C = 3,
        DS_SHAPE_LORENTZIAN = 4, DS_SHAPE_BINARY = 5 };
 
+/* candidate screen of ds_simulate: per-(orientation, hkl line) intervals or a
+ * test per (orientation, row); both keep a superset of the selected spots,
+ * the exact selection follows, so the results are identical */
+enum { DS_SCREEN_AUTO = 0, DS_SCREEN_ROWS = 1, DS_SCREEN_LINES = 2 };
+
 /* precession handling (diffsims/generators/simulation_generator.py:363-411) */
 enum { DS_PRECESSION_NONE = 0,
        DS_PRECESSION_LORENTZIAN = 1, /* approximate_precession=True: lorentzian_precession */
@@ -129,7 +134,7 @@ typedef struct {
     int32_t form;                /* DS_FORM_*                                       */
     int32_t orient_tile;         /* orientations per CTA (0 = library choice)       */
     int32_t stage_cap;           /* staged candidates per CTA (0 = library choice)  */
-    int32_t _pad;
+    int32_t screen;              /* DS_SCREEN_* (0 = library choice)                */
 } ds_sim_params;
 
 /* One phase's candidate table (device arrays of n_hkl rows, in reference order). */

@@ -278,6 +278,35 @@ def test_staging_fallback_agrees(stage_cap):
     pu.compare(b, crystal, q, p)
 
 
+@pytest.mark.parametrize("name, crystal, r, eps", [
+    ("p1", random_p1(30, 17), 1.5, 0.02), ("al", al_fcc(), 1.0, 0.01), ("long_c", random_p1(8, 19, edges=(4, 20)), 1.8, 0.02),
+    ("graphite", graphite(), 1.6768, 0.1), ("si_big", si_crystal(), 3.0, 0.01)])
+def test_line_screen_matches_row_screen(name, crystal, r, eps):
+    """The per-(orientation, hkl line) interval screen and the per-row screen
+    keep different supersets; after the exact selection the spots agree bit
+    for bit."""
+    import torch
+    from diffsims_gb300.engine import PhaseTable, SpotBuffers, simulate_phase
+    dev = torch.device("cuda", 0)
+    q = np.vstack([ok.random_quaternions(300, seed=3), ok.euler_to_quaternion([[0, 0, 0], [0, 90, 0], [45, 54.7356, 0],
+                                                                             [0, 90, 90], [10, 0.05, 3]], degrees=True)])
+    p = ok.SimParams(accelerating_voltage=200, shape_factor_model="linear", reciprocal_radius=r, max_excitation_error=eps)
+    gen = pu.generator_for(p)
+    table = PhaseTable(pu.to_phase(crystal), r, True, "lobato", list(crystal.B), device=dev)
+    qd = torch.as_tensor(q).to(dev)
+    res = {}
+    for screen in ("rows", "lines"):
+        st = gen.settings(eps)
+        st.screen = screen
+        res[screen] = simulate_phase(table, qd, st, r, SpotBuffers(dev))
+    a, b = res["rows"], res["lines"]
+    assert a.total == b.total
+    assert np.array_equal(a.offsets.cpu().numpy(), b.offsets.cpu().numpy())
+    assert np.array_equal(a.hkl_index.cpu().numpy(), b.hkl_index.cpu().numpy())
+    assert np.array_equal(a.xyzi.cpu().numpy(), b.xyzi.cpu().numpy())
+    pu.compare(b, crystal, q, p)
+
+
 def test_capacity_overflow_is_retried():
     import torch
     from diffsims_gb300 import engine
