@@ -731,8 +731,11 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
                 uint4 *bm4 = reinterpret_cast<uint4 *>(bitmap);
                 for (int i = tid; i < (O * c.Ws + 3) / 4; i += SIM_THREADS) bm4[i] = make_uint4(0u, 0u, 0u, 0u);
                 __syncthreads();
-                const int n_lines = T.line_meta[0];
-                const int zero_start = T.line_meta[1];
+                const int n_lines = (int)min((long long)T.line_meta[0], c.n_hkl);  // bounded even if the line pass failed
+                // trailing 000 rows: meta[1] holds the first one, or a large
+                // sentinel when there are none
+                const long long zero_start = min((long long)T.line_meta[1], c.n_hkl);
+                const int n_zero = (int)(c.n_hkl - zero_start);  // 0, 1 or 2
                 float mx[O], my[O], mz[O];
 #pragma unroll
                 for (int o = 0; o < O; ++o) { mx[o] = sop[o].m[2][0]; my[o] = sop[o].m[2][1]; mz[o] = sop[o].m[2][2]; }
@@ -743,9 +746,10 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
                         if (o < n_valid) line_candidates(c, L, mx[o], my[o], mz[o], bitmap + o * c.Ws);
                 }
                 // the trailing 000 rows (direct beam) are always candidates
-                for (int i = tid; i < n_valid * (int)(c.n_hkl - zero_start); i += SIM_THREADS) {
-                    const int o = i / (int)(c.n_hkl - zero_start), j = zero_start + i % (int)(c.n_hkl - zero_start);
-                    atomicOr(&bitmap[o * c.Ws + (j >> 5)], 1u << (j & 31));
+                for (int i = tid; i < n_valid * n_zero; i += SIM_THREADS) {
+                    const int o = i / n_zero;
+                    const long long j = zero_start + i % n_zero;
+                    atomicOr(&bitmap[o * c.Ws + (int)(j >> 5)], 1u << (int)(j & 31));
                 }
             } else if (FORM == DS_FORM_FP64) {
                 for (int wc = warp; wc < c.W; wc += SIM_WARPS) {
@@ -1153,8 +1157,8 @@ static ds_status make_plan(const ds_sim_params *p, const ds_phase_table *t, long
     // screen: per-(orientation, line) intervals for the mixed form without
     // precession (the band of the precessing sphere is not quadratic in l),
     // per-row tests otherwise or on request
-    P.line_mode = (p->form == DS_FORM_MIXED && p->precession_mode == DS_PRECESSION_NONE && p->screen != DS_SCREEN_ROWS)
-                      ? 1 : 0;
+    P.line_mode = (p->form == DS_FORM_MIXED && p->precession_mode == DS_PRECESSION_NONE &&
+                   p->screen != DS_SCREEN_ROWS && t->n_hkl > 0) ? 1 : 0;
     P.line_tiles = (t->n_hkl + LN_TILE - 1) / LN_TILE;
     P.O = pick_O(p, t->n_hkl, n_orient);
     if (p->form == DS_FORM_FP64 && P.O > 16) P.O = 16;
@@ -1332,8 +1336,8 @@ extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t
     }
     T.lines = reinterpret_cast<const LineP *>(sb + P.off_lines);
     T.line_meta = reinterpret_cast<const int *>(sb + P.off_lmeta);
-    if (P.line_mode && t->n_hkl > 0) {
-        DS_CUDA_TRY(cudaMemsetAsync(sb + P.off_lmeta, 0x7f, 256, s));  // [1] = no 000 row yet
+    if (P.line_mode) {
+        DS_CUDA_TRY(cudaMemsetAsync(sb + P.off_lmeta, 0x7f, 256, s));  // [1] = no 000 row yet (0x7f7f7f7f)
         DS_CUDA_TRY(cudaMemsetAsync(sb + P.off_llb, 0, lookback_scratch_bytes(P.line_tiles), s));
         lines_kernel<<<(unsigned)P.line_tiles, LN_THREADS, 0, s>>>(
             c, t->hkl, reinterpret_cast<LineP *>(sb + P.off_lines), reinterpret_cast<int *>(sb + P.off_lmeta),

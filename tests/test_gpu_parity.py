@@ -322,6 +322,29 @@ def test_capacity_overflow_is_retried():
     pu.compare(spots, crystal, q, p)
 
 
+@pytest.mark.parametrize("screen", ["lines", "rows"])
+def test_empty_table_and_no_direct_beam(screen):
+    """A radius below the first reflection and no direct beam: an empty
+    candidate table, empty patterns; and small tables without 000 rows."""
+    import torch
+    from diffsims_gb300.engine import PhaseTable, SpotBuffers, simulate_phase
+    dev = torch.device("cuda", 0)
+    crystal = al_fcc()
+    q = ok.random_quaternions(40, seed=2)
+    for r, db in ((0.1, False), (0.1, True), (0.6, False)):
+        p = ok.SimParams(accelerating_voltage=200, reciprocal_radius=r, with_direct_beam=db, max_excitation_error=0.05)
+        gen = pu.generator_for(p)
+        t = PhaseTable(pu.to_phase(crystal), r, db, device=dev)
+        st = gen.settings(0.05)
+        st.screen = screen
+        sp = simulate_phase(t, torch.as_tensor(q).to(dev), st, r, SpotBuffers(dev))
+        assert sp.offsets.shape[0] == 41
+        if t.n == 0:
+            assert sp.total == 0
+        else:
+            pu.compare(sp, crystal, q, p)
+
+
 def test_empty_and_single_orientation():
     import torch
     from diffsims_gb300.engine import PhaseTable, SpotBuffers, simulate_phase
