@@ -34,6 +34,7 @@ namespace ds {
 constexpr int SIM_THREADS = 256;
 constexpr int SIM_WARPS = SIM_THREADS / 32;
 constexpr float SIM_TAU = 1e-9f;       // | |s| - s_max | below this -> FP64 decision
+constexpr float SIM_TAU_SF = 1e-6f;    // |s| this close to a zero of the shape factor -> FP64 s
 constexpr float SIM_TAU_PREC = 2e-7f;  // precession band margin below this -> FP64 decision
 constexpr float SIM_U_MAX = 0.01f;     // (r / k0)^2 above this -> FP64 (series not used)
 constexpr int SIM_MAX_O = 32;
@@ -330,6 +331,18 @@ __device__ inline bool select_mixed(const SimConst &c, const OrientP &op, const 
             const float d = (fabsf(s.hi) - c.eps_dd.hi) + (sg * s.lo - c.eps_dd.lo);
             if (fabsf(d) < SIM_TAU) fallback = true;
             else sel = d < 0.f;
+            // near a zero of the shape factor the intensity's relative error is
+            // that of |s| - s_zero: take s from FP64 there too
+            if (sel && !fallback) {
+                if (c.shape == DS_SHAPE_LINEAR) {
+                    const float dz = (fabsf(s.hi) - c.width_dd.hi) + (sg * s.lo - c.width_dd.lo);
+                    if (fabsf(dz) < SIM_TAU_SF) fallback = true;
+                } else if (c.shape == DS_SHAPE_SINC || c.shape == DS_SHAPE_SIN2C) {
+                    const float x = fabsf(s.hi + s.lo) * c.mw_dd.hi;  // |s| m / w
+                    const float n = rintf(x);
+                    if (n >= 1.f && fabsf(x - n) < SIM_TAU_SF * c.mw_dd.hi) fallback = true;
+                }
+            }
         } else {
             const float zs = Sa + Sb;
             const float rp = r + c.Pt_f, rm = r - c.Pt_f;

@@ -298,7 +298,7 @@ def test_line_screen_matches_row_screen(name, crystal, r, eps):
     for screen in ("rows", "lines"):
         st = gen.settings(eps)
         st.screen = screen
-        res[screen] = simulate_phase(table, qd, st, r, SpotBuffers(dev))
+        res[screen] = simulate_phase(table, qd, st, r, SpotBuffers(dev, with_excitation_error=True))
     a, b = res["rows"], res["lines"]
     assert a.total == b.total
     assert np.array_equal(a.offsets.cpu().numpy(), b.offsets.cpu().numpy())
