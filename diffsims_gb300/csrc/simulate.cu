@@ -125,7 +125,7 @@ __global__ void sim_prep_kernel(SimConst c, const int32_t *__restrict__ hkl, con
 // ------------------------------------------------------------ hkl lines ----
 // Rows come in descending (h, k, l) order, so rows sharing (h, k) form a run
 // of consecutive l values (|g|^2 is convex in l: the d-spacing filter keeps a
-// contiguous range) -- a "line".  Along a line z = A + m_z l and
+// contiguous range; only (0, 0) has a hole, at the excluded 000) -- a "line".  Along a line z = A + m_z l and
 // |g|^2 = P + 2 Q l + C l^2 (A = m_x h + m_y k, P = |h a* + k b*|^2,
 // Q = (h a* + k b*).c*, C = |c*|^2), so the screen z_a - G < z < z_b + G
 // becomes two quadratic inequalities in l whose roots bound the candidate
@@ -166,7 +166,10 @@ lines_kernel(SimConst c, const int32_t *__restrict__ hkl, LineP *__restrict__ li
             if (row_is_zero(hkl, j)) {
                 atomicMin(&meta[1], (int)j);
             } else {
-                start[it] = j == 0 || hkl[3 * j - 3] != hkl[3 * j] || hkl[3 * j - 2] != hkl[3 * j + 1];
+                // a line is a run of equal (h, k) with consecutive l; the (0, 0) run
+                // is split at the missing 000 row
+                start[it] = j == 0 || hkl[3 * j - 3] != hkl[3 * j] || hkl[3 * j - 2] != hkl[3 * j + 1] ||
+                            hkl[3 * j - 1] != hkl[3 * j + 2] + 1;
             }
         }
         cnt += start[it] ? 1 : 0;
@@ -193,7 +196,9 @@ lines_kernel(SimConst c, const int32_t *__restrict__ hkl, LineP *__restrict__ li
         const long long j = base + it;
         const int h = hkl[3 * j], k = hkl[3 * j + 1];
         long long e = j + 1;
-        while (e < c.n_hkl && hkl[3 * e] == h && hkl[3 * e + 1] == k && !row_is_zero(hkl, e)) ++e;
+        while (e < c.n_hkl && hkl[3 * e] == h && hkl[3 * e + 1] == k && hkl[3 * e + 2] == hkl[3 * e - 1] - 1 &&
+               !row_is_zero(hkl, e))
+            ++e;
         // P, Q in FP64 from the reciprocal basis (rows a*, b*, c*)
         double v[3];
         for (int t = 0; t < 3; ++t) v[t] = (double)h * c.recip[t] + (double)k * c.recip[3 + t];
