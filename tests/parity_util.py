@@ -98,6 +98,9 @@ def compare(spots, crystal, quats, p: ok.SimParams, rtol=1e-5, flip_window=1e-9,
         den = np.maximum(np.abs(Ir), 1e-300)
         rel = np.abs(Ig - Ir) / den
         rel = np.where((Ir == 0) & (Ig == 0), 0.0, rel)
+        noise = (Ir <= 1e-24 * f2_scale) & (Ig <= 1e-24 * f2_scale)  # round-off on both sides
+        stats["noise_spots"] += int(noise.sum())
+        rel = np.where(noise, 0.0, rel)
         if rel.size:
             stats["max_rel_I"] = max(stats["max_rel_I"], float(rel.max()))
             pos = np.abs(xyzi[a:b][ia, :3] - r.xyz[ib]).max(axis=1) / np.maximum(g[common], 1e-3)
