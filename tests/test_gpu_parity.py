@@ -334,7 +334,7 @@ def test_empty_table_and_no_direct_beam(screen):
     for r, db in ((0.1, False), (0.1, True), (0.6, False)):
         p = ok.SimParams(accelerating_voltage=200, reciprocal_radius=r, with_direct_beam=db, max_excitation_error=0.05)
         gen = pu.generator_for(p)
-        t = PhaseTable(pu.to_phase(crystal), r, db, device=dev)
+        t = PhaseTable(pu.to_phase(crystal), r, db, "lobato", list(crystal.B), device=dev)
         st = gen.settings(0.05)
         st.screen = screen
         sp = simulate_phase(t, torch.as_tensor(q).to(dev), st, r, SpotBuffers(dev))
