@@ -181,6 +181,7 @@ def run_gpu(args):
                                  shape_factor_model=WORKLOAD["shape_factor_model"])
     r = WORKLOAD["reciprocal_radius"]
     settings = gen.settings(WORKLOAD["max_excitation_error"], form="mixed")
+    settings.screen = args.screen
     q_dev = torch.from_numpy(q_host).to(dev)
     table = PhaseTable(phase, r, True, "lobato", list(B), form="mixed", device=dev, build=True)
     buffers = SpotBuffers(dev)
@@ -385,6 +386,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=1024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--out-dir", default=None)
+    ap.add_argument("--screen", default="auto", choices=["auto", "rows", "lines"],
+                    help="candidate screen of the orientation kernel (results are identical)")
     ap.add_argument("--device-only", action="store_true",
                     help="time only the device-resident step (for profiling); no e2e, FP64 form or CPU legs")
     args = ap.parse_args()

@@ -58,6 +58,7 @@ struct SimConst {
     int line_mode;                  // phase 1 by per-(orientation, line) intervals
     double alpha0, alpha1, beta0, beta1, csq;  // z_a = alpha0 + alpha1 g^2, z_b = beta0 + beta1 g^2, |c*|^2
     float a2f, b2f;                 // -alpha1 |c*|^2, -beta1 |c*|^2
+    float inv_a2f, inv_b2f;
     long long n_hkl, n_orient, n_tiles, capacity;
 };
 
@@ -131,10 +132,11 @@ __global__ void sim_prep_kernel(SimConst c, const int32_t *__restrict__ hkl, con
 // becomes two quadratic inequalities in l whose roots bound the candidate
 // rows of the line: a few per (orientation, line) instead of a test per row.
 struct LineP {
-    float h, k;    // line indices
-    float pa, qa;  // alpha0 - G + alpha1 P, 2 alpha1 Q
-    float pb, qb;  // beta0 + G + beta1 P, 2 beta1 Q
-    int row0, n, l_top, _pad0, _pad1, _pad2;
+    float h, k;           // line indices
+    float pa, qa;         // alpha0 - G + alpha1 P, 2 alpha1 Q
+    float pb, qb;         // beta0 + G + beta1 P, 2 beta1 Q
+    int row0, n, l_top;   // first row, rows, l of the first row (l descends along the line)
+    float kc, kq, lmax;   // |pa| + |pb|, |qa| + |qb|, max |l| (error bounds)
 };
 
 constexpr int LN_THREADS = 256;
@@ -214,7 +216,9 @@ lines_kernel(SimConst c, const int32_t *__restrict__ hkl, LineP *__restrict__ li
         L.row0 = (int)j;
         L.n = (int)(e - j);
         L.l_top = hkl[3 * j + 2];
-        L._pad0 = L._pad1 = L._pad2 = 0;
+        L.kc = fabsf(L.pa) + fabsf(L.pb);
+        L.kq = fabsf(L.qa) + fabsf(L.qb);
+        L.lmax = (float)max(abs(L.l_top), abs(L.l_top - L.n + 1));
         lines[pos] = L;
         ++pos;
     }
@@ -234,57 +238,48 @@ __device__ __forceinline__ void set_bit_range(uint32_t *row, int j1, int j2) {
 // Candidate rows of one (orientation, line): the l where
 //   qa(l) = a2 l^2 + (m_z - qa) l + (A - pa) > 0    (z > z_a - G; a2 < 0: between roots)
 //   qb(l) = b2 l^2 + (m_z - qb) l + (A - pb) < 0    (z < z_b + G; b2 < 0: outside roots)
-// Roots by the stable quadratic formula; every root is pushed outward (the
-// kept set only grows) by its FP32 error bound, so the rows marked are a
-// superset of the rows the exact screen keeps.
+// Roots by the stable quadratic formula with fast reciprocal / square-root
+// approximations (a few ulp); every root is pushed outward (the kept set only
+// grows) by a bound on its FP32 error plus 1e-3 of a row, so the rows marked
+// are a superset of the rows the exact screen keeps.
 __device__ __forceinline__ void line_candidates(const SimConst &c, const LineP &L, float mx, float my, float mz,
                                                 uint32_t *row) {
     const float A = fmaf(mx, L.h, my * L.k);
     const float ca1 = mz - L.qa, ca0 = A - L.pa;
     const float cb1 = mz - L.qb, cb0 = A - L.pb;
-    // FP32 error of the constant terms (|A| and |p| are O(1)): a few ulps
-    const float lmax = (float)max(abs(L.l_top), abs(L.l_top - L.n + 1));
-    const float dc = 8.f * 5.96e-8f *
-                         (fabsf(mx * L.h) + fabsf(my * L.k) + fabsf(L.pa) + fabsf(L.pb) +
-                          (fabsf(mz) + fabsf(L.qa) + fabsf(L.qb)) * lmax) + 1e-12f;
+    // FP32 error bound of the coefficients (L.kc = |pa| + |pb|, L.kq = |qa| + |qb|, L.lmax = max |l|)
+    const float dc = 8.f * 5.96e-8f * (fabsf(mx * L.h) + fabsf(my * L.k) + L.kc + (fabsf(mz) + L.kq) * L.lmax) + 1e-12f;
     const float fa = -4.f * c.a2f * ca0;
-    float Da = fmaf(ca1, ca1, fa);
-    Da += 1e-5f * (ca1 * ca1 + fabsf(fa)) + 4.f * fabsf(c.a2f) * dc;
+    const float Da = fmaf(ca1, ca1, fa) + 1e-5f * (ca1 * ca1 + fabsf(fa)) + 4.f * fabsf(c.a2f) * dc;
     if (!(Da > 0.f)) return;  // qa <= 0 on the whole line
-    const float sa = sqrtf(Da);
+    const float ia = rsqrtf(Da);
+    const float sa = Da * ia;
     const float ta = -0.5f * (ca1 + copysignf(sa, ca1));
-    const float r1 = ca0 / ta, r2 = ta / c.a2f;
-    const float ma = 2.f * dc / sa + 1e-3f;
+    const float r1 = __fdividef(ca0, ta), r2 = ta * c.inv_a2f;
+    const float ma = 2.f * dc * ia + 1e-3f + 1e-5f * (fabsf(r1) + fabsf(r2));
     const float a_lo = fminf(r1, r2) - ma, a_hi = fmaxf(r1, r2) + ma;
     const float fb = -4.f * c.b2f * cb0;
-    float Db = fmaf(cb1, cb1, fb);
-    Db -= 1e-5f * (cb1 * cb1 + fabsf(fb)) + 4.f * fabsf(c.b2f) * dc;
+    const float Db = fmaf(cb1, cb1, fb) - 1e-5f * (cb1 * cb1 + fabsf(fb)) - 4.f * fabsf(c.b2f) * dc;
     float b_lo = INFINITY, b_hi = -INFINITY;  // excluded open interval (b_lo, b_hi)
     if (Db > 0.f) {
-        const float sb = sqrtf(Db);
+        const float ib = rsqrtf(Db);
+        const float sb = Db * ib;
         const float tb = -0.5f * (cb1 + copysignf(sb, cb1));
-        const float s1 = cb0 / tb, s2 = tb / c.b2f;
-        const float mb = 2.f * dc / sb + 1e-3f;
+        const float s1 = __fdividef(cb0, tb), s2 = tb * c.inv_b2f;
+        const float mb = 2.f * dc * ib + 1e-3f + 1e-5f * (fabsf(s1) + fabsf(s2));
         b_lo = fminf(s1, s2) + mb;
         b_hi = fmaxf(s1, s2) - mb;
     }
-    const int l_bot = L.l_top - L.n + 1;
-    float x1[2], x2[2];
-    int ni;
-    if (!(b_lo < b_hi)) {
-        x1[0] = a_lo; x2[0] = a_hi; ni = 1;
-    } else {
-        x1[0] = a_lo; x2[0] = fminf(a_hi, b_lo);
-        x1[1] = fmaxf(a_lo, b_hi); x2[1] = a_hi;
-        ni = 2;
-    }
-    for (int q = 0; q < ni; ++q) {
-        if (!(x1[q] <= x2[q])) continue;
-        const float flo = fmaxf(ceilf(x1[q]), (float)l_bot);
-        const float fhi = fminf(floorf(x2[q]), (float)L.l_top);
-        if (!(flo <= fhi)) continue;
-        const int lo = (int)flo, hi = (int)fhi;
-        set_bit_range(row, L.row0 + (L.l_top - hi), L.row0 + (L.l_top - lo));
+    const float l_bot = (float)(L.l_top - L.n + 1), l_top = (float)L.l_top;
+    const bool split = b_lo < b_hi;
+    // first interval (a_lo, min(a_hi, b_lo)); second (max(a_lo, b_hi), a_hi) when B excludes a middle part
+    const float x2a = split ? fminf(a_hi, b_lo) : a_hi;
+    float flo = fmaxf(ceilf(a_lo), l_bot), fhi = fminf(floorf(x2a), l_top);
+    if (flo <= fhi) set_bit_range(row, L.row0 + (L.l_top - (int)fhi), L.row0 + (L.l_top - (int)flo));
+    if (split) {
+        flo = fmaxf(ceilf(fmaxf(a_lo, b_hi)), l_bot);
+        fhi = fminf(floorf(a_hi), l_top);
+        if (flo <= fhi) set_bit_range(row, L.row0 + (L.l_top - (int)fhi), L.row0 + (L.l_top - (int)flo));
     }
 }
 
@@ -1334,6 +1329,8 @@ extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t
         c.csq = t->recip[6] * t->recip[6] + t->recip[7] * t->recip[7] + t->recip[8] * t->recip[8];
         c.a2f = (float)(-c.alpha1 * c.csq);
         c.b2f = (float)(-c.beta1 * c.csq);
+        c.inv_a2f = 1.f / c.a2f;
+        c.inv_b2f = 1.f / c.b2f;
     }
     c.n_tiles = P.n_tiles;
     c.capacity = out->capacity;
