@@ -79,13 +79,15 @@ enum { ACC_MAXI = 0, ACC_MINPOS = 1, ACC_CNT = 2, ACC_OFF = 3, ACC_PART0 = 4, AC
 __host__ __device__ constexpr int acc_stride(int O) { return O * ACC_WORDS + 8; }
 
 struct SimSmem {
-    size_t orient, bitmap, acc, total;
+    size_t orient, bitmap, acc, queue, total;
 };
+constexpr int SIM_QCAP = 128;  // per-warp candidate queue (shared memory)
 __host__ __device__ inline SimSmem sim_smem_layout(int O, int Ws) {
     SimSmem L;
     size_t o = 0;
     L.orient = o; o += (size_t)2 * O * sizeof(OrientP);  // two pipeline buffers
     L.acc = o; o += (size_t)2 * acc_stride(O) * sizeof(unsigned long long);
+    L.queue = o; o += (size_t)SIM_WARPS * SIM_QCAP * sizeof(int32_t);
     o = (o + 15) & ~(size_t)15;
     L.bitmap = o; o += (((size_t)O * Ws + 3) & ~(size_t)3) * sizeof(uint32_t);  // whole uint4s (zeroing)
     L.total = o;
@@ -318,7 +320,8 @@ __device__ inline bool select_mixed(const SimConst &c, const OrientP &op, const 
     const float u = r2.hi * c.inv_k0sq;
     bool fallback = u > SIM_U_MAX;
     bool sel = false;
-    r = sqrtf(fmaxf(r2.hi, 0.f));
+    r = 0.f;
+    if (c.prec != DS_PRECESSION_NONE) r = sqrtf(fmaxf(r2.hi, 0.f));
     if (!fallback) {
         const float corr = u * (0.25f + u * (0.125f + u * (0.078125f + u * (0.0546875f + u * 0.041015625f))));
         const float w0h = r2.hi * c.c2k0_dd.hi;
@@ -632,6 +635,63 @@ __device__ __forceinline__ void for_each_bit_pair(const uint32_t *row, int w0, i
     }
 }
 
+// Set bits of bitmap words [w0, w1) of one orientation in row order, as dense
+// pairs: lanes append the rows of their own set bits to a per-warp queue in
+// shared memory (their places known from one scan of the popcounts: no lane
+// searches for its candidate), and full queues are handed to fn two per lane:
+// fn(j0, rank0, valid0, j1, rank1, valid1).  A group denser than the queue is
+// appended in several rounds.
+template <int K, typename Fn>
+__device__ __forceinline__ void for_each_bit_queued(const uint32_t *row, int w0, int w1, int lane, int32_t *q,
+                                                    Fn fn) {
+    int qn = 0, rank_base = 0;
+    for (int g0 = w0; g0 <= w1; g0 += 32 * K) {
+        const bool last = g0 >= w1;
+        uint32_t wd[K];
+        int cnt = 0;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int wi = g0 + lane * K + k;
+            wd[k] = (!last && wi < w1) ? row[wi] : 0u;
+            cnt += __popc(wd[k]);
+        }
+        const int incl = warp_inclusive_scan(cnt, lane);
+        const int total = __shfl_sync(FULL_MASK, incl, 31);
+        int consumed = 0;
+        while (consumed < total || (last && qn > 0)) {
+            const int take = min(SIM_QCAP - qn, total - consumed);
+            if (take > 0) {
+                int r = incl - cnt;  // group rank of this lane's first bit
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    uint32_t w = wd[k];
+                    const int wbase = (g0 + lane * K + k) * 32;
+                    while (w) {
+                        const int b = __ffs(w) - 1;
+                        w &= w - 1u;
+                        if (r >= consumed && r < consumed + take) q[qn + r - consumed] = wbase + b;
+                        ++r;
+                    }
+                }
+                qn += take;
+                consumed += take;
+            }
+            if (qn == SIM_QCAP || (last && qn > 0) || (consumed < total && take <= 0)) {
+                __syncwarp();
+                for (int r0 = 0; r0 < qn; r0 += 64) {
+                    const int ra = r0 + lane, rb = r0 + 32 + lane;
+                    const bool va = ra < qn, vb = rb < qn;
+                    const long long ja = va ? (long long)q[ra] : 0, jb = vb ? (long long)q[rb] : 0;
+                    fn(ja, rank_base + ra, va, jb, rank_base + rb, vb);
+                }
+                rank_base += qn;
+                qn = 0;
+                __syncwarp();
+            }
+        }
+    }
+}
+
 // Per-CTA staging in global scratch (L2-resident): the screened candidate
 // rows of the tile in (orientation, row) order and their intensities, so the
 // refine pass evaluates full warps of candidates once and the write pass
@@ -654,6 +714,7 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
     OrientP *sop_buf = reinterpret_cast<OrientP *>(smem + Ls.orient);                  // [2][O]
     unsigned long long *acc_buf = reinterpret_cast<unsigned long long *>(smem + Ls.acc);  // [2][ACC_STRIDE]
     uint32_t *bitmap = reinterpret_cast<uint32_t *>(smem + Ls.bitmap);                   // [O][Ws]
+    int32_t *wqueue = reinterpret_cast<int32_t *>(smem + Ls.queue) + (threadIdx.x >> 5) * SIM_QCAP;
     __shared__ long long s_tile, s_prefix;
     __shared__ int s_defer;
     __shared__ int s_unit[4];  // work-unit counters of the dynamic phases
@@ -874,8 +935,8 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
                 if (base != NO_STAGE) {
                     // evaluate each screened candidate once; stage (row, x, y, z, I)
                     // in candidate order, I = -1 for rejected candidates
-                    for_each_bit_pair<4>(row, w0, w1, lane,
-                                         [&](long long ja, int ra, bool va, long long jb, int rb, bool vb) {
+                    for_each_bit_queued<4>(row, w0, w1, lane, wqueue,
+                                           [&](long long ja, int ra, bool va, long long jb, int rb, bool vb) {
                         SpotIn ia, ib;
                         if (va) ia = load_spot<FORM>(T, ja);
                         if (vb) ib = load_spot<FORM>(T, jb);
@@ -1167,11 +1228,12 @@ static const void *kernel_ptr(int O, int form) {
 // Launch plan: tile size, persistent grid (resident CTAs, at most one per
 // tile) and the scratch layout.
 static ds_status make_plan(const ds_sim_params *p, const ds_phase_table *t, long long n_orient, SimPlan &P) {
-    // screen: per-(orientation, line) intervals for the mixed form without
-    // precession (the band of the precessing sphere is not quadratic in l),
-    // per-row tests otherwise or on request
+    // screen: per-row tests by default; per-(orientation, line) intervals on
+    // request for the mixed form without precession (the band of the
+    // precessing sphere is not quadratic in l).  With ~30 rows per line the
+    // interval arithmetic costs about what the row tests do.
     P.line_mode = (p->form == DS_FORM_MIXED && p->precession_mode == DS_PRECESSION_NONE &&
-                   p->screen != DS_SCREEN_ROWS && t->n_hkl > 0) ? 1 : 0;
+                   p->screen == DS_SCREEN_LINES && t->n_hkl > 0) ? 1 : 0;
     P.line_tiles = (t->n_hkl + LN_TILE - 1) / LN_TILE;
     P.O = pick_O(p, t->n_hkl, n_orient);
     if (p->form == DS_FORM_FP64 && P.O > 16) P.O = 16;
