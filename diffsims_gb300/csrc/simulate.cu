@@ -645,51 +645,50 @@ template <int K, typename Fn>
 __device__ __forceinline__ void for_each_bit_queued(const uint32_t *row, int w0, int w1, int lane, int32_t *q,
                                                     Fn fn) {
     int qn = 0, rank_base = 0;
-    for (int g0 = w0; g0 <= w1; g0 += 32 * K) {
-        const bool last = g0 >= w1;
+    auto flush = [&]() {
+        __syncwarp();
+        for (int r0 = 0; r0 < qn; r0 += 64) {
+            const int ra = r0 + lane, rb = r0 + 32 + lane;
+            const bool va = ra < qn, vb = rb < qn;
+            const long long ja = va ? (long long)q[ra] : 0, jb = vb ? (long long)q[rb] : 0;
+            fn(ja, rank_base + ra, va, jb, rank_base + rb, vb);
+        }
+        rank_base += qn;
+        qn = 0;
+        __syncwarp();
+    };
+    for (int g0 = w0; g0 < w1; g0 += 32 * K) {
         uint32_t wd[K];
         int cnt = 0;
 #pragma unroll
         for (int k = 0; k < K; ++k) {
             const int wi = g0 + lane * K + k;
-            wd[k] = (!last && wi < w1) ? row[wi] : 0u;
+            wd[k] = wi < w1 ? row[wi] : 0u;
             cnt += __popc(wd[k]);
         }
         const int incl = warp_inclusive_scan(cnt, lane);
         const int total = __shfl_sync(FULL_MASK, incl, 31);
         int consumed = 0;
-        while (consumed < total || (last && qn > 0)) {
+        while (consumed < total) {
+            if (qn == SIM_QCAP) flush();
             const int take = min(SIM_QCAP - qn, total - consumed);
-            if (take > 0) {
-                int r = incl - cnt;  // group rank of this lane's first bit
+            int r = incl - cnt;  // group rank of this lane's first bit
 #pragma unroll
-                for (int k = 0; k < K; ++k) {
-                    uint32_t w = wd[k];
-                    const int wbase = (g0 + lane * K + k) * 32;
-                    while (w) {
-                        const int b = __ffs(w) - 1;
-                        w &= w - 1u;
-                        if (r >= consumed && r < consumed + take) q[qn + r - consumed] = wbase + b;
-                        ++r;
-                    }
+            for (int k = 0; k < K; ++k) {
+                uint32_t w = wd[k];
+                const int wbase = (g0 + lane * K + k) * 32;
+                while (w) {
+                    const int b = __ffs(w) - 1;
+                    w &= w - 1u;
+                    if (r >= consumed && r < consumed + take) q[qn + r - consumed] = wbase + b;
+                    ++r;
                 }
-                qn += take;
-                consumed += take;
             }
-            if (qn == SIM_QCAP || (last && qn > 0) || (consumed < total && take <= 0)) {
-                __syncwarp();
-                for (int r0 = 0; r0 < qn; r0 += 64) {
-                    const int ra = r0 + lane, rb = r0 + 32 + lane;
-                    const bool va = ra < qn, vb = rb < qn;
-                    const long long ja = va ? (long long)q[ra] : 0, jb = vb ? (long long)q[rb] : 0;
-                    fn(ja, rank_base + ra, va, jb, rank_base + rb, vb);
-                }
-                rank_base += qn;
-                qn = 0;
-                __syncwarp();
-            }
+            qn += take;
+            consumed += take;
         }
     }
+    if (qn > 0) flush();
 }
 
 // Per-CTA staging in global scratch (L2-resident): the screened candidate
