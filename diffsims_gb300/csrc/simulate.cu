@@ -41,7 +41,7 @@ constexpr int SIM_MAX_O = 32;
 // tuning knobs (compile time): word ranges per orientation in the refine and
 // write passes, and chunks screened per step in phase 1
 #ifndef DS_SIM_PARTS
-#define DS_SIM_PARTS 4
+#define DS_SIM_PARTS 2
 #endif
 #ifndef DS_SIM_SCREEN_CHUNKS
 #define DS_SIM_SCREEN_CHUNKS 2
