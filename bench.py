@@ -40,6 +40,9 @@ WORKLOAD = dict(workload="triclinic P1, 200 atoms, 200 kV, r=2.0, s_max=0.02, lo
                 cell_seed=1, orientation_seed=0, n_orientations=100_000, n_atoms=200, reciprocal_radius=2.0,
                 max_excitation_error=0.02, accelerating_voltage=200, shape_factor_model="lorentzian")
 METRIC = "orientation patterns/s"
+# measured: (dram__bytes_read.sum + dram__bytes_write.sum) / spots written, one
+# simulate_kernel launch on 8192 orientations of the workload below
+DRAM_BYTES_PER_SPOT = 21.5
 UNIT = "patterns/s"
 
 
@@ -259,11 +262,10 @@ def run_gpu(args):
     except OSError:
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "simulate_kernel_traffic.json")
-    if os.path.exists(tpath):
-        tj = json.load(open(tpath))
-        traffic = tj.get("dram_bytes_per_pair", 0) * n_o * n_h + tj.get("dram_bytes_per_spot", 0) * total_spots or None
+    # DRAM bytes of one launch: the per-spot figure of the ncu capture in
+    # profiles/simulate_kernel_p1_8192.md (8192 orientations of this workload)
+    # scaled by the spots of this launch
+    traffic = DRAM_BYTES_PER_SPOT * total_spots
 
     # ---- FP64 comparator form on a subset, and the error of the mixed form against it
     n_cmp = min(args.fp64_orientations, n_o)

@@ -159,21 +159,26 @@ class PhaseSpots:
         return self.offsets.shape[0] - 1
 
     def host(self, pinned=False):
-        """Host copies (offsets int64, hkl (total, 3) int32, xyz (total, 3)
-        float32, intensity float32).  With ``pinned`` the device arrays land in
-        page-locked staging buffers reused across calls."""
+        """Host copies of the CSR arrays: (offsets int64, hkl_index int32
+        (row of the phase table), xyzi (total, 4) float32: x, y, z, I).  With
+        ``pinned`` the copies go through page-locked memory.  Miller indices
+        are gathered per pattern on access (``hkl_of``)."""
         if self._host is None:
             if pinned:
                 off, idx, xyzi = _fetch_pinned((self.offsets, self.hkl_index, self.xyzi))
             else:
                 off, idx, xyzi = self.offsets.cpu(), self.hkl_index.cpu(), self.xyzi.cpu()
             torch.cuda.current_stream().synchronize()
-            table_hkl = self.table.hkl_host()
-            idx = idx.numpy()
-            hkl = table_hkl[idx] if self.total else np.zeros((0, 3), np.int32)
-            xyzi = xyzi.numpy()
-            self._host = (off.numpy(), hkl, xyzi[:, :3], xyzi[:, 3])
+            self._host = (off.numpy(), idx.numpy(), xyzi.numpy())
         return self._host
+
+    def pattern(self, i):
+        """(hkl (n, 3) int, xyz (n, 3) float64, intensity (n,) float64) of orientation i."""
+        off, idx, xyzi = self.host()
+        a, b = off[i], off[i + 1]
+        hkl = self.table.hkl_host()[idx[a:b]] if b > a else np.zeros((0, 3), np.int32)
+        rec = xyzi[a:b].astype(np.float64)
+        return hkl, rec[:, :3], rec[:, 3]
 
     def nbytes(self):
         return self.offsets.numel() * 8 + self.total * (4 + 16)

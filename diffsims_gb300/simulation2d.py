@@ -115,10 +115,8 @@ class _PhaseCoordinates:
             i += n
         if not 0 <= i < n:
             raise IndexError(i)
-        off, hkl, xyz, inten = self.spots.host()
-        a, b = off[i], off[i + 1]
-        return DiffractingVector(self.phase, xyz[a:b].astype(np.float64), inten[a:b].astype(np.float64), hkl[a:b],
-                                 self.rotation[i])
+        hkl, xyz, inten = self.spots.pattern(i)
+        return DiffractingVector(self.phase, xyz, inten, hkl, self.rotation[i])
 
     def __iter__(self):
         for i in range(len(self)):
