@@ -174,6 +174,19 @@ ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t, const dou
                       int64_t n_orient, ds_spots *out, void *scratch, size_t scratch_bytes,
                       int32_t *status, void *stream);
 
+/* No counterpart in the reference.  ds_simulate for callers that cannot
+ * allocate device memory at all (e.g. a real-time loop that must not enter the
+ * CUDA allocator, or a host whose memory manager owns all device memory):
+ * the scratch of ds_simulate comes from a static 64 MiB device array in the
+ * library instead of a caller buffer; inputs and outputs are still the
+ * caller's.  Sizes whose scratch does not fit (after shrinking the candidate
+ * staging) return DS_ERR_INVALID_ARGUMENT.  All calls share the array: calls
+ * that overlap on the GPU race (one stream is safe).  The first call on a
+ * device looks the array up (cudaGetSymbolAddress): make it before any stream
+ * capture.  Allocates nothing. */
+ds_status ds_simulate_noalloc(const ds_sim_params *p, const ds_phase_table *t, const double *quats,
+                              int64_t n_orient, ds_spots *out, int32_t *status, void *stream);
+
 /* ------------------------------------------------------------------------ */
 /* FP32 FMA throughput probe (no counterpart in the reference): blocks x 256
  * threads, each 8 chains x 16 x iters fused multiply-adds; out holds
