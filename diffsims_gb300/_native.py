@@ -37,7 +37,8 @@ DS_PRECESSION_INTEGRAL = 2
 EXPORTED_SYMBOLS = (
     "ds_box_extent", "ds_enumerate_scratch_bytes", "ds_enumerate_hkl",
     "ds_structure_factor_scratch_bytes", "ds_structure_factors", "ds_kinematical_intensities",
-    "ds_simulate_scratch_bytes", "ds_simulate", "ds_probe_fp32_fma", "ds_last_error", "ds_version",
+    "ds_simulate_scratch_bytes", "ds_simulate", "ds_rasterize_scratch_bytes", "ds_rasterize",
+    "ds_probe_fp32_fma", "ds_last_error", "ds_version",
 )
 
 
@@ -66,6 +67,13 @@ class ds_phase_table(C.Structure):
 class ds_spots(C.Structure):
     _fields_ = [("offsets", C.c_void_p), ("hkl_index", C.c_void_p), ("xyzi", C.c_void_p),
                 ("capacity", C.c_int64), ("total", C.c_void_p), ("excitation_error", C.c_void_p)]
+
+
+class ds_raster_params(C.Structure):
+    _fields_ = [("height", C.c_int32), ("width", C.c_int32), ("mirrored", C.c_int32), ("fast", C.c_int32),
+                ("normalize", C.c_int32), ("_pad", C.c_int32), ("sigma", C.c_double), ("calibration", C.c_double),
+                ("center_x", C.c_double), ("center_y", C.c_double), ("in_plane_angle", C.c_double),
+                ("clip_threshold", C.c_double), ("truncate", C.c_double), ("pixel_snap", C.c_double)]
 
 
 assert C.sizeof(ds_atom) == 48
@@ -102,11 +110,14 @@ def load_library(require_cuda: bool = True):
             lib.ds_simulate_scratch_bytes.restype = sz
             lib.ds_simulate.argtypes = [C.POINTER(ds_sim_params), C.POINTER(ds_phase_table), vp, i64,
                                         C.POINTER(ds_spots), vp, sz, vp, vp]
+            lib.ds_rasterize_scratch_bytes.argtypes = [C.POINTER(ds_raster_params), i64]
+            lib.ds_rasterize_scratch_bytes.restype = sz
+            lib.ds_rasterize.argtypes = [C.POINTER(ds_raster_params), vp, vp, i64, i64, vp, vp, sz, vp, vp]
             lib.ds_probe_fp32_fma.argtypes = [i64, i32, vp, vp]
             lib.ds_last_error.restype = C.c_char_p
             lib.ds_version.restype = C.c_char_p
             for name in ("ds_box_extent", "ds_enumerate_hkl", "ds_structure_factors", "ds_kinematical_intensities",
-                         "ds_simulate", "ds_probe_fp32_fma"):
+                         "ds_simulate", "ds_rasterize", "ds_probe_fp32_fma"):
                 getattr(lib, name).restype = C.c_int32
             _lib = lib
     if require_cuda and not torch.cuda.is_available():

@@ -1,0 +1,541 @@
+// Detector images of spot patterns (the reference's per-pattern
+// Simulation2D.get_diffraction_pattern, diffsims/simulations/simulation2d.py:357-442,
+// with diffsims/pattern/detector_functions.py:251-359), many patterns per launch.
+//
+// Per pattern, in one CTA of a persistent grid:
+//   1. every spot -> pixel coordinates in FP64 (divide by the calibration,
+//      in-plane rotation / mirror, shift to the direct beam), the in-frame test;
+//   2. fast mode: truncate to whole pixels and keep, per pixel, the LAST spot
+//      (numpy's assignment order) through a shared-memory hash of pixel ->
+//      largest spot index; sub-pixel mode: each spot's clip box;
+//   3. ordered compaction of the surviving spots with their row / column ranges;
+//   4. the image row by row, one warp per row: the spots covering the row
+//      (ballot over the compacted list), each adding amp * rowweight *
+//      colweight into the lanes' column registers, stored as float4 streams.
+// Fast mode is a delta image filtered by scipy.ndimage.gaussian_filter (mode
+// "reflect", radius int(truncate sigma + 0.5), weights exp(-x^2 / 2 sigma^2)
+// normalised); the filter is separable and linear, so every spot adds
+// I * A(y, Y) * A(x, X) with A the 1-D weight including the mirrored images of
+// the half-sample symmetric extension.  Sub-pixel mode adds
+// I / (2 pi sigma^2) exp(-d^2 / 2 sigma^2) over the spot's box.  Rows no spot
+// reaches are written as zeros directly; normalisation takes a first pass over
+// the covered rows for the maximum.
+//
+// The image is the only large traffic (4 H W bytes per pattern, written once):
+// the kernel is bound by HBM writes.
+#include <algorithm>
+#include <cmath>
+
+#include "common.cuh"
+
+namespace ds {
+
+constexpr int RAS_THREADS = 256;
+constexpr int RAS_WARPS = RAS_THREADS / 32;
+constexpr int RAS_K = 2;                  // float4 column chunks per lane in one row segment
+constexpr int RAS_SEG = 32 * 4 * RAS_K;   // columns per row segment
+constexpr int RAS_MAX_R = 511;            // fast mode: largest filter radius
+constexpr size_t RAS_SMEM_LIMIT = 200 * 1024;
+
+struct RasterConst {
+    int H, W, R;
+    int fast, normalize;
+    int NS, T;          // arena capacity in spots, hash slots (power of two >= 2 NS)
+    double cal, cx, cy, ca, sa, mf, snap;
+    double pref, exp_pref, clip;
+    float wt[RAS_MAX_R + 1];  // fast: filter weights w[|d|], d = 0..R
+};
+
+struct RasterArena {
+    int *key;     // fast: pixel index Y W + X, or -1; sub-pixel: 0 kept / -1
+    int *slot;    // fast: hash slot of the spot
+    int *hkey, *hidx;
+    float *amp;
+    int *ylo, *yhi, *xlo, *xhi;
+    double *px, *py;
+    unsigned *rows;  // covered-row bitmap
+    int *misc;       // warp totals (RAS_WARPS), scalars
+    float *wmax;     // per-warp maxima (RAS_WARPS)
+};
+
+__host__ __device__ inline size_t ras_align(size_t x) { return (x + 15) & ~(size_t)15; }
+
+__host__ __device__ inline size_t raster_arena_bytes(int NS, int T, int H) {
+    size_t o = 0;
+    o += ras_align((size_t)NS * 4) * 2;       // key, slot
+    o += ras_align((size_t)T * 4) * 2;        // hkey, hidx
+    o += ras_align((size_t)NS * 4) * 5;       // amp, ylo, yhi, xlo, xhi
+    o += ras_align((size_t)NS * 8) * 2;       // px, py
+    o += ras_align((size_t)((H + 31) / 32) * 4);
+    o += ras_align(64 * 4) + ras_align(RAS_WARPS * 4);
+    return o;
+}
+
+__device__ inline RasterArena carve(unsigned char *base, int NS, int T, int H) {
+    RasterArena A;
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        unsigned char *p = base + o;
+        o += ras_align(bytes);
+        return p;
+    };
+    A.key = (int *)take((size_t)NS * 4);
+    A.slot = (int *)take((size_t)NS * 4);
+    A.hkey = (int *)take((size_t)T * 4);
+    A.hidx = (int *)take((size_t)T * 4);
+    A.amp = (float *)take((size_t)NS * 4);
+    A.ylo = (int *)take((size_t)NS * 4);
+    A.yhi = (int *)take((size_t)NS * 4);
+    A.xlo = (int *)take((size_t)NS * 4);
+    A.xhi = (int *)take((size_t)NS * 4);
+    A.px = (double *)take((size_t)NS * 8);
+    A.py = (double *)take((size_t)NS * 8);
+    A.rows = (unsigned *)take((size_t)((H + 31) / 32) * 4);
+    A.misc = (int *)take(64 * 4);
+    A.wmax = (float *)take(RAS_WARPS * 4);
+    return A;
+}
+
+// Pixel coordinates of one spot, in the reference's order of operations:
+// divide by the calibration, rotate by the in-plane angle (mirrored: negated
+// azimuth), shift to the direct beam.  For angle 0 the rotation is exact.
+__device__ inline void pixel_xy(const RasterConst &c, float4 e, double &X, double &Y) {
+    const double u = (double)e.x / c.cal, v = c.mf * ((double)e.y / c.cal);
+    X = (u * c.ca - v * c.sa) + c.cx;
+    Y = (v * c.ca + u * c.sa) + c.cy;
+    if (c.snap > 0.0) {
+        const double rx = rint(X), ry = rint(Y);
+        if (fabs(X - rx) <= c.snap) X = rx;
+        if (fabs(Y - ry) <= c.snap) Y = ry;
+    }
+}
+
+__device__ inline bool in_frame(const RasterConst &c, double X, double Y) {
+    return X >= 0.0 && X < (double)c.W && Y >= 0.0 && Y < (double)c.H;
+}
+
+// Sub-pixel mode: the clip radius of a spot (NaN: the spot is skipped),
+// detector_functions.py:337-343.
+__device__ inline double clip_radius(const RasterConst &c, double I) {
+    return sqrt(log(c.clip / (c.pref * I)) / c.exp_pref);
+}
+
+// 1-D filter weight that a delta at P contributes to position x on a line of
+// n pixels: sum over d in [-R, R] of w[|d|] where the half-sample symmetric
+// extension (period 2n) maps x + d onto P.
+__device__ inline float reflect_weight(const RasterConst &c, int x, int P, int n) {
+    const int R = c.R;
+    float v = 0.f;
+    if (R < n) {
+        const int d = abs(x - P);
+        if (d <= R) v += c.wt[d];
+        const int m1 = x + P + 1;          // image at -P-1
+        if (m1 <= R) v += c.wt[m1];
+        const int m2 = 2 * n - 1 - P - x;  // image at 2n-1-P
+        if (m2 <= R) v += c.wt[m2];
+        return v;
+    }
+    // images P + 2kn and 2kn - 1 - P within [x - R, x + R]
+    const int per = 2 * n;
+    for (int fam = 0; fam < 2; ++fam) {
+        const int base = fam == 0 ? P : -P - 1;
+        const int k0 = (int)floor((double)(x - R - base) / per);
+        for (int k = k0;; ++k) {
+            const int q = base + k * per;
+            if (q > x + R) break;
+            if (q >= x - R) v += c.wt[abs(q - x)];
+        }
+    }
+    return v;
+}
+
+__device__ __forceinline__ float row_weight(const RasterConst &c, const RasterArena &A, int k, int y) {
+    if (c.fast) return reflect_weight(c, y, (int)A.py[k], c.H);
+    const double dy = (double)y - A.py[k];
+    return expf((float)(c.exp_pref * dy * dy));
+}
+
+__device__ __forceinline__ float col_weight(const RasterConst &c, const RasterArena &A, int k, int x) {
+    if (c.fast) return reflect_weight(c, x, (int)A.px[k], c.W);
+    const double dx = (double)x - A.px[k];
+    return expf((float)(c.exp_pref * dx * dx));
+}
+
+__device__ __forceinline__ void st_cs(float4 *p, float4 v) {
+    asm volatile("st.global.cs.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+                 : "memory");
+}
+__device__ __forceinline__ void st_cs1(float *p, float v) {
+    asm volatile("st.global.cs.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
+}
+
+// One row segment [x0, x0 + RAS_SEG) of row y: lane registers acc[i][e] for
+// columns x0 + (lane + 32 i) * 4 + e.
+__device__ inline void row_segment(const RasterConst &c, const RasterArena &A, int n_alive, int y, int x0,
+                                   int lane, float (&acc)[RAS_K][4]) {
+#pragma unroll
+    for (int i = 0; i < RAS_K; ++i)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) acc[i][e] = 0.f;
+    const int x1 = x0 + RAS_SEG;
+    for (int k0 = 0; k0 < n_alive; k0 += 32) {
+        const int k = k0 + lane;
+        bool cov = false;
+        float a = 0.f;
+        if (k < n_alive) {
+            cov = A.ylo[k] <= y && y < A.yhi[k] && A.xlo[k] < x1 && A.xhi[k] > x0;
+            if (cov) a = A.amp[k] * row_weight(c, A, k, y);
+        }
+        unsigned m = __ballot_sync(FULL_MASK, cov);
+        while (m) {
+            const int b = __ffs(m) - 1;
+            m &= m - 1;
+            const float ab = __shfl_sync(FULL_MASK, a, b);
+            const int kk = k0 + b;
+            const int xl = A.xlo[kk], xh = A.xhi[kk];
+#pragma unroll
+            for (int i = 0; i < RAS_K; ++i) {
+                const int base = x0 + (lane + 32 * i) * 4;
+                if (base < xh && base + 4 > xl) {
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const int x = base + e;
+                        if (x >= xl && x < xh) acc[i][e] = fmaf(ab, col_weight(c, A, kk, x), acc[i][e]);
+                    }
+                }
+            }
+        }
+    }
+}
+
+template <bool VEC>
+__global__ void __launch_bounds__(RAS_THREADS, 4) raster_kernel(const RasterConst c, const int64_t *__restrict__ off,
+                                                             const float4 *__restrict__ xyzi, long long n_patterns,
+                                                             float *__restrict__ out, unsigned char *gscratch,
+                                                             size_t arena_bytes, int32_t *status) {
+    extern __shared__ __align__(16) unsigned char ras_smem[];
+    unsigned char *base = gscratch ? gscratch + (size_t)blockIdx.x * arena_bytes : ras_smem;
+    const RasterArena A = carve(base, c.NS, c.T, c.H);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int H = c.H, W = c.W;
+    const size_t img = (size_t)H * W;
+    const int nwords = (H + 31) / 32;
+
+    for (long long p = blockIdx.x; p < n_patterns; p += gridDim.x) {
+        const long long a0 = off[p];
+        const long long n_ll = off[p + 1] - a0;
+        if (n_ll > c.NS || n_ll < 0) {
+            if (tid == 0) atomicOr(status, DS_ERR_CAPACITY);
+            continue;
+        }
+        const int n = (int)n_ll;
+        int Tp = 64;
+        while (Tp < 2 * n) Tp <<= 1;
+        const int tbits = __ffs(Tp) - 1;
+        if (c.fast) {
+            for (int t = tid; t < Tp; t += RAS_THREADS) {
+                A.hkey[t] = -1;
+                A.hidx[t] = -1;
+            }
+        }
+        if (tid == 0) A.misc[RAS_WARPS] = 0;  // in-frame count
+        __syncthreads();
+
+        // ---- 1-2: pixel coordinates, frame test, last-write-wins per pixel
+        int my_in = 0;
+        for (int i = tid; i < n; i += RAS_THREADS) {
+            const float4 e = xyzi[a0 + i];
+            double X, Y;
+            pixel_xy(c, e, X, Y);
+            int key = -1;
+            if (in_frame(c, X, Y)) {
+                ++my_in;
+                if (c.fast) {
+                    key = (int)Y * W + (int)X;
+                    // open addressing; Tp >= 2 n slots, so a free slot is always found
+                    unsigned h = ((unsigned)key * 2654435761u) >> (32 - tbits);
+                    int sl = -1;
+                    for (int t = 0; t < Tp; ++t) {
+                        const int prev = atomicCAS(&A.hkey[h], -1, key);
+                        if (prev == -1 || prev == key) {
+                            atomicMax(&A.hidx[h], i);
+                            sl = (int)h;
+                            break;
+                        }
+                        h = (h + 1) & (unsigned)(Tp - 1);
+                    }
+                    A.slot[i] = sl;
+                    if (sl < 0) key = -1;
+                } else {
+                    const double rad = clip_radius(c, (double)e.w);
+                    if (!isnan(rad)) key = 0;
+                }
+            }
+            A.key[i] = key;
+        }
+        my_in = __reduce_add_sync(FULL_MASK, my_in);
+        if (lane == 0 && my_in) atomicAdd(&A.misc[RAS_WARPS], my_in);
+        __syncthreads();
+        const int n_in = A.misc[RAS_WARPS];
+
+        // ---- 3: ordered compaction of the surviving spots
+        int n_alive = 0;
+        for (int c0 = 0; c0 < n; c0 += RAS_THREADS) {
+            const int i = c0 + tid;
+            bool alive = false;
+            if (i < n && A.key[i] >= 0) alive = !c.fast || A.hidx[A.slot[i]] == i;  // slot >= 0 when key >= 0
+            const unsigned bal = __ballot_sync(FULL_MASK, alive);
+            if (lane == 0) A.misc[warp] = __popc(bal);
+            __syncthreads();
+            int wbase = 0, tot = 0;
+            for (int w = 0; w < RAS_WARPS; ++w) {
+                const int v = A.misc[w];
+                if (w < warp) wbase += v;
+                tot += v;
+            }
+            if (alive) {
+                const int k = n_alive + wbase + __popc(bal & ((1u << lane) - 1));
+                const float4 e = xyzi[a0 + i];
+                if (c.fast) {
+                    const int key = A.key[i];
+                    const int X = key % W, Y = key / W;
+                    A.px[k] = (double)X;
+                    A.py[k] = (double)Y;
+                    A.amp[k] = e.w;
+                    A.ylo[k] = max(0, Y - c.R);
+                    A.yhi[k] = min(H, Y + c.R + 1);
+                    A.xlo[k] = max(0, X - c.R);
+                    A.xhi[k] = min(W, X + c.R + 1);
+                } else {
+                    double X, Y;
+                    pixel_xy(c, e, X, Y);
+                    const double rad = clip_radius(c, (double)e.w);
+                    A.px[k] = X;
+                    A.py[k] = Y;
+                    A.amp[k] = (float)((double)e.w * c.pref);
+                    A.ylo[k] = (int)fmax(0.0, ceil(Y - rad));
+                    A.yhi[k] = (int)fmin((double)H, floor(Y + rad + 1.0));
+                    A.xlo[k] = (int)fmax(0.0, ceil(X - rad));
+                    A.xhi[k] = (int)fmin((double)W, floor(X + rad + 1.0));
+                }
+            }
+            n_alive += tot;
+            __syncthreads();
+        }
+
+        // ---- covered rows
+        for (int w = tid; w < nwords; w += RAS_THREADS) A.rows[w] = 0u;
+        __syncthreads();
+        for (int k = tid; k < n_alive; k += RAS_THREADS) {
+            const int lo = A.ylo[k], hi = A.yhi[k];
+            for (int y = lo; y < hi;) {
+                const int wi = y >> 5, b0 = y & 31;
+                const int nb = min(32 - b0, hi - y);
+                const unsigned m = (nb == 32 ? 0xffffffffu : ((1u << nb) - 1u)) << b0;
+                atomicOr(&A.rows[wi], m);
+                y += nb;
+            }
+        }
+        __syncthreads();
+
+        // ---- maximum over the image (normalise)
+        float mx = 1.f;
+        const bool norm = c.normalize && n_in > 0;
+        if (norm) {
+            float wm = -INFINITY;
+            bool any_empty_row = false;
+            for (int y = warp; y < H; y += RAS_WARPS) {
+                if (!((A.rows[y >> 5] >> (y & 31)) & 1u)) {
+                    any_empty_row = true;
+                    continue;
+                }
+                for (int x0 = 0; x0 < W; x0 += RAS_SEG) {
+                    float acc[RAS_K][4];
+                    row_segment(c, A, n_alive, y, x0, lane, acc);
+#pragma unroll
+                    for (int i = 0; i < RAS_K; ++i)
+#pragma unroll
+                        for (int e = 0; e < 4; ++e)
+                            if (x0 + (lane + 32 * i) * 4 + e < W) wm = fmaxf(wm, acc[i][e]);
+                }
+            }
+            if (any_empty_row) wm = fmaxf(wm, 0.f);
+#pragma unroll
+            for (int d = 16; d >= 1; d >>= 1) wm = fmaxf(wm, __shfl_xor_sync(FULL_MASK, wm, d));
+            if (lane == 0) A.wmax[warp] = wm;
+            __syncthreads();
+            mx = A.wmax[0];
+            for (int w = 1; w < RAS_WARPS; ++w) mx = fmaxf(mx, A.wmax[w]);
+        }
+
+        // ---- the image
+        float *dst = out + (size_t)p * img;
+        const float zero_val = norm ? 0.f / mx : 0.f;
+        for (int y = warp; y < H; y += RAS_WARPS) {
+            float *row = dst + (size_t)y * W;
+            const bool covered = (A.rows[y >> 5] >> (y & 31)) & 1u;
+            if (!covered) {
+                if (VEC) {
+                    const float4 z = make_float4(zero_val, zero_val, zero_val, zero_val);
+                    for (int x = lane * 4; x < W; x += 128) st_cs(reinterpret_cast<float4 *>(row + x), z);
+                } else {
+                    for (int x = lane; x < W; x += 32) st_cs1(row + x, zero_val);
+                }
+                continue;
+            }
+            for (int x0 = 0; x0 < W; x0 += RAS_SEG) {
+                float acc[RAS_K][4];
+                row_segment(c, A, n_alive, y, x0, lane, acc);
+#pragma unroll
+                for (int i = 0; i < RAS_K; ++i) {
+                    const int xb = x0 + (lane + 32 * i) * 4;
+                    float v[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) v[e] = norm ? acc[i][e] / mx : acc[i][e];
+                    if (VEC) {
+                        if (xb < W) st_cs(reinterpret_cast<float4 *>(row + xb), make_float4(v[0], v[1], v[2], v[3]));
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < 4; ++e)
+                            if (xb + e < W) st_cs1(row + xb + e, v[e]);
+                    }
+                }
+            }
+        }
+        __syncthreads();  // the arena is reused by the next pattern
+    }
+}
+
+struct RasterPlan {
+    int NS, T, grid;
+    size_t arena, smem, scratch;
+};
+
+static ds_status raster_plan(const ds_raster_params *p, int64_t max_spots, RasterPlan &P) {
+    DS_REQUIRE(max_spots >= 0 && max_spots < (1ll << 28), "ds_rasterize: max_spots out of range");
+    int NS = (int)std::max<int64_t>(32, (max_spots + 31) / 32 * 32);
+    int T = 64;
+    while (T < 2 * NS) T <<= 1;
+    P.NS = NS;
+    P.T = T;
+    P.arena = raster_arena_bytes(NS, T, p->height);
+    int dev = 0, n_sm = 0;
+    DS_CUDA_TRY(cudaGetDevice(&dev));
+    DS_CUDA_TRY(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+    if (P.arena <= RAS_SMEM_LIMIT) {
+        P.smem = P.arena;
+        P.scratch = 0;
+        int per_sm = 0;
+        DS_CUDA_TRY(cudaFuncSetAttribute(raster_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)P.smem));
+        DS_CUDA_TRY(cudaFuncSetAttribute(raster_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)P.smem));
+        DS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, raster_kernel<true>, RAS_THREADS, P.smem));
+        P.grid = n_sm * std::max(1, per_sm);
+    } else {
+        P.smem = 0;
+        P.grid = 2 * n_sm;
+        P.scratch = (size_t)P.grid * P.arena;
+    }
+    return DS_OK;
+}
+
+static ds_status raster_validate(const ds_raster_params *p) {
+    DS_REQUIRE(p, "ds_rasterize: null params");
+    DS_REQUIRE(p->height > 0 && p->width > 0 && p->height <= 32768 && p->width <= 32768,
+               "ds_rasterize: shape must be 1..32768 pixels per side");
+    DS_REQUIRE((long long)p->height * p->width < (1ll << 31), "ds_rasterize: image too large");
+    DS_REQUIRE(std::isfinite(p->calibration) && p->calibration != 0.0, "ds_rasterize: calibration must be finite, non-zero");
+    DS_REQUIRE(std::isfinite(p->center_x) && std::isfinite(p->center_y) && std::isfinite(p->in_plane_angle),
+               "ds_rasterize: centre and angle must be finite");
+    DS_REQUIRE(std::isfinite(p->sigma), "ds_rasterize: sigma must be finite");
+    DS_REQUIRE(p->pixel_snap >= 0.0 && p->pixel_snap < 0.5, "ds_rasterize: pixel_snap must be in [0, 0.5)");
+    if (p->fast) {
+        DS_REQUIRE(std::isfinite(p->truncate) && p->truncate >= 0.0, "ds_rasterize: truncate must be >= 0");
+        if (p->sigma > 1e-15) {
+            const double r = p->truncate * p->sigma + 0.5;
+            DS_REQUIRE(r < RAS_MAX_R + 1, "ds_rasterize: filter radius int(truncate * sigma + 0.5) must be <= 511");
+        }
+    } else {
+        DS_REQUIRE(p->sigma != 0.0, "ds_rasterize: sigma must be non-zero in sub-pixel mode");
+        DS_REQUIRE(!std::isnan(p->clip_threshold), "ds_rasterize: clip_threshold is NaN");
+    }
+    return DS_OK;
+}
+
+}  // namespace ds
+
+using namespace ds;
+
+extern "C" size_t ds_rasterize_scratch_bytes(const ds_raster_params *p, int64_t max_spots) {
+    clear_error();
+    if (raster_validate(p) != DS_OK) return 0;
+    RasterPlan P;
+    if (raster_plan(p, max_spots, P) != DS_OK) return 0;
+    return P.scratch;
+}
+
+extern "C" ds_status ds_rasterize(const ds_raster_params *p, const int64_t *offsets, const float *xyzi,
+                                  int64_t n_patterns, int64_t max_spots, float *out, void *scratch,
+                                  size_t scratch_bytes, int32_t *status, void *stream) {
+    clear_error();
+    ds_status st = raster_validate(p);
+    if (st) return st;
+    DS_REQUIRE(status, "ds_rasterize: null status");
+    DS_REQUIRE(n_patterns >= 0, "ds_rasterize: n_patterns < 0");
+    if (n_patterns == 0) return DS_OK;
+    DS_REQUIRE(offsets && out, "ds_rasterize: null offsets / out");
+    DS_REQUIRE(xyzi || max_spots == 0, "ds_rasterize: null xyzi");
+    DS_REQUIRE(((uintptr_t)xyzi & 15) == 0, "ds_rasterize: xyzi must be 16-byte aligned");
+    const bool vec = (p->width % 4) == 0 && ((uintptr_t)out & 15) == 0;
+    RasterPlan P;
+    st = raster_plan(p, max_spots, P);
+    if (st) return st;
+    DS_REQUIRE(P.scratch == 0 || (scratch && scratch_bytes >= P.scratch), "ds_rasterize: scratch too small");
+
+    RasterConst c;
+    c.H = p->height;
+    c.W = p->width;
+    c.fast = p->fast ? 1 : 0;
+    c.normalize = p->normalize ? 1 : 0;
+    c.NS = P.NS;
+    c.T = P.T;
+    c.cal = p->calibration;
+    c.cx = p->center_x;
+    c.cy = p->center_y;
+    const double PI = 3.14159265358979323846;
+    const double th = p->in_plane_angle * (PI / 180.0);  // numpy.deg2rad
+    c.ca = cos(th);
+    c.sa = sin(th);
+    c.mf = p->mirrored ? -1.0 : 1.0;
+    c.snap = p->pixel_snap;
+    c.clip = p->clip_threshold;
+    c.pref = 1.0 / (2.0 * PI * p->sigma * p->sigma);
+    c.exp_pref = -1.0 / (2.0 * p->sigma * p->sigma);
+    for (int i = 0; i <= RAS_MAX_R; ++i) c.wt[i] = 0.f;
+    c.R = 0;
+    if (c.fast) {
+        if (p->sigma > 1e-15) {
+            // scipy.ndimage._gaussian_kernel1d: exp(-0.5 / sigma^2 x^2), normalised
+            const int R = (int)(p->truncate * p->sigma + 0.5);
+            const double s2 = p->sigma * p->sigma;
+            double phi[RAS_MAX_R + 1], sum = 0.0;
+            for (int x = 0; x <= R; ++x) phi[x] = exp(-0.5 / s2 * (double)x * (double)x);
+            for (int x = -R; x <= R; ++x) sum += phi[x < 0 ? -x : x];
+            for (int x = 0; x <= R; ++x) c.wt[x] = (float)(phi[x] / sum);
+            c.R = R;
+        } else {
+            c.wt[0] = 1.f;  // the filter is skipped for sigma <= 1e-15
+        }
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const int grid = (int)std::min<long long>(P.grid, n_patterns);
+    unsigned char *g = P.scratch ? reinterpret_cast<unsigned char *>(scratch) : nullptr;
+    if (vec)
+        raster_kernel<true><<<grid, RAS_THREADS, P.smem, s>>>(c, offsets, reinterpret_cast<const float4 *>(xyzi),
+                                                             n_patterns, out, g, P.arena, status);
+    else
+        raster_kernel<false><<<grid, RAS_THREADS, P.smem, s>>>(c, offsets, reinterpret_cast<const float4 *>(xyzi),
+                                                              n_patterns, out, g, P.arena, status);
+    return check_launch("raster_kernel");
+}

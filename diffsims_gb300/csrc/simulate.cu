@@ -37,6 +37,7 @@ constexpr float SIM_TAU = 1e-9f;       // | |s| - s_max | below this -> FP64 dec
 constexpr float SIM_TAU_SF = 1e-6f;    // |s| this close to a zero of the shape factor -> FP64 s
 constexpr float SIM_TAU_PREC = 2e-7f;  // precession band margin below this -> FP64 decision
 constexpr float SIM_U_MAX = 0.01f;     // (r / k0)^2 above this -> FP64 (series not used)
+constexpr float SIM_TAU_INT = 1e-2f;   // FP32 precession average below this -> FP64 quadrature
 constexpr int SIM_MAX_O = 32;
 // tuning knobs (compile time): word ranges per orientation in the refine and
 // write passes, and chunks screened per step in phase 1
@@ -59,6 +60,8 @@ struct SimConst {
     double alpha0, alpha1, beta0, beta1, csq;  // z_a = alpha0 + alpha1 g^2, z_b = beta0 + beta1 g^2, |c*|^2
     float a2f, b2f;                 // -alpha1 |c*|^2, -beta1 |c*|^2
     float inv_a2f, inv_b2f;
+    double int_step;                // precession average: breakpoint spacing in s (0: none)
+    float int_step_f, mw_f;
     long long n_hkl, n_orient, n_tiles, capacity;
 };
 
@@ -311,7 +314,7 @@ __device__ inline bool select_fp64(const SimConst &c, const OrientP &op, double 
 //  s     = w - z as an FP32 pair, error < ~5e-11.  Pairs within 1e-9 of the
 //          cutoff are decided in FP64 (FP64 step #2).
 __device__ inline bool select_mixed(const SimConst &c, const OrientP &op, const float4 &e, float2 g2p, dd &s,
-                                    float &r, float &zf) {
+                                    float &r, dd &r2o, float &zf) {
     const float Sa = fmaf(op.za[0], e.x, fmaf(op.za[1], e.y, op.za[2] * e.z));
     const float Sb = fmaf(op.zb[0], e.x, fmaf(op.zb[1], e.y, op.zb[2] * e.z));
     const float zz = fmaf(Sa, Sa, (2.f * Sa + Sb) * Sb);
@@ -322,6 +325,7 @@ __device__ inline bool select_mixed(const SimConst &c, const OrientP &op, const 
     bool sel = false;
     r = 0.f;
     if (c.prec != DS_PRECESSION_NONE) r = sqrtf(fmaxf(r2.hi, 0.f));
+    r2o = r2;
     if (!fallback) {
         const float corr = u * (0.25f + u * (0.125f + u * (0.078125f + u * (0.0546875f + u * 0.041015625f))));
         const float w0h = r2.hi * c.c2k0_dd.hi;
@@ -366,6 +370,7 @@ __device__ inline bool select_mixed(const SimConst &c, const OrientP &op, const 
         sel = select_fp64(c, op, (double)e.x, (double)e.y, (double)e.z, s64, r64, z64);
         split_double(s64, s.hi, s.lo);
         r = (float)r64;
+        split_double(r64 * r64, r2o.hi, r2o.lo);
         zf = (float)z64;
         return sel;
     }
@@ -374,7 +379,12 @@ __device__ inline bool select_mixed(const SimConst &c, const OrientP &op, const 
 }
 
 // shape factors, mixed form (diffsims/utils/shape_factor_models.py)
-__device__ inline float shape_mixed(const SimConst &c, dd s, float r) {
+__device__ inline float shape_base_f32(const SimConst &c, float s);
+__device__ inline double shape_base_f64(const SimConst &c, double s);
+__device__ float precession_average_f32(const SimConst &c, float s0h, float s0l, float a);
+__device__ double precession_average_f64(const SimConst &c, double s0, double a);
+
+__device__ inline float shape_mixed(const SimConst &c, dd s, float r, dd r2) {
     if (c.prec == DS_PRECESSION_LORENTZIAN) {  // lorentzian_precession, :183-219
         float sf = s.hi + s.lo;
         float rphi = r * c.phi_f, as = fabsf(sf);
@@ -385,6 +395,15 @@ __device__ inline float shape_mixed(const SimConst &c, dd s, float r) {
         float z = sqrtf(fmaf(u, u, q * q));
         float upz = u >= 0.f ? u + z : (q * q) / (z - u);  // u + z, stable for u < 0
         return (sig / 3.14159265358979f) * sqrtf(2.f * upz) / z;
+    }
+    if (c.prec == DS_PRECESSION_INTEGRAL) {  // _shape_factor_precession, :222-268
+        float v = precession_average_f32(c, s.hi, s.lo, r * c.phi_f);
+        if (v < SIM_TAU_INT) {
+            // small averages carry the FP32 rounding of s and a: redo in FP64
+            const double r64 = sqrt(fmax((double)r2.hi + (double)r2.lo, 0.0));
+            v = (float)precession_average_f64(c, (double)s.hi + (double)s.lo, r64 * c.phi);
+        }
+        return v;
     }
     switch (c.shape) {
         case DS_SHAPE_LINEAR: {  // :52-73
@@ -404,16 +423,8 @@ __device__ inline float shape_mixed(const SimConst &c, dd s, float r) {
             }
             return c.shape == DS_SHAPE_SIN2C ? v * v : v;
         }
-        case DS_SHAPE_ATANC: {  // :126-151, s = 0 -> 1
-            float y = c.mfac_f * (s.hi + s.lo);
-            return y == 0.f ? 1.f : atanf(y) / y;
-        }
-        case DS_SHAPE_LORENTZIAN: {  // :154-180 = 1 / (1 + (pi s / w)^2)
-            float x = c.sigma_f * (s.hi + s.lo);
-            return 1.f / fmaf(x, x, 1.f);
-        }
         default:
-            return 1.f;  // binary, :33-49
+            return shape_base_f32(c, s.hi + s.lo);
     }
 }
 
@@ -426,6 +437,40 @@ __device__ inline double shape_fp64(const SimConst &c, double s, double r) {
         double z = sqrt(u * u + 4 * sigma * sigma * s * s);
         return (sigma / PI) * sqrt(2 * (u + z) / (z * z));
     }
+    if (c.prec == DS_PRECESSION_INTEGRAL) return precession_average_f64(c, s, r * c.phi);
+    return shape_base_f64(c, s);
+}
+
+// The un-precessed models at one excitation error, FP32 (single s, used by
+// the precession average; the main path above keeps s as a pair).
+__device__ inline float shape_base_f32(const SimConst &c, float s) {
+    switch (c.shape) {
+        case DS_SHAPE_LINEAR: {
+            const float v = __fdiv_rn(c.width_f - fabsf(s), c.width_f);
+            return v > 0.f ? v : 0.f;
+        }
+        case DS_SHAPE_SINC:
+        case DS_SHAPE_SIN2C: {
+            const float x = s * c.mw_f;  // minima_number * s / width
+            float v = 0.f;
+            if (x != 0.f) v = fabsf(sinpif(x - rintf(x))) / (3.14159265358979f * fabsf(x));
+            return c.shape == DS_SHAPE_SIN2C ? v * v : v;
+        }
+        case DS_SHAPE_ATANC: {
+            const float y = c.mfac_f * s;
+            return y == 0.f ? 1.f : atanf(y) / y;
+        }
+        case DS_SHAPE_LORENTZIAN: {
+            const float x = c.sigma_f * s;
+            return 1.f / fmaf(x, x, 1.f);
+        }
+        default:
+            return 1.f;
+    }
+}
+
+__device__ inline double shape_base_f64(const SimConst &c, double s) {
+    const double PI = 3.14159265358979323846;
     switch (c.shape) {
         case DS_SHAPE_LINEAR: {
             double v = 1 - fabs(s) / c.width;
@@ -450,6 +495,96 @@ __device__ inline double shape_fp64(const SimConst &c, double s, double r) {
         default:
             return 1.0;
     }
+}
+
+// ------------------------------------------- precession rotation average ----
+// shf(s0, r) = (1/2pi) int_0^2pi f(s0 + r phi cos t) dt
+//            = (1/pi)  int_0^pi  f(s0 + a cos t) dt,  a = r phi
+// (diffsims/utils/shape_factor_models.py:222-268 evaluates it per spot with an
+// adaptive quadrature).  Here: the s-range [s0 - a, s0 + a] is cut at the
+// multiples of a per-model spacing h (the kinks of linear at 0 and +-w, the
+// zeros of sinc at multiples of w/n, and a feature-scale grid for the smooth
+// models), each cut maps to t = acos((k h - s0) / a), and every piece gets an
+// 8-point Gauss-Legendre rule in t.  On one piece the integrand is analytic
+// in t, so the rule's error is ~1e-7 relative or below for every model at the
+// chosen spacings (checked against a tight adaptive quadrature).  linear
+// pieces outside |s| < w are zero and skipped.
+
+// 8-point Gauss-Legendre rule on [-1, 1]: the positive roots of P_8 and
+// their weights.
+__constant__ double GL8_X[4] = {0.18343464249564978, 0.525532409916329, 0.7966664774136267, 0.9602898564975362};
+__constant__ double GL8_W[4] = {0.36268378337836166, 0.3137066458778869, 0.22238103445337443, 0.10122853629037706};
+__constant__ float GL8_XF[4] = {0.18343464249564978f, 0.525532409916329f, 0.7966664774136267f, 0.9602898564975362f};
+__constant__ float GL8_WF[4] = {0.36268378337836166f, 0.3137066458778869f, 0.22238103445337443f,
+                                0.10122853629037706f};
+
+__device__ __noinline__ float precession_average_f32(const SimConst &c, float s0h, float s0l, float a) {
+    const float PI_F = 3.14159265358979f;
+    const float s0 = s0h + s0l;
+    if (c.shape == DS_SHAPE_BINARY) return 1.f;
+    if (!(a > 0.f)) return shape_base_f32(c, s0);
+    const float h = c.int_step_f;
+    const float lo = s0 - a, hi = s0 + a;
+    const bool clip = c.shape == DS_SHAPE_LINEAR && c.width_f > 0.f;
+    float kf = (h > 0.f && h < INFINITY) ? ceilf(lo / h) : INFINITY;
+    float th_prev = PI_F, s_prev = lo, sum = 0.f;
+    for (;;) {
+        const float sk = kf * h;
+        const bool last = !(sk < hi);
+        const float s_next = last ? hi : sk;
+        const float th = last ? 0.f : acosf(fminf(fmaxf((sk - s0) / a, -1.f), 1.f));
+        if (th_prev > th && !(clip && (s_next <= -c.width_f || s_prev >= c.width_f))) {
+            const float mid = 0.5f * (th + th_prev), half = 0.5f * (th_prev - th);
+            float acc = 0.f;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const float d = half * GL8_XF[i];
+                const float f1 = shape_base_f32(c, fmaf(a, cosf(mid + d), s0h) + s0l);
+                const float f2 = shape_base_f32(c, fmaf(a, cosf(mid - d), s0h) + s0l);
+                acc = fmaf(GL8_WF[i], f1 + f2, acc);
+            }
+            sum = fmaf(half, acc, sum);
+        }
+        if (last) break;
+        th_prev = th;
+        s_prev = s_next;
+        kf += 1.f;
+    }
+    return sum * (1.f / PI_F);
+}
+
+__device__ __noinline__ double precession_average_f64(const SimConst &c, double s0, double a) {
+    const double PI = 3.14159265358979323846;
+    if (c.shape == DS_SHAPE_BINARY) return 1.0;
+    if (!(a > 0.0)) return shape_base_f64(c, s0);
+    const double h = c.int_step;
+    const double lo = s0 - a, hi = s0 + a;
+    const bool clip = c.shape == DS_SHAPE_LINEAR && c.width > 0.0;
+    double kf = (h > 0.0 && h < INFINITY) ? ceil(lo / h) : INFINITY;
+    double th_prev = PI, s_prev = lo, sum = 0.0;
+    for (;;) {
+        const double sk = kf * h;
+        const bool last = !(sk < hi);
+        const double s_next = last ? hi : sk;
+        const double th = last ? 0.0 : acos(fmin(fmax((sk - s0) / a, -1.0), 1.0));
+        if (th_prev > th && !(clip && (s_next <= -c.width || s_prev >= c.width))) {
+            const double mid = 0.5 * (th + th_prev), half = 0.5 * (th_prev - th);
+            double acc = 0.0;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const double d = half * GL8_X[i];
+                const double f1 = shape_base_f64(c, s0 + a * cos(mid + d));
+                const double f2 = shape_base_f64(c, s0 + a * cos(mid - d));
+                acc += GL8_W[i] * (f1 + f2);
+            }
+            sum += half * acc;
+        }
+        if (last) break;
+        th_prev = th;
+        s_prev = s_next;
+        kf += 1.0;
+    }
+    return sum / PI;
 }
 
 struct TableP {
@@ -495,10 +630,10 @@ __device__ inline bool eval_in(const SimConst &c, const OrientP &op, const SpotI
         sout = s;
         return sel;
     } else {
-        dd s;
+        dd s, r2;
         float r, z;
-        bool sel = select_mixed(c, op, e, in.g2, s, r, z);
-        I = shape_mixed(c, s, r) * in.F2;
+        bool sel = select_mixed(c, op, e, in.g2, s, r, r2, z);
+        I = shape_mixed(c, s, r, r2) * in.F2;
         zout = z;
         sout = (double)s.hi + (double)s.lo;
         return sel;
@@ -1317,10 +1452,6 @@ extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t
     DS_REQUIRE(p->stage_cap >= 0, "ds_simulate: stage_cap < 0");
     DS_REQUIRE(p->precession_mode == DS_PRECESSION_NONE || p->precession_angle > 0,
                "ds_simulate: precession mode needs a positive angle");
-    if (p->precession_mode == DS_PRECESSION_INTEGRAL) {
-        set_error("ds_simulate: DS_PRECESSION_INTEGRAL is not available in this build");
-        return DS_ERR_UNSUPPORTED;
-    }
     cudaStream_t s = (cudaStream_t)stream;
     if (n_orient == 0) {
         DS_CUDA_TRY(cudaMemsetAsync(out->offsets, 0, sizeof(int64_t), s));
@@ -1363,6 +1494,24 @@ extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t
     c.Pz_f = (float)c.Pz;
     c.Pt_f = (float)c.Pt;
     c.k0sq_f = (float)(c.k0 * c.k0);
+    c.mw_f = (float)(c.minima / c.width);
+    // precession average: breakpoint spacing per model (kinks of linear at
+    // 0 and +-w; zeros of sinc at multiples of w/n; feature-scale grids of
+    // the smooth models: w/2n for sin2c and atanc, w/pi for lorentzian)
+    {
+        const double aw = fabs(c.width), n = c.minima;
+        double h = 0.0;
+        switch (p->shape_model) {
+            case DS_SHAPE_LINEAR: h = aw; break;
+            case DS_SHAPE_SINC: h = n > 0 ? aw / n : 0.0; break;
+            case DS_SHAPE_SIN2C:
+            case DS_SHAPE_ATANC: h = n > 0 ? aw / (2.0 * n) : 0.0; break;
+            case DS_SHAPE_LORENTZIAN: h = aw / PI; break;
+            default: h = 0.0;
+        }
+        c.int_step = h;
+        c.int_step_f = (float)h;
+    }
     // FP32 screen guard: bound on |z32 - z| from rounding m to FP32 and the FMA
     // chain, 8 ulp of sum_i |row_i of recip| * max|hkl_i| (|R| = 1), plus the
     // rounding of z_mid and z_half.

@@ -172,11 +172,38 @@ class PhaseSpots:
             self._host = (off.numpy(), idx.numpy(), xyzi.numpy())
         return self._host
 
+    @classmethod
+    def from_vectors(cls, vectors, device=None):
+        """Device CSR spots from host spot vectors (objects with ``data``
+        (n, 3) and ``intensity`` (n,), and optionally ``hkl``), one per
+        pattern: the form ``Simulation2D`` takes for user-built coordinates."""
+        dev = _device(device)
+        counts = [np.asarray(v.data).reshape(-1, 3).shape[0] for v in vectors]
+        off = np.zeros(len(vectors) + 1, dtype=np.int64)
+        off[1:] = np.cumsum(counts)
+        total = int(off[-1])
+        xyzi = np.zeros((max(total, 1), 4), dtype=np.float32)
+        hkl = np.zeros((max(total, 1), 3), dtype=np.float64)
+        for v, a, b in zip(vectors, off[:-1], off[1:]):
+            xyzi[a:b, :3] = np.asarray(v.data, dtype=np.float64).reshape(-1, 3)
+            inten = getattr(v, "intensity", None)
+            xyzi[a:b, 3] = np.nan if inten is None else np.asarray(inten, dtype=np.float64)
+            h = getattr(v, "hkl", None)
+            if h is not None:
+                hkl[a:b] = np.asarray(h, dtype=np.float64).reshape(-1, 3)
+        obj = cls(None, torch.as_tensor(off).to(dev), torch.arange(max(total, 1), dtype=torch.int32).to(dev),
+                  torch.as_tensor(xyzi).to(dev), total)
+        obj._hkl_rows = hkl[:total]
+        return obj
+
     def pattern(self, i):
         """(hkl (n, 3) int, xyz (n, 3) float64, intensity (n,) float64) of orientation i."""
         off, idx, xyzi = self.host()
         a, b = off[i], off[i + 1]
-        hkl = self.table.hkl_host()[idx[a:b]] if b > a else np.zeros((0, 3), np.int32)
+        if self.table is None:
+            hkl = self._hkl_rows[idx[a:b]]
+        else:
+            hkl = self.table.hkl_host()[idx[a:b]] if b > a else np.zeros((0, 3), np.int32)
         rec = xyzi[a:b].astype(np.float64)
         return hkl, rec[:, :3], rec[:, 3]
 
@@ -260,3 +287,87 @@ def simulate_phase(table: PhaseTable, quats: torch.Tensor, settings: SimSettings
             return PhaseSpots(table, offsets, buffers.idx, buffers.xyzi, total, buffers.s)
         cap = total + 1024
     raise N.NativeError("simulate: output capacity still exceeded after resizing")
+
+
+@dataclass
+class RasterSettings:
+    """Arguments of Simulation2D.get_diffraction_pattern
+    (diffsims/simulations/simulation2d.py:357-368) for ``rasterize``;
+    ``truncate`` is scipy.ndimage.gaussian_filter's (4.0) and ``pixel_snap``
+    moves positions within that many pixels of a whole pixel onto it (0: the
+    reference's exact truncation)."""
+    shape: tuple
+    sigma: float = 10.0
+    direct_beam_position: tuple | None = None
+    in_plane_angle: float = 0.0
+    calibration: float = 0.01
+    mirrored: bool = False
+    fast: bool = True
+    normalize: bool = True
+    clip_threshold: float = 1.0
+    truncate: float = 4.0
+    pixel_snap: float = 0.0
+
+    def cstruct(self):
+        if self.shape is None or len(self.shape) != 2:
+            raise ValueError("shape must be (rows, columns)")
+        H, W = int(self.shape[0]), int(self.shape[1])
+        if self.direct_beam_position is None:
+            # simulation2d.py:404-411: whole-pixel centre in fast mode, the
+            # sub-pixel centre otherwise (spot coordinates are floats)
+            cx, cy = (W // 2, H // 2) if self.fast else ((W - 1) / 2, (H - 1) / 2)
+        else:
+            cx, cy = self.direct_beam_position
+        return N.ds_raster_params(H, W, int(bool(self.mirrored)), int(bool(self.fast)), int(bool(self.normalize)), 0,
+                                  float(self.sigma), float(self.calibration), float(cx), float(cy),
+                                  float(self.in_plane_angle), float(self.clip_threshold), float(self.truncate),
+                                  float(self.pixel_snap))
+
+
+class RasterBuffers:
+    """Reusable scratch and status words for ``rasterize``."""
+
+    def __init__(self, device):
+        self.device = device
+        self.status = torch.zeros(1, dtype=torch.int32, device=device)
+        self.scratch = None
+
+    def ensure(self, nbytes):
+        if nbytes and (self.scratch is None or self.scratch.numel() < nbytes):
+            self.scratch = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+
+
+def rasterize(spots: PhaseSpots, settings: RasterSettings, start=0, stop=None, out=None, max_spots=None,
+              buffers: RasterBuffers | None = None, stream=None, sync=True) -> torch.Tensor:
+    """Detector images (stop - start, rows, columns) float32 on the device of
+    patterns ``start:stop`` of one phase, one ds_rasterize launch.
+    ``max_spots`` (spots of the largest pattern) is measured when not given."""
+    lib = N.load_library()
+    n_all = spots.n_orient
+    stop = n_all if stop is None else stop
+    if not 0 <= start <= stop <= n_all:
+        raise IndexError(f"patterns {start}:{stop} of {n_all}")
+    n = stop - start
+    p = settings.cstruct()
+    dev = spots.offsets.device
+    if out is None:
+        out = torch.empty((n, p.height, p.width), dtype=torch.float32, device=dev)
+    elif (tuple(out.shape) != (n, p.height, p.width) or out.dtype != torch.float32 or not out.is_contiguous()
+          or out.device != dev):
+        raise ValueError(f"out must be a contiguous float32 ({n}, {p.height}, {p.width}) tensor on {dev}")
+    if n == 0:
+        return out
+    off = spots.offsets[start:stop + 1]
+    if max_spots is None:
+        max_spots = int((off[1:] - off[:-1]).max().item())
+    buffers = buffers or RasterBuffers(dev)
+    sbytes = lib.ds_rasterize_scratch_bytes(p, max_spots)
+    N.check(0 if sbytes or lib.ds_last_error() == b"" else N.DS_ERR_INVALID_ARGUMENT, "rasterize")
+    buffers.ensure(sbytes)
+    buffers.status.zero_()
+    xyzi = spots.xyzi if spots.total > 0 else None
+    N.check(lib.ds_rasterize(p, N.ptr(off), N.ptr(xyzi), n, max_spots, N.ptr(out), N.ptr(buffers.scratch), sbytes,
+                             N.ptr(buffers.status), N.stream_handle(stream)), "rasterize")
+    if sync:
+        N.check_device_status(buffers.status, "rasterize")
+    return out

@@ -137,5 +137,5 @@ class SimulationGenerator:
             spots.append(simulate_phase(table, q, settings, reciprocal_radius, buffers=SpotBuffers(dev)))
             rots.append(rot)
         if single_phase:
-            return Simulation2D(phases[0], rots[0], spots, self, reciprocal_radius)
-        return Simulation2D(phases, rots, spots, self, reciprocal_radius)
+            return Simulation2D(phases[0], spots, rots[0], self, reciprocal_radius)
+        return Simulation2D(phases, spots, rots, self, reciprocal_radius)

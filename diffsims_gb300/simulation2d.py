@@ -132,17 +132,43 @@ class Simulation2D:
     rotations -> a sequence of N; P phases -> a list of P sequences.
     """
 
-    def __init__(self, phases, rotations, phase_spots, simulation_generator, reciprocal_radius=1.0):
-        self._multi_phase = isinstance(phases, (list, tuple))
+    def __init__(self, phases, coordinates, rotations, simulation_generator, reciprocal_radius=1.0):
+        """Same arguments as the reference (simulation2d.py:115-186).
+        ``coordinates`` is what ``calculate_diffraction2d`` hands over (one
+        ``PhaseSpots`` per phase, device CSR) or, as in the reference,
+        ``DiffractingVector`` objects: one (single rotation), a sequence (one
+        phase), or a list of sequences (several phases); these are uploaded
+        into the same device CSR form."""
+        from .engine import PhaseSpots
+        self._multi_phase = isinstance(phases, (list, tuple, np.ndarray))
+        plist = list(phases) if self._multi_phase else [phases]
+        rlist = list(rotations) if self._multi_phase else [rotations]
+        if len(rlist) != len(plist):
+            raise ValueError(f"The number of rotations: {len(rlist)} must match the number of phases {len(plist)}")
+        if isinstance(coordinates, PhaseSpots):
+            spots = [coordinates]
+        elif (isinstance(coordinates, (list, tuple)) and coordinates
+              and all(isinstance(c, PhaseSpots) for c in coordinates)):
+            spots = list(coordinates)
+        else:
+            clist = list(coordinates) if self._multi_phase else [coordinates]
+            if len(clist) != len(plist):
+                raise ValueError(f"{len(clist)} coordinate sets for {len(plist)} phases")
+            spots = []
+            for c, r in zip(clist, rlist):
+                vecs = [c] if isinstance(c, DiffractingVector) else list(c)
+                n_rot = getattr(r, "size", 1)
+                if n_rot != len(vecs):
+                    raise ValueError(f"The number of rotations: {n_rot} must match the number of "
+                                     f"coordinates {len(vecs)}")
+                spots.append(PhaseSpots.from_vectors(vecs))
         self.phases = phases
         self.rotations = rotations
         self.simulation_generator = simulation_generator
         self.reciporical_radius = reciprocal_radius
         self.reciprocal_radius = reciprocal_radius
-        self._spots = phase_spots  # list of PhaseSpots, one per phase
-        plist = phases if self._multi_phase else [phases]
-        rlist = rotations if self._multi_phase else [rotations]
-        self._coords = [_PhaseCoordinates(p, s, r) for p, s, r in zip(plist, phase_spots, rlist)]
+        self._spots = spots  # list of PhaseSpots, one per phase
+        self._coords = [_PhaseCoordinates(p, s, r) for p, s, r in zip(plist, spots, rlist)]
         self.phase_index = 0
         self.rotation_index = 0
 
@@ -220,6 +246,35 @@ class Simulation2D:
             r_t = np.array(r_t, dtype=int)
             t_t = np.array(t_t, dtype=int)
         return r_t, t_t, i_t
+
+    def get_diffraction_pattern(self, shape=None, sigma: float = 10, direct_beam_position=None,
+                                in_plane_angle: float = 0, calibration: float = 0.01, mirrored: bool = False,
+                                fast: bool = True, normalize: bool = True, clip_threshold: float = 1):
+        """Detector image (rows, columns) of the current pattern
+        (``phase_index``, ``rotation_index``), computed on the GPU
+        (diffsims/simulations/simulation2d.py:357-442).  Returns a float64
+        numpy array holding the kernel's float32 values."""
+        from .engine import RasterSettings, rasterize
+        settings = RasterSettings(shape, sigma, direct_beam_position, in_plane_angle, calibration, mirrored, fast,
+                                  normalize, clip_threshold)
+        spots = self._spots[self.phase_index]
+        i = self.rotation_index if spots.n_orient > 1 else 0
+        img = rasterize(spots, settings, i, i + 1)
+        return img[0].cpu().numpy().astype(np.float64)
+
+    def get_diffraction_patterns(self, shape, sigma: float = 10, direct_beam_position=None, in_plane_angle: float = 0,
+                                 calibration: float = 0.01, mirrored: bool = False, fast: bool = True,
+                                 normalize: bool = True, clip_threshold: float = 1, phase_index: int = 0,
+                                 start: int = 0, stop=None, out=None, pixel_snap: float = 0.0):
+        """Detector images of patterns ``start:stop`` of one phase in one
+        launch: a float32 (n, rows, columns) tensor on the device (no
+        counterpart in the reference, which loops over
+        ``get_diffraction_pattern``).  ``out`` may be a preallocated tensor to
+        stream chunks through."""
+        from .engine import RasterSettings, rasterize
+        settings = RasterSettings(shape, sigma, direct_beam_position, in_plane_angle, calibration, mirrored, fast,
+                                  normalize, clip_threshold, pixel_snap=pixel_snap)
+        return rasterize(self._spots[phase_index], settings, start, stop, out=out)
 
     def __repr__(self):
         return f"Simulation2D({self.num_phases} phase(s), {len(self)} pattern(s))"

@@ -188,6 +188,42 @@ ds_status ds_simulate_noalloc(const ds_sim_params *p, const ds_phase_table *t, c
                               int64_t n_orient, ds_spots *out, int32_t *status, void *stream);
 
 /* ------------------------------------------------------------------------ */
+/* Detector images of spot patterns.  Replaces Simulation2D.get_diffraction_pattern
+ * (diffsims/simulations/simulation2d.py:357-442) with
+ * get_pattern_from_pixel_coordinates_and_intensities and _subpixel_gaussian
+ * (diffsims/pattern/detector_functions.py:251-359), for many patterns per call. */
+typedef struct {
+    int32_t height, width;       /* detector shape (rows, columns), pixels           */
+    int32_t mirrored;            /* 1: mirror across the x axis                      */
+    int32_t fast;                /* 1: truncate to whole pixels, last write wins,
+                                    Gaussian filter (mode reflect); 0: sub-pixel
+                                    boxed Gaussians (_subpixel_gaussian)             */
+    int32_t normalize;           /* 1: divide by the image maximum                   */
+    int32_t _pad;
+    double sigma;                /* Gaussian standard deviation, pixels              */
+    double calibration;          /* 1/Angstrom per pixel                             */
+    double center_x, center_y;   /* direct-beam position, pixels                     */
+    double in_plane_angle;       /* degrees                                          */
+    double clip_threshold;       /* fast == 0: value below which a spot's box ends   */
+    double truncate;             /* fast == 1: filter radius int(truncate*sigma+0.5) */
+    double pixel_snap;           /* >= 0: positions within this of a whole pixel are
+                                    moved onto it (0: the reference's exact rule)    */
+} ds_raster_params;
+
+/* Device scratch ds_rasterize needs for patterns of up to max_spots spots
+ * (0 when the per-pattern work fits in shared memory). */
+size_t ds_rasterize_scratch_bytes(const ds_raster_params *p, int64_t max_spots);
+
+/* n_patterns images of height x width float32 into out (pattern-major).
+ * offsets: n_patterns + 1 int64 (absolute rows of xyzi), xyzi: rows of
+ * (x, y, z, intensity) float32 in the beam frame (the ds_spots layout).
+ * max_spots: an upper bound on offsets[i+1] - offsets[i]; a pattern above it
+ * is left unwritten and DS_ERR_CAPACITY is or-ed into *status. */
+ds_status ds_rasterize(const ds_raster_params *p, const int64_t *offsets, const float *xyzi,
+                       int64_t n_patterns, int64_t max_spots, float *out, void *scratch,
+                       size_t scratch_bytes, int32_t *status, void *stream);
+
+/* ------------------------------------------------------------------------ */
 /* FP32 FMA throughput probe (no counterpart in the reference): blocks x 256
  * threads, each 8 chains x 16 x iters fused multiply-adds; out holds
  * blocks*256 floats.  FLOPs = blocks * 256 * iters * 256.  Used to measure the

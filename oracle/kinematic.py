@@ -197,6 +197,45 @@ def sf_precession_integral(s, r_spot, phi, shape_function, w, **kwargs):
     return out
 
 
+def precession_breakpoint_step(model, w, minima_number=5):
+    """Spacing in s of the points where the named model has a kink (linear:
+    0 and +-w; sinc: its zeros at multiples of w/n), or the grid on which the
+    smooth models are resolved (sin2c, atanc: w/2n; lorentzian: w/pi)."""
+    aw = abs(w)
+    return {"linear": aw, "sinc": aw / minima_number, "sin2c": aw / (2 * minima_number),
+            "atanc": aw / (2 * minima_number), "lorentzian": aw / np.pi}.get(model, 0.0)
+
+
+def sf_precession_integral_tight(s, r_spot, phi, model, w, **kwargs):
+    """The same rotation average as :func:`sf_precession_integral` to ~1e-12:
+    (1/pi) int_0^pi f(s + r phi cos t) dt by adaptive quadrature with the
+    model's kinks given as break points and tight tolerances.  The reference's
+    default tolerances leave an absolute error of up to ~2e-9; this is the
+    yardstick for the relative error of small rotation averages."""
+    from scipy.integrate import quad
+    fn = ALL_SHAPE_MODELS[model]
+    h = precession_breakpoint_step(model, w, **kwargs)
+    out = np.zeros(np.shape(s))
+    for i, (si, ri) in enumerate(zip(np.atleast_1d(s), np.atleast_1d(r_spot))):
+        a = ri * phi
+        if model == "binary":
+            out[i] = 1.0
+            continue
+        if not a > 0:
+            out[i] = fn(np.array([si]), w, **kwargs)[0]
+            continue
+        pts = []
+        if h > 0:
+            ks = np.arange(np.ceil((si - a) / h), np.floor((si + a) / h) + 1)
+            pts = sorted(set(np.arccos(np.clip((ks * h - si) / a, -1, 1)).tolist()) - {0.0, np.pi})
+
+        def integrand(t, si=si, a=a):
+            return fn(np.array([si + a * np.cos(t)]), w, **kwargs)[0]
+        v = quad(integrand, 0, np.pi, points=pts or None, epsabs=1e-15, epsrel=1e-12, limit=1000)[0]
+        out[i] = v / np.pi
+    return out
+
+
 SHAPE_MODELS = {
     "linear": sf_linear,
     "atanc": sf_atanc,
@@ -369,6 +408,10 @@ class SimParams:
     max_excitation_error: float = 1e-2
     shape_factor_width: float = None
     shape_kwargs: dict = field(default_factory=dict)
+    # approximate_precession=False: "reference" = the reference's adaptive
+    # quadrature with its default tolerances, "tight" = break points + tight
+    # tolerances (same integral, ~1e-12)
+    precession_quadrature: str = "reference"
 
 
 @dataclass
@@ -421,6 +464,8 @@ def simulate_orientation(crystal, p, table, R, return_s=False):
         sf = fn(s_sel, w, **p.shape_kwargs)
     elif p.approximate_precession:
         sf = sf_lorentzian_precession(s_sel, w, r_sel, phi)
+    elif p.precession_quadrature == "tight" and isinstance(model, str):
+        sf = sf_precession_integral_tight(s_sel, r_sel, phi, model, w, **p.shape_kwargs)
     else:
         sf = sf_precession_integral(s_sel, r_sel, phi, fn, w, **p.shape_kwargs)
     inten = kinematical_intensities(hkl[idx], gs[idx], crystal.elements, crystal.xyz,

@@ -160,6 +160,56 @@ def test_shapes_and_precession_p1(shape, prec):
     assert st["spots"] > 100
 
 
+_TIGHT_CACHE = {}
+
+
+@pytest.mark.parametrize("form", ["mixed", "fp64"])
+@pytest.mark.parametrize("shape", ["linear", "lorentzian", "sinc", "sin2c", "atanc"])
+def test_precession_rotation_average(shape, form):
+    """approximate_precession=False: the per-spot rotation average against the
+    oracle's tight quadrature, 1e-5 relative on every intensity."""
+    crystal = random_p1(30, 17)
+    q = ok.random_quaternions(8, seed=6)
+    p = ok.SimParams(accelerating_voltage=200, shape_factor_model=shape, reciprocal_radius=1.2,
+                     max_excitation_error=0.015, precession_angle=1.0, approximate_precession=False,
+                     precession_quadrature="tight")
+    if shape not in _TIGHT_CACHE:
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            _TIGHT_CACHE[shape] = ok.simulate(crystal, q, p, return_s=True)
+    spots, _ = pu.gpu_run(crystal, q, p, form)
+    st = pu.compare(spots, crystal, q, p, rtol=1e-5, ref=_TIGHT_CACHE[shape])
+    assert st["spots"] > 100, st
+
+
+@pytest.mark.parametrize("shape", ["linear", "sinc", "lorentzian"])
+def test_precession_rotation_average_vs_reference_quadrature(shape):
+    """Against the reference's own adaptive quadrature (default tolerances):
+    the GPU value is within that quadrature's own error (its distance from
+    the tight integral) plus 1e-5 relative."""
+    crystal = al_fcc()
+    q = ok.random_quaternions(16, seed=3)
+    kw = dict(accelerating_voltage=200, shape_factor_model=shape, reciprocal_radius=2.0,
+              max_excitation_error=0.01, precession_angle=0.5, approximate_precession=False)
+    ref = ok.simulate(crystal, q, ok.SimParams(**kw), return_s=True)
+    tight = ok.simulate(crystal, q, ok.SimParams(precession_quadrature="tight", **kw), return_s=True)
+    spots, _ = pu.gpu_run(crystal, q, ok.SimParams(**kw), "mixed")
+    off = spots.offsets.cpu().numpy()
+    idx = spots.hkl_index.cpu().numpy()
+    inten = spots.xyzi.cpu().numpy()[:, 3].astype(np.float64)
+    n = 0
+    for i, (r, t) in enumerate(zip(ref, tight)):
+        assert np.array_equal(r.index, t.index)
+        gi = idx[off[i]:off[i + 1]]
+        common, ia, ib = np.intersect1d(gi, r.index, return_indices=True)
+        assert len(common) == len(r.index), i
+        got = inten[off[i]:off[i + 1]][ia]
+        allowed = np.abs(r.intensity[ib] - t.intensity[ib]) + 1e-5 * t.intensity[ib] + 1e-30
+        assert np.all(np.abs(got - r.intensity[ib]) <= allowed), i
+        n += len(common)
+    assert n > 50
+
+
 @pytest.mark.parametrize("kw", [dict(with_direct_beam=False), dict(minimum_intensity=1e-3),
                                 dict(shape_factor_width=0.03), dict(scattering_params="xtables"),
                                 dict(scattering_params=None), dict(accelerating_voltage=300),
@@ -175,9 +225,10 @@ def test_generator_options(kw):
     pu.compare(spots, crystal, q, p, rtol=1e-5)
 
 
-@pytest.mark.parametrize("kw, count", [(dict(), 70), (dict(precession_angle=0.5), 250)])
+@pytest.mark.parametrize("kw, count", [(dict(), 70), (dict(precession_angle=0.5), 250),
+                                       (dict(precession_angle=0.5, approximate_precession=False), 250)])
 def test_spot_count_kats(kw, count):
-    # diffsims/tests/generators/test_simulation_generator.py:137-152
+    # diffsims/tests/generators/test_simulation_generator.py:137-161
     import diffsims_gb300 as ds
     gen = ds.SimulationGenerator(300, **kw)
     sim = gen.calculate_diffraction2d(pu.to_phase(si_crystal()), reciprocal_radius=5.0)

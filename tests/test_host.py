@@ -123,3 +123,31 @@ def test_get_closest_matches_reference_rule():
     from diffsims_gb300.simulation2d import _get_closest
     a = np.array([0.0, 1.0, 2.0, 3.0])
     np.testing.assert_array_equal(_get_closest(a, np.array([-1, 0.4, 0.5, 0.6, 2.9, 7.0])), [0, 0, 1, 1, 3, 3])
+
+
+def test_raster_settings_struct():
+    """ds_raster_params layout and the direct-beam default of
+    get_diffraction_pattern (diffsims/simulations/simulation2d.py:404-411)."""
+    import ctypes
+    from diffsims_gb300 import _native as N
+    from diffsims_gb300.engine import RasterSettings
+    assert ctypes.sizeof(N.ds_raster_params) == 88
+    p = RasterSettings((128, 100)).cstruct()
+    assert (p.height, p.width, p.center_x, p.center_y, p.fast, p.normalize) == (128, 100, 50.0, 64.0, 1, 1)
+    p = RasterSettings((128, 100), fast=False).cstruct()
+    assert (p.center_x, p.center_y) == (49.5, 63.5)
+    p = RasterSettings((10, 20), direct_beam_position=(3.5, 4.25), mirrored=True, sigma=2, truncate=3).cstruct()
+    assert (p.center_x, p.center_y, p.mirrored, p.sigma, p.truncate) == (3.5, 4.25, 1, 2.0, 3.0)
+    with pytest.raises(ValueError):
+        RasterSettings(None).cstruct()
+
+
+def test_precession_tight_quadrature_agrees_with_reference_quadrature():
+    """The oracle's tight rotation average and the reference's adaptive
+    quadrature agree where the latter converges (smooth models)."""
+    s = np.array([0.001, -0.012, 0.02, 0.0, 0.03])
+    r = np.array([0.5, 1.0, 1.3, 0.0, 1.6])
+    for m in ("linear", "sin2c", "atanc", "lorentzian"):
+        a = ok.sf_precession_integral_tight(s, r, np.deg2rad(1.0), m, 0.015)
+        b = ok.sf_precession_integral(s, r, np.deg2rad(1.0), ok.ALL_SHAPE_MODELS[m], 0.015)
+        np.testing.assert_allclose(a, b, rtol=1e-7, atol=1e-9)
