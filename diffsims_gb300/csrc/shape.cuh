@@ -1,0 +1,252 @@
+// Rel-rod shape factors (diffsims/utils/shape_factor_models.py), their
+// derivatives, and the precession rotation average -- shared by the forward
+// orientation kernel and the adjoint kernels.
+//
+// Every function is a template over a constant block C that provides:
+//   int shape, prec;                       model and precession mode
+//   double width, minima, phi, int_step;   w, minima_number, phi (rad), breakpoint spacing
+//   float width_f, mw_f, mfac_f, sigma_f, phi_f, int_step_f;
+//     (mw = n / w, mfac = pi n / |w|, sigma = pi / w)
+#pragma once
+
+#include "common.cuh"
+
+namespace ds {
+
+constexpr float SHAPE_PI_F = 3.14159265358979f;
+constexpr double SHAPE_PI = 3.14159265358979323846;
+
+// Breakpoint spacing of the precession average per model: the kinks of
+// linear at 0 and +-w, the zeros of sinc at multiples of w/n, feature-scale
+// grids of the smooth models (w/2n for sin2c and atanc, w/pi for lorentzian);
+// 0 = no breakpoints.
+inline double precession_breakpoint_step(int shape, double width, double minima) {
+    const double aw = fabs(width), n = minima;
+    switch (shape) {
+        case DS_SHAPE_LINEAR: return aw;
+        case DS_SHAPE_SINC: return n > 0 ? aw / n : 0.0;
+        case DS_SHAPE_SIN2C:
+        case DS_SHAPE_ATANC: return n > 0 ? aw / (2.0 * n) : 0.0;
+        case DS_SHAPE_LORENTZIAN: return aw / SHAPE_PI;
+        default: return 0.0;
+    }
+}
+
+// ----------------------------------------------------------- the models ----
+// FP32, one excitation error.
+template <class C>
+__device__ inline float shape_base_f32(const C &c, float s) {
+    switch (c.shape) {
+        case DS_SHAPE_LINEAR: {  // :52-73
+            const float v = __fdiv_rn(c.width_f - fabsf(s), c.width_f);
+            return v > 0.f ? v : 0.f;
+        }
+        case DS_SHAPE_SINC:    // :76-101 (s = 0 -> 0)
+        case DS_SHAPE_SIN2C: { // :104-123
+            const float x = s * c.mw_f;  // minima_number * s / width
+            float v = 0.f;
+            if (x != 0.f) v = fabsf(sinpif(x - rintf(x))) / (SHAPE_PI_F * fabsf(x));
+            return c.shape == DS_SHAPE_SIN2C ? v * v : v;
+        }
+        case DS_SHAPE_ATANC: {  // :126-151 (s = 0 -> 1)
+            const float y = c.mfac_f * s;
+            return y == 0.f ? 1.f : atanf(y) / y;
+        }
+        case DS_SHAPE_LORENTZIAN: {  // :154-180 = 1 / (1 + (pi s / w)^2)
+            const float x = c.sigma_f * s;
+            return 1.f / fmaf(x, x, 1.f);
+        }
+        default:
+            return 1.f;  // binary, :33-49
+    }
+}
+
+// FP64, direct transcription.
+template <class C>
+__device__ inline double shape_base_f64(const C &c, double s) {
+    switch (c.shape) {
+        case DS_SHAPE_LINEAR: {
+            double v = 1 - fabs(s) / c.width;
+            return v < 0 ? 0.0 : v;
+        }
+        case DS_SHAPE_SINC:
+        case DS_SHAPE_SIN2C: {
+            double fac = SHAPE_PI * c.minima / c.width;
+            double den = fac * s;
+            double v = den != 0 ? fabs(sin(fac * s) / den) : 0.0;
+            return c.shape == DS_SHAPE_SIN2C ? v * v : v;
+        }
+        case DS_SHAPE_ATANC: {
+            double fac = SHAPE_PI * c.minima / fabs(c.width);
+            double y = fac * s;
+            return y == 0 ? 1.0 : atan(y) / y;
+        }
+        case DS_SHAPE_LORENTZIAN: {
+            double sigma = SHAPE_PI / c.width;
+            return sigma / (SHAPE_PI * (sigma * sigma * s * s + 1)) * c.width;
+        }
+        default:
+            return 1.0;
+    }
+}
+
+// d f / d s (zero where the model is flat or at its isolated points:
+// s = 0 of sinc, the cut-off of linear).
+template <typename T, class C>
+__device__ inline T shape_deriv(const C &c, T s) {
+    switch (c.shape) {
+        case DS_SHAPE_LINEAR: {
+            const T w = (T)c.width;
+            const T v = (T)1 - fabs(s) / w;
+            if (!(v > (T)0) || s == (T)0) return (T)0;
+            return s > (T)0 ? -(T)1 / w : (T)1 / w;
+        }
+        case DS_SHAPE_SINC:
+        case DS_SHAPE_SIN2C: {
+            const T fac = (T)(SHAPE_PI * c.minima / c.width);
+            const T x = fac * s;
+            if (x == (T)0) return (T)0;
+            const T sx = sin(x), cx = cos(x);
+            const T q = sx / x;                       // sin x / x
+            const T dq = (x * cx - sx) / (x * x);     // d/dx (sin x / x)
+            if (c.shape == DS_SHAPE_SIN2C) return (T)2 * q * dq * fac;
+            return (q < (T)0 ? -dq : dq) * fac;       // |sin x / x|
+        }
+        case DS_SHAPE_ATANC: {
+            const T fac = (T)(SHAPE_PI * c.minima / fabs(c.width));
+            const T y = fac * s;
+            if (y == (T)0) return (T)0;
+            return (y / ((T)1 + y * y) - atan(y)) / (y * y) * fac;
+        }
+        case DS_SHAPE_LORENTZIAN: {
+            const T sg = (T)(SHAPE_PI / c.width);
+            const T d = (T)1 + sg * sg * s * s;
+            return -(T)2 * sg * sg * s / (d * d);
+        }
+        default:
+            return (T)0;
+    }
+}
+
+template <class C>
+__device__ inline float shape_val_t(const C &c, float s) { return shape_base_f32(c, s); }
+template <class C>
+__device__ inline double shape_val_t(const C &c, double s) { return shape_base_f64(c, s); }
+
+// ------------------------------------------- precession rotation average ----
+// shf(s0, r) = (1/2pi) int_0^2pi f(s0 + r phi cos t) dt
+//            = (1/pi)  int_0^pi  f(s0 + a cos t) dt,  a = r phi
+// (diffsims/utils/shape_factor_models.py:222-268 evaluates it per spot with an
+// adaptive quadrature).  Here: the s-range [s0 - a, s0 + a] is cut at the
+// multiples of a per-model spacing h (the kinks of linear at 0 and +-w, the
+// zeros of sinc at multiples of w/n, and a feature-scale grid for the smooth
+// models), each cut maps to t = acos((k h - s0) / a), and every piece gets an
+// 8-point Gauss-Legendre rule in t.  On one piece the integrand is analytic
+// in t, so the rule's error is ~1e-7 relative or below for every model at the
+// chosen spacings (checked against a tight adaptive quadrature).  linear
+// pieces outside |s| < w are zero and skipped.  With GRAD the same nodes also
+// give d shf / d s0 = (1/pi) int f'(.) dt and d shf / d a = (1/pi) int f'(.) cos t dt
+// (f is continuous at the cuts, so moving them adds nothing).
+//
+// 8-point Gauss-Legendre rule on [-1, 1]: the positive roots of P_8 and
+// their weights.
+template <typename T>
+__device__ __forceinline__ T gl8_x(int i) {
+    const T x[4] = {(T)0.18343464249564978, (T)0.525532409916329, (T)0.7966664774136267, (T)0.9602898564975362};
+    return x[i];
+}
+template <typename T>
+__device__ __forceinline__ T gl8_w(int i) {
+    const T w[4] = {(T)0.36268378337836166, (T)0.3137066458778869, (T)0.22238103445337443,
+                    (T)0.10122853629037706};
+    return w[i];
+}
+
+// s0 = s0h + s0l (a pair in FP32, s0l = 0 in FP64).  Returns shf; with GRAD
+// also *ds0 and *da.  Inlined form (for kernels with few live registers at
+// the call) and an out-of-line form (precession_average) for the forward
+// kernel, whose variants without the average must not pay its registers.
+template <typename T, bool GRAD, class C>
+__device__ __forceinline__ T precession_average_inline(const C &c, T s0h, T s0l, T a, T *ds0, T *da) {
+    const T PI_T = (T)SHAPE_PI;
+    const T s0 = s0h + s0l;
+    if (GRAD) { *ds0 = (T)0; *da = (T)0; }
+    if (c.shape == DS_SHAPE_BINARY) return (T)1;
+    if (!(a > (T)0)) {
+        if (GRAD) *ds0 = shape_deriv<T>(c, s0);
+        return shape_val_t(c, s0);
+    }
+    const T h = (T)c.int_step;
+    const T w = (T)c.width;
+    const T lo = s0 - a, hi = s0 + a;
+    const bool clip = c.shape == DS_SHAPE_LINEAR && w > (T)0;
+    T kf = (h > (T)0 && h < (T)INFINITY) ? ceil(lo / h) : (T)INFINITY;
+    T th_prev = PI_T, s_prev = lo, sum = (T)0, g0 = (T)0, g1 = (T)0;
+    for (;;) {
+        const T sk = kf * h;
+        const bool last = !(sk < hi);
+        const T s_next = last ? hi : sk;
+        const T th = last ? (T)0 : acos(fmin(fmax((sk - s0) / a, (T)-1), (T)1));
+        if (th_prev > th && !(clip && (s_next <= -w || s_prev >= w))) {
+            const T mid = (T)0.5 * (th + th_prev), half = (T)0.5 * (th_prev - th);
+            T acc = (T)0, a0 = (T)0, a1 = (T)0;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const T d = half * gl8_x<T>(i);
+                const T c1 = cos(mid + d), c2 = cos(mid - d);
+                const T x1 = fma(a, c1, s0h) + s0l, x2 = fma(a, c2, s0h) + s0l;
+                acc = fma(gl8_w<T>(i), shape_val_t(c, x1) + shape_val_t(c, x2), acc);
+                if (GRAD) {
+                    const T d1 = shape_deriv<T>(c, x1), d2 = shape_deriv<T>(c, x2);
+                    a0 = fma(gl8_w<T>(i), d1 + d2, a0);
+                    a1 = fma(gl8_w<T>(i), d1 * c1 + d2 * c2, a1);
+                }
+            }
+            sum = fma(half, acc, sum);
+            if (GRAD) {
+                g0 = fma(half, a0, g0);
+                g1 = fma(half, a1, g1);
+            }
+        }
+        if (last) break;
+        th_prev = th;
+        s_prev = s_next;
+        kf += (T)1;
+    }
+    if (GRAD) {
+        *ds0 = g0 / PI_T;
+        *da = g1 / PI_T;
+    }
+    return sum / PI_T;
+}
+
+template <typename T, bool GRAD, class C>
+__device__ __noinline__ T precession_average(const C &c, T s0h, T s0l, T a, T *ds0, T *da) {
+    return precession_average_inline<T, GRAD>(c, s0h, s0l, a, ds0, da);
+}
+
+// lorentzian_precession (:183-219) and its partial derivatives, FP64.
+template <class C>
+__device__ inline double lorentzian_precession_grad(const C &c, double s, double r, double &dsf_ds, double &dsf_dr) {
+    const double sig = SHAPE_PI / c.width;
+    const double u = sig * sig * (r * r * c.phi * c.phi - s * s) + 1;
+    const double z = sqrt(u * u + 4 * sig * sig * s * s);
+    const double Q = 2 * (u + z) / (z * z);
+    const double f = (sig / SHAPE_PI) * sqrt(Q);
+    // dQ = 2 [(du + dz) / z^2 - 2 (u + z) dz / z^3],  dz = (u du + 4 sig^2 s ds) / z
+    auto dQ = [&](double du, double dz) { return 2 * ((du + dz) / (z * z) - 2 * (u + z) * dz / (z * z * z)); };
+    const double k = f > 0 ? (sig / SHAPE_PI) * 0.5 / sqrt(Q) : 0.0;
+    {
+        const double du = -2 * sig * sig * s;
+        const double dz = (u * du + 4 * sig * sig * s) / z;
+        dsf_ds = k * dQ(du, dz);
+    }
+    {
+        const double du = 2 * sig * sig * r * c.phi * c.phi;
+        const double dz = u * du / z;
+        dsf_dr = k * dQ(du, dz);
+    }
+    return f;
+}
+
+}  // namespace ds

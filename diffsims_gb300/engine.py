@@ -47,12 +47,32 @@ class PhaseTable:
 
     def __init__(self, phase, reciprocal_radius=1.0, with_direct_beam=True, scattering_params="lobato",
                  debye_waller_factors=None, form="mixed", device=None, stream=None, build=True):
-        lib = N.load_library()
         dev = _device(device)
+        structure = structure_of(phase)
+        els, xyz, occ = sites_of(structure)
+        B = debye_waller_per_atom(els, debye_waller_factors)
+        atoms = PackedAtoms(els, xyz, occ, B, scattering_params, dev)
+        self._setup(reciprocal_basis(structure.lattice), atoms, reciprocal_radius, with_direct_beam, form, dev)
+        if build:
+            self.build(stream)
+
+    @classmethod
+    def from_parts(cls, recip, atoms: PackedAtoms, reciprocal_radius=1.0, with_direct_beam=True, form="mixed",
+                   device=None, stream=None, build=True):
+        """A table from a reciprocal basis (rows a*, b*, c*, 1/Angstrom) and
+        packed atoms, without a phase object (the differentiable path)."""
+        obj = cls.__new__(cls)
+        obj._setup(np.ascontiguousarray(np.asarray(recip, dtype=np.float64).reshape(3, 3)), atoms, reciprocal_radius,
+                   with_direct_beam, form, _device(device))
+        if build:
+            obj.build(stream)
+        return obj
+
+    def _setup(self, recip, atoms, reciprocal_radius, with_direct_beam, form, dev):
+        lib = N.load_library()
         self.device = dev
         self.form = form
-        structure = structure_of(phase)
-        self.recip = reciprocal_basis(structure.lattice)
+        self.recip = recip
         self.dmin = 1.0 / float(reciprocal_radius)
         self.hmax = box_extent(self.recip, self.dmin)
         self.n_zero = 2 if with_direct_beam else 0
@@ -65,16 +85,12 @@ class PhaseTable:
         self._hm = (C.c_int32 * 3)(*self.hmax.tolist())
         self._rb = (C.c_double * 9)(*self.recip.reshape(-1).tolist())
         self._enum_bytes = lib.ds_enumerate_scratch_bytes(self._hm)
-        els, xyz, occ = sites_of(structure)
-        B = debye_waller_per_atom(els, debye_waller_factors)
-        self.atoms = PackedAtoms(els, xyz, occ, B, scattering_params, dev)
+        self.atoms = atoms
         self._sf_bytes = lib.ds_structure_factor_scratch_bytes(self.cap, self.atoms.n_atoms)
         self._scratch = torch.empty(max(self._enum_bytes, self._sf_bytes), dtype=torch.uint8, device=dev)
         self._F2 = torch.empty(self.cap, dtype=torch.float32, device=dev)
         self._F2d = torch.empty(self.cap, dtype=torch.float64, device=dev) if form == "fp64" else None
         self.n = 0
-        if build:
-            self.build(stream)
 
     def build(self, stream=None):
         """Enumerate the hkl rows and compute |F|^2 on the device (inputs

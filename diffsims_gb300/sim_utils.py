@@ -96,6 +96,22 @@ class PackedAtoms:
         return N.ds_atoms(self.n_atoms, self.n_species, self.records.data_ptr(), self.coeffs.data_ptr(),
                           self.kind, 0)
 
+    def with_values(self, xyz, occupancy, B):
+        """A copy whose per-atom values come from device tensors (float64:
+        (N, 3), (N,), (N,)); species and coefficients are shared.  Builds the
+        records on the device (no host round trip)."""
+        n = self.n_atoms
+        rec = torch.empty((n, 12), dtype=torch.int32, device=self.records.device)
+        r64 = rec.view(torch.float64)
+        r64[:, 0:3] = xyz.detach().to(torch.float64)
+        r64[:, 3] = occupancy.detach().to(torch.float64)
+        r64[:, 4] = B.detach().to(torch.float64)
+        rec[:, 10:12] = self.records.view(torch.int32).view(n, 12)[:, 10:12]
+        out = PackedAtoms.__new__(PackedAtoms)
+        out.records = rec.view(torch.uint8).reshape(-1)
+        out.coeffs, out.n_atoms, out.n_species, out.kind = self.coeffs, n, self.n_species, self.kind
+        return out
+
 
 def debye_waller_per_atom(elements, debye_waller_factors):
     """Per-atom B.  A dict maps element -> B (the reference's rule,

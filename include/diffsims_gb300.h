@@ -224,6 +224,30 @@ ds_status ds_rasterize(const ds_raster_params *p, const int64_t *offsets, const 
                        size_t scratch_bytes, int32_t *status, void *stream);
 
 /* ------------------------------------------------------------------------ */
+/* Adjoint of the spot intensities I = shf(s, r) |F_hkl|^2 (no counterpart in
+ * the reference, which is not differentiable).  After a ds_simulate call with
+ * the same p, t and quats: grad_intensity[j] = dL/dI for every output spot j.
+ * Accumulates (+=) dL/d|F|^2 per table row into grad_F2 (n_hkl doubles) and
+ * dL/dB* into grad_recip (9 doubles, B* = t->recip, rows a*, b*, c*); writes
+ * dL/dR (n_orient x 9 doubles, R the active rotation matrix of the normalised
+ * quaternion, row-major).  Selection is piecewise constant and not
+ * differentiated. */
+ds_status ds_simulate_backward(const ds_sim_params *p, const ds_phase_table *t, const double *quats,
+                               int64_t n_orient, const int64_t *offsets, const int32_t *hkl_index,
+                               const double *grad_intensity, double *grad_F2, double *grad_R,
+                               double *grad_recip, void *stream);
+
+size_t ds_structure_factors_backward_scratch_bytes(int64_t n);
+
+/* Adjoint of ds_structure_factors: from dL/d|F|^2 per row, accumulates (+=)
+ * dL/d(x, y, z, occupancy, B) per atom into grad_atoms (n_atoms x 5 doubles)
+ * and dL/dB* through |g|^2 (scattering factors, Debye-Waller) into grad_recip.
+ * recip: host array, the rows' reciprocal basis.  F is recomputed (FP64). */
+ds_status ds_structure_factors_backward(const ds_atoms *atoms, const int32_t *hkl, const double *g2, int64_t n,
+                                        const double recip[9], const double *grad_F2, double *grad_atoms,
+                                        double *grad_recip, void *scratch, size_t scratch_bytes, void *stream);
+
+/* ------------------------------------------------------------------------ */
 /* FP32 FMA throughput probe (no counterpart in the reference): blocks x 256
  * threads, each 8 chains x 16 x iters fused multiply-adds; out holds
  * blocks*256 floats.  FLOPs = blocks * 256 * iters * 256.  Used to measure the
