@@ -16,8 +16,17 @@ Arms:
   default           the CUDA path (mixed form).  value = patterns/s with the
                     inputs resident in HBM; e2e = the same through the public
                     API with host quaternions in and all spots copied back.
+                    Extra legs in the same line: "grad" (gradient step of the
+                    differentiation workload against its forward pass),
+                    "template_library" (three phases simulated and rasterised
+                    to 256x256 detectors in 8192-orientation chunks).
   --impl reference  the reference's CPU path restated in numpy (the FP64
                     oracle) on all host cores, a bounded sample per step.
+
+Several GPUs (torchrun): every rank runs the same per-GPU workload (weak
+scaling; orientations are independent, there is no exchange), the timed
+region is bracketed by barriers, the slowest rank's time counts and rank 0
+reports; the extra legs run on rank 0 only.
 """
 from __future__ import annotations
 
@@ -44,6 +53,20 @@ METRIC = "orientation patterns/s"
 # simulate_kernel launch on 8192 orientations of the workload below
 DRAM_BYTES_PER_SPOT = 21.5
 UNIT = "patterns/s"
+
+
+GRAD_WORKLOAD = dict(workload="orthorhombic 7.1/9.3/12.4, 64 atoms, 4096 orientations in a 5 deg cone about [001], "
+                              "300 kV, r=1.5, sinc with 1 deg precession (rotation average), loss = sum of squared "
+                              "spot-intensity differences to perturbed-parameter targets",
+                     seed=4, n_atoms=64, n_orientations=4096, cone_deg=5.0, accelerating_voltage=300,
+                     reciprocal_radius=1.5, max_excitation_error=0.015, shape_factor_model="sinc",
+                     precession_angle=1.0, approximate_precession=False)
+LIBRARY_WORKLOAD = dict(workload="template library: Al FCC, Fe BCC, P1 60 atoms; 200k orientations per phase, 200 kV, "
+                                 "r=1.2, linear with 0.5 deg precession (rotation average), 256x256 float32 detector, "
+                                 "sigma 1 px, 8192-orientation chunks",
+                        n_orientations=200_000, chunk=8192, accelerating_voltage=200, reciprocal_radius=1.2,
+                        max_excitation_error=0.01, shape_factor_model="linear", precession_angle=0.5,
+                        approximate_precession=False, shape=(256, 256), sigma=1.0, calibration=1.2 / 128, seed=5)
 
 
 def make_crystal(seed=1, n_atoms=200):
@@ -174,8 +197,15 @@ def run_gpu(args):
     from diffsims_gb300.engine import PhaseTable, SpotBuffers, simulate_phase, estimate_spots
 
     lib = N.load_library()
-    torch.cuda.set_device(0)
-    dev = torch.device("cuda", 0)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
     lat, els, xyz, B = make_crystal(WORKLOAD["cell_seed"], WORKLOAD["n_atoms"])
     phase = ds.Phase("P1", ds.Structure([ds.Atom(e, x) for e, x in zip(els, xyz)], ds.Lattice(*lat)))
     n_o = args.orientations
@@ -199,7 +229,9 @@ def run_gpu(args):
         spots = step()
     torch.cuda.synchronize()
     step_ms, kern_ms = [], []
-    with ClockSampler(os.path.join(args.out_dir, "clocks.csv") if args.out_dir else None) as clk:
+    with ClockSampler(os.path.join(args.out_dir, "clocks.csv") if args.out_dir and rank == 0 else None) as clk:
+        if dist:
+            dist.barrier()
         torch.cuda.synchronize()
         t_all = time.perf_counter()
         for _ in range(args.steps):
@@ -211,6 +243,8 @@ def run_gpu(args):
             e1.synchronize()
             step_ms.append(e0.elapsed_time(e1))
         torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
         wall = time.perf_counter() - t_all
         # the dominant kernel alone (simulate), timed on its launch stream
         for _ in range(args.steps):
@@ -223,11 +257,18 @@ def run_gpu(args):
             kern_ms.append(e0.elapsed_time(e1))
     clocks = clk.summary()
     ms = statistics.mean(step_ms)
+    if dist:
+        t = torch.tensor([ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)  # the slowest rank's step time
+        ms = float(t.item())
+        if rank != 0:
+            dist.destroy_process_group()
+            return
     if args.device_only:
         print(json.dumps({"device_only": True, "ms_per_step": ms, "kernel_ms": statistics.mean(kern_ms),
                           "patterns_per_s": n_o / (ms * 1e-3), "n_hkl": table.n, "spots": spots.total}))
         return
-    value = n_o / (ms * 1e-3)
+    value = world * n_o / (ms * 1e-3)
     total_spots = spots.total
     n_h = table.n
 
@@ -285,6 +326,9 @@ def run_gpu(args):
     mixed = simulate_phase(table, q_cmp, settings, r, SpotBuffers(dev, with_excitation_error=True))
     err = compare_forms(mixed, ref64, table, q_host[:n_cmp], settings)
 
+    grad = None if args.skip_grad else run_grad(args, torch, dev)
+    library = None if args.skip_library else run_library(args, torch, dev, hbm_peak)
+
     cpu = None
     if not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
@@ -294,14 +338,14 @@ def run_gpu(args):
                          f"reference path, {cores} spawned processes, {dt:.1f} s"}
 
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded P1 cell and uniform SO(3) orientations)",
         "config": dict(WORKLOAD, n_orientations=n_o, n_hkl=n_h, spots_per_step=total_spots,
                        l2="256 MB buffer written between timed steps", form="mixed"),
         "spots_per_s": total_spots / (ms * 1e-3),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "ms_per_step": statistics.mean(e2e_ms)},
+                "ms_per_step": statistics.mean(e2e_ms), "ranks": 1},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
                      "frac": achieved / peak32, "traffic": traffic, "kernel": "simulate_kernel",
                      "kernel_ms": kms, "peak_source": "measured by bench.py FMA probe (ds_probe_fp32_fma)",
@@ -309,14 +353,160 @@ def run_gpu(args):
                              "frac": bytes_alg / (kms * 1e-3) / 1e9 / hbm_peak,
                              "peak_source": "MEASURED_PEAKS.json" if peaks else "fallback"}},
         "fp64_form": {"value": fp64_rate, "unit": UNIT, "orientations": n_cmp,
-                      "mixed_over_fp64": value / fp64_rate},
+                      "mixed_over_fp64": (n_o / (ms * 1e-3)) / fp64_rate},
         "error_vs_fp64_form": err,
+        "grad": grad,
+        "template_library": library,
         "cpu_baseline": cpu,
         "clocks": clocks,
         "gpu_launches": 5 * args.steps,
         "wall_s_timed_region": wall,
     }
     print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+def cone_quaternions(n, deg, seed):
+    """Rotations within ``deg`` of the identity (axis uniform, cos(angle)
+    uniform): beam directions in a cone about [001]."""
+    rng = np.random.default_rng(seed)
+    ax = rng.standard_normal((n, 3))
+    ax /= np.linalg.norm(ax, axis=1, keepdims=True)
+    th = np.arccos(rng.uniform(np.cos(np.radians(deg)), 1.0, n))
+    return np.c_[np.cos(th / 2), np.sin(th / 2)[:, None] * ax]
+
+
+def run_grad(args, torch, dev):
+    """Gradient step of the differentiation workload: forward (tables,
+    spots, loss) and forward + adjoint, timed with the device synchronised on
+    both sides (the forward reads the row and spot counts on the host)."""
+    import diffsims_gb300 as ds
+    from diffsims_gb300.autograd import (SpotModel, compose_axis_angle, reciprocal_basis, simulate_intensities,
+                                         spot_loss)
+    W = GRAD_WORKLOAD
+    rng = np.random.default_rng(W["seed"])
+    n_a, n_o = W["n_atoms"], W["n_orientations"]
+    els = list(rng.choice(["O", "Si", "Fe"], n_a))
+    lat = np.array([7.1, 9.3, 12.4, 90.0, 90.0, 90.0])
+    xyz, B, occ = rng.random((n_a, 3)), rng.uniform(0.3, 1.5, n_a), np.ones(n_a)
+    q0 = cone_quaternions(n_o, W["cone_deg"], W["seed"] + 1)
+    gen = ds.SimulationGenerator(W["accelerating_voltage"], "lobato", W["precession_angle"], W["shape_factor_model"],
+                                 W["approximate_precession"])
+    model = SpotModel(els, gen, W["reciprocal_radius"], W["max_excitation_error"])
+    T = lambda a: torch.as_tensor(np.asarray(a, dtype=np.float64), device=dev)
+    ax = rng.standard_normal((n_o, 3))
+    ax *= np.radians(0.2) / np.linalg.norm(ax, axis=1, keepdims=True)
+    with torch.no_grad():
+        tq = compose_axis_angle(T(q0), T(ax))
+        target = simulate_intensities(model, T(xyz + rng.normal(0, 0.01, xyz.shape)),
+                                      T(B * (1 + rng.normal(0, 0.1, n_a))), T(occ * rng.uniform(0.9, 1.0, n_a)),
+                                      reciprocal_basis(torch.as_tensor(lat * [1.002, 1.002, 1.002, 1, 1, 1])), tq)
+    q0t = T(q0)
+    # parameters resident where they live in a refinement loop: per-atom and
+    # per-orientation values on the device, the six lattice parameters on the
+    # host (the forward reads the reciprocal basis on the host)
+    ps = [T(xyz), T(B), T(occ), torch.as_tensor(lat, dtype=torch.float64),
+          torch.zeros((n_o, 3), dtype=torch.float64, device=dev)]
+
+    def forward(grad):
+        for t in ps:
+            t.requires_grad_(grad)
+            t.grad = None
+        sim = simulate_intensities(model, ps[0], ps[1], ps[2], reciprocal_basis(ps[3]), compose_axis_angle(q0t, ps[4]))
+        L = spot_loss(sim, target)
+        if grad:
+            L.backward()
+        return L, sim, ps
+
+    def timed(grad):
+        out = []
+        for it in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            L, sim, ps_ = forward(grad)
+            torch.cuda.synchronize()
+            if it >= args.warmup:
+                out.append((time.perf_counter() - t0) * 1e3)
+        return statistics.mean(out), L, sim, ps_
+
+    fwd_ms, L, sim, _ = timed(False)
+    grad_ms, _, _, ps = timed(True)
+    gnorm = {n: float(torch.linalg.norm(t.grad)) for n, t in zip(("xyz", "B", "occupancy", "lattice", "axis_angle"), ps)}
+    return {"ms_per_step": grad_ms, "forward_ms": fwd_ms, "grad_over_forward": grad_ms / fwd_ms,
+            "unit": "ms", "loss": float(L), "spots": int(sim.intensity.shape[0]), "gradient_norms": gnorm,
+            "config": {k: v for k, v in W.items()}, "dtype": "f32 forward with f64 phase; f64 adjoint"}
+
+
+def run_library(args, torch, dev, hbm_peak):
+    """Template-library throughput: three phases simulated and rasterised in
+    8192-orientation chunks through one reused detector buffer."""
+    import diffsims_gb300 as ds
+    from diffsims_gb300.engine import PhaseTable, RasterBuffers, RasterSettings, SpotBuffers, rasterize, simulate_phase
+    W = LIBRARY_WORKLOAD
+    rng = np.random.default_rng(W["seed"])
+    al = ds.Phase("Al", ds.Structure([ds.Atom("Al", x) for x in [[0, 0, 0], [0, .5, .5], [.5, 0, .5], [.5, .5, 0]]],
+                                     ds.Lattice(4.05, 4.05, 4.05, 90, 90, 90)))
+    fe = ds.Phase("Fe", ds.Structure([ds.Atom("Fe", x) for x in [[0, 0, 0], [.5, .5, .5]]],
+                                     ds.Lattice(2.87, 2.87, 2.87, 90, 90, 90)))
+    lat = tuple(rng.uniform(6, 10, 3)) + tuple(rng.uniform(70, 110, 3))
+    p1_els = list(rng.choice(["C", "N", "O", "Si", "Fe"], 60))
+    p1 = ds.Phase("P1", ds.Structure([ds.Atom(e, x) for e, x in zip(p1_els, rng.random((60, 3)))], ds.Lattice(*lat)))
+    dws = [[0.5] * 4, [0.35] * 2, list(rng.uniform(0.3, 1.5, 60))]
+    gen = ds.SimulationGenerator(W["accelerating_voltage"], "lobato", W["precession_angle"], W["shape_factor_model"],
+                                 W["approximate_precession"])
+    settings = gen.settings(W["max_excitation_error"])
+    r = W["reciprocal_radius"]
+    n_o, chunk = W["n_orientations"], W["chunk"]
+    H, Wd = W["shape"]
+    qs = [torch.from_numpy(uniform_quaternions(n_o, 100 + i)).to(dev) for i in range(3)]
+    tables = [PhaseTable(ph, r, True, "lobato", dw, device=dev) for ph, dw in zip((al, fe, p1), dws)]
+    bufs = [SpotBuffers(dev) for _ in range(3)]
+    rs = RasterSettings((H, Wd), sigma=W["sigma"], calibration=W["calibration"])
+    rb = RasterBuffers(dev)
+    img = torch.empty((chunk, H, Wd), dtype=torch.float32, device=dev)
+    st = torch.cuda.current_stream()
+
+    def step(time_raster):
+        spots = [simulate_phase(t, q, settings, r, b) for t, q, b in zip(tables, qs, bufs)]
+        maxes = [int((s.offsets[1:] - s.offsets[:-1]).max().item()) for s in spots]
+        ras_ms = 0.0
+        for s, m in zip(spots, maxes):
+            for a in range(0, n_o, chunk):
+                b = min(a + chunk, n_o)
+                if time_raster:
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(st)
+                rasterize(s, rs, a, b, out=img[:b - a], max_spots=m, buffers=rb, sync=False)
+                if time_raster:
+                    e1.record(st)
+                    e1.synchronize()
+                    ras_ms += e0.elapsed_time(e1)
+        return spots, ras_ms
+
+    for _ in range(args.warmup):
+        step(False)
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        spots, _ = step(False)
+        torch.cuda.synchronize()
+        ms.append((time.perf_counter() - t0) * 1e3)
+    _, ras_ms = step(True)
+    from diffsims_gb300 import _native as N
+    N.check_device_status(rb.status, "rasterize")
+    n_pat = 3 * n_o
+    bytes_img = n_pat * H * Wd * 4
+    ras_gbs = bytes_img / (ras_ms * 1e-3) / 1e9
+    return {"metric": "orientation patterns/s (simulated and rasterised)", "value": n_pat / (statistics.mean(ms) * 1e-3),
+            "unit": "patterns/s", "ms_per_step": statistics.mean(ms), "patterns_per_step": n_pat,
+            "spots_per_step": int(sum(s.total for s in spots)), "n_hkl": [t.n for t in tables],
+            "raster": {"ms": ras_ms, "achieved_gbs": ras_gbs, "peak_gbs": hbm_peak, "frac": ras_gbs / hbm_peak,
+                       "bytes_written": bytes_img, "launches": 3 * ((n_o + chunk - 1) // chunk),
+                       "note": "CUDA events around each chunk's launch; bytes = images written"},
+            "config": {k: (list(v) if isinstance(v, tuple) else v) for k, v in W.items()}}
 
 
 def compare_forms(mixed, ref, table, q_host, settings):
@@ -385,7 +575,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--orientations", type=int, default=WORKLOAD["n_orientations"])
     ap.add_argument("--fp64-orientations", type=int, default=4096)
-    ap.add_argument("--cpu-sample", type=int, default=1024)
+    ap.add_argument("--cpu-sample", type=int, default=16384)
+    ap.add_argument("--skip-grad", action="store_true", help="leave out the gradient-step leg")
+    ap.add_argument("--skip-library", action="store_true", help="leave out the template-library leg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--out-dir", default=None)
     ap.add_argument("--screen", default="auto", choices=["auto", "rows", "lines"],
@@ -396,11 +588,6 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
-    # one process per GPU; the path shards by orientation with no exchange, so
-    # N > 1 runs independent replicas and only rank 0 reports
-    rank = int(os.environ.get("RANK", "0"))
-    if args.gpus > 1 and rank != 0:
-        os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("LOCAL_RANK", "0"))
     run_gpu(args)
 
 

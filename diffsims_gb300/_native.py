@@ -38,7 +38,8 @@ EXPORTED_SYMBOLS = (
     "ds_box_extent", "ds_enumerate_scratch_bytes", "ds_enumerate_hkl",
     "ds_structure_factor_scratch_bytes", "ds_structure_factors", "ds_kinematical_intensities",
     "ds_simulate_scratch_bytes", "ds_simulate", "ds_rasterize_scratch_bytes", "ds_rasterize",
-    "ds_simulate_backward", "ds_structure_factors_backward_scratch_bytes", "ds_structure_factors_backward",
+    "ds_simulate_backward_scratch_bytes", "ds_simulate_backward", "ds_structure_factors_backward_scratch_bytes",
+    "ds_axis_angle_compose", "ds_axis_angle_compose_backward", "ds_structure_factors_backward",
     "ds_probe_fp32_fma", "ds_last_error", "ds_version",
 )
 
@@ -114,17 +115,22 @@ def load_library(require_cuda: bool = True):
             lib.ds_rasterize_scratch_bytes.argtypes = [C.POINTER(ds_raster_params), i64]
             lib.ds_rasterize_scratch_bytes.restype = sz
             lib.ds_rasterize.argtypes = [C.POINTER(ds_raster_params), vp, vp, i64, i64, vp, vp, sz, vp, vp]
+            lib.ds_simulate_backward_scratch_bytes.argtypes = [C.POINTER(ds_sim_params), i64]
+            lib.ds_simulate_backward_scratch_bytes.restype = sz
             lib.ds_simulate_backward.argtypes = [C.POINTER(ds_sim_params), C.POINTER(ds_phase_table), vp, i64, vp,
-                                                 vp, vp, vp, vp, vp, vp]
-            lib.ds_structure_factors_backward_scratch_bytes.argtypes = [i64]
+                                                 vp, i64, vp, vp, vp, vp, vp, sz, vp, vp]
+            lib.ds_structure_factors_backward_scratch_bytes.argtypes = [i64, i32]
             lib.ds_structure_factors_backward_scratch_bytes.restype = sz
             lib.ds_structure_factors_backward.argtypes = [C.POINTER(ds_atoms), vp, vp, i64, C.POINTER(C.c_double), vp,
                                                           vp, vp, vp, sz, vp]
+            lib.ds_axis_angle_compose.argtypes = [vp, vp, i64, vp, vp]
+            lib.ds_axis_angle_compose_backward.argtypes = [vp, vp, i64, vp, vp, vp]
             lib.ds_probe_fp32_fma.argtypes = [i64, i32, vp, vp]
             lib.ds_last_error.restype = C.c_char_p
             lib.ds_version.restype = C.c_char_p
             for name in ("ds_box_extent", "ds_enumerate_hkl", "ds_structure_factors", "ds_kinematical_intensities",
                          "ds_simulate", "ds_rasterize", "ds_simulate_backward", "ds_structure_factors_backward",
+                         "ds_axis_angle_compose", "ds_axis_angle_compose_backward",
                          "ds_probe_fp32_fma"):
                 getattr(lib, name).restype = C.c_int32
             _lib = lib

@@ -26,18 +26,55 @@ from .sim_utils import PackedAtoms
 
 
 # ------------------------------------------------- differentiable geometry ----
-def reciprocal_basis(lattice: torch.Tensor) -> torch.Tensor:
-    """Rows a*, b*, c* (1/Angstrom) of the lattice (a, b, c, alpha, beta,
-    gamma; degrees) in the x || a, z || c* frame, differentiably."""
-    a, b, c, al, be, ga = [lattice[i] for i in range(6)]
-    d = math.pi / 180.0
-    ca, cb, cg, sg = torch.cos(al * d), torch.cos(be * d), torch.cos(ga * d), torch.sin(ga * d)
+def _direct_base(p):
+    """Rows a, b, c of the lattice (a, b, c, alpha, beta, gamma; degrees) in
+    the x || a, z || c* frame, and d(base)/d(param) (6 x 3 x 3)."""
+    a, b, c, al, be, ga = p
+    d = np.pi / 180.0
+    ca, cb, cg = np.cos(al * d), np.cos(be * d), np.cos(ga * d)
+    sa, sb, sg = np.sin(al * d), np.sin(be * d), np.sin(ga * d)
     cx = c * cb
     cy = c * (ca - cb * cg) / sg
-    cz = torch.sqrt(c * c - cx * cx - cy * cy)
-    zero = torch.zeros_like(a)
-    base = torch.stack([torch.stack([a, zero, zero]), torch.stack([b * cg, b * sg, zero]), torch.stack([cx, cy, cz])])
-    return torch.linalg.inv(base).transpose(0, 1)
+    cz = np.sqrt(c * c - cx * cx - cy * cy)
+    L = np.array([[a, 0, 0], [b * cg, b * sg, 0], [cx, cy, cz]])
+    dL = np.zeros((6, 3, 3))
+    dL[0, 0, 0] = 1.0
+    dL[1, 1, 0], dL[1, 1, 1] = cg, sg
+    # c row: (c cb, c (ca - cb cg) / sg, sqrt(c^2 - cx^2 - cy^2))
+    def c_row(dcx, dcy):
+        return dcx, dcy, -(cx * dcx + cy * dcy) / cz
+    dL[2, 2] = [cb, (ca - cb * cg) / sg, cz / c]                                   # d/dc
+    dL[3, 2] = c_row(0.0, c * (-sa * d) / sg)                                        # d/dalpha
+    dL[4, 2] = c_row(c * (-sb * d), c * (sb * d * cg) / sg)                          # d/dbeta
+    dcy_dg = c * ((cb * sg * d) * sg - (ca - cb * cg) * cg * d) / (sg * sg)
+    dL[5, 1, 0], dL[5, 1, 1] = -b * sg * d, b * cg * d                               # d/dgamma, b row
+    dL[5, 2] = c_row(0.0, dcy_dg)
+    return L, dL
+
+
+class _ReciprocalBasis(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, lattice):
+        p = lattice.detach().cpu().numpy().astype(np.float64)
+        L, dL = _direct_base(p)
+        rec = np.linalg.inv(L).T
+        ctx.rec, ctx.dL, ctx.dev = rec, dL, lattice.device
+        return torch.as_tensor(rec, dtype=torch.float64).to(lattice.device)
+
+    @staticmethod
+    def backward(ctx, g):
+        G = g.detach().cpu().numpy().astype(np.float64)
+        # recip = L^-T: d recip = -recip dL^T recip
+        grads = [float(-(G * (ctx.rec @ ctx.dL[k].T @ ctx.rec)).sum()) for k in range(6)]
+        return torch.as_tensor(grads, dtype=torch.float64).to(ctx.dev)
+
+
+def reciprocal_basis(lattice: torch.Tensor) -> torch.Tensor:
+    """Rows a*, b*, c* (1/Angstrom) of the lattice (a, b, c, alpha, beta,
+    gamma; degrees) in the x || a, z || c* frame, differentiable.  Evaluated
+    on the host (3 x 3); keep the lattice parameters on the CPU in a loop to
+    avoid a device round trip."""
+    return _ReciprocalBasis.apply(lattice)
 
 
 def axis_angle_quaternion(v: torch.Tensor) -> torch.Tensor:
@@ -57,6 +94,35 @@ def quaternion_multiply(p: torch.Tensor, q: torch.Tensor) -> torch.Tensor:
     qw, qx, qy, qz = q.unbind(-1)
     return torch.stack([pw * qw - px * qx - py * qy - pz * qz, pw * qx + px * qw + py * qz - pz * qy,
                         pw * qy - px * qz + py * qw + pz * qx, pw * qz + px * qy - py * qx + pz * qw], dim=-1)
+
+
+class _AxisAngleCompose(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, q0, v):
+        lib = N.load_library()
+        q0c, vc = q0.detach().to(torch.float64).contiguous(), v.detach().to(torch.float64).contiguous()
+        out = torch.empty_like(q0c)
+        N.check(lib.ds_axis_angle_compose(N.ptr(q0c), N.ptr(vc), q0c.shape[0], N.ptr(out), N.stream_handle()),
+                "axis_angle_compose")
+        ctx.save_for_backward(q0c, vc)
+        return out
+
+    @staticmethod
+    def backward(ctx, gq):
+        lib = N.load_library()
+        q0c, vc = ctx.saved_tensors
+        gv = torch.empty_like(vc)
+        N.check(lib.ds_axis_angle_compose_backward(N.ptr(q0c), N.ptr(vc), q0c.shape[0],
+                                                   N.ptr(gq.to(torch.float64).contiguous()), N.ptr(gv),
+                                                   N.stream_handle()), "axis_angle_compose_backward")
+        return None, gv
+
+
+def compose_axis_angle(q0: torch.Tensor, v: torch.Tensor) -> torch.Tensor:
+    """q0 (x) exp(v) on the device, one fused kernel each way: orientation
+    quaternions q0 (n, 4) corrected by rotation vectors v (n, 3, radians),
+    differentiable in v."""
+    return _AxisAngleCompose.apply(q0, v)
 
 
 def quaternion_matrix(q: torch.Tensor) -> torch.Tensor:
@@ -117,6 +183,8 @@ class _KinematicalIntensities(torch.autograd.Function):
         hkl = table.hkl[idx.long()] if spots.total else torch.zeros((0, 3), dtype=torch.int32, device=q.device)
         ctx.save_for_backward(q)
         ctx.table, ctx.offsets, ctx.idx, ctx.model = table, spots.offsets, idx, model
+        ctx.recip_device = recip.device
+        model.last_hmax = int(np.max(table.hmax))  # bound on |h|, |k|, |l| of every spot
         ctx.mark_non_differentiable(spots.offsets, hkl)
         return inten, spots.offsets, hkl
 
@@ -131,38 +199,47 @@ class _KinematicalIntensities(torch.autograd.Function):
         g_inten = (torch.zeros(ctx.idx.shape[0], dtype=torch.float64, device=dev) if g_inten is None
                    else g_inten.to(torch.float64).contiguous())
         gF2 = torch.zeros(max(table.n, 1), dtype=torch.float64, device=dev)
-        gR = torch.zeros((n_o, 9), dtype=torch.float64, device=dev)
+        gq = torch.empty((n_o, 4), dtype=torch.float64, device=dev)
         grecip = torch.zeros(9, dtype=torch.float64, device=dev)
         gatoms = torch.zeros((n_a, 5), dtype=torch.float64, device=dev)
         st = N.stream_handle()
-        N.check(lib.ds_simulate_backward(model.settings.cstruct(), table.cstruct(), N.ptr(q), n_o, N.ptr(ctx.offsets),
-                                         N.ptr(ctx.idx), N.ptr(g_inten), N.ptr(gF2), N.ptr(gR), N.ptr(grecip), st),
-                "simulate_backward")
-        nbytes = lib.ds_structure_factors_backward_scratch_bytes(table.n)
+        p = model.settings.cstruct()
+        n_sp = int(ctx.idx.shape[0])
+        bbytes = lib.ds_simulate_backward_scratch_bytes(p, n_sp)
+        bscr = torch.empty(max(bbytes, 16), dtype=torch.uint8, device=dev)
+        status = torch.zeros(1, dtype=torch.int32, device=dev)
+        N.check(lib.ds_simulate_backward(p, table.cstruct(), N.ptr(q), n_o, N.ptr(ctx.offsets), N.ptr(ctx.idx), n_sp,
+                                         N.ptr(g_inten), N.ptr(gF2), N.ptr(gq), N.ptr(grecip), N.ptr(bscr), bbytes,
+                                         N.ptr(status), st), "simulate_backward")
+        nbytes = lib.ds_structure_factors_backward_scratch_bytes(table.n, table.atoms.n_species)
         scratch = torch.empty(max(nbytes, 16), dtype=torch.uint8, device=dev)
         rb = (C.c_double * 9)(*table.recip.reshape(-1).tolist())
         N.check(lib.ds_structure_factors_backward(table.atoms.cstruct(), N.ptr(table.hkl) if table.n else None,
                                                   N.ptr(table.g2) if table.n else None, table.n, rb, N.ptr(gF2),
                                                   N.ptr(gatoms), N.ptr(grecip), N.ptr(scratch), nbytes, st),
                 "structure_factors_backward")
-        with torch.enable_grad():
-            qq = q.detach().requires_grad_(True)
-            (gq,) = torch.autograd.grad(quaternion_matrix(qq), qq, gR.view(n_o, 3, 3))
-        return gatoms[:, 0:3], gatoms[:, 4], gatoms[:, 3], grecip.view(3, 3), gq, None
+        N.check_device_status(status, "simulate_backward")
+        return gatoms[:, 0:3], gatoms[:, 4], gatoms[:, 3], grecip.view(3, 3).to(ctx.recip_device), gq, None
 
 
 def simulate_intensities(model: SpotModel, xyz: torch.Tensor, B: torch.Tensor, occupancy: torch.Tensor,
                          recip: torch.Tensor, quats: torch.Tensor) -> SpotIntensities:
     """Spot intensities of every orientation, differentiable with respect to
     xyz (N, 3) fractional coordinates, B (N,), occupancy (N,), recip (3, 3)
-    (rows a*, b*, c*) and quats (n, 4); all float64 on the device."""
+    (rows a*, b*, c*) and quats (n, 4); float64.  recip is read on the host by
+    the forward (hkl enumeration): keeping it, and the lattice parameters it
+    comes from, on the CPU saves a device round trip; the rest live on the
+    device."""
     inten, off, hkl = _KinematicalIntensities.apply(xyz, B, occupancy, recip, quats, model)
-    return SpotIntensities(inten, off, hkl)
+    out = SpotIntensities(inten, off, hkl)
+    out._hmax = model.last_hmax
+    return out
 
 
 def _spot_keys(sp: SpotIntensities, K: int) -> torch.Tensor:
     counts = sp.offsets[1:] - sp.offsets[:-1]
-    o = torch.repeat_interleave(torch.arange(counts.shape[0], device=counts.device), counts)
+    o = torch.repeat_interleave(torch.arange(counts.shape[0], device=counts.device), counts,
+                                output_size=int(sp.hkl.shape[0]))
     h = sp.hkl.to(torch.int64) + K // 2
     return ((o * K + h[:, 0]) * K + h[:, 1]) * K + h[:, 2]
 
@@ -170,20 +247,29 @@ def _spot_keys(sp: SpotIntensities, K: int) -> torch.Tensor:
 def spot_loss(sim: SpotIntensities, target: SpotIntensities) -> torch.Tensor:
     """Sum of squared intensity differences over the union of the two spot
     sets, matched by (orientation, hkl); a spot missing from one side counts
-    with intensity 0."""
+    with intensity 0.  (Keys are unique per side, so every target spot is
+    matched at most once: the unmatched targets contribute
+    sum T^2 - sum over matched T^2.)"""
     hmax = 1
     for sp in (sim, target):
         if sp.hkl.numel():
-            hmax = max(hmax, int(sp.hkl.abs().max().item()))
+            hm = getattr(sp, "_hmax", None)
+            if hm is None:
+                hm = int(sp.hkl.abs().max().item())
+                sp._hmax = hm
+            hmax = max(hmax, hm)
     K = 2 * hmax + 3
-    ks, kt = _spot_keys(sim, K), _spot_keys(target, K)
     t_int = target.intensity.detach()
-    if kt.numel() == 0:
+    if t_int.numel() == 0:
         return (sim.intensity ** 2).sum()
-    kt_sorted, perm = torch.sort(kt)
-    pos = torch.searchsorted(kt_sorted, ks).clamp(max=kt.numel() - 1)
+    cache = getattr(target, "_sorted_keys", None)
+    if cache is None or cache[0] != K:
+        kt_sorted, perm = torch.sort(_spot_keys(target, K))
+        cache = (K, kt_sorted, perm, (t_int ** 2).sum())
+        target._sorted_keys = cache  # the target is constant: sort its keys once
+    _, kt_sorted, perm, t_sq = cache
+    ks = _spot_keys(sim, K)
+    pos = torch.searchsorted(kt_sorted, ks).clamp(max=kt_sorted.numel() - 1)
     match = kt_sorted[pos] == ks
     matched_t = torch.where(match, t_int[perm[pos]], torch.zeros_like(sim.intensity))
-    used = torch.zeros(kt.numel(), dtype=torch.bool, device=kt.device)
-    used[perm[pos[match]]] = True
-    return ((sim.intensity - matched_t) ** 2).sum() + (t_int[~used] ** 2).sum()
+    return ((sim.intensity - matched_t) ** 2).sum() + (t_sq - (matched_t ** 2).sum())

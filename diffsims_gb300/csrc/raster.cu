@@ -406,19 +406,333 @@ __global__ void __launch_bounds__(RAS_THREADS, 4) raster_kernel(const RasterCons
     }
 }
 
+// ------------------------------------------------------------ fast mode ----
+// Whole-pixel spots and the Gaussian filter (simulation2d.py:425-431 with
+// detector_functions.py:287-294).  Every surviving spot's footprint is at
+// most P = 2R + 1 rows by P columns, with separable weights precomputed per
+// spot (the 1-D reflect-mode weights, rw and cw).  Per-row spot lists (CSR,
+// each row's spots in ascending spot order, so sums are deterministic) let one
+// warp build a row in a shared-memory row buffer: per listed spot, P lanes add
+// amp * rw * cw to their columns.
+struct FastArena {
+    int *key, *slot, *hkey, *hidx;
+    float *amp;
+    int *sx, *sy;       // whole-pixel spot position
+    float *cw;          // NS x P column weights
+    int2 *ent;          // row entries: (amp * row weight as bits, X << 16 | spot)
+    int *rcnt, *rstart, *rfill;  // H + 1 each
+    float *rowbuf;      // RAS_WARPS x RAS_FSEG
+    int *misc;
+    float *wmax;
+};
+constexpr int RAS_FSEG = 256;  // columns per row segment (32 lanes x 2 float4)
+
+__host__ __device__ inline size_t fast_arena_bytes(int NS, int T, int H, int P) {
+    size_t o = 0;
+    o += ras_align((size_t)NS * 4) * 2;              // key, slot
+    o += ras_align((size_t)T * 4) * 2;               // hkey, hidx
+    o += ras_align((size_t)NS * 4) * 3;              // amp, sx, sy
+    o += ras_align((size_t)NS * P * 4);              // cw
+    o += ras_align((size_t)NS * P * 8);              // ent
+    o += ras_align((size_t)(H + 1) * 4) * 3;         // rcnt, rstart, rfill
+    o += ras_align((size_t)RAS_WARPS * RAS_FSEG * 4);
+    o += ras_align(64 * 4) + ras_align(RAS_WARPS * 4);
+    return o;
+}
+
+__device__ inline FastArena carve_fast(unsigned char *base, int NS, int T, int H, int P) {
+    FastArena A;
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        unsigned char *p = base + o;
+        o += ras_align(bytes);
+        return p;
+    };
+    A.key = (int *)take((size_t)NS * 4);
+    A.slot = (int *)take((size_t)NS * 4);
+    A.hkey = (int *)take((size_t)T * 4);
+    A.hidx = (int *)take((size_t)T * 4);
+    A.amp = (float *)take((size_t)NS * 4);
+    A.sx = (int *)take((size_t)NS * 4);
+    A.sy = (int *)take((size_t)NS * 4);
+    A.cw = (float *)take((size_t)NS * P * 4);
+    A.ent = (int2 *)take((size_t)NS * P * 8);
+    A.rcnt = (int *)take((size_t)(H + 1) * 4);
+    A.rstart = (int *)take((size_t)(H + 1) * 4);
+    A.rfill = (int *)take((size_t)(H + 1) * 4);
+    A.rowbuf = (float *)take((size_t)RAS_WARPS * RAS_FSEG * 4);
+    A.misc = (int *)take(64 * 4);
+    A.wmax = (float *)take(RAS_WARPS * 4);
+    return A;
+}
+
+// Row y, columns [x0, x0 + RAS_FSEG) into the warp's buffer; on return lane l
+// holds columns x0 + 4 l + (0..3) in v[0..3] and x0 + 128 + 4 l + (0..3) in v[4..7].
+// An entry carries amp * (row weight) and the spot's column X; its columns
+// are [max(0, X - R), min(W, X + R + 1)) with weights cw[spot][x - max(0, X - R)].
+__device__ inline void fast_row_segment(const RasterConst &c, const FastArena &A, int P, int y, int x0, int lane,
+                                        float *buf, float (&v)[8]) {
+    float4 *b4 = reinterpret_cast<float4 *>(buf);
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    b4[lane] = z;
+    b4[lane + 32] = z;
+    __syncwarp();
+    const int e0 = A.rstart[y], e1 = A.rstart[y + 1];
+    for (int e = e0; e < e1; ++e) {
+        const int2 en = A.ent[e];
+        const int X = en.y >> 16, k = en.y & 0xffff;
+        const int xl = max(0, X - c.R), xh = min(c.W, X + c.R + 1);
+        if (xh > x0 && xl < x0 + RAS_FSEG) {
+            const float a = __int_as_float(en.x);
+            for (int l = lane; l < P; l += 32) {
+                const int x = xl + l;
+                if (x < xh && x >= x0 && x < x0 + RAS_FSEG) buf[x - x0] = fmaf(a, A.cw[k * P + l], buf[x - x0]);
+            }
+        }
+        __syncwarp();
+    }
+    const float4 p = b4[lane], q = b4[lane + 32];
+    v[0] = p.x; v[1] = p.y; v[2] = p.z; v[3] = p.w;
+    v[4] = q.x; v[5] = q.y; v[6] = q.z; v[7] = q.w;
+    __syncwarp();
+}
+
+template <bool VEC>
+__global__ void __launch_bounds__(RAS_THREADS, 4)
+raster_fast_kernel(const RasterConst c, const int64_t *__restrict__ off, const float4 *__restrict__ xyzi,
+                   long long n_patterns, float *__restrict__ out, unsigned char *gscratch, size_t arena_bytes,
+                   int32_t *status) {
+    extern __shared__ __align__(16) unsigned char ras_smem[];
+    unsigned char *base = gscratch ? gscratch + (size_t)blockIdx.x * arena_bytes : ras_smem;
+    const int P = 2 * c.R + 1;
+    const FastArena A = carve_fast(base, c.NS, c.T, c.H, P);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int H = c.H, W = c.W;
+    const size_t img = (size_t)H * W;
+    float *buf = A.rowbuf + warp * RAS_FSEG;
+
+    for (long long p = blockIdx.x; p < n_patterns; p += gridDim.x) {
+        const long long a0 = off[p];
+        const long long n_ll = off[p + 1] - a0;
+        if (n_ll > c.NS || n_ll < 0) {
+            if (tid == 0) atomicOr(status, DS_ERR_CAPACITY);
+            continue;
+        }
+        const int n = (int)n_ll;
+        int Tp = 64;
+        while (Tp < 2 * n) Tp <<= 1;
+        const int tbits = __ffs(Tp) - 1;
+        for (int t = tid; t < Tp; t += RAS_THREADS) {
+            A.hkey[t] = -1;
+            A.hidx[t] = -1;
+        }
+        for (int y = tid; y <= H; y += RAS_THREADS) {
+            A.rcnt[y] = 0;
+            A.rfill[y] = 0;
+        }
+        if (tid == 0) A.misc[RAS_WARPS] = 0;
+        __syncthreads();
+
+        // ---- pixel coordinates, frame test, last write wins per pixel
+        int my_in = 0;
+        for (int i = tid; i < n; i += RAS_THREADS) {
+            const float4 e = xyzi[a0 + i];
+            double X, Y;
+            pixel_xy(c, e, X, Y);
+            int key = -1, sl = -1;
+            if (in_frame(c, X, Y)) {
+                ++my_in;
+                key = (int)Y * W + (int)X;
+                // open addressing; Tp >= 2 n slots, so a free slot is always found
+                unsigned h = ((unsigned)key * 2654435761u) >> (32 - tbits);
+                for (int t = 0; t < Tp; ++t) {
+                    const int prev = atomicCAS(&A.hkey[h], -1, key);
+                    if (prev == -1 || prev == key) {
+                        atomicMax(&A.hidx[h], i);
+                        sl = (int)h;
+                        break;
+                    }
+                    h = (h + 1) & (unsigned)(Tp - 1);
+                }
+                if (sl < 0) key = -1;
+            }
+            A.key[i] = key;
+            A.slot[i] = sl;
+        }
+        my_in = __reduce_add_sync(FULL_MASK, my_in);
+        if (lane == 0 && my_in) atomicAdd(&A.misc[RAS_WARPS], my_in);
+        __syncthreads();
+        const int n_in = A.misc[RAS_WARPS];
+
+        // ---- ordered compaction, column weights, row counts
+        int n_alive = 0;
+        for (int c0 = 0; c0 < n; c0 += RAS_THREADS) {
+            const int i = c0 + tid;
+            bool alive = false;
+            if (i < n && A.key[i] >= 0) alive = A.hidx[A.slot[i]] == i;
+            const unsigned bal = __ballot_sync(FULL_MASK, alive);
+            if (lane == 0) A.misc[warp] = __popc(bal);
+            __syncthreads();
+            int wbase = 0, tot = 0;
+            for (int w = 0; w < RAS_WARPS; ++w) {
+                const int v = A.misc[w];
+                if (w < warp) wbase += v;
+                tot += v;
+            }
+            if (alive) {
+                const int k = n_alive + wbase + __popc(bal & ((1u << lane) - 1));
+                const int key = A.key[i];
+                const int X = key % W, Y = key / W;
+                A.amp[k] = xyzi[a0 + i].w;
+                A.sx[k] = X;
+                A.sy[k] = Y;
+                const int xlo = max(0, X - c.R), xhi = min(W, X + c.R + 1);
+                for (int j = 0; j < xhi - xlo; ++j) A.cw[k * P + j] = reflect_weight(c, xlo + j, X, W);
+                const int ylo = max(0, Y - c.R), yhi = min(H, Y + c.R + 1);
+                for (int y = ylo; y < yhi; ++y) atomicAdd(&A.rcnt[y], 1);
+            }
+            n_alive += tot;
+            __syncthreads();
+        }
+
+        // ---- row starts: exclusive scan of the counts over H + 1 entries
+        {
+            const int per = (H + 1 + RAS_THREADS - 1) / RAS_THREADS;
+            const int y0 = tid * per, y1 = min(H + 1, y0 + per);
+            int sum = 0;
+            for (int y = y0; y < y1; ++y) sum += A.rcnt[y];
+            const int inc = warp_inclusive_scan(sum, lane);
+            if (lane == 31) A.misc[warp] = inc;
+            __syncthreads();
+            int run = inc - sum;
+            for (int w = 0; w < warp; ++w) run += A.misc[w];
+            for (int y = y0; y < y1; ++y) {
+                A.rstart[y] = run;
+                run += A.rcnt[y];
+            }
+            __syncthreads();
+        }
+        // ---- row entries (amp * row weight, X, spot), then each row's in spot order
+        for (int k = tid; k < n_alive; k += RAS_THREADS) {
+            const int X = A.sx[k], Y = A.sy[k];
+            const float am = A.amp[k];
+            const int ylo = max(0, Y - c.R), yhi = min(H, Y + c.R + 1);
+            for (int y = ylo; y < yhi; ++y)
+                A.ent[A.rstart[y] + atomicAdd(&A.rfill[y], 1)] =
+                    make_int2(__float_as_int(am * reflect_weight(c, y, Y, H)), (X << 16) | k);
+        }
+        __syncthreads();
+        for (int y = tid; y < H; y += RAS_THREADS) {
+            const int e0 = A.rstart[y], e1 = A.rstart[y + 1];
+            for (int e = e0 + 1; e < e1; ++e) {
+                const int2 v = A.ent[e];
+                const int kv = v.y & 0xffff;
+                int f = e - 1;
+                while (f >= e0 && (A.ent[f].y & 0xffff) > kv) {
+                    A.ent[f + 1] = A.ent[f];
+                    --f;
+                }
+                A.ent[f + 1] = v;
+            }
+        }
+        __syncthreads();
+
+        // ---- maximum over the image (normalise)
+        float mx = 1.f;
+        const bool norm = c.normalize && n_in > 0;
+        if (norm) {
+            float wm = -INFINITY;
+            bool any_empty = false;
+            for (int y = warp; y < H; y += RAS_WARPS) {
+                if (A.rstart[y + 1] == A.rstart[y]) {
+                    any_empty = true;
+                    continue;
+                }
+                for (int x0 = 0; x0 < W; x0 += RAS_FSEG) {
+                    float v[8];
+                    fast_row_segment(c, A, P, y, x0, lane, buf, v);
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) {
+                        const int x = x0 + (e < 4 ? 4 * lane + e : 128 + 4 * lane + e - 4);
+                        if (x < W) wm = fmaxf(wm, v[e]);
+                    }
+                }
+            }
+            if (any_empty) wm = fmaxf(wm, 0.f);
+#pragma unroll
+            for (int d = 16; d >= 1; d >>= 1) wm = fmaxf(wm, __shfl_xor_sync(FULL_MASK, wm, d));
+            if (lane == 0) A.wmax[warp] = wm;
+            __syncthreads();
+            mx = A.wmax[0];
+            for (int w = 1; w < RAS_WARPS; ++w) mx = fmaxf(mx, A.wmax[w]);
+        }
+
+        // ---- the image
+        float *dst = out + (size_t)p * img;
+        const float zero_val = norm ? 0.f / mx : 0.f;
+        // pattern / max: one reciprocal, then products (within 1 ulp of the quotients)
+        const float inv_mx = norm ? 1.f / mx : 1.f;
+        for (int y = warp; y < H; y += RAS_WARPS) {
+            float *row = dst + (size_t)y * W;
+            if (A.rstart[y + 1] == A.rstart[y]) {
+                if (VEC) {
+                    const float4 z = make_float4(zero_val, zero_val, zero_val, zero_val);
+                    for (int x = lane * 4; x < W; x += 128) st_cs(reinterpret_cast<float4 *>(row + x), z);
+                } else {
+                    for (int x = lane; x < W; x += 32) st_cs1(row + x, zero_val);
+                }
+                continue;
+            }
+            for (int x0 = 0; x0 < W; x0 += RAS_FSEG) {
+                float v[8];
+                fast_row_segment(c, A, P, y, x0, lane, buf, v);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int xb = x0 + 128 * h + 4 * lane;
+                    float s[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const float u = v[4 * h + e];
+                        s[e] = norm ? (u == 0.f ? zero_val : u * inv_mx) : u;
+                    }
+                    if (VEC) {
+                        if (xb < W) st_cs(reinterpret_cast<float4 *>(row + xb), make_float4(s[0], s[1], s[2], s[3]));
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < 4; ++e)
+                            if (xb + e < W) st_cs1(row + xb + e, s[e]);
+                    }
+                }
+            }
+        }
+        __syncthreads();  // the arena is reused by the next pattern
+    }
+}
+
 struct RasterPlan {
     int NS, T, grid;
     size_t arena, smem, scratch;
 };
 
+static int filter_radius(const ds_raster_params *p) {
+    return (p->fast && p->sigma > 1e-15) ? (int)(p->truncate * p->sigma + 0.5) : 0;
+}
+
+template <bool VEC>
+static const void *raster_kernel_ptr(bool fast) {
+    return fast ? (const void *)raster_fast_kernel<VEC> : (const void *)raster_kernel<VEC>;
+}
+
 static ds_status raster_plan(const ds_raster_params *p, int64_t max_spots, RasterPlan &P) {
     DS_REQUIRE(max_spots >= 0 && max_spots < (1ll << 28), "ds_rasterize: max_spots out of range");
+    DS_REQUIRE(!p->fast || max_spots <= 65504, "ds_rasterize: at most 65504 spots per pattern in fast mode");
     int NS = (int)std::max<int64_t>(32, (max_spots + 31) / 32 * 32);
     int T = 64;
     while (T < 2 * NS) T <<= 1;
     P.NS = NS;
     P.T = T;
-    P.arena = raster_arena_bytes(NS, T, p->height);
+    const bool fast = p->fast != 0;
+    P.arena = fast ? fast_arena_bytes(NS, T, p->height, 2 * filter_radius(p) + 1) : raster_arena_bytes(NS, T, p->height);
     int dev = 0, n_sm = 0;
     DS_CUDA_TRY(cudaGetDevice(&dev));
     DS_CUDA_TRY(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
@@ -426,11 +740,10 @@ static ds_status raster_plan(const ds_raster_params *p, int64_t max_spots, Raste
         P.smem = P.arena;
         P.scratch = 0;
         int per_sm = 0;
-        DS_CUDA_TRY(cudaFuncSetAttribute(raster_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)P.smem));
-        DS_CUDA_TRY(cudaFuncSetAttribute(raster_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)P.smem));
-        DS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, raster_kernel<true>, RAS_THREADS, P.smem));
+        for (const void *k : {raster_kernel_ptr<true>(fast), raster_kernel_ptr<false>(fast)})
+            DS_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem));
+        DS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, raster_kernel_ptr<true>(fast), RAS_THREADS,
+                                                                  P.smem));
         P.grid = n_sm * std::max(1, per_sm);
     } else {
         P.smem = 0;
@@ -531,11 +844,11 @@ extern "C" ds_status ds_rasterize(const ds_raster_params *p, const int64_t *offs
     cudaStream_t s = (cudaStream_t)stream;
     const int grid = (int)std::min<long long>(P.grid, n_patterns);
     unsigned char *g = P.scratch ? reinterpret_cast<unsigned char *>(scratch) : nullptr;
-    if (vec)
-        raster_kernel<true><<<grid, RAS_THREADS, P.smem, s>>>(c, offsets, reinterpret_cast<const float4 *>(xyzi),
-                                                             n_patterns, out, g, P.arena, status);
-    else
-        raster_kernel<false><<<grid, RAS_THREADS, P.smem, s>>>(c, offsets, reinterpret_cast<const float4 *>(xyzi),
-                                                              n_patterns, out, g, P.arena, status);
-    return check_launch("raster_kernel");
+    const float4 *x4 = reinterpret_cast<const float4 *>(xyzi);
+    size_t arena = P.arena;
+    long long np = n_patterns;
+    void *args[] = {&c, const_cast<int64_t **>(&offsets), const_cast<float4 **>(&x4), &np, &out, &g, &arena, &status};
+    const void *kern = vec ? raster_kernel_ptr<true>(c.fast != 0) : raster_kernel_ptr<false>(c.fast != 0);
+    DS_CUDA_TRY(cudaLaunchKernel(kern, dim3(grid), dim3(RAS_THREADS), args, P.smem, s));
+    return check_launch(c.fast ? "raster_fast_kernel" : "raster_kernel");
 }

@@ -32,6 +32,21 @@ inline double precession_breakpoint_step(int shape, double width, double minima)
     }
 }
 
+// FP32 precession average below this -> redone in FP64.  Measured against a
+// tight adaptive quadrature on random (s0, r phi) over the selection band,
+// FP32 max relative error per decade of the average: linear (a small
+// difference of O(1) terms near the band edge) 3e-5 at 1e-5..1e-4, 7e-6 at
+// 1e-3..1e-2, 2e-6 above; sin2c 8e-6 at 1e-3..1e-2, 5e-6 above; sinc 3e-6
+// above 1e-3; atanc and lorentzian ~1e-6 above 1e-4.
+inline float precession_fp64_threshold(int shape) {
+    switch (shape) {
+        case DS_SHAPE_LINEAR:
+        case DS_SHAPE_SIN2C: return 1e-2f;
+        case DS_SHAPE_SINC: return 1e-3f;
+        default: return 1e-4f;
+    }
+}
+
 // ----------------------------------------------------------- the models ----
 // FP32, one excitation error.
 template <class C>
@@ -128,11 +143,6 @@ __device__ inline T shape_deriv(const C &c, T s) {
     }
 }
 
-template <class C>
-__device__ inline float shape_val_t(const C &c, float s) { return shape_base_f32(c, s); }
-template <class C>
-__device__ inline double shape_val_t(const C &c, double s) { return shape_base_f64(c, s); }
-
 // ------------------------------------------- precession rotation average ----
 // shf(s0, r) = (1/2pi) int_0^2pi f(s0 + r phi cos t) dt
 //            = (1/pi)  int_0^pi  f(s0 + a cos t) dt,  a = r phi
@@ -146,7 +156,9 @@ __device__ inline double shape_val_t(const C &c, double s) { return shape_base_f
 // chosen spacings (checked against a tight adaptive quadrature).  linear
 // pieces outside |s| < w are zero and skipped.  With GRAD the same nodes also
 // give d shf / d s0 = (1/pi) int f'(.) dt and d shf / d a = (1/pi) int f'(.) cos t dt
-// (f is continuous at the cuts, so moving them adds nothing).
+// (f is continuous at the cuts, so moving them adds nothing).  The nodes of a
+// piece come in pairs mid +- d: cos(mid +- d) = cos mid cos d -+ sin mid sin d,
+// one sincos per pair.
 //
 // 8-point Gauss-Legendre rule on [-1, 1]: the positive roots of P_8 and
 // their weights.
@@ -162,24 +174,94 @@ __device__ __forceinline__ T gl8_w(int i) {
     return w[i];
 }
 
-// s0 = s0h + s0l (a pair in FP32, s0l = 0 in FP64).  Returns shf; with GRAD
-// also *ds0 and *da.  Inlined form (for kernels with few live registers at
-// the call) and an out-of-line form (precession_average) for the forward
-// kernel, whose variants without the average must not pay its registers.
-template <typename T, bool GRAD, class C>
-__device__ __forceinline__ T precession_average_inline(const C &c, T s0h, T s0l, T a, T *ds0, T *da) {
+__device__ __forceinline__ void sincos_t(float x, float *s, float *c) { sincosf(x, s, c); }
+__device__ __forceinline__ void sincos_t(double x, double *s, double *c) { sincos(x, s, c); }
+__device__ __forceinline__ void sincospi_t(float x, float *s, float *c) { sincospif(x, s, c); }
+__device__ __forceinline__ void sincospi_t(double x, double *s, double *c) { sincospi(x, s, c); }
+__device__ __forceinline__ float sinpi_t(float x) { return sinpif(x); }
+__device__ __forceinline__ double sinpi_t(double x) { return sinpi(x); }
+
+// The per-model constants in the quadrature's type, formed once per spot
+// (not per node): w, n / w, pi n / |w|, pi / w.
+template <typename T>
+struct ShapeK {
+    T w, mw, mfac, sigma;
+};
+template <class C>
+__device__ __forceinline__ ShapeK<float> shape_k(const C &c, float) {
+    return {c.width_f, c.mw_f, c.mfac_f, c.sigma_f};
+}
+template <class C>
+__device__ __forceinline__ ShapeK<double> shape_k(const C &c, double) {
+    return {c.width, c.minima / c.width, SHAPE_PI * c.minima / fabs(c.width), SHAPE_PI / c.width};
+}
+
+// Model SHAPE at s: value, and with GRAD the derivative d f / d s.
+template <int SHAPE, bool GRAD, typename T>
+__device__ __forceinline__ T shape_vd(const ShapeK<T> &K, T s, T &df) {
+    const T PI_T = (T)SHAPE_PI;
+    if (SHAPE == DS_SHAPE_LINEAR) {
+        const T w = K.w;
+        const T v = (w - fabs(s)) / w;
+        if (GRAD) df = (v > (T)0 && s != (T)0) ? (s > (T)0 ? -(T)1 / w : (T)1 / w) : (T)0;
+        return v > (T)0 ? v : (T)0;
+    } else if (SHAPE == DS_SHAPE_SINC || SHAPE == DS_SHAPE_SIN2C) {
+        const T x = s * K.mw;  // x = n s / w, u = pi x
+        if (x == (T)0) {
+            if (GRAD) df = (T)0;
+            return (T)0;
+        }
+        const T m = rint(x);
+        const T t = x - m;
+        const T u = PI_T * x;
+        if (!GRAD) {
+            const T g = sinpi_t(t) / u;  // +-sin(u) / u: the sign does not matter here
+            return (SHAPE == DS_SHAPE_SIN2C) ? g * g : fabs(g);
+        }
+        // sin(pi (t + m)) = (-1)^m sin(pi t), likewise cos
+        const T sg = ((long long)m & 1) ? (T)-1 : (T)1;
+        T sn, cs;
+        sincospi_t(t, &sn, &cs);
+        const T ru = (T)1 / u;
+        const T g = sg * sn * ru;                       // sin u / u
+        const T dg = (sg * cs - g) * ru * (PI_T * K.mw);  // d/ds (sin u / u)
+        df = (SHAPE == DS_SHAPE_SIN2C) ? (T)2 * g * dg : (g < (T)0 ? -dg : dg);
+        return (SHAPE == DS_SHAPE_SIN2C) ? g * g : fabs(g);
+    } else if (SHAPE == DS_SHAPE_ATANC) {
+        const T y = K.mfac * s;
+        if (y == (T)0) {
+            if (GRAD) df = (T)0;
+            return (T)1;
+        }
+        const T f = atan(y) / y;
+        if (GRAD) df = ((T)1 / ((T)1 + y * y) - f) / y * K.mfac;
+        return f;
+    } else if (SHAPE == DS_SHAPE_LORENTZIAN) {
+        const T x = K.sigma * s;
+        const T f = (T)1 / ((T)1 + x * x);
+        if (GRAD) df = -(T)2 * x * K.sigma * f * f;
+        return f;
+    } else {
+        if (GRAD) df = (T)0;
+        return (T)1;
+    }
+}
+
+template <typename T, bool GRAD, int SHAPE, class C>
+__device__ __forceinline__ T precession_average_impl(const C &c, T s0h, T s0l, T a, T *ds0, T *da) {
     const T PI_T = (T)SHAPE_PI;
     const T s0 = s0h + s0l;
-    if (GRAD) { *ds0 = (T)0; *da = (T)0; }
-    if (c.shape == DS_SHAPE_BINARY) return (T)1;
+    const ShapeK<T> K = shape_k(c, s0);
+    T dfd;
     if (!(a > (T)0)) {
-        if (GRAD) *ds0 = shape_deriv<T>(c, s0);
-        return shape_val_t(c, s0);
+        const T v = shape_vd<SHAPE, GRAD>(K, s0, dfd);
+        if (GRAD) { *ds0 = dfd; *da = (T)0; }
+        return v;
     }
     const T h = (T)c.int_step;
-    const T w = (T)c.width;
+    const T w = K.w;
     const T lo = s0 - a, hi = s0 + a;
-    const bool clip = c.shape == DS_SHAPE_LINEAR && w > (T)0;
+    const bool clip = SHAPE == DS_SHAPE_LINEAR && w > (T)0;
     T kf = (h > (T)0 && h < (T)INFINITY) ? ceil(lo / h) : (T)INFINITY;
     T th_prev = PI_T, s_prev = lo, sum = (T)0, g0 = (T)0, g1 = (T)0;
     for (;;) {
@@ -189,15 +271,19 @@ __device__ __forceinline__ T precession_average_inline(const C &c, T s0h, T s0l,
         const T th = last ? (T)0 : acos(fmin(fmax((sk - s0) / a, (T)-1), (T)1));
         if (th_prev > th && !(clip && (s_next <= -w || s_prev >= w))) {
             const T mid = (T)0.5 * (th + th_prev), half = (T)0.5 * (th_prev - th);
+            T sm, cm;
+            sincos_t(mid, &sm, &cm);
             T acc = (T)0, a0 = (T)0, a1 = (T)0;
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                const T d = half * gl8_x<T>(i);
-                const T c1 = cos(mid + d), c2 = cos(mid - d);
-                const T x1 = fma(a, c1, s0h) + s0l, x2 = fma(a, c2, s0h) + s0l;
-                acc = fma(gl8_w<T>(i), shape_val_t(c, x1) + shape_val_t(c, x2), acc);
+                T sd, cd;
+                sincos_t(half * gl8_x<T>(i), &sd, &cd);
+                const T c1 = cm * cd - sm * sd, c2 = cm * cd + sm * sd;  // cos(mid + d), cos(mid - d)
+                T d1, d2;
+                const T f1 = shape_vd<SHAPE, GRAD>(K, fma(a, c1, s0h) + s0l, d1);
+                const T f2 = shape_vd<SHAPE, GRAD>(K, fma(a, c2, s0h) + s0l, d2);
+                acc = fma(gl8_w<T>(i), f1 + f2, acc);
                 if (GRAD) {
-                    const T d1 = shape_deriv<T>(c, x1), d2 = shape_deriv<T>(c, x2);
                     a0 = fma(gl8_w<T>(i), d1 + d2, a0);
                     a1 = fma(gl8_w<T>(i), d1 * c1 + d2 * c2, a1);
                 }
@@ -218,6 +304,24 @@ __device__ __forceinline__ T precession_average_inline(const C &c, T s0h, T s0l,
         *da = g1 / PI_T;
     }
     return sum / PI_T;
+}
+
+// s0 = s0h + s0l (a pair in FP32, s0l = 0 in FP64).  Returns shf; with GRAD
+// also *ds0 and *da.  Inlined form (for kernels with few live registers at
+// the call) and an out-of-line form (precession_average) for the forward
+// kernel, whose variants without the average must not pay its registers.
+template <typename T, bool GRAD, class C>
+__device__ __forceinline__ T precession_average_inline(const C &c, T s0h, T s0l, T a, T *ds0, T *da) {
+    switch (c.shape) {
+        case DS_SHAPE_LINEAR: return precession_average_impl<T, GRAD, DS_SHAPE_LINEAR>(c, s0h, s0l, a, ds0, da);
+        case DS_SHAPE_SINC: return precession_average_impl<T, GRAD, DS_SHAPE_SINC>(c, s0h, s0l, a, ds0, da);
+        case DS_SHAPE_SIN2C: return precession_average_impl<T, GRAD, DS_SHAPE_SIN2C>(c, s0h, s0l, a, ds0, da);
+        case DS_SHAPE_ATANC: return precession_average_impl<T, GRAD, DS_SHAPE_ATANC>(c, s0h, s0l, a, ds0, da);
+        case DS_SHAPE_LORENTZIAN: return precession_average_impl<T, GRAD, DS_SHAPE_LORENTZIAN>(c, s0h, s0l, a, ds0, da);
+        default:
+            if (GRAD) { *ds0 = (T)0; *da = (T)0; }
+            return (T)1;
+    }
 }
 
 template <typename T, bool GRAD, class C>

@@ -298,6 +298,7 @@ extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t
     c.mw_f = (float)(c.minima / c.width);
     c.int_step = precession_breakpoint_step(p->shape_model, c.width, c.minima);
     c.int_step_f = (float)c.int_step;
+    c.int_tau = precession_fp64_threshold(p->shape_model);
     // FP32 screen guard: bound on |z32 - z| from rounding m to FP32 and the FMA
     // chain, 8 ulp of sum_i |row_i of recip| * max|hkl_i| (|R| = 1), plus the
     // rounding of z_mid and z_half.

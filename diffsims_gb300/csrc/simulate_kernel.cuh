@@ -40,7 +40,6 @@ constexpr float SIM_TAU = 1e-9f;       // | |s| - s_max | below this -> FP64 dec
 constexpr float SIM_TAU_SF = 1e-6f;    // |s| this close to a zero of the shape factor -> FP64 s
 constexpr float SIM_TAU_PREC = 2e-7f;  // precession band margin below this -> FP64 decision
 constexpr float SIM_U_MAX = 0.01f;     // (r / k0)^2 above this -> FP64 (series not used)
-constexpr float SIM_TAU_INT = 1e-2f;   // FP32 precession average below this -> FP64 quadrature
 constexpr int SIM_MAX_O = 32;
 // tuning knobs (compile time): word ranges per orientation in the refine and
 // write passes, and chunks screened per step in phase 1
@@ -65,6 +64,7 @@ struct SimConst {
     float inv_a2f, inv_b2f;
     double int_step;                // precession average: breakpoint spacing in s (0: none)
     float int_step_f, mw_f;
+    float int_tau;                  // precession average: FP32 result below this -> FP64
     long long n_hkl, n_orient, n_tiles, capacity;
 };
 
@@ -292,7 +292,7 @@ __device__ inline float shape_mixed(const SimConst &c, dd s, float r, dd r2) {
     }
     if (INTEG) {  // _shape_factor_precession, :222-268 (its own kernel instantiation)
         float v = precession_average<float, false>(c, s.hi, s.lo, r * c.phi_f, nullptr, nullptr);
-        if (v < SIM_TAU_INT) {
+        if (v < c.int_tau) {
             // small averages carry the FP32 rounding of s and a: redo in FP64
             const double r64 = sqrt(fmax((double)r2.hi + (double)r2.lo, 0.0));
             v = (float)precession_average<double, false>(c, (double)s.hi + (double)s.lo, 0.0, r64 * c.phi,

@@ -226,23 +226,36 @@ ds_status ds_rasterize(const ds_raster_params *p, const int64_t *offsets, const 
 /* ------------------------------------------------------------------------ */
 /* Adjoint of the spot intensities I = shf(s, r) |F_hkl|^2 (no counterpart in
  * the reference, which is not differentiable).  After a ds_simulate call with
- * the same p, t and quats: grad_intensity[j] = dL/dI for every output spot j.
- * Accumulates (+=) dL/d|F|^2 per table row into grad_F2 (n_hkl doubles) and
- * dL/dB* into grad_recip (9 doubles, B* = t->recip, rows a*, b*, c*); writes
- * dL/dR (n_orient x 9 doubles, R the active rotation matrix of the normalised
- * quaternion, row-major).  Selection is piecewise constant and not
- * differentiated. */
+ * the same p, t and quats, whose output had n_spots spots:
+ * grad_intensity[j] = dL/dI for every output spot j.  Accumulates (+=)
+ * dL/d|F|^2 per table row into grad_F2 (n_hkl doubles) and dL/dB* into
+ * grad_recip (9 doubles, B* = t->recip, rows a*, b*, c*); writes dL/dq
+ * (n_orient x 4 doubles, through the normalisation of q).  Selection is
+ * piecewise constant and not differentiated.  Scratch (the rotation average's
+ * per-spot partials) from ds_simulate_backward_scratch_bytes. */
+size_t ds_simulate_backward_scratch_bytes(const ds_sim_params *p, int64_t n_spots);
 ds_status ds_simulate_backward(const ds_sim_params *p, const ds_phase_table *t, const double *quats,
                                int64_t n_orient, const int64_t *offsets, const int32_t *hkl_index,
-                               const double *grad_intensity, double *grad_F2, double *grad_R,
-                               double *grad_recip, void *stream);
+                               int64_t n_spots, const double *grad_intensity, double *grad_F2,
+                               double *grad_quats, double *grad_recip, void *scratch, size_t scratch_bytes,
+                               int32_t *status, void *stream);
 
-size_t ds_structure_factors_backward_scratch_bytes(int64_t n);
+/* Orientation corrections (no counterpart in the reference): quats_out = q0 (x)
+ * exp(rotvec), the Hamilton product with the unit quaternion of each rotation
+ * vector (n x 3 doubles, angle = length in radians); and its adjoint,
+ * grad_rotvec = dL/drotvec from grad_quats = dL/dquats_out. */
+ds_status ds_axis_angle_compose(const double *q0, const double *rotvec, int64_t n, double *quats_out,
+                                void *stream);
+ds_status ds_axis_angle_compose_backward(const double *q0, const double *rotvec, int64_t n,
+                                         const double *grad_quats, double *grad_rotvec, void *stream);
+
+size_t ds_structure_factors_backward_scratch_bytes(int64_t n, int32_t n_species);
 
 /* Adjoint of ds_structure_factors: from dL/d|F|^2 per row, accumulates (+=)
  * dL/d(x, y, z, occupancy, B) per atom into grad_atoms (n_atoms x 5 doubles)
  * and dL/dB* through |g|^2 (scattering factors, Debye-Waller) into grad_recip.
- * recip: host array, the rows' reciprocal basis.  F is recomputed (FP64). */
+ * recip: host array, the rows' reciprocal basis.  F is recomputed (phase
+ * reduced in FP64, FP32 products, FP64 sums). */
 ds_status ds_structure_factors_backward(const ds_atoms *atoms, const int32_t *hkl, const double *g2, int64_t n,
                                         const double recip[9], const double *grad_F2, double *grad_atoms,
                                         double *grad_recip, void *scratch, size_t scratch_bytes, void *stream);

@@ -33,6 +33,35 @@ def quaternion_matrix(q):
         torch.stack([2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)], -1)], -2)
 
 
+def reciprocal_basis_torch(lattice):
+    """Rows a*, b*, c* of the lattice (a, b, c, alpha, beta, gamma; degrees),
+    x || a, z || c* frame, as plain torch operations (autograd)."""
+    a, b, c, al, be, ga = [lattice[i] for i in range(6)]
+    d = math.pi / 180.0
+    ca, cb, cg, sg = torch.cos(al * d), torch.cos(be * d), torch.cos(ga * d), torch.sin(ga * d)
+    cx = c * cb
+    cy = c * (ca - cb * cg) / sg
+    cz = torch.sqrt(c * c - cx * cx - cy * cy)
+    zero = torch.zeros_like(a)
+    base = torch.stack([torch.stack([a, zero, zero]), torch.stack([b * cg, b * sg, zero]), torch.stack([cx, cy, cz])])
+    return torch.inverse(base.cpu()).to(base.device).transpose(0, 1)
+
+
+def compose_axis_angle_torch(q0, v):
+    """q0 (x) exp(v) (Hamilton product with the unit quaternion of rotation
+    vector v) as plain torch operations (autograd)."""
+    th = torch.linalg.vector_norm(v, dim=-1, keepdim=True)
+    half = 0.5 * th
+    small = th < 1e-6
+    safe = torch.where(small, torch.ones_like(th), th)
+    k = torch.where(small, 0.5 - th * th / 48.0, torch.sin(half) / safe)
+    e = torch.cat([torch.cos(half), k * v], dim=-1)
+    pw, px, py, pz = q0.unbind(-1)
+    qw, qx, qy, qz = e.unbind(-1)
+    return torch.stack([pw * qw - px * qx - py * qy - pz * qz, pw * qx + px * qw + py * qz - pz * qy,
+                        pw * qy - px * qz + py * qw + pz * qx, pw * qz + px * qy - py * qx + pz * qw], dim=-1)
+
+
 def _model(name, s, w, n):
     pi = math.pi
     if name == "linear":
@@ -87,6 +116,7 @@ def spot_intensities(xyz, B, occ, recip, quats, elements, scattering_params, spo
     w = p.max_excitation_error if p.shape_factor_width is None else p.shape_factor_width
     n = p.shape_kwargs.get("minima_number", 5)
     hkl = spot_hkl.to(torch.float64)
+    recip = recip.to(dev)
     g = hkl @ recip                                   # g = B*^T h
     R = quaternion_matrix(quats)[spot_orient]          # (m, 3, 3)
     u = torch.einsum("mkc,mk->mc", R, g)              # R^T g

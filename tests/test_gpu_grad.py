@@ -66,8 +66,8 @@ CASES = [
 @pytest.mark.parametrize("kw", CASES, ids=lambda k: "-".join(f"{v}" for v in k.values()))
 def test_gradient_matches_reference_and_finite_differences(kw):
     import torch
-    from diffsims_gb300.autograd import (SpotIntensities, SpotModel, axis_angle_quaternion, quaternion_multiply,
-                                         reciprocal_basis, simulate_intensities, spot_loss)
+    from diffsims_gb300.autograd import (SpotIntensities, SpotModel, compose_axis_angle, reciprocal_basis,
+                                         simulate_intensities, spot_loss)
     dev = torch.device("cuda", 0)
     els, base, tgt = make_case()
     p = ok.SimParams(accelerating_voltage=300, reciprocal_radius=1.0, max_excitation_error=0.015, **kw)
@@ -78,13 +78,14 @@ def test_gradient_matches_reference_and_finite_differences(kw):
                                       reciprocal_basis(T(tgt["lattice"])), T(tgt["q"]))
 
     def params():
+        # a non-zero starting rotation vector exercises the general axis-angle Jacobian
+        rv0 = np.random.default_rng(11).normal(0, 1e-3, (len(base["q"]), 3))
         return [T(base["xyz"]).requires_grad_(), T(base["B"]).requires_grad_(), T(base["occ"]).requires_grad_(),
-                T(base["lattice"]).requires_grad_(), torch.zeros((len(base["q"]), 3), dtype=torch.float64,
-                                                                   device=dev).requires_grad_()]
+                torch.as_tensor(base["lattice"], dtype=torch.float64).requires_grad_(), T(rv0).requires_grad_()]
 
     q0 = T(base["q"])
     xyz, B, occ, lat, rv = params()
-    sim = simulate_intensities(model, xyz, B, occ, reciprocal_basis(lat), quaternion_multiply(q0, axis_angle_quaternion(rv)))
+    sim = simulate_intensities(model, xyz, B, occ, reciprocal_basis(lat), compose_axis_angle(q0, rv))
     L = spot_loss(sim, target)
     L.backward()
     g_gpu = [t.grad.detach().cpu().numpy() for t in (xyz, B, occ, lat, rv)]
@@ -95,7 +96,7 @@ def test_gradient_matches_reference_and_finite_differences(kw):
     hkl = sim.hkl
 
     def ref_loss(xyz, B, occ, lat, rv):
-        I = ar.spot_intensities(xyz, B, occ, reciprocal_basis(lat), quaternion_multiply(q0, axis_angle_quaternion(rv)),
+        I = ar.spot_intensities(xyz, B, occ, ar.reciprocal_basis_torch(lat), ar.compose_axis_angle_torch(q0, rv),
                                 els, "lobato", orient, hkl, p)
         return spot_loss(SpotIntensities(I, sim.offsets, hkl), target)
 
