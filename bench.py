@@ -18,6 +18,8 @@ Arms:
                     API with host quaternions in and all spots copied back.
                     Extra legs in the same line: "grad" (gradient step of the
                     differentiation workload against its forward pass),
+                    "batched_phases" (32 uneven phases in one launch, graph
+                    replay, tile by the autotuner),
                     "template_library" (three phases simulated and rasterised
                     to 256x256 detectors in 8192-orientation chunks).
   --impl reference  the reference's CPU path restated in numpy (the FP64
@@ -61,6 +63,11 @@ GRAD_WORKLOAD = dict(workload="orthorhombic 7.1/9.3/12.4, 64 atoms, 4096 orienta
                      seed=4, n_atoms=64, n_orientations=4096, cone_deg=5.0, accelerating_voltage=300,
                      reciprocal_radius=1.5, max_excitation_error=0.015, shape_factor_model="sinc",
                      precession_angle=1.0, approximate_precession=False)
+BATCH_WORKLOAD = dict(workload="32 phases, cell edges 3-20 A, angles 80-100 deg, 1-500 atoms, 1k-50k orientations each, "
+                               "200 kV, r=1.5, sinc, s_max=0.015; one persistent launch in a CUDA graph, tile by the "
+                               "autotuner",
+                      n_phases=32, seed=3, accelerating_voltage=200, reciprocal_radius=1.5, max_excitation_error=0.015,
+                      shape_factor_model="sinc")
 LIBRARY_WORKLOAD = dict(workload="template library: Al FCC, Fe BCC, P1 60 atoms; 200k orientations per phase, 200 kV, "
                                  "r=1.2, linear with 0.5 deg precession (rotation average), 256x256 float32 detector, "
                                  "sigma 1 px, 8192-orientation chunks",
@@ -327,6 +334,7 @@ def run_gpu(args):
     err = compare_forms(mixed, ref64, table, q_host[:n_cmp], settings)
 
     grad = None if args.skip_grad else run_grad(args, torch, dev)
+    batched = None if args.skip_batch else run_batch(args, torch, dev)
     library = None if args.skip_library else run_library(args, torch, dev, hbm_peak)
 
     cpu = None
@@ -356,6 +364,7 @@ def run_gpu(args):
                       "mixed_over_fp64": (n_o / (ms * 1e-3)) / fp64_rate},
         "error_vs_fp64_form": err,
         "grad": grad,
+        "batched_phases": batched,
         "template_library": library,
         "cpu_baseline": cpu,
         "clocks": clocks,
@@ -436,6 +445,69 @@ def run_grad(args, torch, dev):
     return {"ms_per_step": grad_ms, "forward_ms": fwd_ms, "grad_over_forward": grad_ms / fwd_ms,
             "unit": "ms", "loss": float(L), "spots": int(sim.intensity.shape[0]), "gradient_norms": gnorm,
             "config": {k: v for k, v in W.items()}, "dtype": "f32 forward with f64 phase; f64 adjoint"}
+
+
+def run_batch(args, torch, dev):
+    """Batched uneven phases: every phase's orientations in one persistent
+    launch (CUDA graph replay), against the same phases launched one by one."""
+    import diffsims_gb300 as ds
+    from diffsims_gb300.engine import AUTOTUNER, Autotuner, PhaseBatch, PhaseTable, SpotBuffers, simulate_phase
+    W = BATCH_WORKLOAD
+    rng = np.random.default_rng(W["seed"])
+    zs = ["C", "N", "O", "Al", "Si", "Ti", "Fe", "Cu"]
+    gen = ds.SimulationGenerator(W["accelerating_voltage"], "lobato", shape_factor_model=W["shape_factor_model"])
+    settings = gen.settings(W["max_excitation_error"])
+    r = W["reciprocal_radius"]
+    tables, qs = [], []
+    t_tab = time.perf_counter()
+    for k in range(W["n_phases"]):
+        lat = tuple(rng.uniform(3, 20, 3)) + tuple(rng.uniform(80, 100, 3))
+        n_a = int(rng.integers(1, 501))
+        els = list(rng.choice(zs, n_a))
+        ph = ds.Phase(f"p{k}", ds.Structure([ds.Atom(e, x) for e, x in zip(els, rng.random((n_a, 3)))],
+                                            ds.Lattice(*lat)))
+        tables.append(PhaseTable(ph, r, True, "lobato", list(rng.uniform(0.3, 1.5, n_a)), device=dev))
+        qs.append(torch.from_numpy(uniform_quaternions(int(rng.integers(1000, 50001)), 1000 + k)).to(dev))
+    torch.cuda.synchronize()
+    table_s = time.perf_counter() - t_tab
+    n_pat = sum(int(q.shape[0]) for q in qs)
+    batch = PhaseBatch(tables, qs, settings, r)  # tile from the autotuner
+    key = Autotuner.key(batch)
+    batch.run()
+    batch.capture()
+    st = torch.cuda.current_stream()
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            fn()
+            e1.record(st)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return statistics.mean(ms)
+
+    graph_ms = timed(batch.replay)
+    if int(batch.status.abs().sum()) != 0:
+        raise RuntimeError("batched launch reported a device status")
+    spots = batch.spots()
+    n_spots = sum(s.total for s in spots)
+    bufs = [SpotBuffers(dev) for _ in tables]
+    for t, q, b in zip(tables, qs, bufs):
+        simulate_phase(t, q, settings, r, b)  # size the buffers
+    seq_ms = timed(lambda: [simulate_phase(t, q, settings, r, b, sync=False) for t, q, b in zip(tables, qs, bufs)])
+    return {"metric": "orientation patterns/s (32 uneven phases, one launch)", "value": n_pat / (graph_ms * 1e-3),
+            "unit": "patterns/s", "ms_per_step": graph_ms, "patterns_per_step": n_pat, "spots_per_step": int(n_spots),
+            "per_phase_launches_ms": seq_ms, "speedup_over_per_phase_launches": seq_ms / graph_ms,
+            "orient_tile": batch.orient_tile, "autotuner_ms_by_tile": AUTOTUNER.timings.get(key),
+            "n_hkl_range": [min(t.n for t in tables), max(t.n for t in tables)],
+            "orientations_range": [min(int(q.shape[0]) for q in qs), max(int(q.shape[0]) for q in qs)],
+            "table_build_s": table_s, "launches_per_step": len(tables) + 2,
+            "config": {k: v for k, v in W.items()}}
 
 
 def run_library(args, torch, dev, hbm_peak):
@@ -578,6 +650,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=16384)
     ap.add_argument("--skip-grad", action="store_true", help="leave out the gradient-step leg")
     ap.add_argument("--skip-library", action="store_true", help="leave out the template-library leg")
+    ap.add_argument("--skip-batch", action="store_true", help="leave out the batched-phases leg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--out-dir", default=None)
     ap.add_argument("--screen", default="auto", choices=["auto", "rows", "lines"],

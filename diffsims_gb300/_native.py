@@ -37,7 +37,8 @@ DS_PRECESSION_INTEGRAL = 2
 EXPORTED_SYMBOLS = (
     "ds_box_extent", "ds_enumerate_scratch_bytes", "ds_enumerate_hkl",
     "ds_structure_factor_scratch_bytes", "ds_structure_factors", "ds_kinematical_intensities",
-    "ds_simulate_scratch_bytes", "ds_simulate", "ds_rasterize_scratch_bytes", "ds_rasterize",
+    "ds_simulate_scratch_bytes", "ds_simulate", "ds_simulate_batch_scratch_bytes", "ds_simulate_batch_tile",
+    "ds_simulate_batch", "ds_rasterize_scratch_bytes", "ds_rasterize",
     "ds_simulate_backward_scratch_bytes", "ds_simulate_backward", "ds_structure_factors_backward_scratch_bytes",
     "ds_axis_angle_compose", "ds_axis_angle_compose_backward", "ds_structure_factors_backward",
     "ds_probe_fp32_fma", "ds_last_error", "ds_version",
@@ -64,6 +65,10 @@ class ds_sim_params(C.Structure):
 class ds_phase_table(C.Structure):
     _fields_ = [("n_hkl", C.c_int64), ("hkl", C.c_void_p), ("g2", C.c_void_p), ("F2", C.c_void_p),
                 ("F2d", C.c_void_p), ("recip", C.c_double * 9), ("hmax", C.c_int32 * 3), ("_pad", C.c_int32)]
+
+
+class ds_batch_phase(C.Structure):
+    _fields_ = [("table", ds_phase_table), ("quats", C.c_void_p), ("n_orient", C.c_int64)]
 
 
 class ds_spots(C.Structure):
@@ -112,6 +117,12 @@ def load_library(require_cuda: bool = True):
             lib.ds_simulate_scratch_bytes.restype = sz
             lib.ds_simulate.argtypes = [C.POINTER(ds_sim_params), C.POINTER(ds_phase_table), vp, i64,
                                         C.POINTER(ds_spots), vp, sz, vp, vp]
+            lib.ds_simulate_batch_scratch_bytes.argtypes = [C.POINTER(ds_sim_params), C.POINTER(ds_batch_phase), i32]
+            lib.ds_simulate_batch_scratch_bytes.restype = sz
+            lib.ds_simulate_batch_tile.argtypes = [C.POINTER(ds_sim_params), C.POINTER(ds_batch_phase), i32]
+            lib.ds_simulate_batch_tile.restype = i32
+            lib.ds_simulate_batch.argtypes = [C.POINTER(ds_sim_params), C.POINTER(ds_batch_phase), i32,
+                                              C.POINTER(ds_spots), vp, sz, vp, vp]
             lib.ds_rasterize_scratch_bytes.argtypes = [C.POINTER(ds_raster_params), i64]
             lib.ds_rasterize_scratch_bytes.restype = sz
             lib.ds_rasterize.argtypes = [C.POINTER(ds_raster_params), vp, vp, i64, i64, vp, vp, sz, vp, vp]
@@ -129,7 +140,8 @@ def load_library(require_cuda: bool = True):
             lib.ds_last_error.restype = C.c_char_p
             lib.ds_version.restype = C.c_char_p
             for name in ("ds_box_extent", "ds_enumerate_hkl", "ds_structure_factors", "ds_kinematical_intensities",
-                         "ds_simulate", "ds_rasterize", "ds_simulate_backward", "ds_structure_factors_backward",
+                         "ds_simulate", "ds_simulate_batch", "ds_rasterize", "ds_simulate_backward",
+                         "ds_structure_factors_backward",
                          "ds_axis_angle_compose", "ds_axis_angle_compose_backward",
                          "ds_probe_fp32_fma"):
                 getattr(lib, name).restype = C.c_int32
@@ -151,7 +163,11 @@ def check(status: int, what: str):
 
 def check_device_status(status_tensor: torch.Tensor, what: str, allow=0) -> int:
     """Read the device status word (synchronises) and raise on unexpected bits."""
-    v = int(status_tensor.item())
+    return check_status_value(int(status_tensor.item()), what, allow)
+
+
+def check_status_value(v: int, what: str, allow=0) -> int:
+    """Raise on the unexpected bits of a status word already read."""
     bad = v & ~allow
     if bad & DS_ERR_TIMEOUT:
         raise NativeError(f"{what}: a bounded device wait timed out (status {v})")

@@ -210,6 +210,13 @@ static ds_status make_plan(const ds_sim_params *p, const ds_phase_table *t, long
     return DS_OK;
 }
 
+ds_status launch_sim_prep(const SimConst &c, const int32_t *hkl, const double *g2, float4 *scr, float *zh, float2 *g2dd,
+                          long long n_hkl, cudaStream_t s) {
+    if (n_hkl <= 0) return DS_OK;
+    sim_prep_kernel<<<(unsigned)((n_hkl + 255) / 256), 256, 0, s>>>(c, hkl, g2, scr, zh, g2dd);
+    return check_launch("sim_prep_kernel");
+}
+
 static ds_status launch_sim(const void *kern, SimConst c, TableP T, const double *quats, ds_spots *out,
                             LookbackScratch lb, StageP stg, const SimPlan &P, int32_t *status, cudaStream_t s) {
     int64_t *offsets = out->offsets, *total = out->total;
@@ -239,20 +246,10 @@ extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t
     DS_REQUIRE(p && t && out && status, "ds_simulate: null pointer");
     DS_REQUIRE(n_orient >= 0, "ds_simulate: n_orient < 0");
     DS_REQUIRE(t->n_hkl >= 0 && t->n_hkl < (1ll << 31), "ds_simulate: n_hkl out of range");
-    DS_REQUIRE(p->k0 > 0 && isfinite(p->k0), "ds_simulate: k0 must be finite and > 0");
-    DS_REQUIRE(p->max_excitation_error > 0 && isfinite(p->max_excitation_error),
-               "ds_simulate: max_excitation_error must be > 0");
-    DS_REQUIRE(p->shape_width != 0 && isfinite(p->shape_width), "ds_simulate: shape width must be finite, non-zero");
-    DS_REQUIRE(p->shape_model >= DS_SHAPE_LINEAR && p->shape_model <= DS_SHAPE_BINARY, "ds_simulate: bad shape model");
-    DS_REQUIRE(p->precession_mode >= DS_PRECESSION_NONE && p->precession_mode <= DS_PRECESSION_INTEGRAL,
-               "ds_simulate: bad precession mode");
-    DS_REQUIRE(p->form == DS_FORM_MIXED || p->form == DS_FORM_FP64, "ds_simulate: bad form");
-    DS_REQUIRE(p->orient_tile == 0 || p->orient_tile == 1 || p->orient_tile == 2 || p->orient_tile == 4 ||
-                   p->orient_tile == 8 || p->orient_tile == 16 || p->orient_tile == 32,
-               "ds_simulate: orient_tile must be 0, 1, 2, 4, 8, 16 or 32");
-    DS_REQUIRE(p->stage_cap >= 0, "ds_simulate: stage_cap < 0");
-    DS_REQUIRE(p->precession_mode == DS_PRECESSION_NONE || p->precession_angle > 0,
-               "ds_simulate: precession mode needs a positive angle");
+    {
+        ds_status vs = validate_params(p, "ds_simulate");
+        if (vs) return vs;
+    }
     cudaStream_t s = (cudaStream_t)stream;
     if (n_orient == 0) {
         DS_CUDA_TRY(cudaMemsetAsync(out->offsets, 0, sizeof(int64_t), s));
@@ -271,64 +268,12 @@ extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t
     DS_REQUIRE(scratch && scratch_bytes >= P.total, "ds_simulate: scratch too small");
 
     SimConst c;
-    c.k0 = p->k0;
-    c.eps = p->max_excitation_error;
-    c.width = p->shape_width;
-    c.phi = p->precession_angle;
-    c.thr = p->minimum_intensity;
-    c.minima = p->minima_number;
-    c.Pz = p->k0 * cos(p->precession_angle);
-    c.Pt = p->k0 * sin(p->precession_angle);
-    for (int i = 0; i < 9; ++i) c.recip[i] = t->recip[i];
-    split_double(c.eps, c.eps_dd.hi, c.eps_dd.lo);
-    split_double(1.0 / (2.0 * c.k0), c.c2k0_dd.hi, c.c2k0_dd.lo);
-    split_double(c.width, c.width_dd.hi, c.width_dd.lo);
-    split_double(c.minima / c.width, c.mw_dd.hi, c.mw_dd.lo);
-    const double PI = 3.14159265358979323846;
-    c.k0f = (float)c.k0;
-    c.inv_k0sq = (float)(1.0 / (c.k0 * c.k0));
-    c.eps_f = (float)c.eps;
-    c.width_f = (float)c.width;
-    c.sigma_f = (float)(PI / c.width);
-    c.mfac_f = (float)(PI * c.minima / fabs(c.width));
-    c.phi_f = (float)c.phi;
-    c.Pz_f = (float)c.Pz;
-    c.Pt_f = (float)c.Pt;
-    c.k0sq_f = (float)(c.k0 * c.k0);
-    c.mw_f = (float)(c.minima / c.width);
-    c.int_step = precession_breakpoint_step(p->shape_model, c.width, c.minima);
-    c.int_step_f = (float)c.int_step;
-    c.int_tau = precession_fp64_threshold(p->shape_model);
-    // FP32 screen guard: bound on |z32 - z| from rounding m to FP32 and the FMA
-    // chain, 8 ulp of sum_i |row_i of recip| * max|hkl_i| (|R| = 1), plus the
-    // rounding of z_mid and z_half.
-    double zmax = 0;
-    for (int i = 0; i < 3; ++i)
-        zmax += sqrt(t->recip[3 * i] * t->recip[3 * i] + t->recip[3 * i + 1] * t->recip[3 * i + 1] +
-                     t->recip[3 * i + 2] * t->recip[3 * i + 2]) * (double)t->hmax[i];
-    c.guard = (float)(8.0 * 5.96e-8 * zmax + 4.0 * 5.96e-8 * (c.eps + zmax * zmax / (2 * c.k0)) + 1e-7);
-    c.shape = p->shape_model;
-    c.prec = p->precession_mode;
-    c.form = p->form;
+    fill_const(p, t, c);
     c.O = P.O;
     c.W = P.W;
     c.Ws = P.Ws;
-    for (int i = 0; i < 3; ++i) c.hmax[i] = t->hmax[i] > 0 ? t->hmax[i] : 1;
-    c.n_hkl = t->n_hkl;
     c.n_orient = n_orient;
     c.line_mode = P.line_mode;
-    {
-        const double e = c.eps, k0 = c.k0;
-        c.alpha1 = 1.0 / (2.0 * (k0 - e));
-        c.alpha0 = (e * e - 2.0 * e * k0) * c.alpha1;
-        c.beta1 = 1.0 / (2.0 * (k0 + e));
-        c.beta0 = (e * e + 2.0 * e * k0) * c.beta1;
-        c.csq = t->recip[6] * t->recip[6] + t->recip[7] * t->recip[7] + t->recip[8] * t->recip[8];
-        c.a2f = (float)(-c.alpha1 * c.csq);
-        c.b2f = (float)(-c.beta1 * c.csq);
-        c.inv_a2f = 1.f / c.a2f;
-        c.inv_b2f = 1.f / c.b2f;
-    }
     c.n_tiles = P.n_tiles;
     c.capacity = out->capacity;
 

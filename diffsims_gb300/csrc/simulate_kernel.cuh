@@ -29,6 +29,8 @@
 #pragma once
 #include <math.h>
 
+#include <string>
+
 #include "common.cuh"
 #include "shape.cuh"
 
@@ -588,12 +590,35 @@ struct StageP {
 };
 constexpr unsigned long long NO_STAGE = ~0ull;
 
-template <int O, int FORM, bool INTEG>
-__global__ void __launch_bounds__(SIM_THREADS, 2)
-simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t *__restrict__ offsets,
-                int32_t *__restrict__ out_idx, float4 *__restrict__ out_xyzi, double *__restrict__ out_s,
-                int64_t *__restrict__ out_total, LookbackScratch lb, StageP stg, int32_t *status) {
+// One phase of a batched launch: its candidate table, orientations and the
+// per-phase geometry; tiles [tile0, tile0 + n_tiles) of the launch are its,
+// its patterns are rows [orient0, orient0 + n_orient) of the output CSR.
+struct PhaseP {
+    TableP T;
+    const double *quats;
+    double recip[9];
+    int hmax[3];
+    int W, Ws;
+    int O;  // orientations per tile of this phase (<= the kernel's O)
+    long long n_hkl, n_orient, tile0, n_tiles, orient0;
+};
+constexpr int SIM_BATCH_MAX = 96;  // phases per launch (the descriptors travel as a kernel parameter)
+struct PhaseBatch {
+    int n;
+    PhaseP ph[SIM_BATCH_MAX];
+};
+
+// The orientation kernel's body.  MULTI: many phases in one persistent
+// launch, each tile of one phase; the phase's constants come from the batch
+// descriptors (copied to shared memory per tile), the rest from c.
+template <int O, int FORM, bool INTEG, bool MULTI>
+__device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T1, const double *__restrict__ quats1,
+                                              int64_t *__restrict__ offsets, int32_t *__restrict__ out_idx,
+                                              float4 *__restrict__ out_xyzi, double *__restrict__ out_s,
+                                              int64_t *__restrict__ out_total, LookbackScratch lb, StageP stg,
+                                              int32_t *status, const PhaseP *batch, int n_batch) {
     extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ PhaseP s_ph[MULTI ? 2 : 1];
     const SimSmem Ls = sim_smem_layout(O, c.Ws);
     OrientP *sop_buf = reinterpret_cast<OrientP *>(smem + Ls.orient);                  // [2][O]
     unsigned long long *acc_buf = reinterpret_cast<unsigned long long *>(smem + Ls.acc);  // [2][ACC_STRIDE]
@@ -611,10 +636,19 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
     constexpr int NP = O >= 2 ? DS_SIM_PARTS : 8;
     const bool all_zero_drop = c.thr >= 0.0;
     const unsigned lanemask_lt = (1u << lane) - 1u;
-    auto part_range = [&](int p, int &w0, int &w1) {
-        w0 = (int)(((long long)c.W * p) / NP);
-        w1 = (int)(((long long)c.W * (p + 1)) / NP);
+    auto part_range = [&](int Wp, int p, int &w0, int &w1) {
+        w0 = (int)(((long long)Wp * p) / NP);
+        w1 = (int)(((long long)Wp * (p + 1)) / NP);
     };
+    // the phase constants of pipeline buffer b (one phase without MULTI)
+    auto PW = [&](int b) -> int { return MULTI ? s_ph[b].W : c.W; };
+    auto PWs = [&](int b) -> int { return MULTI ? s_ph[b].Ws : c.Ws; };
+    auto PNH = [&](int b) -> long long { return MULTI ? s_ph[b].n_hkl : c.n_hkl; };
+    auto PNO = [&](int b) -> long long { return MULTI ? s_ph[b].n_orient : c.n_orient; };
+    auto PT0 = [&](int b) -> long long { return MULTI ? s_ph[b].tile0 : 0ll; };
+    auto PO0 = [&](int b) -> long long { return MULTI ? s_ph[b].orient0 : 0ll; };
+    auto PTab = [&](int b) -> const TableP & { return MULTI ? s_ph[b].T : T1; };
+    auto POp = [&](int b) -> int { return MULTI ? s_ph[b].O : O; };
     auto next_unit = [&](int k) -> int {
         int u = 0;
         if (lane == 0) u = atomicAdd(&s_unit[k], 1);
@@ -630,7 +664,20 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
     int cur = 0;
     long long pend_tile = -1;
     for (;;) {
-        if (tid == 0) s_tile = (long long)atomicAdd(lb.ticket, 1ull);
+        if (tid == 0) {
+            const long long tk = (long long)atomicAdd(lb.ticket, 1ull);
+            s_tile = tk;
+            if (MULTI && tk < c.n_tiles) {
+                // the phase holding this tile (tile0 ascends with the phase index)
+                int lo = 0, hi = n_batch - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (batch[mid].tile0 <= tk) lo = mid;
+                    else hi = mid - 1;
+                }
+                s_ph[cur] = batch[lo];
+            }
+        }
         if (tid < 4) s_unit[tid] = 0;
         OrientP *sop = sop_buf + cur * O;
         unsigned long long *acc = acc_buf + cur * ACC_STRIDE;
@@ -642,8 +689,12 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
         __syncthreads();
         const long long tile = s_tile;
         const bool have_new = tile < c.n_tiles;
-        const long long o_base = tile * O;
-        const int n_valid = have_new ? (int)min((long long)O, c.n_orient - o_base) : 0;
+        const TableP &T = PTab(cur);
+        const int W = PW(cur), Ws = PWs(cur);
+        const long long n_hkl = PNH(cur);
+        const int OP = POp(cur);  // this phase's tile (O without MULTI)
+        const long long o_base = (tile - PT0(cur)) * OP;  // within the phase
+        const int n_valid = have_new ? (int)min((long long)OP, PNO(cur) - o_base) : 0;
         const int n_units = n_valid * NP;
         if (have_new) {
             // ---------------- per-orientation rotation: beam frame = g @ R, R the active matrix of q
@@ -651,7 +702,7 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
                 OrientP &op = sop[tid];
                 double R[3][3];
                 if (tid < n_valid) {
-                    const double *q = quats + 4 * (o_base + tid);
+                    const double *q = (MULTI ? s_ph[cur].quats : quats1) + 4 * (o_base + tid);
                     double w = q[0], x = q[1], y = q[2], z = q[3];
                     double nrm = sqrt(w * w + x * x + y * y + z * z);
                     if (!(nrm > 0) || !isfinite(nrm)) {
@@ -667,13 +718,14 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
                 }
                 for (int cc = 0; cc < 3; ++cc)
                     for (int i = 0; i < 3; ++i) {
-                        double v = c.recip[3 * i] * R[0][cc] + c.recip[3 * i + 1] * R[1][cc] + c.recip[3 * i + 2] * R[2][cc];
+                        auto rc = [&](int k) -> double { return MULTI ? s_ph[cur].recip[k] : c.recip[k]; };
+                        double v = rc(3 * i) * R[0][cc] + rc(3 * i + 1) * R[1][cc] + rc(3 * i + 2) * R[2][cc];
                         op.M[cc][i] = v;
                         op.m[cc][i] = (float)v;
                     }
                 // exact-product split of the z column: grid 2^q with 2^(q+24) >= 2 sum_i |M_zi| hmax_i
                 double Z = 0.0;
-                for (int i = 0; i < 3; ++i) Z += fabs(op.M[2][i]) * (double)c.hmax[i];
+                for (int i = 0; i < 3; ++i) Z += fabs(op.M[2][i]) * (double)(MULTI ? s_ph[cur].hmax[i] : c.hmax[i]);
                 const int q = (Z > 0.0 ? ilogb(Z) : -100) + 2 - 24;
                 for (int i = 0; i < 3; ++i) {
                     const double a = ldexp(rint(ldexp(op.M[2][i], -q)), q);
@@ -687,13 +739,13 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
             if (FORM == DS_FORM_MIXED && c.line_mode) {
                 // per-(orientation, line) candidate intervals, OR-ed into a zeroed bitmap
                 uint4 *bm4 = reinterpret_cast<uint4 *>(bitmap);
-                for (int i = tid; i < (O * c.Ws + 3) / 4; i += SIM_THREADS) bm4[i] = make_uint4(0u, 0u, 0u, 0u);
+                for (int i = tid; i < (O * Ws + 3) / 4; i += SIM_THREADS) bm4[i] = make_uint4(0u, 0u, 0u, 0u);
                 __syncthreads();
-                const int n_lines = (int)min((long long)T.line_meta[0], c.n_hkl);  // bounded even if the line pass failed
+                const int n_lines = (int)min((long long)T.line_meta[0], n_hkl);  // bounded even if the line pass failed
                 // trailing 000 rows: meta[1] holds the first one, or a large
                 // sentinel when there are none
-                const long long zero_start = min((long long)T.line_meta[1], c.n_hkl);
-                const int n_zero = (int)(c.n_hkl - zero_start);  // 0, 1 or 2
+                const long long zero_start = min((long long)T.line_meta[1], n_hkl);
+                const int n_zero = (int)(n_hkl - zero_start);  // 0, 1 or 2
                 float mx[O], my[O], mz[O];
 #pragma unroll
                 for (int o = 0; o < O; ++o) { mx[o] = sop[o].m[2][0]; my[o] = sop[o].m[2][1]; mz[o] = sop[o].m[2][2]; }
@@ -701,29 +753,29 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
                     const LineP L = T.lines[li];
 #pragma unroll
                     for (int o = 0; o < O; ++o)
-                        if (o < n_valid) line_candidates(c, L, mx[o], my[o], mz[o], bitmap + o * c.Ws);
+                        if (o < n_valid) line_candidates(c, L, mx[o], my[o], mz[o], bitmap + o * Ws);
                 }
                 // the trailing 000 rows (direct beam) are always candidates
                 for (int i = tid; i < n_valid * n_zero; i += SIM_THREADS) {
                     const int o = i / n_zero;
                     const long long j = zero_start + i % n_zero;
-                    atomicOr(&bitmap[o * c.Ws + (int)(j >> 5)], 1u << (int)(j & 31));
+                    atomicOr(&bitmap[o * Ws + (int)(j >> 5)], 1u << (int)(j & 31));
                 }
             } else if (FORM == DS_FORM_FP64) {
-                for (int wc = warp; wc < c.W; wc += SIM_WARPS) {
+                for (int wc = warp; wc < W; wc += SIM_WARPS) {
                     const long long j = (long long)wc * 32 + lane;
                     float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (j < c.n_hkl) e = T.scr[j];
+                    if (j < n_hkl) e = T.scr[j];
                     uint32_t myword = 0;
                     const double hd = e.x, kd = e.y, ld = e.z;
 #pragma unroll 1
-                    for (int o = 0; o < O; ++o) {
+                    for (int o = 0; o < OP; ++o) {
                         double sx, rx, zx;
-                        const bool hit = (j < c.n_hkl) && (o < n_valid) && select_fp64(c, sop[o], hd, kd, ld, sx, rx, zx);
+                        const bool hit = (j < n_hkl) && (o < n_valid) && select_fp64(c, sop[o], hd, kd, ld, sx, rx, zx);
                         const uint32_t b = __ballot_sync(FULL_MASK, hit);
                         if (lane == o) myword = b;
                     }
-                    if (lane < O) bitmap[lane * c.Ws + wc] = myword;
+                    if (lane < OP) bitmap[lane * Ws + wc] = myword;
                 }
             } else {
                 float m0[O], m1[O], m2[O];
@@ -742,9 +794,9 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
                     const long long jk = ((long long)warp + k * SIM_WARPS) * 32 + lane;
                     en[k] = make_float4(0.f, 0.f, 0.f, 0.f);
                     zn[k] = -1.f;
-                    if (jk < c.n_hkl) { en[k] = T.scr[jk]; zn[k] = T.zh[jk]; }
+                    if (jk < n_hkl) { en[k] = T.scr[jk]; zn[k] = T.zh[jk]; }
                 }
-                for (int wc = warp; wc < c.W; wc += CH * SIM_WARPS) {
+                for (int wc = warp; wc < W; wc += CH * SIM_WARPS) {
                     float4 e[CH];
                     float zh[CH];
 #pragma unroll
@@ -754,17 +806,19 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
                         const long long jn = ((long long)wc + (CH + k) * SIM_WARPS) * 32 + lane;
                         en[k] = make_float4(0.f, 0.f, 0.f, 0.f);
                         zn[k] = -1.f;
-                        if (jn < c.n_hkl) { en[k] = T.scr[jn]; zn[k] = T.zh[jn]; }
+                        if (jn < n_hkl) { en[k] = T.scr[jn]; zn[k] = T.zh[jn]; }
                     }
                     uint32_t bits[CH];
 #pragma unroll
                     for (int k = 0; k < CH; ++k) bits[k] = 0;
 #pragma unroll
                     for (int o = 0; o < O; ++o) {
+                        if (o < OP) {  // uniform; OP = O without MULTI
 #pragma unroll
-                        for (int k = 0; k < CH; ++k) {
-                            const float z = fmaf(m0[o], e[k].x, fmaf(m1[o], e[k].y, fmaf(m2[o], e[k].z, e[k].w)));
-                            bits[k] = __funnelshift_l(__float_as_uint(fabsf(z) - zh[k]), bits[k], 1);
+                            for (int k = 0; k < CH; ++k) {
+                                const float z = fmaf(m0[o], e[k].x, fmaf(m1[o], e[k].y, fmaf(m2[o], e[k].z, e[k].w)));
+                                bits[k] = __funnelshift_l(__float_as_uint(fabsf(z) - zh[k]), bits[k], 1);
+                            }
                         }
                     }
 #pragma unroll
@@ -772,7 +826,7 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
 #pragma unroll
                     for (int k = 0; k < CH; ++k) {
                         const int wck = wc + k * SIM_WARPS;
-                        if (lane < O && wck < c.W) bitmap[(O - 1 - lane) * c.Ws + wck] = bits[k];
+                        if (lane < OP && wck < W) bitmap[(OP - 1 - lane) * Ws + wck] = bits[k];
                     }
                 }
             }
@@ -782,8 +836,8 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
             for (int u = warp; u < n_units; u += SIM_WARPS) {
                 const int o = u / NP, p = u % NP;
                 int w0, w1;
-                part_range(p, w0, w1);
-                const uint32_t *row = bitmap + o * c.Ws;
+                part_range(W, p, w0, w1);
+                const uint32_t *row = bitmap + o * Ws;
                 int cnt = 0;
                 for (int wi = w0 + lane; wi < w1; wi += 32) cnt += __popc(row[wi]);
 #pragma unroll
@@ -810,8 +864,8 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
             for (int u = next_unit(0); u < n_units; u = next_unit(0)) {
                 const int o = u / NP, p = u % NP;
                 int w0, w1;
-                part_range(p, w0, w1);
-                uint32_t *row = bitmap + o * c.Ws;
+                part_range(W, p, w0, w1);
+                uint32_t *row = bitmap + o * Ws;
                 const OrientP &op = sop[o];
                 const unsigned long long base = acc[o * ACC_WORDS + ACC_CBASE0 + p];
                 float lmax = 0.f, lminpos = INFINITY;
@@ -883,8 +937,8 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
                     const float mnp = __uint_as_float((unsigned)acc[o * ACC_WORDS + ACC_MINPOS]);
                     if (!((double)mnp <= (double)mx * c.thr)) continue;
                     int w0, w1;
-                    part_range(p, w0, w1);
-                    uint32_t *row = bitmap + o * c.Ws;
+                    part_range(W, p, w0, w1);
+                    uint32_t *row = bitmap + o * Ws;
                     const OrientP &op = sop[o];
                     const unsigned long long base = acc[o * ACC_WORDS + ACC_CBASE0 + p];
                     const int cc = (int)acc[o * ACC_WORDS + ACC_CCNT0 + p];
@@ -943,8 +997,12 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
             const unsigned long long *bacc = acc_buf + bbuf * ACC_STRIDE;
             const int32_t *b_idx = stg.idx + (2 * (long long)blockIdx.x + bbuf) * stg.cap;
             const float *b_I = stg.inten + (2 * (long long)blockIdx.x + bbuf) * stg.cap;
-            const long long bo_base = btile * O;
-            const int bn_valid = (int)min((long long)O, c.n_orient - bo_base);
+            const TableP &T = PTab(bbuf);
+            const int W = PW(bbuf), Ws = PWs(bbuf);
+            const int BOP = POp(bbuf);
+            const long long bo_base = (btile - PT0(bbuf)) * BOP;
+            const long long bo_out = PO0(bbuf) + bo_base;  // first output row of the tile
+            const int bn_valid = (int)min((long long)BOP, PNO(bbuf) - bo_base);
             if (tid == 0) {
                 const long long run = (long long)bacc[ACC_TILE_TOTAL];
                 const long long prefix = lookback_resolve(lb, btile, run, status);
@@ -958,12 +1016,12 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
             const long long prefix = s_prefix;
             if (prefix < 0) return false;  // bounded wait gave up: DS_ERR_TIMEOUT is set
             for (int o = tid; o < bn_valid; o += SIM_THREADS)
-                offsets[bo_base + o] = prefix + (long long)bacc[o * ACC_WORDS + ACC_OFF];
+                offsets[bo_out + o] = prefix + (long long)bacc[o * ACC_WORDS + ACC_OFF];
             for (int u = next_unit(counter); u < bn_valid * NP; u = next_unit(counter)) {
                 const int o = u / NP, p = u % NP;
                 int w0, w1;
-                part_range(p, w0, w1);
-                const uint32_t *row = bitmap + o * c.Ws;
+                part_range(W, p, w0, w1);
+                const uint32_t *row = bitmap + o * Ws;
                 const OrientP &op = bsop[o];
                 long long pos0 = prefix + (long long)bacc[o * ACC_WORDS + ACC_OFF];
                 for (int pp = 0; pp < p; ++pp) pos0 += (long long)bacc[o * ACC_WORDS + ACC_PART0 + pp];
@@ -1062,10 +1120,125 @@ simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t 
     }
 }
 
+template <int O, int FORM, bool INTEG>
+__global__ void __launch_bounds__(SIM_THREADS, 2)
+simulate_kernel(SimConst c, TableP T, const double *__restrict__ quats, int64_t *__restrict__ offsets,
+                int32_t *__restrict__ out_idx, float4 *__restrict__ out_xyzi, double *__restrict__ out_s,
+                int64_t *__restrict__ out_total, LookbackScratch lb, StageP stg, int32_t *status) {
+    simulate_body<O, FORM, INTEG, false>(c, T, quats, offsets, out_idx, out_xyzi, out_s, out_total, lb, stg, status,
+                                         nullptr, 0);
+}
+
+// Many phases in one persistent launch: the tile ticket runs over the phases'
+// tiles in order and the look-back orders the output across phases.
+template <int O, int FORM, bool INTEG>
+__global__ void __launch_bounds__(SIM_THREADS, 2)
+simulate_batch_kernel(SimConst c, const __grid_constant__ PhaseBatch B, int64_t *__restrict__ offsets,
+                      int32_t *__restrict__ out_idx, float4 *__restrict__ out_xyzi, double *__restrict__ out_s,
+                      int64_t *__restrict__ out_total, LookbackScratch lb, StageP stg, int32_t *status) {
+    simulate_body<O, FORM, INTEG, true>(c, B.ph[0].T, nullptr, offsets, out_idx, out_xyzi, out_s, out_total, lb, stg,
+                                        status, B.ph, B.n);
+}
+
+// ----------------------------------------------------------- host helpers ----
+// Argument checks shared by the single-phase and batched entries.
+inline ds_status validate_params(const ds_sim_params *p, const char *who) {
+    const std::string w(who);
+    DS_REQUIRE(p->k0 > 0 && isfinite(p->k0), w + ": k0 must be finite and > 0");
+    DS_REQUIRE(p->max_excitation_error > 0 && isfinite(p->max_excitation_error),
+               w + ": max_excitation_error must be > 0");
+    DS_REQUIRE(p->shape_width != 0 && isfinite(p->shape_width), w + ": shape width must be finite, non-zero");
+    DS_REQUIRE(p->shape_model >= DS_SHAPE_LINEAR && p->shape_model <= DS_SHAPE_BINARY, w + ": bad shape model");
+    DS_REQUIRE(p->precession_mode >= DS_PRECESSION_NONE && p->precession_mode <= DS_PRECESSION_INTEGRAL,
+               w + ": bad precession mode");
+    DS_REQUIRE(p->form == DS_FORM_MIXED || p->form == DS_FORM_FP64, w + ": bad form");
+    DS_REQUIRE(p->orient_tile == 0 || p->orient_tile == 1 || p->orient_tile == 2 || p->orient_tile == 4 ||
+                   p->orient_tile == 8 || p->orient_tile == 16 || p->orient_tile == 32,
+               w + ": orient_tile must be 0, 1, 2, 4, 8, 16 or 32");
+    DS_REQUIRE(p->stage_cap >= 0, w + ": stage_cap < 0");
+    DS_REQUIRE(p->precession_mode == DS_PRECESSION_NONE || p->precession_angle > 0,
+               w + ": precession mode needs a positive angle");
+
+    return DS_OK;
+}
+
+// The kernel constants of one phase; the per-launch fields (O, W, Ws,
+// n_orient, n_tiles, capacity, line_mode) are set by the caller.
+inline void fill_const(const ds_sim_params *p, const ds_phase_table *t, SimConst &c) {
+    c.k0 = p->k0;
+    c.eps = p->max_excitation_error;
+    c.width = p->shape_width;
+    c.phi = p->precession_angle;
+    c.thr = p->minimum_intensity;
+    c.minima = p->minima_number;
+    c.Pz = p->k0 * cos(p->precession_angle);
+    c.Pt = p->k0 * sin(p->precession_angle);
+    for (int i = 0; i < 9; ++i) c.recip[i] = t->recip[i];
+    split_double(c.eps, c.eps_dd.hi, c.eps_dd.lo);
+    split_double(1.0 / (2.0 * c.k0), c.c2k0_dd.hi, c.c2k0_dd.lo);
+    split_double(c.width, c.width_dd.hi, c.width_dd.lo);
+    split_double(c.minima / c.width, c.mw_dd.hi, c.mw_dd.lo);
+    const double PI = 3.14159265358979323846;
+    c.k0f = (float)c.k0;
+    c.inv_k0sq = (float)(1.0 / (c.k0 * c.k0));
+    c.eps_f = (float)c.eps;
+    c.width_f = (float)c.width;
+    c.sigma_f = (float)(PI / c.width);
+    c.mfac_f = (float)(PI * c.minima / fabs(c.width));
+    c.phi_f = (float)c.phi;
+    c.Pz_f = (float)c.Pz;
+    c.Pt_f = (float)c.Pt;
+    c.k0sq_f = (float)(c.k0 * c.k0);
+    c.mw_f = (float)(c.minima / c.width);
+    c.int_step = precession_breakpoint_step(p->shape_model, c.width, c.minima);
+    c.int_step_f = (float)c.int_step;
+    c.int_tau = precession_fp64_threshold(p->shape_model);
+    // FP32 screen guard: bound on |z32 - z| from rounding m to FP32 and the FMA
+    // chain, 8 ulp of sum_i |row_i of recip| * max|hkl_i| (|R| = 1), plus the
+    // rounding of z_mid and z_half.
+    double zmax = 0;
+    for (int i = 0; i < 3; ++i)
+        zmax += sqrt(t->recip[3 * i] * t->recip[3 * i] + t->recip[3 * i + 1] * t->recip[3 * i + 1] +
+                     t->recip[3 * i + 2] * t->recip[3 * i + 2]) * (double)t->hmax[i];
+    c.guard = (float)(8.0 * 5.96e-8 * zmax + 4.0 * 5.96e-8 * (c.eps + zmax * zmax / (2 * c.k0)) + 1e-7);
+    c.shape = p->shape_model;
+    c.prec = p->precession_mode;
+    c.form = p->form;
+    for (int i = 0; i < 3; ++i) c.hmax[i] = t->hmax[i] > 0 ? t->hmax[i] : 1;
+    c.n_hkl = t->n_hkl;
+    {
+        const double e = c.eps, k0 = c.k0;
+        c.alpha1 = 1.0 / (2.0 * (k0 - e));
+        c.alpha0 = (e * e - 2.0 * e * k0) * c.alpha1;
+        c.beta1 = 1.0 / (2.0 * (k0 + e));
+        c.beta0 = (e * e + 2.0 * e * k0) * c.beta1;
+        c.csq = t->recip[6] * t->recip[6] + t->recip[7] * t->recip[7] + t->recip[8] * t->recip[8];
+        c.a2f = (float)(-c.alpha1 * c.csq);
+        c.b2f = (float)(-c.beta1 * c.csq);
+        c.inv_a2f = 1.f / c.a2f;
+        c.inv_b2f = 1.f / c.b2f;
+    }
+    c.O = 0;
+    c.W = (int)((t->n_hkl + 31) / 32);
+    c.Ws = c.W | 1;
+    c.n_orient = 0;
+    c.line_mode = 0;
+    c.n_tiles = 0;
+    c.capacity = 0;
+}
+
+// sim_prep_kernel launcher (simulate.cu): the screen arrays of one table.
+ds_status launch_sim_prep(const SimConst &c, const int32_t *hkl, const double *g2, float4 *scr, float *zh, float2 *g2dd,
+                          long long n_hkl, cudaStream_t s);
+
 // ------------------------------------------------------------- host side ----
 
 // Kernel entry of (O, FORM) with the precession rotation average compiled in
 // (simulate_integral.cu); the other instantiations live in simulate.cu.
 const void *simulate_kernel_integral(int O, int form);
+// Batched entries (simulate_batch.cu, simulate_batch_integral.cu); O in {1, 2,
+// 4, 8, 16} (mixed) or {1, 2, 4, 8} (FP64).
+const void *simulate_batch_kernel_plain(int O, int form);
+const void *simulate_batch_kernel_integral(int O, int form);
 
 }  // namespace ds

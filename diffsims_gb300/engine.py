@@ -387,3 +387,198 @@ def rasterize(spots: PhaseSpots, settings: RasterSettings, start=0, stop=None, o
     if sync:
         N.check_device_status(buffers.status, "rasterize")
     return out
+
+
+# ---------------------------------------------------------------- batches ----
+BATCH_MAX = 96  # phases per launch (include/diffsims_gb300.h)
+
+
+class PhaseBatch:
+    """Many phases simulated in one persistent launch per group of up to 96
+    phases (``ds_simulate_batch``): one CSR output over all phases'
+    orientations.  ``run`` launches; ``capture`` records the launch sequence
+    in a CUDA graph that ``replay`` re-issues (inputs and outputs stay at
+    the same addresses); ``spots`` gives one ``PhaseSpots`` per phase.
+
+    The orientation tile is chosen by ``Autotuner`` unless ``orient_tile``
+    is given."""
+
+    def __init__(self, tables, quats, settings: SimSettings, radius: float, orient_tile=None, autotuner=None,
+                 device=None):
+        if len(tables) != len(quats) or not tables:
+            raise ValueError("one quaternion set per phase table is needed")
+        self.device = tables[0].device if device is None else torch.device(device)
+        self.tables = list(tables)
+        self.quats = [q.to(self.device, torch.float64).contiguous() for q in quats]
+        self.settings = settings
+        self.radius = float(radius)
+        self.n_orient = [int(q.shape[0]) for q in self.quats]
+        self.groups = [list(range(i, min(i + BATCH_MAX, len(tables)))) for i in range(0, len(tables), BATCH_MAX)]
+        self._items = [self._items_of(g) for g in self.groups]
+        self.status = torch.zeros(len(self.groups), dtype=torch.int32, device=self.device)
+        self.totals = torch.zeros(len(self.groups), dtype=torch.int64, device=self.device)
+        self.offsets = [torch.zeros(sum(self.n_orient[i] for i in g) + 1, dtype=torch.int64, device=self.device)
+                        for g in self.groups]
+        self.graph = None
+        if orient_tile is None:
+            orient_tile = (autotuner or AUTOTUNER).tile_for(self)
+        self.orient_tile = int(orient_tile)
+        self._plan()
+
+    def _items_of(self, group):
+        arr = (N.ds_batch_phase * len(group))()
+        for k, i in enumerate(group):
+            arr[k].table = self.tables[i].cstruct()
+            arr[k].quats = self.quats[i].data_ptr() if self.n_orient[i] else None
+            arr[k].n_orient = self.n_orient[i]
+        return arr
+
+    def cparams(self, orient_tile=None):
+        p = self.settings.cstruct()
+        p.orient_tile = int(self.orient_tile if orient_tile is None else orient_tile)
+        return p
+
+    def _plan(self, capacity=None):
+        lib = N.load_library()
+        p = self.cparams()
+        self.scratch_bytes = [lib.ds_simulate_batch_scratch_bytes(p, it, len(it)) for it in self._items]
+        if any(b == 0 for b, g in zip(self.scratch_bytes, self.groups) if sum(self.n_orient[i] for i in g)):
+            N.check(N.DS_ERR_INVALID_ARGUMENT, "simulate_batch")
+        self.scratch = [torch.empty(max(int(b), 16), dtype=torch.uint8, device=self.device) for b in self.scratch_bytes]
+        if capacity is None:
+            capacity = [max(1024, sum(self.n_orient[i] * estimate_spots(self.tables[i], self.settings, self.radius)
+                                      for i in g) * 5 // 4) for g in self.groups]
+        self.capacity = [int(c) for c in capacity]
+        self.idx = [torch.empty(c, dtype=torch.int32, device=self.device) for c in self.capacity]
+        self.xyzi = [torch.empty((c, 4), dtype=torch.float32, device=self.device) for c in self.capacity]
+        self.graph = None
+
+    def _launch(self, stream=None, orient_tile=None):
+        lib = N.load_library()
+        st = N.stream_handle(stream)
+        p = self.cparams(orient_tile)
+        self.status.zero_()
+        for gi, it in enumerate(self._items):
+            out = N.ds_spots(self.offsets[gi].data_ptr(), self.idx[gi].data_ptr(), self.xyzi[gi].data_ptr(),
+                             self.capacity[gi], self.totals[gi:gi + 1].data_ptr(), None)
+            N.check(lib.ds_simulate_batch(p, it, len(it), out, N.ptr(self.scratch[gi]), self.scratch[gi].numel(),
+                                          N.ptr(self.status[gi:gi + 1]), st), "simulate_batch")
+
+    def run(self, stream=None, sync=True):
+        """Launch (or replay the captured graph); with ``sync`` check the status
+        words and, on output overflow, grow the outputs and run again."""
+        for attempt in range(2):
+            if self.graph is not None:
+                self.graph.replay()
+            else:
+                self._launch(stream)
+            if not sync:
+                return self
+            st = [int(v) for v in self.status.cpu().numpy()]
+            for t in self.tables:
+                N.check_device_status(t._status, "structure_factors")
+            for v in st:
+                N.check_status_value(v, "simulate_batch", allow=N.DS_ERR_CAPACITY)
+            if not any(v & N.DS_ERR_CAPACITY for v in st):
+                return self
+            totals = self.totals.cpu().numpy()
+            self._plan([int(t) + 1024 for t in totals])  # drops the graph: outputs moved
+        raise N.NativeError("simulate_batch: output capacity still exceeded after resizing")
+
+    def capture(self, warmup=True):
+        """Record the launch sequence in a CUDA graph (after a checked run that
+        sizes the outputs)."""
+        if warmup:
+            self.run()
+        s = torch.cuda.Stream(device=self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s, capture_error_mode="relaxed"):
+                self._launch(stream=s)
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        self.graph = g
+        return self
+
+    def replay(self):
+        self.graph.replay()
+        return self
+
+    def spots(self):
+        """One ``PhaseSpots`` per phase (views into the batch outputs)."""
+        out = []
+        for gi, g in enumerate(self.groups):
+            off = self.offsets[gi]
+            bounds = np.cumsum([0] + [self.n_orient[i] for i in g])
+            starts = off[torch.as_tensor(bounds, device=self.device)].cpu().numpy()
+            for k, i in enumerate(g):
+                a, b = int(starts[k]), int(starts[k + 1])
+                o = off[bounds[k]:bounds[k + 1] + 1] - a
+                out.append(PhaseSpots(self.tables[i], o, self.idx[gi][a:b], self.xyzi[gi][a:b], b - a))
+        return out
+
+
+class Autotuner:
+    """Picks the orientation tile of a batched launch by timing the feasible
+    candidates on the batch itself (CUDA events, best of a few launches) and
+    remembers the choice per problem class (phases, orientations and table
+    sizes in powers of two, shape model, precession, form)."""
+
+    CANDIDATES = (4, 8, 16, 32)
+
+    def __init__(self, repeats=3):
+        self.repeats = repeats
+        self.cache = {}
+        self.timings = {}
+
+    @staticmethod
+    def key(batch: "PhaseBatch"):
+        lg = lambda v: int(np.ceil(np.log2(max(int(v), 1))))
+        s = batch.settings
+        return (len(batch.tables), lg(sum(batch.n_orient)), lg(max(t.n for t in batch.tables)),
+                s.shape_model, int(s.precession_mode), s.form)
+
+    def tile_for(self, batch: "PhaseBatch") -> int:
+        k = self.key(batch)
+        if k in self.cache:
+            return self.cache[k]
+        lib = N.load_library()
+        fp64 = batch.settings.form == "fp64"
+        integ = batch.settings.precession_mode == N.DS_PRECESSION_INTEGRAL
+        cands = [c for c in self.CANDIDATES if c <= (8 if fp64 else 16 if integ else 32)]
+        best, best_ms, times = None, None, {}
+        for c in cands:
+            batch.orient_tile = c
+            p = batch.cparams(c)
+            if any(lib.ds_simulate_batch_scratch_bytes(p, it, len(it)) == 0 for it in batch._items):
+                continue  # infeasible (tile does not fit shared memory)
+            try:
+                batch._plan()
+                batch.run()  # sizes the outputs, checks the status
+            except (ValueError, N.NativeError):
+                continue
+            ms = []
+            for _ in range(self.repeats):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                batch._launch()
+                e1.record()
+                e1.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            times[c] = min(ms)
+            if best_ms is None or times[c] < best_ms:
+                best, best_ms = c, times[c]
+        if best is None:
+            best = 4
+        self.cache[k] = best
+        self.timings[k] = times
+        return best
+
+
+AUTOTUNER = Autotuner()
+
+
+def simulate_batch(tables, quats, settings: SimSettings, radius: float, orient_tile=None):
+    """Spots of many phases (one quaternion set each) from batched launches;
+    returns one ``PhaseSpots`` per phase."""
+    return PhaseBatch(tables, quats, settings, radius, orient_tile=orient_tile).run().spots()

@@ -10,7 +10,7 @@ import torch
 
 from . import _native as N
 from .crystal import Phase, Rotation, quaternions_of
-from .engine import PhaseTable, SimSettings, SpotBuffers, simulate_phase
+from .engine import PhaseBatch, PhaseTable, SimSettings, SpotBuffers, simulate_phase
 from .simulation2d import Simulation2D
 from .sim_utils import get_electron_wavelength
 
@@ -128,14 +128,20 @@ class SimulationGenerator:
         N.load_library()
         dev = torch.device("cuda", torch.cuda.current_device())
         settings = self.settings(max_excitation_error, shape_factor_width, form, orient_tile)
-        rots, spots = [], []
+        rots, tables, qs = [], [], []
         for p, r in zip(phases, rotations):
             rot = r if isinstance(r, Rotation) else Rotation(quaternions_of(r))
-            table = PhaseTable(p, reciprocal_radius, with_direct_beam, self.scattering_params,
-                               debye_waller_factors, form=form, device=dev)
-            q = torch.from_numpy(quaternions_of(rot)).to(dev)
-            spots.append(simulate_phase(table, q, settings, reciprocal_radius, buffers=SpotBuffers(dev)))
+            tables.append(PhaseTable(p, reciprocal_radius, with_direct_beam, self.scattering_params,
+                                     debye_waller_factors, form=form, device=dev))
+            qs.append(torch.from_numpy(quaternions_of(rot)).to(dev))
             rots.append(rot)
+        if len(tables) == 1:
+            spots = [simulate_phase(tables[0], qs[0], settings, reciprocal_radius, buffers=SpotBuffers(dev))]
+        else:
+            # all phases in one persistent launch (per group of up to 96); tile
+            # 0 = the library's choice
+            tile = min(int(orient_tile), 16 if form == "mixed" else 8) if orient_tile else 0
+            spots = PhaseBatch(tables, qs, settings, reciprocal_radius, orient_tile=tile).run().spots()
         if single_phase:
             return Simulation2D(phases[0], spots, rots[0], self, reciprocal_radius)
         return Simulation2D(phases, spots, rots, self, reciprocal_radius)

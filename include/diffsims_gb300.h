@@ -174,6 +174,33 @@ ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t, const dou
                       int64_t n_orient, ds_spots *out, void *scratch, size_t scratch_bytes,
                       int32_t *status, void *stream);
 
+/* One phase of a batched call: its candidate table and its orientations. */
+typedef struct {
+    ds_phase_table table;
+    const double *quats;         /* n_orient x 4 (device)                           */
+    int64_t n_orient;
+} ds_batch_phase;
+
+size_t ds_simulate_batch_scratch_bytes(const ds_sim_params *p, const ds_batch_phase *phases,
+                                       int32_t n_phases);
+/* Orientations per tile the batched launch would use (0 on bad arguments). */
+int32_t ds_simulate_batch_tile(const ds_sim_params *p, const ds_batch_phase *phases, int32_t n_phases);
+
+/* No counterpart in the reference (calculate_diffraction2d loops over phases,
+ * diffsims/generators/simulation_generator.py:198-241): ds_simulate for up to 96
+ * phases in ONE persistent launch (plus one small prep launch per phase).
+ * Tiles of up to p->orient_tile orientations (0: library choice; at most 32,
+ * 16 with the precession average, 8 for the FP64 form; phases whose tables
+ * would overflow shared memory use smaller tiles) run phase after phase from
+ * one tile ticket.  The output is
+ * one CSR over all phases' orientations in phase order (offsets:
+ * sum n_orient + 1); hkl_index holds rows of each spot's own phase table.
+ * Capacity rules as ds_simulate.  Graph-capturable: the phase descriptors are
+ * a kernel parameter. */
+ds_status ds_simulate_batch(const ds_sim_params *p, const ds_batch_phase *phases, int32_t n_phases,
+                            ds_spots *out, void *scratch, size_t scratch_bytes, int32_t *status,
+                            void *stream);
+
 /* No counterpart in the reference.  ds_simulate for callers that cannot
  * allocate device memory at all (e.g. a real-time loop that must not enter the
  * CUDA allocator, or a host whose memory manager owns all device memory):
