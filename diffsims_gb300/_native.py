@@ -40,7 +40,7 @@ EXPORTED_SYMBOLS = (
     "ds_simulate_scratch_bytes", "ds_simulate", "ds_simulate_batch_scratch_bytes", "ds_simulate_batch_tile",
     "ds_simulate_batch", "ds_rasterize_scratch_bytes", "ds_rasterize",
     "ds_simulate_backward_scratch_bytes", "ds_simulate_backward", "ds_structure_factors_backward_scratch_bytes",
-    "ds_axis_angle_compose", "ds_axis_angle_compose_backward", "ds_structure_factors_backward",
+    "ds_axis_angle_compose", "ds_axis_angle_compose_backward", "ds_polar_flatten", "ds_structure_factors_backward",
     "ds_probe_fp32_fma", "ds_last_error", "ds_version",
 )
 
@@ -135,6 +135,7 @@ def load_library(require_cuda: bool = True):
             lib.ds_structure_factors_backward.argtypes = [C.POINTER(ds_atoms), vp, vp, i64, C.POINTER(C.c_double), vp,
                                                           vp, vp, vp, sz, vp]
             lib.ds_axis_angle_compose.argtypes = [vp, vp, i64, vp, vp]
+            lib.ds_polar_flatten.argtypes = [vp, vp, i64, i64, vp, i64, vp, i64, vp, vp, vp, vp]
             lib.ds_axis_angle_compose_backward.argtypes = [vp, vp, i64, vp, vp, vp]
             lib.ds_probe_fp32_fma.argtypes = [i64, i32, vp, vp]
             lib.ds_last_error.restype = C.c_char_p
@@ -142,7 +143,7 @@ def load_library(require_cuda: bool = True):
             for name in ("ds_box_extent", "ds_enumerate_hkl", "ds_structure_factors", "ds_kinematical_intensities",
                          "ds_simulate", "ds_simulate_batch", "ds_rasterize", "ds_simulate_backward",
                          "ds_structure_factors_backward",
-                         "ds_axis_angle_compose", "ds_axis_angle_compose_backward",
+                         "ds_axis_angle_compose", "ds_axis_angle_compose_backward", "ds_polar_flatten",
                          "ds_probe_fp32_fma"):
                 getattr(lib, name).restype = C.c_int32
             _lib = lib

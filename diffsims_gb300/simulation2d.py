@@ -223,25 +223,17 @@ class Simulation2D:
         """Device CSR arrays of one phase (``PhaseSpots``)."""
         return self._spots[phase_index]
 
-    def polar_flatten_simulations(self, radial_axes=None, azimuthal_axes=None):
+    def polar_flatten_simulations(self, radial_axes=None, azimuthal_axes=None, as_tensor=False):
         """(r, theta, intensity) templates padded to the largest pattern
-        (diffsims/simulations/simulation2d.py:313-355)."""
-        vecs = list(self)
-        max_n = max([v.size for v in vecs]) if vecs else 0
-        r_t = np.zeros((len(vecs), max_n))
-        t_t = np.zeros((len(vecs), max_n))
-        i_t = np.zeros((len(vecs), max_n))
-        for i, v in enumerate(vecs):
-            r, t = v.to_flat_polar()
-            inten = v.intensity
-            if radial_axes is not None and azimuthal_axes is not None:
-                r = _get_closest(radial_axes, r)
-                t = _get_closest(azimuthal_axes, t)
-                mask = (r < len(radial_axes) - 1) & (t < len(azimuthal_axes) - 1)
-                r, t, inten = r[mask], t[mask], inten[mask]
-            r_t[i, :len(r)] = r
-            t_t[i, :len(r)] = t
-            i_t[i, :len(inten)] = inten
+        (diffsims/simulations/simulation2d.py:313-355), computed on the GPU
+        (``ds_polar_flatten``).  numpy arrays as the reference returns them
+        (int indices when both axes are given); ``as_tensor`` keeps float64
+        device tensors instead."""
+        from .engine import polar_flatten
+        r_t, t_t, i_t = polar_flatten(self._spots, radial_axes, azimuthal_axes)
+        if as_tensor:
+            return r_t, t_t, i_t
+        r_t, t_t, i_t = r_t.cpu().numpy(), t_t.cpu().numpy(), i_t.cpu().numpy()
         if radial_axes is not None and azimuthal_axes is not None:
             r_t = np.array(r_t, dtype=int)
             t_t = np.array(t_t, dtype=int)

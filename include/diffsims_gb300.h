@@ -251,6 +251,19 @@ ds_status ds_rasterize(const ds_raster_params *p, const int64_t *offsets, const 
                        size_t scratch_bytes, int32_t *status, void *stream);
 
 /* ------------------------------------------------------------------------ */
+/* Padded polar templates: Simulation2D.polar_flatten_simulations
+ * (diffsims/simulations/simulation2d.py:313-355) for n_patterns CSR patterns
+ * (offsets absolute rows of xyzi).  Outputs n_patterns x max_spots doubles
+ * each, zero padded: r = |(x, y)|, theta = atan2(y, x), intensity.  With both
+ * axes (sorted ascending), r and theta become the indices of the closest axis
+ * entries (get_closest, simulation2d.py:767-781) and spots whose index reaches
+ * the last entry of either axis are dropped (the kept ones stay in order). */
+ds_status ds_polar_flatten(const int64_t *offsets, const float *xyzi, int64_t n_patterns, int64_t max_spots,
+                           const double *radial_axes, int64_t n_radial, const double *azimuthal_axes,
+                           int64_t n_azimuthal, double *r_out, double *theta_out, double *intensity_out,
+                           void *stream);
+
+/* ------------------------------------------------------------------------ */
 /* Adjoint of the spot intensities I = shf(s, r) |F_hkl|^2 (no counterpart in
  * the reference, which is not differentiable).  After a ds_simulate call with
  * the same p, t and quats, whose output had n_spots spots:

@@ -565,3 +565,45 @@ def diffraction_pattern(xyz, intensity, shape, sigma=10, calibration=0.01, in_pl
     if normalize:
         out = np.divide(out, np.max(out))
     return out
+
+
+# --------------------------------------------------------------------------
+# polar templates
+# --------------------------------------------------------------------------
+def get_closest(array, values):
+    """Index of the closest entry of the sorted ``array`` for each value, the
+    upper one on ties.  Follows diffsims/simulations/simulation2d.py:767-781."""
+    array = np.asarray(array)
+    idxs = np.searchsorted(array, values, side="left")
+    prev = (idxs == len(array)) | (np.fabs(values - array[np.maximum(idxs - 1, 0)])
+                                   < np.fabs(values - array[np.minimum(idxs, len(array) - 1)]))
+    idxs[prev] -= 1
+    return idxs
+
+
+def polar_flatten(patterns, radial_axes=None, azimuthal_axes=None):
+    """(r, theta, intensity) templates padded to the largest pattern, from a
+    list of (xyz (n, 3), intensity (n,)).  Follows
+    diffsims/simulations/simulation2d.py:313-355 and
+    diffsims/crystallography/_diffracting_vector.py:186-194."""
+    max_n = max(len(i) for _, i in patterns)
+    r_t = np.zeros((len(patterns), max_n))
+    t_t = np.zeros((len(patterns), max_n))
+    i_t = np.zeros((len(patterns), max_n))
+    for k, (xyz, inten) in enumerate(patterns):
+        xyz = np.asarray(xyz, dtype=np.float64).reshape(-1, 3)
+        r = np.linalg.norm(xyz[:, :2], axis=1)
+        t = np.arctan2(xyz[:, 1], xyz[:, 0])
+        inten = np.asarray(inten, dtype=np.float64)
+        if radial_axes is not None and azimuthal_axes is not None:
+            r = get_closest(radial_axes, r)
+            t = get_closest(azimuthal_axes, t)
+            mask = (r < len(radial_axes) - 1) & (t < len(azimuthal_axes) - 1)
+            r, t, inten = r[mask], t[mask], inten[mask]
+        r_t[k, :len(r)] = r
+        t_t[k, :len(r)] = t
+        i_t[k, :len(inten)] = inten
+    if radial_axes is not None and azimuthal_axes is not None:
+        r_t = np.array(r_t, dtype=int)
+        t_t = np.array(t_t, dtype=int)
+    return r_t, t_t, i_t
