@@ -581,6 +581,90 @@ def run_library(args, torch, dev, hbm_peak):
             "config": {k: (list(v) if isinstance(v, tuple) else v) for k, v in W.items()}}
 
 
+def run_case(args):
+    """Small fixed cases for profiler captures (one kernel of interest each;
+    a few GB on the device at most).  Prints what ran."""
+    import torch
+    import diffsims_gb300 as ds
+    from diffsims_gb300 import _native as N
+    from diffsims_gb300.engine import (PhaseBatch, PhaseTable, RasterSettings, SpotBuffers, rasterize,
+                                       simulate_phase)
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    out = {"case": args.case}
+    if args.case == "raster":
+        # the template library's 60-atom P1 phase, 2048 patterns, two rasterisations
+        W = LIBRARY_WORKLOAD
+        rng = np.random.default_rng(W["seed"])
+        lat = tuple(rng.uniform(6, 10, 3)) + tuple(rng.uniform(70, 110, 3))
+        els = list(rng.choice(["C", "N", "O", "Si", "Fe"], 60))
+        p1 = ds.Phase("P1", ds.Structure([ds.Atom(e, x) for e, x in zip(els, rng.random((60, 3)))], ds.Lattice(*lat)))
+        gen = ds.SimulationGenerator(W["accelerating_voltage"], "lobato", W["precession_angle"],
+                                     W["shape_factor_model"], W["approximate_precession"])
+        tab = PhaseTable(p1, W["reciprocal_radius"], True, "lobato", list(rng.uniform(0.3, 1.5, 60)), device=dev)
+        q = torch.from_numpy(uniform_quaternions(2048, 1)).to(dev)
+        sp = simulate_phase(tab, q, gen.settings(W["max_excitation_error"]), W["reciprocal_radius"], SpotBuffers(dev))
+        img = torch.empty((2048,) + tuple(W["shape"]), dtype=torch.float32, device=dev)
+        rs = RasterSettings(W["shape"], sigma=W["sigma"], calibration=W["calibration"])
+        for _ in range(2):
+            rasterize(sp, rs, 0, 2048, out=img)
+        out.update(patterns=2048, spots=sp.total)
+    elif args.case == "adjoint":
+        # the differentiation workload at 1024 orientations: forward, then the adjoint kernels
+        from diffsims_gb300.autograd import SpotModel, reciprocal_basis
+        W = GRAD_WORKLOAD
+        rng = np.random.default_rng(W["seed"])
+        els = list(rng.choice(["O", "Si", "Fe"], W["n_atoms"]))
+        lat = torch.tensor([7.1, 9.3, 12.4, 90.0, 90.0, 90.0], dtype=torch.float64)
+        xyz = torch.as_tensor(rng.random((W["n_atoms"], 3))).to(dev)
+        B = torch.as_tensor(rng.uniform(0.3, 1.5, W["n_atoms"])).to(dev)
+        gen = ds.SimulationGenerator(W["accelerating_voltage"], "lobato", W["precession_angle"],
+                                     W["shape_factor_model"], W["approximate_precession"])
+        model = SpotModel(els, gen, W["reciprocal_radius"], W["max_excitation_error"])
+        table = model.table(reciprocal_basis(lat).numpy(), xyz, torch.ones_like(B), B)
+        q = torch.as_tensor(cone_quaternions(1024, W["cone_deg"], W["seed"] + 1)).to(dev)
+        sp = simulate_phase(table, q, model.settings, W["reciprocal_radius"], SpotBuffers(dev))
+        lib = N.load_library()
+        p = model.settings.cstruct()
+        n = sp.total
+        gI = torch.ones(n, dtype=torch.float64, device=dev)
+        gF2 = torch.zeros(table.n, dtype=torch.float64, device=dev)
+        gq = torch.zeros((1024, 4), dtype=torch.float64, device=dev)
+        grec = torch.zeros(9, dtype=torch.float64, device=dev)
+        nb = lib.ds_simulate_backward_scratch_bytes(p, n, 1024)
+        scr = torch.empty(max(nb, 16), dtype=torch.uint8, device=dev)
+        st = torch.zeros(1, dtype=torch.int32, device=dev)
+        idx = sp.hkl_index.contiguous()
+        for _ in range(2):
+            N.check(lib.ds_simulate_backward(p, table.cstruct(), N.ptr(q), 1024, N.ptr(sp.offsets), N.ptr(idx), n,
+                                             N.ptr(gI), N.ptr(gF2), N.ptr(gq), N.ptr(grec), N.ptr(scr), nb, N.ptr(st),
+                                             N.stream_handle()), "simulate_backward")
+        N.check_device_status(st, "simulate_backward")
+        out.update(orientations=1024, spots=n)
+    elif args.case == "batch":
+        # the 32 uneven phases with 1/16 of their orientations, one batched launch (tile 16)
+        W = BATCH_WORKLOAD
+        rng = np.random.default_rng(W["seed"])
+        zs = ["C", "N", "O", "Al", "Si", "Ti", "Fe", "Cu"]
+        gen = ds.SimulationGenerator(W["accelerating_voltage"], "lobato", shape_factor_model=W["shape_factor_model"])
+        tables, qs = [], []
+        for k in range(W["n_phases"]):
+            lat = tuple(rng.uniform(3, 20, 3)) + tuple(rng.uniform(80, 100, 3))
+            n_a = int(rng.integers(1, 501))
+            els = list(rng.choice(zs, n_a))
+            ph = ds.Phase(f"p{k}", ds.Structure([ds.Atom(e, x) for e, x in zip(els, rng.random((n_a, 3)))],
+                                                ds.Lattice(*lat)))
+            tables.append(PhaseTable(ph, W["reciprocal_radius"], True, "lobato", list(rng.uniform(0.3, 1.5, n_a)),
+                                     device=dev))
+            qs.append(torch.from_numpy(uniform_quaternions(int(rng.integers(1000, 50001)) // 16, 1000 + k)).to(dev))
+        batch = PhaseBatch(tables, qs, gen.settings(W["max_excitation_error"]), W["reciprocal_radius"], orient_tile=16)
+        batch.run()
+        batch.run()
+        out.update(patterns=sum(int(x.shape[0]) for x in qs), spots=int(batch.totals.sum()))
+    torch.cuda.synchronize()
+    print(json.dumps(out))
+
+
 def compare_forms(mixed, ref, table, q_host, settings):
     """Errors of the mixed form against the all-FP64 GPU form: max relative
     intensity error, max |s| difference, selection flips (and how far from
@@ -651,6 +735,8 @@ def main():
     ap.add_argument("--skip-grad", action="store_true", help="leave out the gradient-step leg")
     ap.add_argument("--skip-library", action="store_true", help="leave out the template-library leg")
     ap.add_argument("--skip-batch", action="store_true", help="leave out the batched-phases leg")
+    ap.add_argument("--case", default=None, choices=["raster", "adjoint", "batch"],
+                    help="run one small profiling case instead of the benchmark")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--out-dir", default=None)
     ap.add_argument("--screen", default="auto", choices=["auto", "rows", "lines"],
@@ -658,6 +744,9 @@ def main():
     ap.add_argument("--device-only", action="store_true",
                     help="time only the device-resident step (for profiling); no e2e, FP64 form or CPU legs")
     args = ap.parse_args()
+    if args.case:
+        run_case(args)
+        return
     if args.impl == "reference":
         run_reference(args)
         return

@@ -126,7 +126,7 @@ def load_library(require_cuda: bool = True):
             lib.ds_rasterize_scratch_bytes.argtypes = [C.POINTER(ds_raster_params), i64]
             lib.ds_rasterize_scratch_bytes.restype = sz
             lib.ds_rasterize.argtypes = [C.POINTER(ds_raster_params), vp, vp, i64, i64, vp, vp, sz, vp, vp]
-            lib.ds_simulate_backward_scratch_bytes.argtypes = [C.POINTER(ds_sim_params), i64]
+            lib.ds_simulate_backward_scratch_bytes.argtypes = [C.POINTER(ds_sim_params), i64, i64]
             lib.ds_simulate_backward_scratch_bytes.restype = sz
             lib.ds_simulate_backward.argtypes = [C.POINTER(ds_sim_params), C.POINTER(ds_phase_table), vp, i64, vp,
                                                  vp, i64, vp, vp, vp, vp, vp, sz, vp, vp]

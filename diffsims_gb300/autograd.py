@@ -205,7 +205,7 @@ class _KinematicalIntensities(torch.autograd.Function):
         st = N.stream_handle()
         p = model.settings.cstruct()
         n_sp = int(ctx.idx.shape[0])
-        bbytes = lib.ds_simulate_backward_scratch_bytes(p, n_sp)
+        bbytes = lib.ds_simulate_backward_scratch_bytes(p, n_sp, n_o)
         bscr = torch.empty(max(bbytes, 16), dtype=torch.uint8, device=dev)
         status = torch.zeros(1, dtype=torch.int32, device=dev)
         N.check(lib.ds_simulate_backward(p, table.cstruct(), N.ptr(q), n_o, N.ptr(ctx.offsets), N.ptr(ctx.idx), n_sp,

@@ -207,31 +207,40 @@ __device__ __forceinline__ void spot_geometry(const BwdConst &c, const OrientB &
 
 // Precession rotation average: the shape factor and its partials of every
 // spot, in their own pass (the quadrature needs registers the accumulating
-// pass holds for its sums).  part[j] = (shf, d shf / d s, d shf / d r).
+// pass holds for its sums), one thread per spot for balance (the quadrature's
+// cost varies with the spot's radius): part[j] = (shf, d shf / d s, d shf / d r).
+// The orientation constants come from orient_prep_kernel.
+__global__ void orient_prep_kernel(const BwdConst c, const double *__restrict__ quats, OrientB *__restrict__ ob) {
+    const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= c.n_orient) return;
+    OrientB O;
+    orient_setup(c, quats + 4 * o, O);
+    ob[o] = O;
+}
+
 __global__ void __launch_bounds__(BW_THREADS)
-shape_partials_kernel(const BwdConst c, const double *__restrict__ quats, const int64_t *__restrict__ offsets,
+shape_partials_kernel(const BwdConst c, const OrientB *__restrict__ ob, const int64_t *__restrict__ offsets,
                       const int32_t *__restrict__ hkl_index, const int32_t *__restrict__ hkl,
                       const double *__restrict__ g2, long long n_spots, double *__restrict__ part, int32_t *status) {
-    const int lane = threadIdx.x & 31;
-    const long long warp0 = ((long long)blockIdx.x * BW_THREADS + threadIdx.x) >> 5;
-    const long long n_warps = ((long long)gridDim.x * BW_THREADS) >> 5;
-    for (long long o = warp0; o < c.n_orient; o += n_warps) {
-        OrientB O;
-        orient_setup(c, quats + 4 * o, O);
-        const long long a = offsets[o], b = offsets[o + 1];
-        if (b > n_spots) {
-            if (lane == 0) atomicOr(status, DS_ERR_CAPACITY);
-            continue;
+    const long long total = min((long long)offsets[c.n_orient], n_spots);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && offsets[c.n_orient] > n_spots) atomicOr(status, DS_ERR_CAPACITY);
+    for (long long j = (long long)blockIdx.x * BW_THREADS + threadIdx.x; j < total;
+         j += (long long)gridDim.x * BW_THREADS) {
+        // orientation of spot j: last o with offsets[o] <= j
+        long long lo = 0, hi = c.n_orient - 1;
+        while (lo < hi) {
+            const long long mid = (lo + hi + 1) >> 1;
+            if (offsets[mid] <= j) lo = mid;
+            else hi = mid - 1;
         }
-        for (long long j = a + lane; j < b; j += 32) {
-            SpotGeom G;
-            spot_geometry(c, O, hkl, g2, hkl_index[j], G);
-            double ds, dr;
-            const double shf = shape_and_grad<DS_PRECESSION_INTEGRAL>(c, G.s, (double)G.r, ds, dr);
-            part[3 * j] = shf;
-            part[3 * j + 1] = ds;
-            part[3 * j + 2] = dr;
-        }
+        const OrientB O = ob[lo];
+        SpotGeom G;
+        spot_geometry(c, O, hkl, g2, hkl_index[j], G);
+        double ds, dr;
+        const double shf = shape_and_grad<DS_PRECESSION_INTEGRAL>(c, G.s, (double)G.r, ds, dr);
+        part[3 * j] = shf;
+        part[3 * j + 1] = ds;
+        part[3 * j + 2] = dr;
     }
 }
 
@@ -460,9 +469,9 @@ sf_atoms_backward_kernel(const SfbConst c, const ds_atoms A, const int32_t *__re
 
 using namespace ds;
 
-extern "C" size_t ds_simulate_backward_scratch_bytes(const ds_sim_params *p, int64_t n_spots) {
-    if (!p || n_spots <= 0 || p->precession_mode != DS_PRECESSION_INTEGRAL) return 0;
-    return (size_t)n_spots * 3 * sizeof(double);
+extern "C" size_t ds_simulate_backward_scratch_bytes(const ds_sim_params *p, int64_t n_spots, int64_t n_orient) {
+    if (!p || n_spots < 0 || n_orient <= 0 || p->precession_mode != DS_PRECESSION_INTEGRAL) return 0;
+    return (((size_t)n_spots * 3 * sizeof(double) + 255) / 256) * 256 + (size_t)n_orient * sizeof(OrientB);
 }
 
 extern "C" ds_status ds_simulate_backward(const ds_sim_params *p, const ds_phase_table *t, const double *quats,
@@ -483,8 +492,8 @@ extern "C" ds_status ds_simulate_backward(const ds_sim_params *p, const ds_phase
     if (n_orient == 0) return DS_OK;
     DS_REQUIRE(quats && offsets && grad_F2 && grad_quats && grad_recip && status, "ds_simulate_backward: null array");
     DS_REQUIRE(n_spots == 0 || (hkl_index && grad_intensity), "ds_simulate_backward: null spot arrays");
-    DS_REQUIRE(scratch_bytes >= ds_simulate_backward_scratch_bytes(p, n_spots) &&
-                   (ds_simulate_backward_scratch_bytes(p, n_spots) == 0 || scratch),
+    DS_REQUIRE(scratch_bytes >= ds_simulate_backward_scratch_bytes(p, n_spots, n_orient) &&
+                   (ds_simulate_backward_scratch_bytes(p, n_spots, n_orient) == 0 || scratch),
                "ds_simulate_backward: scratch too small");
     DS_REQUIRE(t->n_hkl == 0 || (t->hkl && t->g2 && (t->F2 || t->F2d)), "ds_simulate_backward: table arrays missing");
     BwdConst c;
@@ -516,10 +525,19 @@ extern "C" ds_status ds_simulate_backward(const ds_sim_params *p, const ds_phase
     const long long ns = n_spots;
     if (c.prec == DS_PRECESSION_INTEGRAL) {
         double *part = reinterpret_cast<double *>(scratch);
-        shape_partials_kernel<<<grid, BW_THREADS, 0, s>>>(c, quats, offsets, hkl_index, t->hkl, t->g2, ns, part,
-                                                          status);
-        ds_status st = check_launch("shape_partials_kernel");
+        OrientB *ob = reinterpret_cast<OrientB *>(reinterpret_cast<unsigned char *>(scratch) +
+                                                  (((size_t)ns * 3 * sizeof(double) + 255) / 256) * 256);
+        orient_prep_kernel<<<(unsigned)((n_orient + 127) / 128), 128, 0, s>>>(c, quats, ob);
+        ds_status st = check_launch("orient_prep_kernel");
         if (st) return st;
+        const long long pblocks = std::min<long long>((ns + BW_THREADS - 1) / BW_THREADS, (long long)n_sm * 16);
+        if (ns > 0) {
+            shape_partials_kernel<<<(unsigned)std::max(1ll, pblocks), BW_THREADS, 0, s>>>(c, ob, offsets, hkl_index,
+                                                                                         t->hkl, t->g2, ns, part,
+                                                                                         status);
+            st = check_launch("shape_partials_kernel");
+            if (st) return st;
+        }
         spot_backward_kernel<DS_PRECESSION_INTEGRAL, true><<<grid, BW_THREADS, 0, s>>>(
             c, quats, offsets, hkl_index, grad_intensity, t->hkl, t->g2, t->F2, F2d, part, ns, grad_F2, grad_quats, grad_recip);
     } else if (c.prec == DS_PRECESSION_LORENTZIAN) {

@@ -273,7 +273,7 @@ ds_status ds_polar_flatten(const int64_t *offsets, const float *xyzi, int64_t n_
  * (n_orient x 4 doubles, through the normalisation of q).  Selection is
  * piecewise constant and not differentiated.  Scratch (the rotation average's
  * per-spot partials) from ds_simulate_backward_scratch_bytes. */
-size_t ds_simulate_backward_scratch_bytes(const ds_sim_params *p, int64_t n_spots);
+size_t ds_simulate_backward_scratch_bytes(const ds_sim_params *p, int64_t n_spots, int64_t n_orient);
 ds_status ds_simulate_backward(const ds_sim_params *p, const ds_phase_table *t, const double *quats,
                                int64_t n_orient, const int64_t *offsets, const int32_t *hkl_index,
                                int64_t n_spots, const double *grad_intensity, double *grad_F2,
