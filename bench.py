@@ -503,7 +503,8 @@ def run_batch(args, torch, dev):
     return {"metric": "orientation patterns/s (32 uneven phases, one launch)", "value": n_pat / (graph_ms * 1e-3),
             "unit": "patterns/s", "ms_per_step": graph_ms, "patterns_per_step": n_pat, "spots_per_step": int(n_spots),
             "per_phase_launches_ms": seq_ms, "speedup_over_per_phase_launches": seq_ms / graph_ms,
-            "orient_tile": batch.orient_tile, "autotuner_ms_by_tile": AUTOTUNER.timings.get(key),
+            "orient_tile": batch.orient_tile, "stage_cap": batch.stage_cap,
+            "autotuner_ms": AUTOTUNER.timings.get(key),
             "n_hkl_range": [min(t.n for t in tables), max(t.n for t in tables)],
             "orientations_range": [min(int(q.shape[0]) for q in qs), max(int(q.shape[0]) for q in qs)],
             "table_build_s": table_s, "launches_per_step": len(tables) + 2,

@@ -40,6 +40,7 @@ constexpr size_t RAS_SMEM_LIMIT = 200 * 1024;
 struct RasterConst {
     int H, W, R;
     int fast, normalize;
+    int one_pass;       // fast + normalise: build each covered row once (flags below)
     int NS, T;          // arena capacity in spots, hash slots (power of two >= 2 NS)
     double cal, cx, cy, ca, sa, mf, snap;
     double pref, exp_pref, clip;
@@ -422,12 +423,15 @@ struct FastArena {
     int2 *ent;          // row entries: (amp * row weight as bits, X << 16 | spot)
     int *rcnt, *rstart, *rfill;  // H + 1 each
     float *rowbuf;      // RAS_WARPS x RAS_FSEG
+    unsigned *flags;    // one pass: per (row, segment, half) the lanes whose float4 is non-zero
     int *misc;
     float *wmax;
 };
 constexpr int RAS_FSEG = 256;  // columns per row segment (32 lanes x 2 float4)
+constexpr size_t RAS_FLAGS_MAX = 32 * 1024;  // bytes of one-pass flags the arena may hold
+__host__ __device__ inline size_t fast_flag_bytes(int H, int W) { return (size_t)H * ((W + RAS_FSEG - 1) / RAS_FSEG) * 8; }
 
-__host__ __device__ inline size_t fast_arena_bytes(int NS, int T, int H, int P) {
+__host__ __device__ inline size_t fast_arena_bytes(int NS, int T, int H, int P, size_t flag_bytes) {
     size_t o = 0;
     o += ras_align((size_t)NS * 4) * 2;              // key, slot
     o += ras_align((size_t)T * 4) * 2;               // hkey, hidx
@@ -436,11 +440,12 @@ __host__ __device__ inline size_t fast_arena_bytes(int NS, int T, int H, int P) 
     o += ras_align((size_t)NS * P * 8);              // ent
     o += ras_align((size_t)(H + 1) * 4) * 3;         // rcnt, rstart, rfill
     o += ras_align((size_t)RAS_WARPS * RAS_FSEG * 4);
+    o += ras_align(flag_bytes);
     o += ras_align(64 * 4) + ras_align(RAS_WARPS * 4);
     return o;
 }
 
-__device__ inline FastArena carve_fast(unsigned char *base, int NS, int T, int H, int P) {
+__device__ inline FastArena carve_fast(unsigned char *base, int NS, int T, int H, int P, size_t flag_bytes) {
     FastArena A;
     size_t o = 0;
     auto take = [&](size_t bytes) {
@@ -461,10 +466,13 @@ __device__ inline FastArena carve_fast(unsigned char *base, int NS, int T, int H
     A.rstart = (int *)take((size_t)(H + 1) * 4);
     A.rfill = (int *)take((size_t)(H + 1) * 4);
     A.rowbuf = (float *)take((size_t)RAS_WARPS * RAS_FSEG * 4);
+    A.flags = (unsigned *)take(flag_bytes);
     A.misc = (int *)take(64 * 4);
     A.wmax = (float *)take(RAS_WARPS * 4);
     return A;
 }
+
+__device__ __forceinline__ void st_wb(float4 *p, float4 v) { *p = v; }  // default policy: stays in L2 for the rescale
 
 // Row y, columns [x0, x0 + RAS_FSEG) into the warp's buffer; on return lane l
 // holds columns x0 + 4 l + (0..3) in v[0..3] and x0 + 128 + 4 l + (0..3) in v[4..7].
@@ -505,7 +513,7 @@ raster_fast_kernel(const RasterConst c, const int64_t *__restrict__ off, const f
     extern __shared__ __align__(16) unsigned char ras_smem[];
     unsigned char *base = gscratch ? gscratch + (size_t)blockIdx.x * arena_bytes : ras_smem;
     const int P = 2 * c.R + 1;
-    const FastArena A = carve_fast(base, c.NS, c.T, c.H, P);
+    const FastArena A = carve_fast(base, c.NS, c.T, c.H, P, c.one_pass ? fast_flag_bytes(c.H, c.W) : 0);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int H = c.H, W = c.W;
     const size_t img = (size_t)H * W;
@@ -637,6 +645,85 @@ raster_fast_kernel(const RasterConst c, const int64_t *__restrict__ off, const f
         }
         __syncthreads();
 
+        // ---- one pass (normalised, float4 rows): every covered row built once and
+        // stored unscaled (the stores stay in L2), its non-zero float4 flagged;
+        // then the maximum, and the flagged float4 rescaled in place (each lane
+        // rereads only its own stores)
+        if (VEC && c.one_pass && n_in > 0) {
+            float *dst = out + (size_t)p * img;
+            const int nseg = (W + RAS_FSEG - 1) / RAS_FSEG;
+            float wm = -INFINITY;
+            bool any_empty = false;
+            for (int y = warp; y < H; y += RAS_WARPS) {
+                float *row = dst + (size_t)y * W;
+                if (A.rstart[y + 1] == A.rstart[y]) {
+                    any_empty = true;
+                    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+                    for (int x = lane * 4; x < W; x += 128) st_cs(reinterpret_cast<float4 *>(row + x), z);
+                    continue;
+                }
+                for (int si = 0; si < nseg; ++si) {
+                    const int x0 = si * RAS_FSEG;
+                    float v[8];
+                    fast_row_segment(c, A, P, y, x0, lane, buf, v);
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int xb = x0 + 128 * h + 4 * lane;
+                        const bool in = xb < W;
+                        const bool nz = in && (v[4 * h] != 0.f || v[4 * h + 1] != 0.f || v[4 * h + 2] != 0.f ||
+                                               v[4 * h + 3] != 0.f);
+                        if (in) {
+                            st_wb(reinterpret_cast<float4 *>(row + xb),
+                                  make_float4(v[4 * h], v[4 * h + 1], v[4 * h + 2], v[4 * h + 3]));
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) wm = fmaxf(wm, v[4 * h + e]);
+                        }
+                        const unsigned bal = __ballot_sync(FULL_MASK, nz);
+                        if (lane == 0) A.flags[((size_t)y * nseg + si) * 2 + h] = bal;
+                    }
+                }
+            }
+            if (any_empty) wm = fmaxf(wm, 0.f);
+#pragma unroll
+            for (int d = 16; d >= 1; d >>= 1) wm = fmaxf(wm, __shfl_xor_sync(FULL_MASK, wm, d));
+            if (lane == 0) A.wmax[warp] = wm;
+            __syncthreads();
+            float mx = A.wmax[0];
+            for (int w = 1; w < RAS_WARPS; ++w) mx = fmaxf(mx, A.wmax[w]);
+            if (mx > 0.f && mx < INFINITY) {
+                const float inv_mx = 1.f / mx;  // one reciprocal, then products (within 1 ulp of the quotients)
+                for (int y = warp; y < H; y += RAS_WARPS) {
+                    if (A.rstart[y + 1] == A.rstart[y]) continue;
+                    float *row = dst + (size_t)y * W;
+                    for (int si = 0; si < nseg; ++si) {
+#pragma unroll
+                        for (int h = 0; h < 2; ++h) {
+                            const unsigned bal = A.flags[((size_t)y * nseg + si) * 2 + h];
+                            if ((bal >> lane) & 1u) {
+                                float4 *q = reinterpret_cast<float4 *>(row + si * RAS_FSEG + 128 * h + 4 * lane);
+                                float4 t = *q;
+                                t.x *= inv_mx; t.y *= inv_mx; t.z *= inv_mx; t.w *= inv_mx;
+                                st_cs(q, t);
+                            }
+                        }
+                    }
+                }
+            } else {
+                // a maximum of zero, infinite or NaN: pattern / max everywhere, as numpy divides
+                for (int y = warp; y < H; y += RAS_WARPS) {
+                    float *row = dst + (size_t)y * W;
+                    for (int x = lane * 4; x < W; x += 128) {
+                        float4 *q = reinterpret_cast<float4 *>(row + x);
+                        float4 t = *q;
+                        t.x /= mx; t.y /= mx; t.z /= mx; t.w /= mx;
+                        st_cs(q, t);
+                    }
+                }
+            }
+            __syncthreads();  // the arena is reused by the next pattern
+            continue;
+        }
+
         // ---- maximum over the image (normalise)
         float mx = 1.f;
         const bool norm = c.normalize && n_in > 0;
@@ -711,6 +798,7 @@ raster_fast_kernel(const RasterConst c, const int64_t *__restrict__ off, const f
 
 struct RasterPlan {
     int NS, T, grid;
+    bool one_pass;
     size_t arena, smem, scratch;
 };
 
@@ -732,7 +820,10 @@ static ds_status raster_plan(const ds_raster_params *p, int64_t max_spots, Raste
     P.NS = NS;
     P.T = T;
     const bool fast = p->fast != 0;
-    P.arena = fast ? fast_arena_bytes(NS, T, p->height, 2 * filter_radius(p) + 1) : raster_arena_bytes(NS, T, p->height);
+    P.one_pass = fast && p->normalize && (p->width % 4) == 0 && fast_flag_bytes(p->height, p->width) <= RAS_FLAGS_MAX;
+    P.arena = fast ? fast_arena_bytes(NS, T, p->height, 2 * filter_radius(p) + 1,
+                                      P.one_pass ? fast_flag_bytes(p->height, p->width) : 0)
+                   : raster_arena_bytes(NS, T, p->height);
     int dev = 0, n_sm = 0;
     DS_CUDA_TRY(cudaGetDevice(&dev));
     DS_CUDA_TRY(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
@@ -813,6 +904,7 @@ extern "C" ds_status ds_rasterize(const ds_raster_params *p, const int64_t *offs
     c.normalize = p->normalize ? 1 : 0;
     c.NS = P.NS;
     c.T = P.T;
+    c.one_pass = P.one_pass && vec ? 1 : 0;
     c.cal = p->calibration;
     c.cx = p->center_x;
     c.cy = p->center_y;

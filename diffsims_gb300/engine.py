@@ -420,6 +420,8 @@ class PhaseBatch:
         self.offsets = [torch.zeros(sum(self.n_orient[i] for i in g) + 1, dtype=torch.int64, device=self.device)
                         for g in self.groups]
         self.graph = None
+        self.stage_cap = int(settings.stage_cap)
+        self.orient_tile = 0
         if orient_tile is None:
             orient_tile = (autotuner or AUTOTUNER).tile_for(self)
         self.orient_tile = int(orient_tile)
@@ -436,6 +438,7 @@ class PhaseBatch:
     def cparams(self, orient_tile=None):
         p = self.settings.cstruct()
         p.orient_tile = int(self.orient_tile if orient_tile is None else orient_tile)
+        p.stage_cap = int(self.stage_cap)
         return p
 
     def _plan(self, capacity=None):
@@ -519,12 +522,17 @@ class PhaseBatch:
 
 
 class Autotuner:
-    """Picks the orientation tile of a batched launch by timing the feasible
-    candidates on the batch itself (CUDA events, best of a few launches) and
-    remembers the choice per problem class (phases, orientations and table
-    sizes in powers of two, shape model, precession, form)."""
+    """Picks the tile shape of a batched launch by timing the feasible
+    candidates on the batch itself (CUDA events, best of a few launches):
+    orientations per tile (the largest any phase may use; bigger tables get
+    smaller tiles so their bitmap fits shared memory) and the per-CTA
+    candidate staging (screened reflections held per tile before the ordered
+    writes).  Remembers the choice per problem class (phases, orientations
+    and table sizes in powers of two, shape model, precession, form)."""
 
-    CANDIDATES = (4, 8, 16, 32)
+    TILES = (4, 8, 16, 32)
+    STAGES = (6144, 24576)
+    CANDIDATES = TILES
 
     def __init__(self, repeats=3):
         self.repeats = repeats
@@ -538,41 +546,48 @@ class Autotuner:
         return (len(batch.tables), lg(sum(batch.n_orient)), lg(max(t.n for t in batch.tables)),
                 s.shape_model, int(s.precession_mode), s.form)
 
-    def tile_for(self, batch: "PhaseBatch") -> int:
+    def tune(self, batch: "PhaseBatch"):
+        """(orient_tile, stage_cap) for this batch (cached per class)."""
         k = self.key(batch)
         if k in self.cache:
             return self.cache[k]
         lib = N.load_library()
         fp64 = batch.settings.form == "fp64"
         integ = batch.settings.precession_mode == N.DS_PRECESSION_INTEGRAL
-        cands = [c for c in self.CANDIDATES if c <= (8 if fp64 else 16 if integ else 32)]
+        tiles = [c for c in self.TILES if c <= (8 if fp64 else 16 if integ else 32)]
         best, best_ms, times = None, None, {}
-        for c in cands:
-            batch.orient_tile = c
-            p = batch.cparams(c)
-            if any(lib.ds_simulate_batch_scratch_bytes(p, it, len(it)) == 0 for it in batch._items):
-                continue  # infeasible (tile does not fit shared memory)
-            try:
-                batch._plan()
-                batch.run()  # sizes the outputs, checks the status
-            except (ValueError, N.NativeError):
-                continue
-            ms = []
-            for _ in range(self.repeats):
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record()
-                batch._launch()
-                e1.record()
-                e1.synchronize()
-                ms.append(e0.elapsed_time(e1))
-            times[c] = min(ms)
-            if best_ms is None or times[c] < best_ms:
-                best, best_ms = c, times[c]
+        for c in tiles:
+            for sc in self.STAGES:
+                batch.orient_tile, batch.stage_cap = c, sc
+                p = batch.cparams()
+                if any(lib.ds_simulate_batch_scratch_bytes(p, it, len(it)) == 0 for it in batch._items):
+                    continue  # infeasible (tile does not fit shared memory)
+                try:
+                    batch._plan()
+                    batch.run()  # sizes the outputs, checks the status
+                except (ValueError, N.NativeError):
+                    continue
+                ms = []
+                for _ in range(self.repeats):
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    batch._launch()
+                    e1.record()
+                    e1.synchronize()
+                    ms.append(e0.elapsed_time(e1))
+                times[f"tile{c}_stage{sc}"] = min(ms)
+                if best_ms is None or min(ms) < best_ms:
+                    best, best_ms = (c, sc), min(ms)
         if best is None:
-            best = 4
+            best = (4, 0)
         self.cache[k] = best
         self.timings[k] = times
         return best
+
+    def tile_for(self, batch: "PhaseBatch") -> int:
+        tile, stage = self.tune(batch)
+        batch.stage_cap = stage
+        return tile
 
 
 AUTOTUNER = Autotuner()

@@ -119,10 +119,11 @@ def test_autotuner_picks_and_caches():
     tuner = Autotuner(repeats=2)
     batch = PhaseBatch(tables, qs, settings, p.reciprocal_radius, autotuner=tuner)
     key = Autotuner.key(batch)
-    assert batch.orient_tile in Autotuner.CANDIDATES and tuner.cache[key] == batch.orient_tile
-    assert set(tuner.timings[key]) <= set(Autotuner.CANDIDATES) and tuner.timings[key]
+    assert batch.orient_tile in Autotuner.TILES and batch.stage_cap in Autotuner.STAGES
+    assert tuner.cache[key] == (batch.orient_tile, batch.stage_cap) and tuner.timings[key]
     batch.run()
-    assert PhaseBatch(tables, qs, settings, p.reciprocal_radius, autotuner=tuner).orient_tile == batch.orient_tile
+    again = PhaseBatch(tables, qs, settings, p.reciprocal_radius, autotuner=tuner)
+    assert (again.orient_tile, again.stage_cap) == (batch.orient_tile, batch.stage_cap)
 
 
 def test_more_phases_than_one_launch_holds():
