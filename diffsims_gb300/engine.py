@@ -305,6 +305,182 @@ def simulate_phase(table: PhaseTable, quats: torch.Tensor, settings: SimSettings
     raise N.NativeError("simulate: output capacity still exceeded after resizing")
 
 
+class StreamedSpots(PhaseSpots):
+    """Spots of one phase simulated in orientation chunks, each chunk's CSR
+    copied to page-locked host memory on a side stream while the later
+    chunks compute.  For a result wanted on the host the device-to-host link
+    (about 190 GB/s against 20 bytes per spot) bounds the call, not the
+    kernel, so the copies start as soon as the first chunk is done.
+
+    ``host()`` waits for the copies in flight.  The device CSR (``offsets``
+    is global; ``hkl_index``, ``xyzi``, ``excitation_error``) is assembled
+    from the chunks' regions on first access."""
+
+    def __init__(self, table, chunks, regions, host_bufs, done, total):
+        self.table = table
+        self._chunks = chunks        # per chunk: (first orientation, chunk offsets on the device, spot base)
+        self._regions = regions      # per chunk: (idx, xyzi, s, n_spots)
+        self._host_bufs = host_bufs  # page-locked (offsets, hkl_index, xyzi)
+        self._done = done            # event after the last copy
+        self.total = total
+        self._n = sum(c[1].shape[0] - 1 for c in chunks)
+        self._host = None
+        self._dev = None
+        self._off = None
+
+    @property
+    def n_orient(self):
+        return self._n
+
+    def _device_csr(self):
+        if self._dev is None:
+            regs = [r for r in self._regions if r[3] > 0] or self._regions[:1]
+            idx = torch.cat([r[0][:r[3]] for r in regs])
+            xyzi = torch.cat([r[1][:r[3]] for r in regs])
+            s = torch.cat([r[2][:r[3]] for r in regs]) if regs[0][2] is not None else None
+            self._dev = (idx, xyzi, s)
+            self._regions = None  # the chunk regions are no longer needed
+        return self._dev
+
+    @property
+    def offsets(self):
+        if self._off is None:
+            parts = [o[:-1] + base for _, o, base in self._chunks]
+            parts.append(torch.full((1,), self.total, dtype=torch.int64, device=self._chunks[0][1].device))
+            self._off = torch.cat(parts)
+        return self._off
+
+    @property
+    def hkl_index(self):
+        return self._device_csr()[0]
+
+    @property
+    def xyzi(self):
+        return self._device_csr()[1]
+
+    @property
+    def excitation_error(self):
+        return self._device_csr()[2]
+
+    def host(self, pinned=False):
+        if self._host is None:
+            self._done.synchronize()
+            off, idx, xyzi = self._host_bufs
+            off = off.numpy()
+            for a, o, base in self._chunks:  # chunk-relative offsets made global
+                off[a:a + o.shape[0] - 1] += base
+            off[self._n] = self.total
+            self._host = (off, idx[:self.total].numpy(), xyzi[:self.total].numpy())
+        return self._host
+
+
+def simulate_phase_streamed(table: PhaseTable, quats: torch.Tensor, settings: SimSettings, radius: float,
+                            chunk=32768, first_chunk=2048, with_excitation_error=False) -> StreamedSpots:
+    """``simulate_phase`` for a result wanted on the host: the orientations
+    run in chunks on the current stream, each into its own device region,
+    and each chunk's spots are copied to page-locked host memory on a side
+    stream as soon as its count is known, while the next chunks compute.
+    Chunk sizes double from ``first_chunk`` up to ``chunk``: the copies
+    start early, and the copy of a chunk (at about twice the kernel's time
+    per orientation) overlaps the next, twice larger, chunk.  A chunk whose
+    spots overflow its region is re-run alone with the exact size."""
+    lib = N.load_library()
+    dev = table.device
+    n = int(quats.shape[0])
+    comp = torch.cuda.current_stream(dev)
+    copy = torch.cuda.Stream(dev)
+    bounds = [0]
+    size = max(1, min(first_chunk, chunk))
+    while bounds[-1] < n:
+        bounds.append(min(n, bounds[-1] + size))
+        size = min(chunk, 2 * size)
+    if len(bounds) == 1:
+        bounds.append(0)
+    n_chunks = len(bounds) - 1
+    p = settings.cstruct()
+    t = table.cstruct()
+    longest = max(b - a for a, b in zip(bounds[:-1], bounds[1:]))
+    sbytes = lib.ds_simulate_scratch_bytes(p, t, longest)
+    per = estimate_spots(table, settings, radius)
+    scratch = torch.empty(max(int(sbytes), 16), dtype=torch.uint8, device=dev)
+    status = torch.zeros(n_chunks, dtype=torch.int32, device=dev)
+    totals = torch.zeros(n_chunks, dtype=torch.int64, device=dev)
+    totals_h = torch.empty(n_chunks, dtype=torch.int64, pin_memory=True)
+    status_h = torch.empty(n_chunks, dtype=torch.int32, pin_memory=True)
+    chunk_off = [torch.empty(b - a + 1, dtype=torch.int64, device=dev) for a, b in zip(bounds[:-1], bounds[1:])]
+    sf_status_h = torch.empty(1, dtype=torch.int32, pin_memory=True)
+    sf_status_h.copy_(table._status, non_blocking=True)  # read after the first chunk, without a stall
+
+    def launch(k, cap):
+        a, b = bounds[k], bounds[k + 1]
+        idx = torch.empty(cap, dtype=torch.int32, device=dev)
+        xyzi = torch.empty((cap, 4), dtype=torch.float32, device=dev)
+        s = torch.empty(cap, dtype=torch.float64, device=dev) if with_excitation_error else None
+        out = N.ds_spots(chunk_off[k].data_ptr(), idx.data_ptr(), xyzi.data_ptr(), cap, totals[k:].data_ptr(),
+                         s.data_ptr() if s is not None else None)
+        N.check(lib.ds_simulate(p, t, N.ptr(quats[a:b]) if b > a else N.ptr(quats), b - a, out, N.ptr(scratch),
+                                sbytes, N.ptr(status[k:]), N.stream_handle(comp)), "simulate")
+        totals_h[k:k + 1].copy_(totals[k:k + 1], non_blocking=True)
+        status_h[k:k + 1].copy_(status[k:k + 1], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(comp)
+        return [idx, xyzi, s, ev]
+
+    caps = [max(1024, (b - a) * per * 5 // 4) for a, b in zip(bounds[:-1], bounds[1:])]
+    regions = [launch(k, caps[k]) for k in range(min(2, n_chunks))]
+    host_cap = sum(caps)
+    h_idx = torch.empty(host_cap, dtype=torch.int32, pin_memory=True)
+    h_xyzi = torch.empty((host_cap, 4), dtype=torch.float32, pin_memory=True)
+    h_off = torch.empty(n + 1, dtype=torch.int64, pin_memory=True)
+    base = 0
+    out_regions, chunks = [], []
+    for k in range(n_chunks):
+        if k + 2 < n_chunks:
+            regions.append(launch(k + 2, caps[k + 2]))  # two chunks queued ahead of the copies
+        idx, xyzi, s, ev = regions[k]
+        ev.synchronize()
+        v = N.check_status_value(int(status_h[k]), "simulate", allow=N.DS_ERR_CAPACITY)
+        if k == 0:
+            N.check_status_value(int(sf_status_h[0]), "structure_factors")
+        cnt = int(totals_h[k])
+        if v & N.DS_ERR_CAPACITY:
+            status[k:k + 1].zero_()
+            idx, xyzi, s, ev = launch(k, cnt + 1024)
+            ev.synchronize()
+            N.check_status_value(int(status_h[k]), "simulate")
+            cnt = int(totals_h[k])
+        if base + cnt > h_idx.shape[0]:
+            # the host arrays outgrew the estimate: grow them (waits for the copies so far)
+            copy.synchronize()
+            grow = max(base + cnt, h_idx.shape[0] * 3 // 2)
+            ni = torch.empty(grow, dtype=torch.int32, pin_memory=True)
+            nx = torch.empty((grow, 4), dtype=torch.float32, pin_memory=True)
+            ni[:base].copy_(h_idx[:base])
+            nx[:base].copy_(h_xyzi[:base])
+            h_idx, h_xyzi = ni, nx
+        a, b = bounds[k], bounds[k + 1]
+        copy.wait_event(ev)
+        # copies only on the side stream: a kernel there would wait for an
+        # SM behind the persistent simulation kernel, and the copies behind it
+        with torch.cuda.stream(copy):
+            if b > a:
+                h_off[a:b].copy_(chunk_off[k][:b - a], non_blocking=True)
+            if cnt:
+                h_idx[base:base + cnt].copy_(idx[:cnt], non_blocking=True)
+                h_xyzi[base:base + cnt].copy_(xyzi[:cnt], non_blocking=True)
+        out_regions.append((idx, xyzi, s, cnt))
+        chunks.append((a, chunk_off[k], base))
+        base += cnt
+    done = torch.cuda.Event()
+    done.record(copy)
+    # the chunk buffers were read on the copy stream as well
+    for r in out_regions + [(c, None, None, 0) for c in chunk_off]:
+        for x in r[:3]:
+            if x is not None:
+                x.record_stream(copy)
+    return StreamedSpots(table, chunks, out_regions, (h_off, h_idx, h_xyzi), done, base)
+
+
 @dataclass
 class RasterSettings:
     """Arguments of Simulation2D.get_diffraction_pattern

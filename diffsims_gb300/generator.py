@@ -10,7 +10,7 @@ import torch
 
 from . import _native as N
 from .crystal import Phase, Rotation, quaternions_of
-from .engine import PhaseBatch, PhaseTable, SimSettings, SpotBuffers, simulate_phase
+from .engine import PhaseBatch, PhaseTable, SimSettings, SpotBuffers, simulate_phase, simulate_phase_streamed
 from .simulation2d import Simulation2D
 from .sim_utils import get_electron_wavelength
 
@@ -106,14 +106,19 @@ class SimulationGenerator:
                                 reciprocal_radius: float = 1.0, with_direct_beam: bool = True,
                                 max_excitation_error: float = 1e-2, shape_factor_width: float = None,
                                 debye_waller_factors: dict = None, show_progressbar: bool = False,
-                                form: str = "mixed", orient_tile: int = 0):
+                                form: str = "mixed", orient_tile: int = 0, stream_to_host: bool = True):
         """Spot patterns of one or more phases, each under its own rotations.
 
         Arguments as diffsims/generators/simulation_generator.py:134-146;
         ``form`` selects the arithmetic ('mixed': FP32 bulk with FP64 phase
         reduction and FP64 excitation error near the cutoff; 'fp64': the plain
         all-FP64 comparator).  ``show_progressbar`` is accepted and ignored
-        (each phase is one kernel launch).  Returns ``Simulation2D``.
+        (each phase is one kernel launch).  With ``stream_to_host`` (the
+        default, as the results are normally read on the host) a single
+        phase runs in orientation chunks whose spots are copied to
+        page-locked host memory while later chunks compute; ``False`` keeps
+        the spots on the device only (for device-side consumers such as
+        ``get_diffraction_patterns``).  Returns ``Simulation2D``.
         """
         if rotation is None:
             rotation = Rotation.from_euler((0, 0, 0), degrees=True)
@@ -135,7 +140,9 @@ class SimulationGenerator:
                                      debye_waller_factors, form=form, device=dev))
             qs.append(torch.from_numpy(quaternions_of(rot)).to(dev))
             rots.append(rot)
-        if len(tables) == 1:
+        if len(tables) == 1 and stream_to_host:
+            spots = [simulate_phase_streamed(tables[0], qs[0], settings, reciprocal_radius)]
+        elif len(tables) == 1:
             spots = [simulate_phase(tables[0], qs[0], settings, reciprocal_radius, buffers=SpotBuffers(dev))]
         else:
             # all phases in one persistent launch (per group of up to 96); tile

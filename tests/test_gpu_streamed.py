@@ -1,0 +1,93 @@
+"""Chunked simulation with the spots streamed to host memory
+(``simulate_phase_streamed``, the default single-phase path of
+``calculate_diffraction2d``): the host CSR and the assembled device CSR equal
+a single ``simulate_phase`` launch bit for bit, for any chunking, with chunks
+that overflow their region, and with no orientations at all."""
+import numpy as np
+import pytest
+
+from oracle import kinematic as ok
+from tests import parity_util as pu
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import __graft_entry__
+    __graft_entry__.build()
+    torch.cuda.set_device(0)
+
+
+def _case(torch, n_orient, seed=1, model="sinc"):
+    from diffsims_gb300.engine import PhaseTable
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(seed)
+    cr = ok.Crystal(tuple(rng.uniform(5, 9, 3)) + (90.0, 95.0, 90.0), list(rng.choice(["O", "Si", "Fe"], 20)),
+                    rng.random((20, 3)), B=rng.uniform(0.3, 1.2, 20))
+    p = ok.SimParams(accelerating_voltage=200, reciprocal_radius=1.5, max_excitation_error=0.02,
+                     shape_factor_model=model)
+    settings = pu.generator_for(p).settings(p.max_excitation_error)
+    table = PhaseTable(pu.to_phase(cr), p.reciprocal_radius, True, "lobato", list(cr.B), device=dev)
+    q = torch.as_tensor(ok.random_quaternions(n_orient, seed=seed + 7)).to(dev)
+    return table, q, settings, p.reciprocal_radius
+
+
+def _check(torch, got, want):
+    off, idx, xyzi = got.host()
+    w_off, w_idx, w_xyzi = want.host()
+    assert got.total == want.total
+    assert np.array_equal(off, w_off)
+    assert np.array_equal(idx, w_idx)
+    assert np.array_equal(xyzi, w_xyzi)
+    assert torch.equal(got.offsets, want.offsets)
+    assert torch.equal(got.hkl_index, want.hkl_index)
+    assert torch.equal(got.xyzi, want.xyzi)
+
+
+@pytest.mark.parametrize("n_orient,chunk,first", [(5000, 1024, 300), (777, 16384, 4096), (3000, 1000, 1000),
+                                                   (1, 16, 16)])
+def test_streamed_equals_one_launch(n_orient, chunk, first):
+    import torch
+    from diffsims_gb300.engine import SpotBuffers, simulate_phase, simulate_phase_streamed
+    table, q, settings, r = _case(torch, n_orient)
+    want = simulate_phase(table, q, settings, r, SpotBuffers(q.device))
+    got = simulate_phase_streamed(table, q, settings, r, chunk=chunk, first_chunk=first)
+    _check(torch, got, want)
+
+
+def test_streamed_chunk_overflow_and_host_growth(monkeypatch):
+    """An estimate far too small: every chunk overflows its region and is
+    re-run, and the page-locked host arrays grow."""
+    import torch
+    from diffsims_gb300 import engine
+    table, q, settings, r = _case(torch, 2500, seed=4, model="lorentzian")
+    want = engine.simulate_phase(table, q, settings, r, engine.SpotBuffers(q.device))
+    monkeypatch.setattr(engine, "estimate_spots", lambda *a: 1)
+    got = engine.simulate_phase_streamed(table, q, settings, r, chunk=700, first_chunk=200)
+    _check(torch, got, want)
+
+
+def test_streamed_no_orientations():
+    import torch
+    from diffsims_gb300.engine import simulate_phase_streamed
+    table, q, settings, r = _case(torch, 0)
+    got = simulate_phase_streamed(table, q, settings, r)
+    off, idx, xyzi = got.host()
+    assert got.total == 0 and off.tolist() == [0] and idx.shape == (0,) and xyzi.shape == (0, 4)
+
+
+def test_calculate_diffraction2d_streamed_and_device_only_agree():
+    import diffsims_gb300 as ds
+    rng = np.random.default_rng(9)
+    cr = ok.Crystal((5.1, 6.2, 7.3, 90.0, 90.0, 90.0), ["Si"] * 4, rng.random((4, 3)), B=[0.5] * 4)
+    rot = ds.Rotation(ok.random_quaternions(6000, seed=2))
+    gen = ds.SimulationGenerator(200, shape_factor_model="linear")
+    a = gen.calculate_diffraction2d(pu.to_phase(cr), rot, reciprocal_radius=1.2)
+    b = gen.calculate_diffraction2d(pu.to_phase(cr), rot, reciprocal_radius=1.2, stream_to_host=False)
+    for x, y in zip(a.coordinates[::97], b.coordinates[::97]):
+        assert np.array_equal(x.data, y.data) and np.array_equal(x.intensity, y.intensity)
+        assert np.array_equal(x.hkl, y.hkl)
