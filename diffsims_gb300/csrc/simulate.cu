@@ -130,8 +130,8 @@ static int pick_O(const ds_sim_params *p, long long n_hkl, long long n_orient) {
     const int o_cap = p->form == DS_FORM_FP64 ? 16 : SIM_MAX_O;
     if (p->orient_tile > 0) return p->orient_tile < o_cap ? p->orient_tile : o_cap;
     int O = o_cap;
-    const long long budget = 100 * 1024;  // two CTAs per SM
-    while (O > 1 && (long long)O * Ws * 4 + O * (long long)sizeof(OrientP) > budget) O >>= 1;
+    const long long budget = sim_two_cta_smem();  // two CTAs per SM
+    while (O > 1 && (long long)sim_smem_layout(O, (int)Ws).total > budget) O >>= 1;
     // keep at least ~2 tiles per SM when the orientation count allows it
     while (O > 4 && (n_orient + O - 1) / O < 304) O >>= 1;
     return O;

@@ -55,15 +55,16 @@ static ds_status batch_plan(const ds_sim_params *p, const ds_batch_phase *ph, in
     const int o_cap = p->form == DS_FORM_FP64 ? 8 : (p->precession_mode == DS_PRECESSION_INTEGRAL ? 16 : 32);
     int O = std::min(p->orient_tile > 0 ? (int)p->orient_tile : 16, o_cap);
     O = O >= 32 ? 32 : O >= 16 ? 16 : O >= 8 ? 8 : O >= 4 ? 4 : O >= 2 ? 2 : 1;  // an instantiated tile
-    // per phase: the largest tile <= O whose bitmap fits the shared-memory
-    // budget (two CTAs per SM); the launch's bitmap holds the largest of them
-    const long long budget = 100 * 1024;
+    // per phase: the largest tile <= O whose bitmap, with the O-tile's fixed
+    // shared data, fits two CTAs per SM; the launch's bitmap holds the
+    // largest of them
+    const long long budget = sim_two_cta_smem();
     long long words = 1;
     P.n_tiles = 0;
     for (int i = 0; i < n; ++i) {
         const long long Ws = ((ph[i].table.n_hkl + 31) / 32) | 1;
         int Op = O;
-        while (Op > 1 && (long long)Op * Ws * 4 + Op * (long long)sizeof(OrientP) > budget) Op >>= 1;
+        while (Op > 1 && (long long)sim_smem_layout(O, (int)((Op * Ws + O - 1) / O)).total > budget) Op >>= 1;
         P.Op[i] = Op;
         words = std::max(words, (long long)Op * Ws);
         P.n_tiles += (ph[i].n_orient + Op - 1) / Op;

@@ -30,6 +30,7 @@
 #include <math.h>
 
 #include <string>
+#include <type_traits>
 
 #include "common.cuh"
 #include "shape.cuh"
@@ -71,6 +72,7 @@ struct SimConst {
 };
 
 struct __align__(16) OrientP {
+    float4 mz;       // m[2][0..2], 0: the screen's row, one 16-byte shared load
     float m[3][3];   // beam-frame coordinate c = sum_i m[c][i] * hkl_i   (FP32)
     float za[3];     // z column split: za on a power-of-two grid coarse enough that
     float zb[3];     //   sum_i za_i hkl_i is exact in FP32; zb = m - za (small)
@@ -608,6 +610,17 @@ struct PhaseBatch {
     PhaseP ph[SIM_BATCH_MAX];
 };
 
+// f(integral_constant<int, v>) for v a power of two <= C (1 otherwise).
+template <int C, class F>
+__device__ __forceinline__ void dispatch_pow2(int v, F &f) {
+    if constexpr (C <= 1) {
+        f(std::integral_constant<int, 1>{});
+    } else {
+        if (v >= C) f(std::integral_constant<int, C>{});
+        else dispatch_pow2<C / 2>(v, f);
+    }
+}
+
 // The orientation kernel's body.  MULTI: many phases in one persistent
 // launch, each tile of one phase; the phase's constants come from the batch
 // descriptors (copied to shared memory per tile), the rest from c.
@@ -689,7 +702,10 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
         __syncthreads();
         const long long tile = s_tile;
         const bool have_new = tile < c.n_tiles;
-        const TableP &T = PTab(cur);
+        // the table pointers: kernel parameters for one phase; for many, a
+        // register copy (a shared-memory reference would be reloaded at
+        // every use)
+        std::conditional_t<MULTI, const TableP, const TableP &> T = PTab(cur);
         const int W = PW(cur), Ws = PWs(cur);
         const long long n_hkl = PNH(cur);
         const int OP = POp(cur);  // this phase's tile (O without MULTI)
@@ -723,6 +739,7 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
                         op.M[cc][i] = v;
                         op.m[cc][i] = (float)v;
                     }
+                op.mz = make_float4(op.m[2][0], op.m[2][1], op.m[2][2], 0.f);
                 // exact-product split of the z column: grid 2^q with 2^(q+24) >= 2 sum_i |M_zi| hmax_i
                 double Z = 0.0;
                 for (int i = 0; i < 3; ++i) Z += fabs(op.M[2][i]) * (double)(MULTI ? s_ph[cur].hmax[i] : c.hmax[i]);
@@ -746,14 +763,26 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
                 // sentinel when there are none
                 const long long zero_start = min((long long)T.line_meta[1], n_hkl);
                 const int n_zero = (int)(n_hkl - zero_start);  // 0, 1 or 2
-                float mx[O], my[O], mz[O];
+                // the z rows in registers up to 16 orientations; above, one
+                // broadcast shared load per use (3 O registers would spill)
+                constexpr bool MREG = O <= 16;
+                float mx[MREG ? O : 1], my[MREG ? O : 1], mz[MREG ? O : 1];
+                if constexpr (MREG) {
 #pragma unroll
-                for (int o = 0; o < O; ++o) { mx[o] = sop[o].m[2][0]; my[o] = sop[o].m[2][1]; mz[o] = sop[o].m[2][2]; }
+                    for (int o = 0; o < O; ++o) { mx[o] = sop[o].m[2][0]; my[o] = sop[o].m[2][1]; mz[o] = sop[o].m[2][2]; }
+                }
                 for (int li = tid; li < n_lines; li += SIM_THREADS) {
                     const LineP L = T.lines[li];
 #pragma unroll
-                    for (int o = 0; o < O; ++o)
-                        if (o < n_valid) line_candidates(c, L, mx[o], my[o], mz[o], bitmap + o * Ws);
+                    for (int o = 0; o < O; ++o) {
+                        if (o >= n_valid) continue;
+                        if constexpr (MREG) {
+                            line_candidates(c, L, mx[o], my[o], mz[o], bitmap + o * Ws);
+                        } else {
+                            const float4 m4 = sop[o].mz;
+                            line_candidates(c, L, m4.x, m4.y, m4.z, bitmap + o * Ws);
+                        }
+                    }
                 }
                 // the trailing 000 rows (direct beam) are always candidates
                 for (int i = tid; i < n_valid * n_zero; i += SIM_THREADS) {
@@ -778,9 +807,12 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
                     if (lane < OP) bitmap[lane * Ws + wc] = myword;
                 }
             } else {
-                float m0[O], m1[O], m2[O];
+                constexpr bool MREG = O <= 16;  // as in the line screen
+                float m0[MREG ? O : 1], m1[MREG ? O : 1], m2[MREG ? O : 1];
+                if constexpr (MREG) {
 #pragma unroll
-                for (int o = 0; o < O; ++o) { m0[o] = sop[o].m[2][0]; m1[o] = sop[o].m[2][1]; m2[o] = sop[o].m[2][2]; }
+                    for (int o = 0; o < O; ++o) { m0[o] = sop[o].m[2][0]; m1[o] = sop[o].m[2][1]; m2[o] = sop[o].m[2][2]; }
+                }
                 // Each step screens two chunks (wc, wc + 8) with independent
                 // dependency chains; the rows of the next step are in flight.
                 // Per orientation: the sign bit of |z - z_mid| - z_half, collected
@@ -796,39 +828,52 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
                     zn[k] = -1.f;
                     if (jk < n_hkl) { en[k] = T.scr[jk]; zn[k] = T.zh[jk]; }
                 }
-                for (int wc = warp; wc < W; wc += CH * SIM_WARPS) {
-                    float4 e[CH];
-                    float zh[CH];
+                // OPC: the tile's orientation count as a constant (a power of
+                // two <= O; O without MULTI), so the unrolled per-orientation
+                // chains carry no guard and interleave freely
+                auto screen = [&](auto opc) {
+                    constexpr int OPC = decltype(opc)::value;
+                    for (int wc = warp; wc < W; wc += CH * SIM_WARPS) {
+                        float4 e[CH];
+                        float zh[CH];
 #pragma unroll
-                    for (int k = 0; k < CH; ++k) {
-                        e[k] = en[k];
-                        zh[k] = zn[k];
-                        const long long jn = ((long long)wc + (CH + k) * SIM_WARPS) * 32 + lane;
-                        en[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-                        zn[k] = -1.f;
-                        if (jn < n_hkl) { en[k] = T.scr[jn]; zn[k] = T.zh[jn]; }
-                    }
-                    uint32_t bits[CH];
+                        for (int k = 0; k < CH; ++k) {
+                            e[k] = en[k];
+                            zh[k] = zn[k];
+                            const long long jn = ((long long)wc + (CH + k) * SIM_WARPS) * 32 + lane;
+                            en[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                            zn[k] = -1.f;
+                            if (jn < n_hkl) { en[k] = T.scr[jn]; zn[k] = T.zh[jn]; }
+                        }
+                        uint32_t bits[CH];
 #pragma unroll
-                    for (int k = 0; k < CH; ++k) bits[k] = 0;
+                        for (int k = 0; k < CH; ++k) bits[k] = 0;
 #pragma unroll
-                    for (int o = 0; o < O; ++o) {
-                        if (o < OP) {  // uniform; OP = O without MULTI
+                        for (int o = 0; o < OPC; ++o) {
+                            float a0, a1, a2;
+                            if constexpr (MREG) {
+                                a0 = m0[o]; a1 = m1[o]; a2 = m2[o];
+                            } else {
+                                const float4 m4 = sop[o].mz;
+                                a0 = m4.x; a1 = m4.y; a2 = m4.z;
+                            }
 #pragma unroll
                             for (int k = 0; k < CH; ++k) {
-                                const float z = fmaf(m0[o], e[k].x, fmaf(m1[o], e[k].y, fmaf(m2[o], e[k].z, e[k].w)));
+                                const float z = fmaf(a0, e[k].x, fmaf(a1, e[k].y, fmaf(a2, e[k].z, e[k].w)));
                                 bits[k] = __funnelshift_l(__float_as_uint(fabsf(z) - zh[k]), bits[k], 1);
                             }
                         }
-                    }
 #pragma unroll
-                    for (int k = 0; k < CH; ++k) bits[k] = transpose32(bits[k], lane);
+                        for (int k = 0; k < CH; ++k) bits[k] = transpose32(bits[k], lane);
 #pragma unroll
-                    for (int k = 0; k < CH; ++k) {
-                        const int wck = wc + k * SIM_WARPS;
-                        if (lane < OP && wck < W) bitmap[(OP - 1 - lane) * Ws + wck] = bits[k];
+                        for (int k = 0; k < CH; ++k) {
+                            const int wck = wc + k * SIM_WARPS;
+                            if (lane < OPC && wck < W) bitmap[(OPC - 1 - lane) * Ws + wck] = bits[k];
+                        }
                     }
-                }
+                };
+                if constexpr (!MULTI) screen(std::integral_constant<int, O>{});
+                else dispatch_pow2<O>(OP, screen);
             }
             __syncthreads();
 
@@ -997,7 +1042,7 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
             const unsigned long long *bacc = acc_buf + bbuf * ACC_STRIDE;
             const int32_t *b_idx = stg.idx + (2 * (long long)blockIdx.x + bbuf) * stg.cap;
             const float *b_I = stg.inten + (2 * (long long)blockIdx.x + bbuf) * stg.cap;
-            const TableP &T = PTab(bbuf);
+            std::conditional_t<MULTI, const TableP, const TableP &> T = PTab(bbuf);
             const int W = PW(bbuf), Ws = PWs(bbuf);
             const int BOP = POp(bbuf);
             const long long bo_base = (btile - PT0(bbuf)) * BOP;
@@ -1141,6 +1186,17 @@ simulate_batch_kernel(SimConst c, const __grid_constant__ PhaseBatch B, int64_t 
 }
 
 // ----------------------------------------------------------- host helpers ----
+// Dynamic shared memory one CTA may take with two CTAs resident per SM (the
+// occupancy the kernels are built for), less a margin for static shared data.
+inline long long sim_two_cta_smem() {
+    int dev = 0, per_sm = 0, reserved = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess)
+        return 100 * 1024;
+    return (long long)per_sm / 2 - reserved - 512;
+}
+
 // Argument checks shared by the single-phase and batched entries.
 inline ds_status validate_params(const ds_sim_params *p, const char *who) {
     const std::string w(who);

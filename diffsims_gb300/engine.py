@@ -707,7 +707,7 @@ class Autotuner:
     and table sizes in powers of two, shape model, precession, form)."""
 
     TILES = (4, 8, 16, 32)
-    STAGES = (6144, 24576)
+    STAGE_PER_ORIENT = (384, 1536, 4096)  # staging capacity = tile x this
     CANDIDATES = TILES
 
     def __init__(self, repeats=3):
@@ -733,7 +733,7 @@ class Autotuner:
         tiles = [c for c in self.TILES if c <= (8 if fp64 else 16 if integ else 32)]
         best, best_ms, times = None, None, {}
         for c in tiles:
-            for sc in self.STAGES:
+            for sc in (c * spo for spo in self.STAGE_PER_ORIENT):
                 batch.orient_tile, batch.stage_cap = c, sc
                 p = batch.cparams()
                 if any(lib.ds_simulate_batch_scratch_bytes(p, it, len(it)) == 0 for it in batch._items):

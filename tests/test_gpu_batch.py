@@ -119,7 +119,8 @@ def test_autotuner_picks_and_caches():
     tuner = Autotuner(repeats=2)
     batch = PhaseBatch(tables, qs, settings, p.reciprocal_radius, autotuner=tuner)
     key = Autotuner.key(batch)
-    assert batch.orient_tile in Autotuner.TILES and batch.stage_cap in Autotuner.STAGES
+    assert batch.orient_tile in Autotuner.TILES
+    assert batch.stage_cap in [batch.orient_tile * s for s in Autotuner.STAGE_PER_ORIENT]
     assert tuner.cache[key] == (batch.orient_tile, batch.stage_cap) and tuner.timings[key]
     batch.run()
     again = PhaseBatch(tables, qs, settings, p.reciprocal_radius, autotuner=tuner)
