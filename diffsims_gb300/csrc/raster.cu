@@ -528,7 +528,7 @@ raster_fast_kernel(const RasterConst c, const int64_t *__restrict__ off, const f
         }
         const int n = (int)n_ll;
         int Tp = 64;
-        while (Tp < 2 * n) Tp <<= 1;
+        while (Tp < n + n / 2) Tp <<= 1;
         const int tbits = __ffs(Tp) - 1;
         for (int t = tid; t < Tp; t += RAS_THREADS) {
             A.hkey[t] = -1;
@@ -551,7 +551,7 @@ raster_fast_kernel(const RasterConst c, const int64_t *__restrict__ off, const f
             if (in_frame(c, X, Y)) {
                 ++my_in;
                 key = (int)Y * W + (int)X;
-                // open addressing; Tp >= 2 n slots, so a free slot is always found
+                // open addressing; Tp >= 1.5 n slots, so a free slot is always found
                 unsigned h = ((unsigned)key * 2654435761u) >> (32 - tbits);
                 for (int t = 0; t < Tp; ++t) {
                     const int prev = atomicCAS(&A.hkey[h], -1, key);
@@ -815,11 +815,11 @@ static ds_status raster_plan(const ds_raster_params *p, int64_t max_spots, Raste
     DS_REQUIRE(max_spots >= 0 && max_spots < (1ll << 28), "ds_rasterize: max_spots out of range");
     DS_REQUIRE(!p->fast || max_spots <= 65504, "ds_rasterize: at most 65504 spots per pattern in fast mode");
     int NS = (int)std::max<int64_t>(32, (max_spots + 31) / 32 * 32);
+    const bool fast = p->fast != 0;
     int T = 64;
-    while (T < 2 * NS) T <<= 1;
+    while (fast ? T < NS + NS / 2 : T < 2 * NS) T <<= 1;  // the kernels' per-pattern hash sizes
     P.NS = NS;
     P.T = T;
-    const bool fast = p->fast != 0;
     P.one_pass = fast && p->normalize && (p->width % 4) == 0 && fast_flag_bytes(p->height, p->width) <= RAS_FLAGS_MAX;
     P.arena = fast ? fast_arena_bytes(NS, T, p->height, 2 * filter_radius(p) + 1,
                                       P.one_pass ? fast_flag_bytes(p->height, p->width) : 0)
