@@ -122,13 +122,17 @@ inline LookbackScratch lookback_scratch(void *base) {
     return {p, p + 32};
 }
 
+// A state word carries its flag and value together and no other data is
+// handed over through it, so relaxed gpu-scope accesses suffice.  (A release
+// store would wait for every write the CTA issued before the barrier that
+// precedes it -- a whole tile's staging -- before publishing.)
 __device__ __forceinline__ unsigned long long lb_load(const unsigned long long *p) {
     unsigned long long v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
 __device__ __forceinline__ void lb_store(unsigned long long *p, unsigned long long v) {
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
 // Publish a tile's count (its inclusive prefix directly for tile 0).  ONE thread.
@@ -225,6 +229,16 @@ __device__ __forceinline__ int warp_inclusive_scan(int v, int lane) {
         if (lane >= d) v += n;
     }
     return v;
+}
+
+__device__ __forceinline__ long long warp_exclusive_scan_ll(long long v, int lane) {
+    long long incl = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const long long n = __shfl_up_sync(FULL_MASK, incl, d);
+        if (lane >= d) incl += n;
+    }
+    return incl - v;
 }
 
 }  // namespace ds

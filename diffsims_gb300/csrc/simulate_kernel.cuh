@@ -29,6 +29,7 @@
 #pragma once
 #include <math.h>
 
+#include <cmath>
 #include <string>
 #include <type_traits>
 
@@ -68,6 +69,8 @@ struct SimConst {
     double int_step;                // precession average: breakpoint spacing in s (0: none)
     float int_step_f, mw_f;
     float int_tau;                  // precession average: FP32 result below this -> FP64
+    int mask_on, zero_drop;         // thr > 0, thr >= 0 (the FP64 compares done once, on the host)
+    float thr_up;                   // >= thr, with margin: FP32 pre-check of I <= max * thr
     long long n_hkl, n_orient, n_tiles, capacity;
 };
 
@@ -647,7 +650,7 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
     // phases 2-3 run over units (orientation, part): NP word ranges per
     // orientation, taken by warps from a shared counter for load balance
     constexpr int NP = O >= 2 ? DS_SIM_PARTS : 8;
-    const bool all_zero_drop = c.thr >= 0.0;
+    const bool all_zero_drop = c.zero_drop != 0;
     const unsigned lanemask_lt = (1u << lane) - 1u;
     auto part_range = [&](int Wp, int p, int &w0, int &w1) {
         w0 = (int)(((long long)Wp * p) / NP);
@@ -714,18 +717,24 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
         const int n_units = n_valid * NP;
         if (have_new) {
             // ---------------- per-orientation rotation: beam frame = g @ R, R the active matrix of q
-            if (tid < O) {
-                OrientP &op = sop[tid];
+            // Orientation lane * 4 + warp on warps 0-3: the FP64 work (a warp
+            // instruction holds its sub-partition's FP64 pipe for many
+            // cycles whatever its active lanes) spread over the four SM
+            // sub-partitions.
+            const int orot = lane * 4 + warp;
+            if (warp < 4 && orot < O) {
+                OrientP &op = sop[orot];
                 double R[3][3];
-                if (tid < n_valid) {
-                    const double *q = (MULTI ? s_ph[cur].quats : quats1) + 4 * (o_base + tid);
+                if (orot < n_valid) {
+                    const double *q = (MULTI ? s_ph[cur].quats : quats1) + 4 * (o_base + orot);
                     double w = q[0], x = q[1], y = q[2], z = q[3];
                     double nrm = sqrt(w * w + x * x + y * y + z * z);
                     if (!(nrm > 0) || !isfinite(nrm)) {
                         atomicOr(status, DS_ERR_NONFINITE);
                         nrm = 1; w = 1; x = y = z = 0;
                     }
-                    w /= nrm; x /= nrm; y /= nrm; z /= nrm;
+                    const double inv = 1.0 / nrm;
+                    w *= inv; x *= inv; y *= inv; z *= inv;
                     R[0][0] = 1 - 2 * (y * y + z * z); R[0][1] = 2 * (x * y - w * z); R[0][2] = 2 * (x * z + w * y);
                     R[1][0] = 2 * (x * y + w * z); R[1][1] = 1 - 2 * (x * x + z * z); R[1][2] = 2 * (y * z - w * x);
                     R[2][0] = 2 * (x * z - w * y); R[2][1] = 2 * (y * z + w * x); R[2][2] = 1 - 2 * (x * x + y * y);
@@ -890,17 +899,25 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
                 if (lane == 0) acc[o * ACC_WORDS + ACC_CCNT0 + p] = (unsigned long long)cnt;
             }
             __syncthreads();
-            if (tid == 0) {
-                long long run = 0;
-                for (int u = 0; u < n_units; ++u) {
-                    const int o = u / NP, p = u % NP;
-                    const long long cc = (long long)acc[o * ACC_WORDS + ACC_CCNT0 + p];
-                    if (run + cc <= stg.cap) {
-                        acc[o * ACC_WORDS + ACC_CBASE0 + p] = (unsigned long long)run;
-                        run += cc;
-                    } else {
-                        acc[o * ACC_WORDS + ACC_CBASE0 + p] = NO_STAGE;
-                    }
+            if (warp == 0) {
+                // staging bases: the units in (orientation, part) order, the
+                // longest prefix that fits the staging is staged
+                constexpr int UPL = (O * NP + 31) / 32;  // units per lane
+                long long cc[UPL], sum = 0;
+#pragma unroll
+                for (int i = 0; i < UPL; ++i) {
+                    const int u = lane * UPL + i;
+                    cc[i] = u < n_units ? (long long)acc[(u / NP) * ACC_WORDS + ACC_CCNT0 + u % NP] : 0ll;
+                    sum += cc[i];
+                }
+                long long run = warp_exclusive_scan_ll(sum, lane);
+#pragma unroll
+                for (int i = 0; i < UPL; ++i) {
+                    const int u = lane * UPL + i;
+                    if (u < n_units)
+                        acc[(u / NP) * ACC_WORDS + ACC_CBASE0 + u % NP] =
+                            run + cc[i] <= stg.cap ? (unsigned long long)run : NO_STAGE;
+                    run += cc[i];
                 }
             }
             __syncthreads();
@@ -975,7 +992,21 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
             __syncthreads();
 
             // ---------------- mask pass (only where some I is positive but <= max * thr)
-            if (c.thr > 0.0) {
+            bool need_mask = false;
+            if (c.mask_on) {
+                bool nm = false;
+                for (int o = lane; o < n_valid; o += 32) {
+                    const float mx = __uint_as_float((unsigned)acc[o * ACC_WORDS + ACC_MAXI]);
+                    const float mnp = __uint_as_float((unsigned)acc[o * ACC_WORDS + ACC_MINPOS]);
+                    // FP32 first: t bounds max * thr from above unless it is
+                    // near the FP32 underflow; only then the exact FP64 test
+                    // (FP64 instructions are scarce here and queue behind others)
+                    const float t = mx * c.thr_up;
+                    if (!(mnp > t * 1.000002f) || t < 1e-30f) nm = nm || (double)mnp <= (double)mx * c.thr;
+                }
+                need_mask = __any_sync(FULL_MASK, nm);
+            }
+            if (need_mask) {
                 for (int u = next_unit(1); u < n_units; u = next_unit(1)) {
                     const int o = u / NP, p = u % NP;
                     const float mx = __uint_as_float((unsigned)acc[o * ACC_WORDS + ACC_MAXI]);
@@ -1016,22 +1047,30 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
             }
 
             // ---------------- tile count, published for the look-back of later tiles
-            if (tid == 0) {
-                long long run = 0;
-                int defer = 1;
-                for (int o = 0; o < n_valid; ++o) {
-                    acc[o * ACC_WORDS + ACC_OFF] = (unsigned long long)run;
-                    long long co = 0;
+            if (warp == 0) {
+                // per orientation (one lane each; O <= 32): kept count and
+                // offset within the tile; the tile total, published
+                long long co = 0;
+                bool staged = true;
+                if (lane < n_valid) {
+#pragma unroll
                     for (int p = 0; p < NP; ++p) {
-                        co += (long long)acc[o * ACC_WORDS + ACC_PART0 + p];
-                        if (acc[o * ACC_WORDS + ACC_CBASE0 + p] == NO_STAGE) defer = 0;
+                        co += (long long)acc[lane * ACC_WORDS + ACC_PART0 + p];
+                        staged = staged && acc[lane * ACC_WORDS + ACC_CBASE0 + p] != NO_STAGE;
                     }
-                    acc[o * ACC_WORDS + ACC_CNT] = (unsigned long long)co;
-                    run += co;
                 }
-                acc[ACC_TILE_TOTAL] = (unsigned long long)run;
-                lookback_publish(lb, tile, run);
-                s_defer = defer;
+                const long long excl = warp_exclusive_scan_ll(co, lane);
+                if (lane < n_valid) {
+                    acc[lane * ACC_WORDS + ACC_OFF] = (unsigned long long)excl;
+                    acc[lane * ACC_WORDS + ACC_CNT] = (unsigned long long)co;
+                }
+                const long long run = __shfl_sync(FULL_MASK, excl + co, 31);
+                const bool defer = __all_sync(FULL_MASK, staged);
+                if (lane == 0) {
+                    acc[ACC_TILE_TOTAL] = (unsigned long long)run;
+                    lookback_publish(lb, tile, run);
+                    s_defer = defer ? 1 : 0;
+                }
             }
             __syncthreads();
         }  // have_new
@@ -1226,6 +1265,9 @@ inline void fill_const(const ds_sim_params *p, const ds_phase_table *t, SimConst
     c.width = p->shape_width;
     c.phi = p->precession_angle;
     c.thr = p->minimum_intensity;
+    c.mask_on = c.thr > 0.0;
+    c.zero_drop = c.thr >= 0.0;
+    c.thr_up = std::nextafter((float)(c.thr * (1.0 + 1e-6)), INFINITY);
     c.minima = p->minima_number;
     c.Pz = p->k0 * cos(p->precession_angle);
     c.Pt = p->k0 * sin(p->precession_angle);
