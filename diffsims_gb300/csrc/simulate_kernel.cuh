@@ -994,17 +994,26 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
             // ---------------- mask pass (only where some I is positive but <= max * thr)
             bool need_mask = false;
             if (c.mask_on) {
-                bool nm = false;
+                // FP32 first: t bounds max * thr from above unless it is near
+                // the FP32 underflow; the exact FP64 test only where that
+                // cannot decide (a warp-uniform branch: FP64 instructions are
+                // scarce on this part and queue behind others)
+                bool maybe = false;
                 for (int o = lane; o < n_valid; o += 32) {
                     const float mx = __uint_as_float((unsigned)acc[o * ACC_WORDS + ACC_MAXI]);
                     const float mnp = __uint_as_float((unsigned)acc[o * ACC_WORDS + ACC_MINPOS]);
-                    // FP32 first: t bounds max * thr from above unless it is
-                    // near the FP32 underflow; only then the exact FP64 test
-                    // (FP64 instructions are scarce here and queue behind others)
                     const float t = mx * c.thr_up;
-                    if (!(mnp > t * 1.000002f) || t < 1e-30f) nm = nm || (double)mnp <= (double)mx * c.thr;
+                    maybe = maybe || !(mnp > t * 1.000002f) || t < 1e-30f;
                 }
-                need_mask = __any_sync(FULL_MASK, nm);
+                if (__any_sync(FULL_MASK, maybe)) {
+                    bool nm = false;
+                    for (int o = lane; o < n_valid; o += 32) {
+                        const float mx = __uint_as_float((unsigned)acc[o * ACC_WORDS + ACC_MAXI]);
+                        const float mnp = __uint_as_float((unsigned)acc[o * ACC_WORDS + ACC_MINPOS]);
+                        nm = nm || (double)mnp <= (double)mx * c.thr;
+                    }
+                    need_mask = __any_sync(FULL_MASK, nm);
+                }
             }
             if (need_mask) {
                 for (int u = next_unit(1); u < n_units; u = next_unit(1)) {
