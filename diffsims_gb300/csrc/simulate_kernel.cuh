@@ -530,20 +530,31 @@ __device__ __forceinline__ void for_each_bit_pair(const uint32_t *row, int w0, i
 // Set bits of bitmap words [w0, w1) of one orientation in row order, as dense
 // pairs: lanes append the rows of their own set bits to a per-warp queue in
 // shared memory (their places known from one scan of the popcounts: no lane
-// searches for its candidate), and full queues are handed to fn two per lane:
-// fn(j0, rank0, valid0, j1, rank1, valid1).  A group denser than the queue is
-// appended in several rounds.
-template <int K, typename Fn>
+// searches for its candidate), and full queues are evaluated one candidate
+// per lane per round: load(j, valid) fetches a candidate's data, eval(j,
+// rank, data) uses it.  A group denser than the queue is appended in
+// several rounds.
+template <int K, typename Load, typename Eval>
 __device__ __forceinline__ void for_each_bit_queued(const uint32_t *row, int w0, int w1, int lane, int32_t *q,
-                                                    Fn fn) {
+                                                    Load load, Eval eval) {
     int qn = 0, rank_base = 0;
+    // one candidate per lane per round; the next round's table data is
+    // loaded before this round is evaluated, so the gather latency overlaps
+    // the evaluation (one exposed latency per flush)
     auto flush = [&]() {
         __syncwarp();
-        for (int r0 = 0; r0 < qn; r0 += 64) {
-            const int ra = r0 + lane, rb = r0 + 32 + lane;
-            const bool va = ra < qn, vb = rb < qn;
-            const long long ja = va ? (long long)q[ra] : 0, jb = vb ? (long long)q[rb] : 0;
-            fn(ja, rank_base + ra, va, jb, rank_base + rb, vb);
+        bool vc = lane < qn;
+        long long jc = vc ? (long long)q[lane] : 0;
+        auto cur = load(jc, vc);
+        for (int r0 = 0; r0 < qn; r0 += 32) {
+            const int rn = r0 + 32 + lane;
+            const bool vn = rn < qn;
+            const long long jn = vn ? (long long)q[rn] : 0;
+            const auto nxt = load(jn, vn);
+            if (vc) eval(jc, rank_base + r0 + lane, cur);
+            cur = nxt;
+            jc = jn;
+            vc = vn;
         }
         rank_base += qn;
         qn = 0;
@@ -935,30 +946,26 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
                 if (base != NO_STAGE) {
                     // evaluate each screened candidate once; stage (row, x, y, z, I)
                     // in candidate order, I = -1 for rejected candidates
-                    for_each_bit_queued<4>(row, w0, w1, lane, wqueue,
-                                           [&](long long ja, int ra, bool va, long long jb, int rb, bool vb) {
-                        SpotIn ia, ib;
-                        if (va) ia = load_spot<FORM>(T, ja);
-                        if (vb) ib = load_spot<FORM>(T, jb);
-#pragma unroll
-                        for (int h = 0; h < 2; ++h) {
-                            const bool v = h ? vb : va;
-                            if (!v) continue;
-                            const SpotIn &in = h ? ib : ia;
-                                float I, z;
+                    for_each_bit_queued<4>(
+                        row, w0, w1, lane, wqueue,
+                        [&](long long j, bool v) {
+                            SpotIn in;
+                            if (v) in = load_spot<FORM>(T, j);
+                            return in;
+                        },
+                        [&](long long j, int rk, const SpotIn &in) {
+                            float I, z;
                             double sv;
                             bool sel = eval_in<FORM, INTEG>(c, op, in, I, z, sv);
                             if (sel && I == 0.f && all_zero_drop) sel = false;
-                            const int rk = h ? rb : ra;
-                            my_idx[base + rk] = (int32_t)(h ? jb : ja);
+                            my_idx[base + rk] = (int32_t)j;
                             my_I[base + rk] = sel ? I : -1.f;
                             if (sel) {
                                 ++lcnt;
                                 lmax = fmaxf(lmax, I);
                                 if (I > 0.f) lminpos = fminf(lminpos, I);
                             }
-                        }
-                    });
+                        });
                 } else {
                     for_each_bit(row, w0, w1, lane, [&](long long j, int, bool valid, int wi, int bit) {
                         if (!valid) return;
