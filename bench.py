@@ -21,7 +21,10 @@ Arms:
                     "batched_phases" (32 uneven phases in one launch, graph
                     replay, tile by the autotuner),
                     "template_library" (three phases simulated and rasterised
-                    to 256x256 detectors in 8192-orientation chunks).
+                    to 256x256 detectors in 8192-orientation chunks),
+                    "family_structure_factors" (Doyle-Turner structure
+                    factors of 2^20 lattice-plane families in one launch,
+                    against the oracle's per-family loop on one core).
   --impl reference  the reference's CPU path restated in numpy (the FP64
                     oracle) on all host cores, a bounded sample per step.
 
@@ -336,6 +339,7 @@ def run_gpu(args):
     grad = None if args.skip_grad else run_grad(args, torch, dev)
     batched = None if args.skip_batch else run_batch(args, torch, dev)
     library = None if args.skip_library else run_library(args, torch, dev, hbm_peak)
+    families = None if args.skip_families else run_families(args, torch, dev)
 
     cpu = None
     if not args.no_cpu_baseline:
@@ -366,6 +370,7 @@ def run_gpu(args):
         "grad": grad,
         "batched_phases": batched,
         "template_library": library,
+        "family_structure_factors": families,
         "cpu_baseline": cpu,
         "clocks": clocks,
         "gpu_launches": 5 * args.steps,
@@ -509,6 +514,84 @@ def run_batch(args, torch, dev):
             "orientations_range": [min(int(q.shape[0]) for q in qs), max(int(q.shape[0]) for q in qs)],
             "table_build_s": table_s, "launches_per_step": len(tables) + 2,
             "config": {k: v for k, v in W.items()}}
+
+
+def run_families(args, torch, dev):
+    """Per-family structure factors (diffsims/structure_factor/structure_factor.py:103-185):
+    2^20 Doyle-Turner families at 200 kV of a mixed site at a general
+    position of Pm-3m (two 48-position orbits), one ds_family_structure_factors
+    launch; and the public call from host arrays (copies in, values out)."""
+    from diffsims_gb300 import _native as N
+    from diffsims_gb300 import structure_factor as gsf
+    from diffsims_gb300.crystal import Atom, Lattice, Phase, Structure
+    from oracle import structure_factor_families as osf
+    lib = N.load_library()
+    ops = osf.space_group_operations(221)
+    atoms = [Atom("Fe", [0.11, 0.23, 0.37], 0.6, 0.005), Atom("Ni", [0.11, 0.23, 0.37], 0.4, 0.009),
+             Atom("O", [0.5, 0.5, 0.5], 1.0, 0.011)]
+    phase = Phase(structure=Structure(atoms, Lattice(4.1, 4.1, 4.1)), space_group=ops)
+    rng = np.random.default_rng(3)
+    n = 1 << 20
+    hkl = rng.integers(-25, 26, (n, 3)).astype(np.float64)
+    s = np.sqrt(np.sum(hkl * hkl, axis=1)) / (2 * 4.1)
+    sites = gsf._asymmetric_sites(phase.structure, phase.space_group)
+    n_pos = sum(len(p) for _, p, _, _ in sites)
+    volume = phase.structure.lattice.volume
+    # device-resident launch
+    from diffsims_gb300.sim_utils import PackedAtoms
+    species, rows, xyz, occ, B = [], [], [], [], []
+    for k, (z, positions, o, biso) in enumerate(sites):
+        rows.append(gsf._coeff_row(z, N.DS_SCATTER_DOYLETURNER, volume))
+        for p in positions:
+            species.append(k); xyz.append(p); occ.append(o); B.append(4.0 * biso)
+    packed = PackedAtoms.from_rows(species, rows, np.asarray(xyz), occ, B, N.DS_SCATTER_DOYLETURNER, dev)
+    hkl_d = torch.from_numpy(hkl).to(dev)
+    s_d = torch.from_numpy(s).to(dev)
+    F = torch.empty((n, 2), dtype=torch.float64, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    st = torch.cuda.current_stream()
+
+    def launch():
+        N.check(lib.ds_family_structure_factors(packed.cstruct(), N.ptr(hkl_d), N.ptr(s_d), n, N.ptr(F),
+                                                N.ptr(status), N.stream_handle()), "families")
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            fn()
+            e1.record(st)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return statistics.mean(ms)
+
+    k_ms = timed(launch)
+    N.check_device_status(status, "families")
+    t_e2e = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        gsf.get_doyleturner_structure_factor(phase, hkl, s, 200e3)
+        if i >= args.warmup:
+            t_e2e.append(time.perf_counter() - t0)
+    # the oracle's per-family loop (the reference's algorithm) on one core, a bounded sample
+    atoms_o = [(a.element, a.xyz, a.occupancy, a.Bisoequiv) for a in atoms]
+    n_cpu = 2000
+    t0 = time.perf_counter()
+    for i in range(n_cpu):
+        osf.doyleturner_structure_factor(atoms_o, ops, hkl[i], s[i], volume, 200e3)
+    cpu_rate = n_cpu / (time.perf_counter() - t0)
+    return {"metric": "lattice-plane families/s (Doyle-Turner structure factor, 200 kV)",
+            "value": n / (k_ms * 1e-3), "unit": "families/s", "kernel_ms": k_ms, "families": n,
+            "orbit_positions": n_pos, "terms_per_s": n * n_pos / (k_ms * 1e-3),
+            "e2e": {"value": n / statistics.mean(t_e2e), "unit": "families/s",
+                    "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 8},
+            "cpu_baseline": {"value": cpu_rate, "unit": "families/s", "cores": 1, "kind": "port",
+                             "sample": f"{n_cpu} families, FP64 numpy restatement of the reference's per-family loop"},
+            "dtype": "f64"}
 
 
 def run_library(args, torch, dev, hbm_peak):
@@ -736,6 +819,7 @@ def main():
     ap.add_argument("--skip-grad", action="store_true", help="leave out the gradient-step leg")
     ap.add_argument("--skip-library", action="store_true", help="leave out the template-library leg")
     ap.add_argument("--skip-batch", action="store_true", help="leave out the batched-phases leg")
+    ap.add_argument("--skip-families", action="store_true", help="leave out the per-family structure-factor leg")
     ap.add_argument("--case", default=None, choices=["raster", "adjoint", "batch"],
                     help="run one small profiling case instead of the benchmark")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -28,6 +28,8 @@ DS_FORM_MIXED = 0
 DS_FORM_FP64 = 1
 
 DS_SCATTER = {"lobato": 0, "xtables": 1, None: 2}
+DS_SCATTER_KINEMATICAL = 3
+DS_SCATTER_DOYLETURNER = 4
 DS_SHAPE = {"linear": 0, "atanc": 1, "sinc": 2, "sin2c": 3, "lorentzian": 4, "binary": 5}
 DS_SCREEN = {"auto": 0, "rows": 1, "lines": 2}
 DS_PRECESSION_NONE = 0
@@ -37,7 +39,7 @@ DS_PRECESSION_INTEGRAL = 2
 EXPORTED_SYMBOLS = (
     "ds_box_extent", "ds_enumerate_scratch_bytes", "ds_enumerate_hkl",
     "ds_structure_factor_scratch_bytes", "ds_structure_factors", "ds_kinematical_intensities",
-    "ds_simulate_scratch_bytes", "ds_simulate", "ds_simulate_batch_scratch_bytes", "ds_simulate_batch_tile",
+    "ds_family_structure_factors", "ds_simulate_scratch_bytes", "ds_simulate", "ds_simulate_batch_scratch_bytes", "ds_simulate_batch_tile",
     "ds_simulate_batch", "ds_rasterize_scratch_bytes", "ds_rasterize",
     "ds_simulate_backward_scratch_bytes", "ds_simulate_backward", "ds_structure_factors_backward_scratch_bytes",
     "ds_axis_angle_compose", "ds_axis_angle_compose_backward", "ds_polar_flatten", "ds_structure_factors_backward",
@@ -113,6 +115,7 @@ def load_library(require_cuda: bool = True):
             lib.ds_structure_factor_scratch_bytes.restype = sz
             lib.ds_structure_factors.argtypes = [C.POINTER(ds_atoms), vp, vp, vp, i64, i32, vp, vp, vp, vp, sz, vp, vp]
             lib.ds_kinematical_intensities.argtypes = [C.POINTER(ds_atoms), vp, vp, vp, i64, vp, vp, sz, vp, vp]
+            lib.ds_family_structure_factors.argtypes = [C.POINTER(ds_atoms), vp, vp, i64, vp, vp, vp]
             lib.ds_simulate_scratch_bytes.argtypes = [C.POINTER(ds_sim_params), C.POINTER(ds_phase_table), i64]
             lib.ds_simulate_scratch_bytes.restype = sz
             lib.ds_simulate.argtypes = [C.POINTER(ds_sim_params), C.POINTER(ds_phase_table), vp, i64,
@@ -141,6 +144,7 @@ def load_library(require_cuda: bool = True):
             lib.ds_last_error.restype = C.c_char_p
             lib.ds_version.restype = C.c_char_p
             for name in ("ds_box_extent", "ds_enumerate_hkl", "ds_structure_factors", "ds_kinematical_intensities",
+                         "ds_family_structure_factors",
                          "ds_simulate", "ds_simulate_batch", "ds_rasterize", "ds_simulate_backward",
                          "ds_structure_factors_backward",
                          "ds_axis_angle_compose", "ds_axis_angle_compose_backward", "ds_polar_flatten",

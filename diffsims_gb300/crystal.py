@@ -46,6 +46,12 @@ class Lattice:
         return np.linalg.inv(self.base)
 
     @property
+    def volume(self) -> float:
+        """Cell volume (Angstrom^3), as diffpy ``Lattice.volume``."""
+        ca, cb, cg = np.cos(np.deg2rad([self.alpha, self.beta, self.gamma]))
+        return float(self.a * self.b * self.c * math.sqrt(1 + 2 * ca * cb * cg - ca * ca - cb * cb - cg * cg))
+
+    @property
     def reciprocal_base(self) -> np.ndarray:
         """Rows a*, b*, c* (no 2 pi): g = hkl @ reciprocal_base."""
         return np.linalg.inv(self.base).T
@@ -67,9 +73,15 @@ class Atom:
     element: str
     xyz: Sequence[float]
     occupancy: float = 1.0
+    Uisoequiv: float = 0.0
 
     def __post_init__(self):
         self.xyz = np.asarray(self.xyz, dtype=np.float64)
+
+    @property
+    def Bisoequiv(self) -> float:
+        """Isotropic Debye-Waller B = 8 pi^2 U (Angstrom^2), as diffpy ``Atom``."""
+        return 8 * math.pi ** 2 * self.Uisoequiv
 
 
 class Structure(list):

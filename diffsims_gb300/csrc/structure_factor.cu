@@ -64,9 +64,20 @@ __device__ __forceinline__ void load_hkl(const SfConst &c, const int32_t *hkl_i,
     }
 }
 
-// f_s(g^2) -- the formulas of diffsims/utils/sim_utils.py:249-253
+// f_s(g^2) -- the formulas of diffsims/utils/sim_utils.py:249-253.  For the
+// two per-family kinds the argument is s^2 = (|g|/2)^2 and the row holds four
+// Doyle-Turner pairs plus a constant c0 in slot 8:
+//   kinematical  f = c0 - 41.78214 s^2 sum_i a_i exp(-b_i s^2), c0 = Z
+//                (diffsims/structure_factor/atomic_scattering_factor.py:55-60)
+//   Doyle-Turner f = c0 sum_i a_i exp(-b_i s^2), c0 = 47.87801 / V
+//                (diffsims/structure_factor/atomic_scattering_factor.py:111-114)
 __device__ __forceinline__ double scatter_f64(const double *cf, int kind, double g2) {
     if (kind == DS_SCATTER_NONE) return 1.0;
+    if (kind >= DS_SCATTER_KINEMATICAL) {
+        double sum = 0.0;
+        for (int i = 0; i < 4; ++i) sum += cf[2 * i] * exp(-cf[2 * i + 1] * g2);
+        return kind == DS_SCATTER_KINEMATICAL ? cf[8] - 41.78214 * g2 * sum : cf[8] * sum;
+    }
     double f = 0.0;
     for (int i = 0; i < 5; ++i) {
         double a = cf[2 * i], b = cf[2 * i + 1];
@@ -357,6 +368,26 @@ extern "C" ds_status ds_structure_factors(const ds_atoms *atoms, const int32_t *
     else st = launch_mixed<8>(c, *atoms, hkl_i, hkl_d, g2, F2, F2d, F, queue, queue_len, status, s);
     if (st) return st;
     return launch_fp64(c, *atoms, hkl_i, hkl_d, g2, nullptr, F2, F2d, F, queue, queue_len, n, status, s);
+}
+
+extern "C" ds_status ds_family_structure_factors(const ds_atoms *atoms, const double *hkl_d,
+                                                 const double *scattering_parameter, int64_t n, double *F,
+                                                 int32_t *status, void *stream) {
+    clear_error();
+    DS_REQUIRE(atoms && atoms->atoms && atoms->coeffs, "ds_family_structure_factors: null atoms");
+    DS_REQUIRE(atoms->n_atoms >= 1, "ds_family_structure_factors: n_atoms must be >= 1");
+    DS_REQUIRE(atoms->n_species >= 1 && atoms->n_species <= SF_MAX_SPECIES,
+               "ds_family_structure_factors: n_species must be in [1, 32]");
+    DS_REQUIRE(atoms->kind == DS_SCATTER_KINEMATICAL || atoms->kind == DS_SCATTER_DOYLETURNER,
+               "ds_family_structure_factors: kind must be DS_SCATTER_KINEMATICAL or DS_SCATTER_DOYLETURNER");
+    DS_REQUIRE(((uintptr_t)atoms->atoms & 15) == 0, "ds_family_structure_factors: atoms must be 16-byte aligned");
+    DS_REQUIRE(hkl_d && scattering_parameter && F && status, "ds_family_structure_factors: null pointer");
+    DS_REQUIRE(n >= 0, "ds_family_structure_factors: n < 0");
+    if (n == 0) return DS_OK;
+    // g_is_spacing squares the per-reflection input: the kernel sees s^2
+    SfConst c{n, atoms->n_atoms, atoms->n_species, atoms->kind, 0, 1, 0};
+    return launch_fp64(c, *atoms, nullptr, hkl_d, scattering_parameter, nullptr, nullptr, nullptr, F, nullptr,
+                       nullptr, n, status, (cudaStream_t)stream);
 }
 
 extern "C" ds_status ds_kinematical_intensities(const ds_atoms *atoms, const double *hkl_d, const double *g_spacing,

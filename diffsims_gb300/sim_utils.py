@@ -75,9 +75,20 @@ class PackedAtoms:
                                       "scattering parameter library.")
                 coeff_rows.append(row)
             species.append(index[sym])
+        self._fill(species, coeff_rows, xyz, occupancy, B, N.DS_SCATTER[scattering_params], device)
+
+    @classmethod
+    def from_rows(cls, species, coeff_rows, xyz, occupancy, B, kind, device):
+        """Records from explicit per-species coefficient rows (10 doubles
+        each) and a ``DS_SCATTER_*`` kind."""
+        out = cls.__new__(cls)
+        out._fill(species, coeff_rows, xyz, occupancy, B, kind, device)
+        return out
+
+    def _fill(self, species, coeff_rows, xyz, occupancy, B, kind, device):
         if len(coeff_rows) > 32:
             raise ValueError("at most 32 distinct elements per phase are supported")
-        n = len(elements)
+        n = len(species)
         rec = np.zeros(n, dtype=[("x", "f8"), ("y", "f8"), ("z", "f8"), ("occ", "f8"), ("B", "f8"),
                                  ("species", "i4"), ("pad", "i4")])
         xyz = np.asarray(xyz, dtype=np.float64).reshape(-1, 3)
@@ -90,7 +101,7 @@ class PackedAtoms:
         self.coeffs = torch.from_numpy(np.asarray(coeff_rows, dtype=np.float64).reshape(-1)).to(device)
         self.n_atoms = n
         self.n_species = len(coeff_rows)
-        self.kind = N.DS_SCATTER[scattering_params]
+        self.kind = kind
 
     def cstruct(self) -> N.ds_atoms:
         return N.ds_atoms(self.n_atoms, self.n_species, self.records.data_ptr(), self.coeffs.data_ptr(),

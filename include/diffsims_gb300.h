@@ -38,8 +38,11 @@ enum {
 enum { DS_FORM_MIXED = 0, /* FP32 bulk, FP64 phase reduction + FP64 s near the cutoff */
        DS_FORM_FP64 = 1   /* plain all-FP64 comparator                              */ };
 
-/* scattering factor parameterisation (diffsims/utils/sim_utils.py:139-162,227-253) */
-enum { DS_SCATTER_LOBATO = 0, DS_SCATTER_XTABLES = 1, DS_SCATTER_NONE = 2 };
+/* scattering factor parameterisation (diffsims/utils/sim_utils.py:139-162,227-253);
+ * the last two serve ds_family_structure_factors only
+ * (diffsims/structure_factor/atomic_scattering_factor.py:27-124) */
+enum { DS_SCATTER_LOBATO = 0, DS_SCATTER_XTABLES = 1, DS_SCATTER_NONE = 2,
+       DS_SCATTER_KINEMATICAL = 3, DS_SCATTER_DOYLETURNER = 4 };
 
 /* rel-rod shape models (diffsims/utils/shape_factor_models.py) */
 enum { DS_SHAPE_LINEAR = 0, DS_SHAPE_ATANC = 1, DS_SHAPE_SINC = 2, DS_SHAPE_SIN2C = 3,
@@ -113,6 +116,21 @@ ds_status ds_structure_factors(const ds_atoms *atoms, const int32_t *hkl_i, cons
                                const double *g2, int64_t n, int32_t form, float *F2, double *F2d,
                                double *F, void *scratch, size_t scratch_bytes, int32_t *status,
                                void *stream);
+
+/* Structure factors of lattice-plane families, batched over n reflections:
+ * get_kinematical_structure_factor and get_doyleturner_structure_factor
+ * (diffsims/structure_factor/structure_factor.py:55-185) before their scalar
+ * epilogues.  F[2i], F[2i+1] = sum_j f_j(s_i) occ_j exp(-B_j s_i^2) (cos, +sin)
+ * (2 pi h_i.x_j), all FP64 with the phase reduced modulo 1 first; the
+ * reference's sign is exp(-2 pi i h.x), i.e. the conjugate.  atoms->kind is
+ * DS_SCATTER_KINEMATICAL or DS_SCATTER_DOYLETURNER; each coeffs row holds
+ * a1,b1,...,a4,b4 (Doyle-Turner, 1/Angstrom^2), then c0 (Z, or 47.87801 / unit
+ * cell volume) and 0; each record's B holds 4 x Bisoequiv (the kernel's
+ * Debye-Waller term is exp(-B s^2 / 4) in s = scattering_parameter).  The atom
+ * list is the expanded orbit (the caller applies the space group). */
+ds_status ds_family_structure_factors(const ds_atoms *atoms, const double *hkl_d,
+                                      const double *scattering_parameter, int64_t n, double *F,
+                                      int32_t *status, void *stream);
 
 /* get_kinematical_intensities (diffsims/utils/sim_utils.py:307-354):
  * out[i] = prefactor[i] * |F_i|^2 with |g| given (not derived from the lattice).

@@ -14,7 +14,14 @@ need the reference.  What it does:
   a stub module -- sim_utils uses it only in docstrings) and records their
   outputs on seeded inputs: wavelengths, every shape-factor model, the
   Lorentzian precession form, the ``quad`` precession integral and
-  ``get_kinematical_intensities`` on several structures.
+  ``get_kinematical_intensities`` on several structures;
+* imports the reference's own ``diffsims/structure_factor/`` modules
+  (``atomic_scattering_parameters``, ``atomic_scattering_factor``,
+  ``structure_factor``; diffpy's ``expandPosition`` / ``SymmetryConstraints``
+  are stubbed by the oracle's restatement of them, over space-group
+  operations the oracle generates) and records the family structure factors,
+  Doyle-Turner parameters, atomic scattering factors and refraction-corrected
+  wavelengths of several phases (``reference_structure_factor.npz``).
 
 Usage::
 
@@ -151,5 +158,124 @@ def main(ref_root="/root/reference"):
     print("wrote", HERE / "reference_numerics.npz", len(g), "arrays")
 
 
+class _SfAtom:
+    def __init__(self, element, xyz, occ, biso):
+        self.element, self.xyz, self.occupancy, self.Bisoequiv = element, np.asarray(xyz, float), occ, biso
+
+
+class _SfLattice:
+    def __init__(self, params):
+        from oracle import structure_factor_families as osf
+        self.volume = osf.cell_volume(*params)
+
+
+class _SfStructure(list):
+    def __init__(self, atoms, params):
+        super().__init__(atoms)
+        self.lattice = _SfLattice(params)
+        self.xyz = np.array([a.xyz for a in atoms])
+
+
+class _SfSpaceGroup:
+    def __init__(self, number):
+        from oracle import structure_factor_families as osf
+        self.number = number
+        self.ops = osf.space_group_operations(number)
+
+
+class _SfPhase:
+    def __init__(self, sg, atoms, params):
+        self.space_group = _SfSpaceGroup(sg)
+        self.structure = _SfStructure(atoms, params)
+
+
+def sf_phases():
+    """Named phases: (space group, lattice params, atoms (element, xyz, occupancy, Bisoequiv))."""
+    b = 8 * np.pi ** 2 * 0.006332
+    rng = np.random.default_rng(23)
+    out = {
+        "nickel": (225, (3.5236,) * 3 + (90, 90, 90), [("Ni0+", [0, 0, 0], 1.0, b)]),
+        "ferrite": (229, (2.8665,) * 3 + (90, 90, 90), [("Fe", [0, 0, 0], 1.0, b), ("Fe", [.5, .5, .5], 1.0, b)]),
+        "sic4h": (186, (3.073, 3.073, 10.053, 90, 90, 120),
+                  [("Si", [0, 0, 0], 1.0, b), ("Si", [0.33, 0.667, 0.25], 1.0, b),
+                   ("C", [0, 0, 0.188], 1.0, b), ("C", [0.333, 0.667, 0.438], 1.0, b)]),
+        # a mixed site at a general position of Pm-3m (orbit of 48), then other atoms
+        "mixed_pm3m": (221, (4.1,) * 3 + (90, 90, 90),
+                       [("Fe", [0.11, 0.23, 0.37], 0.6, 0.4), ("Ni", [0.11, 0.23, 0.37], 0.4, 0.7),
+                        ("O", [0.5, 0.5, 0.5], 1.0, 0.9)]),
+        "p1_random": (1, (7.3, 8.1, 9.6, 84.0, 96.0, 101.0),
+                      [(str(e), x, float(o), float(bb)) for e, x, o, bb in
+                       zip(rng.choice(["C", "N", "O", "Si", "Fe", "Cu"], 30), rng.random((30, 3)),
+                           rng.uniform(0.5, 1.0, 30), rng.uniform(0.2, 1.5, 30))]),
+        "pm1_centric": (2, (5.2, 6.3, 7.4, 88.0, 92.0, 95.0),
+                        [("Ti", [0.21, 0.34, 0.45], 1.0, 0.5), ("O", [0.1, 0.6, 0.2], 1.0, 0.8)]),
+    }
+    return out
+
+
+def load_reference_structure_factor(ref_root):
+    from oracle import structure_factor_families as osf
+    load_reference(ref_root)
+    sym = sys.modules["diffpy.structure.symmetryutilities"]
+
+    def expand_position(spacegroup, xyz, sgoffset=(0, 0, 0), eps=None):
+        # (positions, operations per position, multiplicity); the reference reads [0]
+        return list(osf.orbit(spacegroup.ops, xyz)), None, None
+
+    class SymmetryConstraints:
+        def __init__(self, spacegroup, positions):
+            core = []
+            for p in positions:
+                p = np.asarray(p, float)
+                if not any(any(np.all(np.abs((q - p) - np.rint(q - p)) < 1e-5) for q in osf.orbit(spacegroup.ops, c))
+                           for c in core):
+                    core.append(p)
+            self.corepos = core
+
+    sym.expandPosition = expand_position
+    sym.SymmetryConstraints = SymmetryConstraints
+    import diffsims.structure_factor.atomic_scattering_parameters as asp
+    import diffsims.structure_factor.atomic_scattering_factor as asf
+    import diffsims.structure_factor.structure_factor as ssf
+    return asp, asf, ssf
+
+
+def main_structure_factor(ref_root="/root/reference"):
+    asp, asf, ssf = load_reference_structure_factor(ref_root)
+    rng = np.random.default_rng(29)
+    g = {}
+    for name, (sg, params, atoms) in sf_phases().items():
+        phase = _SfPhase(sg, [_SfAtom(*a) for a in atoms], params)
+        hkl = rng.integers(-7, 8, (48, 3)).astype(np.float64)
+        hkl = np.vstack([hkl, [[0, 0, 0], [1, 1, 1], [0.5, -1.25, 2.0]]])
+        s = rng.uniform(0.0, 1.6, hkl.shape[0])
+        s[-3] = 0.0
+        g[f"{name}_hkl"], g[f"{name}_s"] = hkl, s
+        g[f"{name}_asym"] = np.asarray(ssf.find_asymmetric_positions(phase.structure.xyz, phase.space_group))
+        g[f"{name}_kin"] = np.array([ssf.get_kinematical_structure_factor(phase, h, si) for h, si in zip(hkl, s)])
+        for kv in (20e3, 200e3):
+            vals = [ssf.get_doyleturner_structure_factor(phase, h, si, kv, return_parameters=True)
+                    for h, si in zip(hkl, s)]
+            g[f"{name}_dt{int(kv)}"] = np.array([v[0] for v in vals])
+            g[f"{name}_dt{int(kv)}_vg"] = np.array([v[1]["v_g"] for v in vals])
+            g[f"{name}_dt{int(kv)}_vmod"] = np.array([v[1]["v_mod"] for v in vals])
+        g[f"{name}_voltages"] = np.array([10e3, 20e3, 100e3, 200e3, 300e3])
+        g[f"{name}_wavelength"] = np.array([ssf.get_refraction_corrected_wavelength(phase, v)
+                                            for v in g[f"{name}_voltages"]])
+    # atomic scattering factors and parameters
+    els = ["H", "C", "O", "Si", "Fe", "Ni", "Cu", "Au", "U", "Bk"]
+    s = np.linspace(0.0, 1.8, 13)
+    g["atom_elements"] = np.array(els)
+    g["atom_s"] = s
+    g["atom_kin"] = np.array([[asf.get_kinematical_atomic_scattering_factor(_SfAtom(e, [0, 0, 0], 0.7, 0.45), si)
+                               for si in s] for e in els])
+    g["atom_dt"] = np.array([[asf.get_doyleturner_atomic_scattering_factor(_SfAtom(e, [0, 0, 0], 0.7, 0.45), si, 61.3)
+                              for si in s] for e in els])
+    g["atom_params"] = np.array([np.concatenate(asp.get_atomic_scattering_parameters(e)) for e in els])
+    np.savez_compressed(HERE / "reference_structure_factor.npz", **g)
+    print("wrote", HERE / "reference_structure_factor.npz", len(g), "arrays")
+
+
 if __name__ == "__main__":
     main(*sys.argv[1:])
+    main_structure_factor(*sys.argv[1:])
