@@ -241,6 +241,10 @@ sf_fp64_kernel(SfConst c, ds_atoms A, const int32_t *__restrict__ hkl_i, const d
         double fsp[SF_MAX_SPECIES];
         for (int s = 0; s < c.n_species; ++s) fsp[s] = scatter_f64(cd + 10 * s, c.kind, g2);
         double re = 0.0, im = 0.0;
+        // amplitude of the previous atom: consecutive atoms with the same
+        // species, occupancy and B (the positions of one orbit) reuse it
+        double amp = 0.0, occ_prev = 0.0, B_prev = 0.0;
+        int sp_prev = -1;
         for (int start = 0; start < c.n_atoms; start += chunk_cap) {
             int cnt = min(chunk_cap, c.n_atoms - start);
             if (!sf_stage_chunk(A, smem, Ls, start, cnt, parity, status, false)) return;
@@ -251,7 +255,10 @@ sf_fp64_kernel(SfConst c, ds_atoms A, const int32_t *__restrict__ hkl_i, const d
                     double r = t - rint(t);
                     double sn, cs;
                     sincospi(2.0 * r, &sn, &cs);
-                    double amp = fsp[a.species] * a.occupancy * exp(-0.25 * g2 * a.B);
+                    if (a.species != sp_prev || a.occupancy != occ_prev || a.B != B_prev) {
+                        amp = fsp[a.species] * a.occupancy * exp(-0.25 * g2 * a.B);
+                        sp_prev = a.species; occ_prev = a.occupancy; B_prev = a.B;
+                    }
                     re = fma(amp, cs, re);
                     im = fma(amp, sn, im);
                 }
@@ -381,9 +388,9 @@ extern "C" ds_status ds_family_structure_factors(const ds_atoms *atoms, const do
     DS_REQUIRE(atoms->kind == DS_SCATTER_KINEMATICAL || atoms->kind == DS_SCATTER_DOYLETURNER,
                "ds_family_structure_factors: kind must be DS_SCATTER_KINEMATICAL or DS_SCATTER_DOYLETURNER");
     DS_REQUIRE(((uintptr_t)atoms->atoms & 15) == 0, "ds_family_structure_factors: atoms must be 16-byte aligned");
-    DS_REQUIRE(hkl_d && scattering_parameter && F && status, "ds_family_structure_factors: null pointer");
     DS_REQUIRE(n >= 0, "ds_family_structure_factors: n < 0");
     if (n == 0) return DS_OK;
+    DS_REQUIRE(hkl_d && scattering_parameter && F && status, "ds_family_structure_factors: null pointer");
     // g_is_spacing squares the per-reflection input: the kernel sees s^2
     SfConst c{n, atoms->n_atoms, atoms->n_species, atoms->kind, 0, 1, 0};
     return launch_fp64(c, *atoms, nullptr, hkl_d, scattering_parameter, nullptr, nullptr, nullptr, F, nullptr,
