@@ -24,7 +24,10 @@ Arms:
                     to 256x256 detectors in 8192-orientation chunks),
                     "family_structure_factors" (Doyle-Turner structure
                     factors of 2^20 lattice-plane families in one launch,
-                    against the oracle's per-family loop on one core).
+                    against the oracle's per-family loop on one core),
+                    "legacy_ed_data" (the legacy DiffractionGenerator:
+                    100,000 Euler triples of one structure in one launch,
+                    against the oracle's per-orientation call on one core).
   --impl reference  the reference's CPU path restated in numpy (the FP64
                     oracle) on all host cores, a bounded sample per step.
 
@@ -340,6 +343,7 @@ def run_gpu(args):
     batched = None if args.skip_batch else run_batch(args, torch, dev)
     library = None if args.skip_library else run_library(args, torch, dev, hbm_peak)
     families = None if args.skip_families else run_families(args, torch, dev)
+    legacy = None if args.skip_legacy else run_legacy(args, torch, dev)
 
     cpu = None
     if not args.no_cpu_baseline:
@@ -371,6 +375,7 @@ def run_gpu(args):
         "batched_phases": batched,
         "template_library": library,
         "family_structure_factors": families,
+        "legacy_ed_data": legacy,
         "cpu_baseline": cpu,
         "clocks": clocks,
         "gpu_launches": 5 * args.steps,
@@ -592,6 +597,74 @@ def run_families(args, torch, dev):
             "cpu_baseline": {"value": cpu_rate, "unit": "families/s", "cores": 1, "kind": "port",
                              "sample": f"{n_cpu} families, FP64 numpy restatement of the reference's per-family loop"},
             "dtype": "f64"}
+
+
+def run_legacy(args, torch, dev):
+    """Legacy DiffractionGenerator.calculate_ed_data
+    (diffsims/generators/diffraction_generator.py:192-331): a 12-atom P1 cell
+    (a, b, c = 6.3, 7.1, 8.2 A), 200 kV, r = 2.0, lorentzian, 100,000 Euler
+    triples in one call (the loop of DiffractionLibraryGenerator.get_diffraction_library,
+    diffsims/generators/library_generator.py:51-155, for one phase)."""
+    from diffsims_gb300.crystal import Atom, Lattice, Structure
+    from diffsims_gb300.diffraction_generator import DiffractionGenerator, euler_rzxz_quaternions, structure_base
+    from diffsims_gb300.engine import PhaseTable, SpotBuffers, simulate_phase
+    from diffsims_gb300.sim_utils import PackedAtoms
+    from oracle import legacy as ol
+    rng = np.random.default_rng(31)
+    els = list(rng.choice(["C", "O", "Si", "Fe"], 12))
+    xyz = rng.random((12, 3))
+    occ = rng.uniform(0.6, 1.0, 12)
+    lat = (6.3, 7.1, 8.2, 84.0, 97.0, 103.0)
+    structure = Structure([Atom(e, x, o) for e, x, o in zip(els, xyz, occ)], Lattice(*lat))
+    n, r = 100_000, 2.0
+    eul = np.random.default_rng(7).uniform(-180, 180, (n, 3))
+    gen = DiffractionGenerator(200)
+    # device-resident: the sphere table and the orientation launch
+    recip = np.ascontiguousarray(np.linalg.inv(structure_base(structure.lattice)).T)
+    atoms = PackedAtoms(els, xyz, occ, np.zeros(12), "lobato", dev)
+    q = euler_rzxz_quaternions(eul)
+    q[:, 1:] *= -1
+    quats = torch.from_numpy(q).to(dev)
+    settings = gen._gen.settings(1e-2)
+    bufs = SpotBuffers(dev)
+    st = torch.cuda.current_stream()
+
+    def step():
+        t = PhaseTable.sphere(recip, atoms, r, device=dev)
+        return simulate_phase(t, quats, settings, r, bufs)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        spots = step()
+        e1.record(st)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    dev_ms = statistics.mean(ms)
+    # the public call, host Euler angles in, DiffractionSimulation objects out
+    t0 = time.perf_counter()
+    sims = gen.calculate_ed_data(structure, r, rotation=eul)
+    e2e_s = time.perf_counter() - t0
+    # the oracle's per-orientation call (the reference's algorithm), one core
+    n_cpu = 500
+    dl = ol.DiffpyLattice(*lat)
+    t0 = time.perf_counter()
+    for k in range(n_cpu):
+        ol.calculate_ed_data(dl, els, xyz, occ, np.zeros(12), 200, r, rotation=eul[k])
+    cpu_rate = n_cpu / (time.perf_counter() - t0)
+    return {"metric": "orientation patterns/s (legacy calculate_ed_data, Euler rzxz)", "value": n / (dev_ms * 1e-3),
+            "unit": "patterns/s", "ms_per_step": dev_ms, "patterns_per_step": n, "spots_per_step": int(spots.total),
+            "n_hkl": int(spots.table.n),
+            "e2e": {"value": n / e2e_s, "unit": "patterns/s", "s": e2e_s, "simulations": len(sims),
+                    "note": "public call with host Euler angles; includes building 100k DiffractionSimulation objects"},
+            "cpu_baseline": {"value": cpu_rate, "unit": "patterns/s", "cores": 1, "kind": "port",
+                             "sample": f"{n_cpu} orientations, FP64 numpy restatement of calculate_ed_data"},
+            "config": {"workload": "legacy calculate_ed_data: P1 12 atoms (6.3, 7.1, 8.2 A; 84, 97, 103 deg), "
+                                   "200 kV, r=2.0, s_max=0.01, lorentzian, 100k Euler triples", "seed": 31}}
 
 
 def run_library(args, torch, dev, hbm_peak):
@@ -820,6 +893,7 @@ def main():
     ap.add_argument("--skip-library", action="store_true", help="leave out the template-library leg")
     ap.add_argument("--skip-batch", action="store_true", help="leave out the batched-phases leg")
     ap.add_argument("--skip-families", action="store_true", help="leave out the per-family structure-factor leg")
+    ap.add_argument("--skip-legacy", action="store_true", help="leave out the legacy calculate_ed_data leg")
     ap.add_argument("--case", default=None, choices=["raster", "adjoint", "batch"],
                     help="run one small profiling case instead of the benchmark")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -37,7 +37,7 @@ DS_PRECESSION_LORENTZIAN = 1
 DS_PRECESSION_INTEGRAL = 2
 
 EXPORTED_SYMBOLS = (
-    "ds_box_extent", "ds_enumerate_scratch_bytes", "ds_enumerate_hkl",
+    "ds_box_extent", "ds_enumerate_scratch_bytes", "ds_enumerate_hkl", "ds_enumerate_sphere",
     "ds_structure_factor_scratch_bytes", "ds_structure_factors", "ds_kinematical_intensities",
     "ds_family_structure_factors", "ds_simulate_scratch_bytes", "ds_simulate", "ds_simulate_batch_scratch_bytes", "ds_simulate_batch_tile",
     "ds_simulate_batch", "ds_rasterize_scratch_bytes", "ds_rasterize",
@@ -111,6 +111,8 @@ def load_library(require_cuda: bool = True):
             lib.ds_enumerate_scratch_bytes.restype = sz
             lib.ds_enumerate_hkl.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_int32), dp, i32, vp, vp, i64, vp,
                                              vp, sz, vp, vp]
+            lib.ds_enumerate_sphere.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_int32), dp, vp, vp, i64, vp,
+                                                vp, sz, vp, vp]
             lib.ds_structure_factor_scratch_bytes.argtypes = [i64, i32]
             lib.ds_structure_factor_scratch_bytes.restype = sz
             lib.ds_structure_factors.argtypes = [C.POINTER(ds_atoms), vp, vp, vp, i64, i32, vp, vp, vp, vp, sz, vp, vp]
@@ -144,7 +146,7 @@ def load_library(require_cuda: bool = True):
             lib.ds_last_error.restype = C.c_char_p
             lib.ds_version.restype = C.c_char_p
             for name in ("ds_box_extent", "ds_enumerate_hkl", "ds_structure_factors", "ds_kinematical_intensities",
-                         "ds_family_structure_factors",
+                         "ds_family_structure_factors", "ds_enumerate_sphere",
                          "ds_simulate", "ds_simulate_batch", "ds_rasterize", "ds_simulate_backward",
                          "ds_structure_factors_backward",
                          "ds_axis_angle_compose", "ds_axis_angle_compose_backward", "ds_polar_flatten",

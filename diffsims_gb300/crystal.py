@@ -68,6 +68,22 @@ def lattice_base(a, b, c, alpha, beta, gamma) -> np.ndarray:
     return np.array([[a, 0.0, 0.0], [b * cg, b * sg, 0.0], [cx, cy, math.sqrt(cz2)]])
 
 
+def diffpy_base(a, b, c, alpha, beta, gamma) -> np.ndarray:
+    """Direct base vectors (rows a, b, c) in diffpy's standard Cartesian frame,
+    the frame of diffpy ``Structure`` objects and of the legacy
+    ``DiffractionGenerator``: c along z, b in the yz-plane (so a* is along x).
+    Built from the cell geometry: b = b (0, sin alpha, cos alpha); a_z from
+    a.c, a_y from a.b, a_x > 0 from |a|."""
+    al, be, ga = np.deg2rad([alpha, beta, gamma])
+    bv = np.array([0.0, b * math.sin(al), b * math.cos(al)])
+    az = a * math.cos(be)
+    ay = (a * b * math.cos(ga) - az * bv[2]) / bv[1]
+    ax2 = a * a - ay * ay - az * az
+    if not ax2 > 0:
+        raise ValueError(f"degenerate lattice: a={a} b={b} c={c} alpha={alpha} beta={beta} gamma={gamma}")
+    return np.array([[math.sqrt(ax2), ay, az], bv, [0.0, 0.0, c]])
+
+
 @dataclass
 class Atom:
     element: str

@@ -42,6 +42,11 @@ constexpr int ENUM_THREADS = 256;
 constexpr int ENUM_ITEMS = 4;
 constexpr int ENUM_TILE = ENUM_THREADS * ENUM_ITEMS;
 
+// MODE 0: ReciprocalLatticeVector.from_min_dspacing -- descending box, 000
+//         removed, keep 1/|g| >= dmin, n_zero trailing 000 rows.
+// MODE 1: get_points_in_sphere (diffsims/utils/sim_utils.py:436-474) -- the
+//         box in itertools.product order (h, then k, then l ascending from
+//         -H, -K, -L), 000 kept in place, keep |g| < radius (held in dmin).
 struct EnumConst {
     double r[9];
     double dmin;
@@ -52,6 +57,7 @@ struct EnumConst {
     long long capacity;
 };
 
+template <int MODE>
 __global__ void __launch_bounds__(ENUM_THREADS)
 enumerate_kernel(EnumConst c, int32_t *__restrict__ hkl_out, double *__restrict__ g2_out,
                  int64_t *__restrict__ count_out, LookbackScratch lb, int32_t *status) {
@@ -75,14 +81,23 @@ enumerate_kernel(EnumConst c, int32_t *__restrict__ hkl_out, double *__restrict_
         keep[it] = false;
         if (i < c.total) {
             long long q = i / nl;
-            l[it] = c.L - (int)(i - q * nl);
-            k[it] = c.K - (int)(q % nk);
-            h[it] = c.H - (int)(q / nk);
-            if (h[it] != 0 || k[it] != 0 || l[it] != 0) {
+            if (MODE == 0) {
+                l[it] = c.L - (int)(i - q * nl);
+                k[it] = c.K - (int)(q % nk);
+                h[it] = c.H - (int)(q / nk);
+                if (h[it] != 0 || k[it] != 0 || l[it] != 0) {
+                    double g2 = g2_fixed_order(c.r, (double)h[it], (double)k[it], (double)l[it]);
+                    double d = __ddiv_rn(1.0, __dsqrt_rn(g2));
+                    g2v[it] = g2;
+                    keep[it] = d >= c.dmin;
+                }
+            } else {
+                l[it] = (int)(i - q * nl) - c.L;
+                k[it] = (int)(q % nk) - c.K;
+                h[it] = (int)(q / nk) - c.H;
                 double g2 = g2_fixed_order(c.r, (double)h[it], (double)k[it], (double)l[it]);
-                double d = __ddiv_rn(1.0, __dsqrt_rn(g2));
                 g2v[it] = g2;
-                keep[it] = d >= c.dmin;
+                keep[it] = __dsqrt_rn(g2) < c.dmin;
             }
         }
         cnt += keep[it] ? 1 : 0;
@@ -182,8 +197,34 @@ extern "C" ds_status ds_enumerate_hkl(const double recip[9], const int32_t hmax[
     DS_REQUIRE(scratch_bytes >= lookback_scratch_bytes(c.n_tiles), "ds_enumerate_hkl: scratch too small");
     cudaStream_t s = (cudaStream_t)stream;
     DS_CUDA_TRY(cudaMemsetAsync(scratch, 0, lookback_scratch_bytes(c.n_tiles), s));
-    enumerate_kernel<<<(unsigned)c.n_tiles, ENUM_THREADS, 0, s>>>(c, hkl_out, g2_out, count_out,
-                                                                  lookback_scratch(scratch), status);
+    enumerate_kernel<0><<<(unsigned)c.n_tiles, ENUM_THREADS, 0, s>>>(c, hkl_out, g2_out, count_out,
+                                                                     lookback_scratch(scratch), status);
+    return check_launch("enumerate_kernel");
+}
+
+extern "C" ds_status ds_enumerate_sphere(const double recip[9], const int32_t hmax[3], double radius,
+                                         int32_t *hkl_out, double *g2_out, int64_t capacity, int64_t *count_out,
+                                         void *scratch, size_t scratch_bytes, int32_t *status, void *stream) {
+    clear_error();
+    DS_REQUIRE(recip && hmax && hkl_out && g2_out && count_out && scratch && status,
+               "ds_enumerate_sphere: null pointer");
+    DS_REQUIRE(hmax[0] >= 0 && hmax[1] >= 0 && hmax[2] >= 0, "ds_enumerate_sphere: negative box");
+    DS_REQUIRE(hmax[0] < (1 << 15) && hmax[1] < (1 << 15) && hmax[2] < (1 << 15), "ds_enumerate_sphere: box too large");
+    DS_REQUIRE(radius > 0 && isfinite(radius), "ds_enumerate_sphere: radius must be > 0");
+    EnumConst c;
+    for (int i = 0; i < 9; ++i) c.r[i] = recip[i];
+    c.dmin = radius;
+    c.H = hmax[0]; c.K = hmax[1]; c.L = hmax[2];
+    c.n_zero = 0;
+    c.total = (long long)(2 * c.H + 1) * (2 * c.K + 1) * (2 * c.L + 1);
+    c.n_tiles = (c.total + ENUM_TILE - 1) / ENUM_TILE;
+    c.capacity = capacity;
+    DS_REQUIRE(capacity >= c.total, "ds_enumerate_sphere: capacity below box size");
+    DS_REQUIRE(scratch_bytes >= lookback_scratch_bytes(c.n_tiles), "ds_enumerate_sphere: scratch too small");
+    cudaStream_t s = (cudaStream_t)stream;
+    DS_CUDA_TRY(cudaMemsetAsync(scratch, 0, lookback_scratch_bytes(c.n_tiles), s));
+    enumerate_kernel<1><<<(unsigned)c.n_tiles, ENUM_THREADS, 0, s>>>(c, hkl_out, g2_out, count_out,
+                                                                     lookback_scratch(scratch), status);
     return check_launch("enumerate_kernel");
 }
 

@@ -1,0 +1,106 @@
+"""``DiffractionGenerator``: drop-in for the legacy single-structure generator
+of diffsims/generators/diffraction_generator.py (``calculate_ed_data``),
+running on the same CUDA kernels as ``SimulationGenerator``.
+
+The legacy path differs from ``calculate_diffraction2d`` only in its inputs
+and candidate set: a diffpy ``Structure`` in diffpy's standard frame (c along
+z, b in the yz-plane), Euler angles in degrees in the rotating z-x-z
+convention (transforms3d ``euler2mat(..., "rzxz")``, applied as ``R @ g``),
+and the reciprocal-lattice points of ``get_points_in_sphere``
+(diffsims/utils/sim_utils.py:436-474: the box of half-widths floor(r/|a*|),
+... in itertools.product order, 000 included, |g| < r).  Excitation error,
+selection, shape factors, intensities and the minimum-intensity mask are the
+orientation kernel's.  Several Euler triples run as one launch.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .crystal import Lattice, diffpy_base, lattice_params, sites_of
+from .diffraction_simulation import DiffractionSimulation
+from .engine import PhaseTable, simulate_phase
+from .generator import SimulationGenerator
+from .sim_utils import PackedAtoms, debye_waller_per_atom, get_electron_wavelength
+
+
+def structure_base(lattice) -> np.ndarray:
+    """Direct base (rows a, b, c) of the legacy path's frame: a diffpy
+    lattice's own ``base`` (which includes any ``baserot``), else diffpy's
+    standard frame built from the cell parameters."""
+    if not isinstance(lattice, Lattice) and hasattr(lattice, "base"):
+        return np.asarray(lattice.base, dtype=np.float64).reshape(3, 3)
+    return diffpy_base(*lattice_params(lattice))
+
+
+def euler_rzxz_quaternions(euler_deg) -> np.ndarray:
+    """Unit quaternions (w, x, y, z) of Rz(a) Rx(b) Rz(c) for Euler triples
+    (degrees) in the rotating z-x-z convention: qz(a) * qx(b) * qz(c)."""
+    e = np.deg2rad(np.atleast_2d(np.asarray(euler_deg, dtype=np.float64)).reshape(-1, 3)) / 2
+    ca, sa = np.cos(e[:, 0]), np.sin(e[:, 0])
+    cb, sb = np.cos(e[:, 1]), np.sin(e[:, 1])
+    cc, sc = np.cos(e[:, 2]), np.sin(e[:, 2])
+    # qz(a) * qx(b) = (ca cb, ca sb, sa sb, sa cb); then * qz(c)
+    w1, x1, y1, z1 = ca * cb, ca * sb, sa * sb, sa * cb
+    return np.stack([w1 * cc - z1 * sc, x1 * cc + y1 * sc, y1 * cc - x1 * sc, z1 * cc + w1 * sc], axis=1)
+
+
+class DiffractionGenerator:
+    """Electron diffraction spot patterns of one structure at given Euler
+    angles.  Constructor arguments as diffsims/generators/diffraction_generator.py:155-191
+    (``accelerating_voltage`` in kV, ``scattering_params``, ``precession_angle``
+    in degrees, ``shape_factor_model`` by name or as the reference's model
+    function, ``approximate_precession``, ``minimum_intensity``, shape-model
+    keyword arguments); the same ``NotImplementedError`` for unknown names.
+    ``shape_factor_model`` holds the model's name."""
+
+    def __init__(self, accelerating_voltage, scattering_params="lobato", precession_angle=0,
+                 shape_factor_model="lorentzian", approximate_precession=True, minimum_intensity=1e-20, **kwargs):
+        self._gen = SimulationGenerator(accelerating_voltage, scattering_params, precession_angle,
+                                        shape_factor_model, approximate_precession, minimum_intensity, **kwargs)
+        self.wavelength = get_electron_wavelength(accelerating_voltage)
+        self.precession_angle = self._gen.precession_angle
+        self.approximate_precession = approximate_precession
+        self.shape_factor_model = shape_factor_model
+        self.minimum_intensity = minimum_intensity
+        self.shape_factor_kwargs = kwargs
+        self.scattering_params = scattering_params
+
+    def calculate_ed_data(self, structure, reciprocal_radius, rotation=(0, 0, 0), with_direct_beam=True,
+                          max_excitation_error=1e-2, shape_factor_width=None, debye_waller_factors={},
+                          form="mixed"):
+        """Spot pattern(s) of ``structure`` (diffraction_generator.py:192-331).
+
+        ``rotation``: one Euler triple (degrees, rotating z-x-z) -> one
+        ``DiffractionSimulation``; an (N, 3) array -> a list of N, from one
+        launch.  ``form`` as ``SimulationGenerator.calculate_diffraction2d``.
+        Fractional coordinates are used as given (the reference's re-basing
+        at diffsims/utils/sim_utils.py:290-291 is the identity for lattices
+        built from their parameters).  An orientation where nothing is
+        selected gives an empty simulation (the reference raises).
+        """
+        if form not in ("mixed", "fp64"):
+            raise ValueError("form must be 'mixed' or 'fp64'")
+        N.load_library()
+        dev = torch.device("cuda", torch.cuda.current_device())
+        rot = np.asarray(rotation, dtype=np.float64)
+        single = rot.ndim == 1
+        rot = rot.reshape(-1, 3)
+        recip = np.ascontiguousarray(np.linalg.inv(structure_base(structure.lattice)).T)
+        els, xyz, occ = sites_of(structure)
+        B = debye_waller_per_atom(els, debye_waller_factors)
+        atoms = PackedAtoms(els, xyz, occ, B, self.scattering_params, dev)
+        table = PhaseTable.sphere(recip, atoms, reciprocal_radius, form=form, device=dev)
+        # the kernel writes R(q)^T g; the legacy path applies R(euler) g
+        q = euler_rzxz_quaternions(rot)
+        q[:, 1:] *= -1
+        quats = torch.from_numpy(np.ascontiguousarray(q)).to(dev)
+        settings = self._gen.settings(max_excitation_error, shape_factor_width, form)
+        spots = simulate_phase(table, quats, settings, reciprocal_radius)
+        out = []
+        for i in range(rot.shape[0]):
+            hkl, g, inten = spots.pattern(i)
+            out.append(DiffractionSimulation(g, indices=hkl.astype(np.float64), intensities=inten,
+                                             with_direct_beam=with_direct_beam))
+        return out[0] if single else out

@@ -68,13 +68,30 @@ class PhaseTable:
             obj.build(stream)
         return obj
 
-    def _setup(self, recip, atoms, reciprocal_radius, with_direct_beam, form, dev):
+    @classmethod
+    def sphere(cls, recip, atoms: PackedAtoms, reciprocal_radius, form="mixed", device=None, stream=None,
+               build=True):
+        """The candidate rows of the legacy ``DiffractionGenerator``:
+        get_points_in_sphere (diffsims/utils/sim_utils.py:436-474) -- the box
+        of half-widths floor(r / |a*|), ... in itertools.product order, 000 in
+        place, |g| < r.  ``recip``: rows a*, b*, c* in the structure's frame."""
+        obj = cls.__new__(cls)
+        recip = np.ascontiguousarray(np.asarray(recip, dtype=np.float64).reshape(3, 3))
+        hmax = np.floor(float(reciprocal_radius) / np.linalg.norm(recip, axis=1)).astype(np.int64)
+        obj._setup(recip, atoms, reciprocal_radius, False, form, _device(device), sphere_hmax=hmax)
+        if build:
+            obj.build(stream)
+        return obj
+
+    def _setup(self, recip, atoms, reciprocal_radius, with_direct_beam, form, dev, sphere_hmax=None):
         lib = N.load_library()
         self.device = dev
         self.form = form
         self.recip = recip
         self.dmin = 1.0 / float(reciprocal_radius)
-        self.hmax = box_extent(self.recip, self.dmin)
+        self.radius = float(reciprocal_radius)
+        self.sphere_rule = sphere_hmax is not None
+        self.hmax = box_extent(self.recip, self.dmin) if sphere_hmax is None else sphere_hmax
         self.n_zero = 2 if with_direct_beam else 0
         box = int(np.prod(2 * self.hmax + 1))
         self.cap = box + self.n_zero
@@ -98,9 +115,14 @@ class PhaseTable:
         lib = N.load_library()
         st = N.stream_handle(stream)
         self._status.zero_()
-        N.check(lib.ds_enumerate_hkl(self._rb, self._hm, self.dmin, self.n_zero, N.ptr(self._hkl), N.ptr(self._g2),
-                                     self.cap, N.ptr(self._count), N.ptr(self._scratch), self._enum_bytes,
-                                     N.ptr(self._status), st), "enumerate_hkl")
+        if self.sphere_rule:
+            N.check(lib.ds_enumerate_sphere(self._rb, self._hm, self.radius, N.ptr(self._hkl), N.ptr(self._g2),
+                                            self.cap, N.ptr(self._count), N.ptr(self._scratch), self._enum_bytes,
+                                            N.ptr(self._status), st), "enumerate_sphere")
+        else:
+            N.check(lib.ds_enumerate_hkl(self._rb, self._hm, self.dmin, self.n_zero, N.ptr(self._hkl),
+                                         N.ptr(self._g2), self.cap, N.ptr(self._count), N.ptr(self._scratch),
+                                         self._enum_bytes, N.ptr(self._status), st), "enumerate_hkl")
         n = int(self._count.item())
         N.check_device_status(self._status, "enumerate_hkl")
         self.n = n

@@ -81,6 +81,18 @@ ds_status ds_enumerate_hkl(const double recip[9], const int32_t hmax[3], double 
                            int64_t *count_out, void *scratch, size_t scratch_bytes,
                            int32_t *status, void *stream);
 
+/* get_points_in_sphere (diffsims/utils/sim_utils.py:436-474), the candidate
+ * set of the legacy DiffractionGenerator.calculate_ed_data
+ * (diffsims/generators/diffraction_generator.py:238-241): the box
+ * [-H..H] x [-K..K] x [-L..L] in itertools.product order (h slowest, l
+ * fastest, ascending), 000 included where it falls, kept where |g| < radius
+ * (|g|^2 in the fixed operation order of ds_enumerate_hkl, then sqrt).
+ * hmax: floor(radius / |a*|), floor(radius / |b*|), floor(radius / |c*|);
+ * capacity >= box size; scratch sized by ds_enumerate_scratch_bytes. */
+ds_status ds_enumerate_sphere(const double recip[9], const int32_t hmax[3], double radius,
+                              int32_t *hkl_out, double *g2_out, int64_t capacity, int64_t *count_out,
+                              void *scratch, size_t scratch_bytes, int32_t *status, void *stream);
+
 /* ---------------------------------------------------------------- A3 ---- */
 /* One atom of a phase: 48-byte record (a multiple of 16 so the atom table can
  * be staged into shared memory with 1-D TMA bulk copies). */

@@ -21,7 +21,13 @@ need the reference.  What it does:
   are stubbed by the oracle's restatement of them, over space-group
   operations the oracle generates) and records the family structure factors,
   Doyle-Turner parameters, atomic scattering factors and refraction-corrected
-  wavelengths of several phases (``reference_structure_factor.npz``).
+  wavelengths of several phases (``reference_structure_factor.npz``);
+* imports the reference's own ``diffsims/generators/diffraction_generator.py``
+  (numba, matplotlib and PIL stubbed -- used only by code this path does not
+  run; transforms3d's ``euler2mat`` and diffpy's ``Lattice`` are the
+  oracle's restatements) and records ``DiffractionGenerator.calculate_ed_data``
+  outputs for several structures, rotations, shape models and precession
+  settings (``reference_legacy.npz``).
 
 Usage::
 
@@ -276,6 +282,114 @@ def main_structure_factor(ref_root="/root/reference"):
     print("wrote", HERE / "reference_structure_factor.npz", len(g), "arrays")
 
 
+def _stub_module(name, **attrs):
+    m = sys.modules.get(name) or types.ModuleType(name)
+    for k, v in attrs.items():
+        setattr(m, k, v)
+    sys.modules[name] = m
+    return m
+
+
+def load_reference_legacy(ref_root):
+    from oracle import legacy as ol
+    load_reference(ref_root)
+
+    def _decorator(*args, **kwargs):
+        if len(args) == 1 and callable(args[0]) and not kwargs:
+            return args[0]
+        return lambda f: f
+
+    _stub_module("numba", jit=_decorator, njit=_decorator, prange=range,
+                 config=types.SimpleNamespace(NUMBA_DEFAULT_NUM_THREADS=1))
+    _stub_module("matplotlib")
+    _stub_module("matplotlib.pyplot")
+    _stub_module("PIL", ImageDraw=None, Image=None)
+    _stub_module("PIL.ImageDraw")
+    _stub_module("PIL.Image")
+
+    def euler2mat(ai, aj, ak, axes="sxyz"):
+        assert axes == "rzxz"
+        return ol.euler2mat_rzxz(ai, aj, ak)
+
+    _stub_module("transforms3d")
+    _stub_module("transforms3d.euler", euler2mat=euler2mat)
+    for pkg, sub in [("diffsims.generators", "diffsims/generators"), ("diffsims.sims", "diffsims/sims"),
+                     ("diffsims.pattern", "diffsims/pattern")]:
+        if pkg not in sys.modules:
+            m = types.ModuleType(pkg)
+            m.__path__ = [str(pathlib.Path(ref_root) / sub)]
+            sys.modules[pkg] = m
+    import diffsims.generators.diffraction_generator as dg
+    return dg
+
+
+class _LegacySite:
+    def __init__(self, element, xyz, occ):
+        self.element, self.xyz, self.occupancy = element, np.asarray(xyz, float), float(occ)
+
+
+class _LegacyStructure(list):
+    def __init__(self, sites, lattice):
+        super().__init__(sites)
+        self.lattice = lattice
+
+
+def legacy_structures():
+    """Named structures for the legacy path: (lattice params, elements, xyz, occupancy)."""
+    xyz = []
+    for c in [[0, 0, 0], [0.5, 0, 0.5], [0, 0.5, 0.5], [0.5, 0.5, 0]]:
+        xyz += [c, [c[0] + .25, c[1] + .25, c[2] + .25]]
+    rng = np.random.default_rng(31)
+    return {
+        "si": ((5.431,) * 3 + (90, 90, 90), ["Si"] * 8, xyz, [1.0] * 8),
+        "graphite": ((2.464, 2.464, 6.711, 90, 90, 120), ["C"] * 4,
+                     [[0, 0, .25], [0, 0, .75], [1 / 3, 2 / 3, .25], [2 / 3, 1 / 3, .75]], [1.0] * 4),
+        "p1": ((6.3, 7.1, 8.2, 84.0, 97.0, 103.0), list(rng.choice(["C", "O", "Si", "Fe"], 12)),
+               rng.random((12, 3)).tolist(), rng.uniform(0.6, 1.0, 12).tolist()),
+    }
+
+
+def legacy_cases():
+    """(structure, kwargs of DiffractionGenerator, kwargs of calculate_ed_data)."""
+    cases = []
+    for name, rot in [("si", (0, 0, 0)), ("si", (10, 20, 30)), ("graphite", (0, 90, 90)),
+                      ("p1", (35, 47, 112)), ("p1", (-80, 133, 5))]:
+        cases.append((name, dict(accelerating_voltage=300), dict(reciprocal_radius=2.0, rotation=rot)))
+    for model in ("linear", "sinc", "sin2c", "atanc"):
+        cases.append(("si", dict(accelerating_voltage=200, shape_factor_model=model),
+                      dict(reciprocal_radius=2.5, rotation=(5, 12, 40), max_excitation_error=0.02)))
+    cases.append(("p1", dict(accelerating_voltage=200, precession_angle=0.5),
+                  dict(reciprocal_radius=1.5, rotation=(12, 34, 56))))
+    cases.append(("p1", dict(accelerating_voltage=200, precession_angle=0.5, approximate_precession=False,
+                             shape_factor_model="linear"),
+                  dict(reciprocal_radius=1.2, rotation=(12, 34, 56))))
+    cases.append(("graphite", dict(accelerating_voltage=200, scattering_params="xtables"),
+                  dict(reciprocal_radius=3.0, rotation=(0, 0, 0), shape_factor_width=0.05,
+                       debye_waller_factors={"C": 0.6})))
+    cases.append(("si", dict(accelerating_voltage=300), dict(reciprocal_radius=5.0)))
+    return cases
+
+
+def main_legacy(ref_root="/root/reference"):
+    from oracle import legacy as ol
+    dg = load_reference_legacy(ref_root)
+    g = {}
+    structs = legacy_structures()
+    for i, (name, gen_kw, call_kw) in enumerate(legacy_cases()):
+        lat, els, xyz, occ = structs[name]
+        structure = _LegacyStructure([_LegacySite(e, x, o) for e, x, o in zip(els, xyz, occ)],
+                                     ol.DiffpyLattice(*lat))
+        gen = dg.DiffractionGenerator(**gen_kw)
+        sim = gen.calculate_ed_data(structure, **call_kw)
+        g[f"case{i}_coordinates"] = np.asarray(sim._coordinates)
+        g[f"case{i}_indices"] = np.asarray(sim._indices)
+        g[f"case{i}_intensities"] = np.asarray(sim._intensities)
+    g["n_cases"] = np.array(len(legacy_cases()))
+    np.savez_compressed(HERE / "reference_legacy.npz", **g)
+    print("wrote", HERE / "reference_legacy.npz", len(g), "arrays")
+
+
 if __name__ == "__main__":
     main(*sys.argv[1:])
     main_structure_factor(*sys.argv[1:])
+    main_legacy(*sys.argv[1:])
