@@ -98,9 +98,11 @@ class DiffractionGenerator:
         quats = torch.from_numpy(np.ascontiguousarray(q)).to(dev)
         settings = self._gen.settings(max_excitation_error, shape_factor_width, form)
         spots = simulate_phase(table, quats, settings, reciprocal_radius)
-        out = []
-        for i in range(rot.shape[0]):
-            hkl, g, inten = spots.pattern(i)
-            out.append(DiffractionSimulation(g, indices=hkl.astype(np.float64), intensities=inten,
-                                             with_direct_beam=with_direct_beam))
+        off, idx, xyzi = spots.host(pinned=True)
+        # one gather and one cast for all patterns; each simulation holds views
+        hkl = table.hkl_host()[idx].astype(np.float64) if spots.total else np.zeros((0, 3))
+        rec = xyzi.astype(np.float64)
+        xyz, inten, o = rec[:, :3], rec[:, 3], off.tolist()
+        make = DiffractionSimulation._from_arrays
+        out = [make(xyz[a:b], hkl[a:b], inten[a:b], with_direct_beam) for a, b in zip(o[:-1], o[1:])]
         return out[0] if single else out

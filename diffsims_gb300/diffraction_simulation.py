@@ -40,6 +40,17 @@ class DiffractionSimulation:
         self.offset = np.array(offset)
         self.with_direct_beam = with_direct_beam
 
+    @classmethod
+    def _from_arrays(cls, coordinates, indices, intensities, with_direct_beam):
+        """A simulation from arrays already known to match (n, 3), (n, 3),
+        (n,): the library's own results, without the constructor's checks."""
+        obj = cls.__new__(cls)
+        obj._coordinates, obj._indices, obj._intensities = coordinates, indices, intensities
+        obj._calibration = None
+        obj.offset = np.zeros(2)
+        obj.with_direct_beam = with_direct_beam
+        return obj
+
     def __len__(self):
         return self.coordinates.shape[0]
 

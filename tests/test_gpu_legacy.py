@@ -173,3 +173,29 @@ def test_reference_structural_checks():
         DiffractionGenerator(300, scattering_params="_empty")
     nobeam = gen.calculate_ed_data(si(5.431), 2.0, with_direct_beam=False)
     assert (0, 0, 0) not in [tuple(x) for x in nobeam.indices]
+
+
+def test_library_generator_matches_single_calls():
+    """get_diffraction_library (library_generator.py:51-155): every entry
+    equals its own calculate_ed_data call; pixel coordinates are
+    rint(calibrated xy + half_shape)."""
+    from diffsims_gb300.diffraction_generator import DiffractionGenerator
+    from diffsims_gb300.library import DiffractionLibraryGenerator, StructureLibrary
+    gen = DiffractionGenerator(300)
+    eul_si = [(0, 0, 0), (10, 20, 30), (45, 54.7356, 0)]
+    eul_p1 = [(12, 34, 56)]
+    sl = StructureLibrary(["si", "p1"], [structure_of("si"), structure_of("p1")], [eul_si, eul_p1])
+    lib = DiffractionLibraryGenerator(gen).get_diffraction_library(sl, 0.02, 1.5, (72, 72), with_direct_beam=False)
+    assert lib.reciprocal_radius == 1.5 and lib.with_direct_beam is False
+    for name, eul in (("si", eul_si), ("p1", eul_p1)):
+        entry = lib[name]
+        assert list(entry["orientations"]) == eul
+        for k, e in enumerate(eul):
+            one = gen.calculate_ed_data(structure_of(name), 1.5, rotation=e, with_direct_beam=False)
+            sim = entry["simulations"][k]
+            np.testing.assert_array_equal(sim.indices, one.indices)
+            np.testing.assert_array_equal(entry["intensities"][k], one.intensities)
+            np.testing.assert_array_equal(entry["pixel_coords"][k],
+                                          np.rint(one.coordinates[:, :2] / 0.02 + 72).astype(int))
+    e = lib.get_library_entry("si", (10, 20, 30))
+    assert e["Sim"] is lib["si"]["simulations"][1]

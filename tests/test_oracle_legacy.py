@@ -123,3 +123,30 @@ def test_diffraction_simulation_container():
     sim.rotate_shift_coordinates(90, center=(1, 0))
     np.testing.assert_allclose(sim.coordinates[1, :2], [1 - 0.2, 0.1], atol=1e-15)
     assert len(sim + sim) == 6
+
+
+def test_structure_and_diffraction_library_containers(tmp_path):
+    # diffsims/tests/library/test_structure_library.py, test_diffraction_library.py (host logic)
+    from diffsims_gb300.library import DiffractionLibrary, StructureLibrary, load_DiffractionLibrary
+    lib = StructureLibrary(["a", "b"], [None, None], [[(0, 0, 0)], [(0, 0, 0), (0, 10, 0), (5, 5, 5)]])
+    assert lib.get_library_size() == 4 and set(lib.struct_lib) == {"a", "b"}
+    with pytest.raises(ValueError):
+        StructureLibrary(["a"], [None, None], [[(0, 0, 0)]])
+    with pytest.raises(ValueError):
+        StructureLibrary(["a", "b"], [None, None], [[(0, 0, 0)]])
+    dl = DiffractionLibrary()
+    dl["a"] = {"simulations": ["s0", "s1"], "orientations": [(0, 0, 0), (0, 10, 0)],
+               "pixel_coords": [np.zeros((1, 2)), np.ones((1, 2))], "intensities": [np.array([3.0, 4.0]),
+                                                                                   np.array([1.0])]}
+    e = dl.get_library_entry("a", (0, 10.001, 0))
+    assert e["Sim"] == "s1" and e["pattern_norm"] == 1.0
+    assert dl.get_library_entry()["pattern_norm"] == 5.0
+    with pytest.raises(ValueError):
+        dl.get_library_entry("a", (1, 1, 1))
+    with pytest.raises(ValueError):
+        dl.get_library_entry(angle=(0, 0, 0))
+    f = tmp_path / "lib.pickle"
+    dl.pickle_library(f)
+    with pytest.raises(RuntimeError):
+        load_DiffractionLibrary(f)
+    assert load_DiffractionLibrary(f, safety=True)["a"]["orientations"] == dl["a"]["orientations"]
