@@ -19,10 +19,10 @@ import torch
 
 from . import _native as N
 from .crystal import Lattice, diffpy_base, lattice_params, sites_of
-from .diffraction_simulation import DiffractionSimulation
+from .diffraction_simulation import DiffractionSimulation, ProfileSimulation
 from .engine import PhaseTable, simulate_phase
 from .generator import SimulationGenerator
-from .sim_utils import PackedAtoms, debye_waller_per_atom, get_electron_wavelength
+from .sim_utils import PackedAtoms, debye_waller_per_atom, get_electron_wavelength, get_kinematical_intensities
 
 
 def structure_base(lattice) -> np.ndarray:
@@ -106,3 +106,49 @@ class DiffractionGenerator:
         make = DiffractionSimulation._from_arrays
         out = [make(xyz[a:b], hkl[a:b], inten[a:b], with_direct_beam) for a, b in zip(o[:-1], o[1:])]
         return out[0] if single else out
+
+    def calculate_profile_data(self, structure, reciprocal_radius=1.0, minimum_intensity=1e-3,
+                               debye_waller_factors={}):
+        """1-D profile of ``structure`` (diffraction_generator.py:333-416):
+        the sphere's reciprocal-lattice points (GPU enumeration) grouped into
+        families of indices equal up to signs and order
+        (get_unique_families, diffsims/utils/sim_utils.py:101-136; each keyed
+        by its lexicographically largest member, weighted by its size), their
+        intensities on the GPU, peaks labelled by hkl and scaled so the
+        largest is 100; 000 and peaks at or below ``minimum_intensity`` are
+        dropped.  A hexagonal cell (a == b, 90, 90, 120) is labelled as the
+        reference does: with rows 0, 1, -(0 + 1) and 2 of the family array,
+        which leaves four labels."""
+        N.load_library()
+        dev = torch.device("cuda", torch.cuda.current_device())
+        lat = structure.lattice
+        recip = np.ascontiguousarray(np.linalg.inv(structure_base(lat)).T)
+        atoms = PackedAtoms(["H"], np.zeros((1, 3)), [1.0], [0.0], None, dev)  # enumeration only
+        table = PhaseTable.sphere(recip, atoms, reciprocal_radius, device=dev)
+        hkl = table.hkl_host()
+        dist = np.sqrt(table.g2.cpu().numpy())
+        classes = {}
+        for h in hkl.tolist():
+            classes.setdefault(tuple(sorted(abs(v) for v in h)), []).append(h)
+        row_of = {tuple(h): r for r, h in enumerate(hkl.tolist())}
+        reps = np.array([sorted(v)[-1] for v in classes.values()], dtype=np.float64).reshape(-1, 3)
+        mult = np.array([len(v) for v in classes.values()], dtype=np.float64)
+        g = dist[[row_of[tuple(int(x) for x in u)] for u in reps]]
+        inten = get_kinematical_intensities(structure, reps, g, debye_waller_factors=debye_waller_factors,
+                                            scattering_params=self.scattering_params, prefactor=mult)
+        a, b, c, al, be, ga = lattice_params(lat)
+        labels_of = reps
+        if a == b and al == 90 and be == 90 and ga == 120:
+            labels_of = (reps[0], reps[1], -reps[0] - reps[1], reps[2])
+        labels = ["".join(str(int(x)) for x in xs) for xs in labels_of]
+        peaks = {}
+        for lab, i, gg in zip(labels, inten, g):
+            peaks[lab] = [i, gg]
+        top = max(v[0] for v in peaks.values())
+        x, y, hkls = [], [], []
+        for k, v in peaks.items():
+            if v[0] / top * 100 > minimum_intensity and k != "000":
+                x.append(v[1])
+                y.append(v[0])
+                hkls.append(k)
+        return ProfileSimulation(x, np.asarray(y) / max(y) * 100, hkls)

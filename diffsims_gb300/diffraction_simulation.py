@@ -157,3 +157,14 @@ class DiffractionSimulation:
     def rotate_shift_coordinates(self, angle, center=(0, 0), mirrored=False):
         """In-plane rotation (degrees), mirror across x and shift, in place."""
         self.coordinates = self._get_transformed_coordinates(angle, center, mirrored, units="real")
+
+
+class ProfileSimulation:
+    """A 1-D diffraction profile: peak magnitudes |g| (1/Angstrom),
+    intensities (largest 100) and hkl labels (diffsims/sims/diffraction_simulation.py:460-480;
+    ``get_plot`` is not provided)."""
+
+    def __init__(self, magnitudes, intensities, hkls):
+        self.magnitudes = magnitudes
+        self.intensities = intensities
+        self.hkls = hkls

@@ -51,13 +51,17 @@ class DiffpyLattice:
 
     def __init__(self, a=1.0, b=1.0, c=1.0, alpha=90.0, beta=90.0, gamma=90.0, base=None):
         if base is None:
+            # parameters are kept as given (diffpy's setLatPar)
+            self.a, self.b, self.c, self.alpha, self.beta, self.gamma = a, b, c, alpha, beta, gamma
             base = diffpy_stdbase(a, b, c, alpha, beta, gamma)
         base = np.asarray(base, dtype=np.float64)
         self.base = base
-        self.a, self.b, self.c = (float(np.linalg.norm(base[i])) for i in range(3))
-        self.alpha = math.degrees(math.acos(np.dot(base[1], base[2]) / (self.b * self.c)))
-        self.beta = math.degrees(math.acos(np.dot(base[0], base[2]) / (self.a * self.c)))
-        self.gamma = math.degrees(math.acos(np.dot(base[0], base[1]) / (self.a * self.b)))
+        if not hasattr(self, "a"):
+            # parameters derived from the base vectors (diffpy's setLatBase)
+            self.a, self.b, self.c = (float(np.linalg.norm(base[i])) for i in range(3))
+            self.alpha = math.degrees(math.acos(np.dot(base[1], base[2]) / (self.b * self.c)))
+            self.beta = math.degrees(math.acos(np.dot(base[0], base[2]) / (self.a * self.c)))
+            self.gamma = math.degrees(math.acos(np.dot(base[0], base[1]) / (self.a * self.b)))
         self.stdbase = diffpy_stdbase(self.a, self.b, self.c, self.alpha, self.beta, self.gamma)
         self.recbase = np.linalg.inv(base)
         self.metrics = base @ base.T
@@ -142,3 +146,47 @@ def calculate_ed_data(lattice: DiffpyLattice, elements, xyz, occupancy, dw, volt
     inten = ok.kinematical_intensities(idx, gsp, elements, xyz, occupancy, dw, scattering_params, prefactor=shf)
     keep = inten > np.max(inten) * minimum_intensity
     return g[keep], idx[keep], inten[keep], s[keep]
+
+
+def unique_families(hkls):
+    """get_unique_families (diffsims/utils/sim_utils.py:101-136): classes of
+    indices equal up to signs and order, in order of first appearance; each
+    class is keyed by its lexicographically largest member, with its size."""
+    classes = {}
+    for h in hkls:
+        key = tuple(sorted(np.abs(h)))
+        classes.setdefault(key, []).append(list(h))
+    return {tuple(sorted(v)[-1]): len(v) for v in classes.values()}
+
+
+def calculate_profile_data(lattice: DiffpyLattice, elements, xyz, occupancy, dw, reciprocal_radius=1.0,
+                           minimum_intensity=1e-3, scattering_params="lobato"):
+    """DiffractionGenerator.calculate_profile_data
+    (diffsims/generators/diffraction_generator.py:333-416) with
+    get_intensities_params (diffsims/utils/sim_utils.py:513-556).  Returns
+    (magnitudes, intensities scaled to 100, labels)."""
+    rl = lattice.reciprocal()
+    idx, _, dist = points_in_sphere(rl, reciprocal_radius)
+    i_to_d = {tuple(i): d for i, d in zip(idx, dist)}
+    fam = unique_families(idx.tolist())
+    mult = np.fromiter(fam.values(), dtype=float)
+    reps = np.array(list(fam))
+    g = [i_to_d[tuple(u)] for u in reps]
+    inten = ok.kinematical_intensities(reps, np.asarray(g), elements, xyz, occupancy, dw, scattering_params,
+                                       prefactor=mult)
+    labels_of = reps
+    if (lattice.a == lattice.b and lattice.alpha == 90 and lattice.beta == 90 and lattice.gamma == 120):
+        # the reference relabels with rows 0, 1, -(0 + 1), 2 of the family array
+        labels_of = (reps[0], reps[1], -reps[0] - reps[1], reps[2])
+    labels = ["".join(str(int(x)) for x in xs) for xs in labels_of]
+    peaks = {}
+    for lab, i, gg in zip(labels, inten, g):
+        peaks[lab] = [i, gg]
+    top = max(v[0] for v in peaks.values())
+    x, y, hk = [], [], []
+    for k, v in peaks.items():
+        if v[0] / top * 100 > minimum_intensity and k != "000":
+            x.append(v[1])
+            y.append(v[0])
+            hk.append(k)
+    return x, np.asarray(y) / max(y) * 100, hk

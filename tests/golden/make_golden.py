@@ -370,6 +370,12 @@ def legacy_cases():
     return cases
 
 
+def profile_cases():
+    """(structure, reciprocal_radius, DiffractionGenerator kwargs) of the 1-D profiles."""
+    return [("si", 1.0, {}), ("si", 2.5, {}), ("ni_hex", 1.0, {}), ("graphite", 2.0, {}),
+            ("p1", 1.2, {}), ("p1", 1.6, {"scattering_params": "xtables"})]
+
+
 def main_legacy(ref_root="/root/reference"):
     from oracle import legacy as ol
     dg = load_reference_legacy(ref_root)
@@ -385,6 +391,16 @@ def main_legacy(ref_root="/root/reference"):
         g[f"case{i}_indices"] = np.asarray(sim._indices)
         g[f"case{i}_intensities"] = np.asarray(sim._intensities)
     g["n_cases"] = np.array(len(legacy_cases()))
+    # 1-D profiles (calculate_profile_data)
+    profile_structs = dict(structs, ni_hex=((3.0, 3.0, 5.0, 90, 90, 120), ["Ni"], [[0, 0, 0]], [1.0]))
+    for j, (name, r, kw) in enumerate(profile_cases()):
+        lat, els, xyz, occ = profile_structs[name]
+        structure = _LegacyStructure([_LegacySite(e, x, o) for e, x, o in zip(els, xyz, occ)],
+                                     ol.DiffpyLattice(*lat))
+        prof = dg.DiffractionGenerator(300, **kw).calculate_profile_data(structure, reciprocal_radius=r)
+        g[f"profile{j}_magnitudes"] = np.asarray(prof.magnitudes, dtype=np.float64)
+        g[f"profile{j}_intensities"] = np.asarray(prof.intensities, dtype=np.float64)
+        g[f"profile{j}_hkls"] = np.asarray(prof.hkls, dtype=str)
     np.savez_compressed(HERE / "reference_legacy.npz", **g)
     print("wrote", HERE / "reference_legacy.npz", len(g), "arrays")
 

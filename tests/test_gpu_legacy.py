@@ -199,3 +199,20 @@ def test_library_generator_matches_single_calls():
                                           np.rint(one.coordinates[:, :2] / 0.02 + 72).astype(int))
     e = lib.get_library_entry("si", (10, 20, 30))
     assert e["Sim"] is lib["si"]["simulations"][1]
+
+
+@pytest.mark.parametrize("j", range(6))
+def test_profiles_match_reference_fixtures(ref, j):
+    """calculate_profile_data (diffraction_generator.py:333-416): the
+    reference's labels in its order, magnitudes and intensities (1e-9 on the
+    0-100 scale: FP64 on both sides)."""
+    from diffsims_gb300.diffraction_generator import DiffractionGenerator
+    from tests.golden.make_golden import profile_cases
+    from tests.test_oracle_legacy import profile_structures
+    name, r, kw = profile_cases()[j]
+    lat, els, xyz, occ = profile_structures()[name]
+    st = _LegacyStructure([_LegacySite(e, x, o) for e, x, o in zip(els, xyz, occ)], ol.DiffpyLattice(*lat))
+    prof = DiffractionGenerator(300, **kw).calculate_profile_data(st, reciprocal_radius=r)
+    assert list(prof.hkls) == list(ref[f"profile{j}_hkls"])
+    np.testing.assert_allclose(prof.magnitudes, ref[f"profile{j}_magnitudes"], rtol=1e-13)
+    np.testing.assert_allclose(prof.intensities, ref[f"profile{j}_intensities"], rtol=1e-9, atol=1e-9)

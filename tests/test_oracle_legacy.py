@@ -150,3 +150,20 @@ def test_structure_and_diffraction_library_containers(tmp_path):
     with pytest.raises(RuntimeError):
         load_DiffractionLibrary(f)
     assert load_DiffractionLibrary(f, safety=True)["a"]["orientations"] == dl["a"]["orientations"]
+
+
+def profile_structures():
+    from tests.golden.make_golden import legacy_structures as ls
+    return dict(ls(), ni_hex=((3.0, 3.0, 5.0, 90, 90, 120), ["Ni"], [[0, 0, 0]], [1.0]))
+
+
+@pytest.mark.parametrize("j", range(6))
+def test_oracle_profiles_match_reference_fixtures(ref, j):
+    from tests.golden.make_golden import profile_cases
+    name, r, kw = profile_cases()[j]
+    lat, els, xyz, occ = profile_structures()[name]
+    x, y, h = ol.calculate_profile_data(ol.DiffpyLattice(*lat), els, xyz, occ, np.zeros(len(els)), r,
+                                        scattering_params=kw.get("scattering_params", "lobato"))
+    assert list(h) == list(ref[f"profile{j}_hkls"])
+    np.testing.assert_allclose(x, ref[f"profile{j}_magnitudes"], rtol=1e-14)
+    np.testing.assert_allclose(y, ref[f"profile{j}_intensities"], rtol=1e-12, atol=1e-11)
