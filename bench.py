@@ -203,6 +203,24 @@ def fp32_peak_tflops(torch, lib, N):
     return best
 
 
+def rank_shard(n_per_rank, seed, rank):
+    """This rank's orientations: an independent uniform set drawn from
+    ``seed + 1000 * rank`` (weak scaling -- each rank simulates its own
+    shard; rank 0's shard is the single-GPU workload)."""
+    return uniform_quaternions(n_per_rank, seed + 1000 * rank)
+
+
+def max_over_ranks(value, dist, device):
+    """The largest value over all ranks (one all-reduce of one number; the
+    slowest rank's step time sets the whole job's)."""
+    import torch
+    if dist is None:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_gpu(args):
     import torch
     import diffsims_gb300 as ds
@@ -222,7 +240,7 @@ def run_gpu(args):
     lat, els, xyz, B = make_crystal(WORKLOAD["cell_seed"], WORKLOAD["n_atoms"])
     phase = ds.Phase("P1", ds.Structure([ds.Atom(e, x) for e, x in zip(els, xyz)], ds.Lattice(*lat)))
     n_o = args.orientations
-    q_host = uniform_quaternions(n_o, WORKLOAD["orientation_seed"])
+    q_host = rank_shard(n_o, WORKLOAD["orientation_seed"], rank)
     gen = ds.SimulationGenerator(WORKLOAD["accelerating_voltage"], "lobato",
                                  shape_factor_model=WORKLOAD["shape_factor_model"])
     r = WORKLOAD["reciprocal_radius"]
@@ -271,9 +289,7 @@ def run_gpu(args):
     clocks = clk.summary()
     ms = statistics.mean(step_ms)
     if dist:
-        t = torch.tensor([ms], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)  # the slowest rank's step time
-        ms = float(t.item())
+        ms = max_over_ranks(ms, dist, dev)  # the slowest rank's step time
         if rank != 0:
             dist.destroy_process_group()
             return
@@ -818,6 +834,48 @@ def run_case(args):
         batch.run()
         batch.run()
         out.update(patterns=sum(int(x.shape[0]) for x in qs), spots=int(batch.totals.sum()))
+    elif args.case == "families":
+        # the per-family leg's 2^20 Doyle-Turner families (96 orbit positions), two launches
+        from diffsims_gb300 import structure_factor as gsf
+        from diffsims_gb300.sim_utils import PackedAtoms
+        from oracle import structure_factor_families as osf
+        atoms = [ds.Atom("Fe", [0.11, 0.23, 0.37], 0.6, 0.005), ds.Atom("Ni", [0.11, 0.23, 0.37], 0.4, 0.009)]
+        sites = gsf._asymmetric_sites(atoms, osf.space_group_operations(221))
+        species, rows, xyz, occ, B = [], [], [], [], []
+        for k, (z, positions, o, biso) in enumerate(sites):
+            rows.append(gsf._coeff_row(z, N.DS_SCATTER_DOYLETURNER, 4.1 ** 3))
+            for p_ in positions:
+                species.append(k); xyz.append(p_); occ.append(o); B.append(4.0 * biso)
+        packed = PackedAtoms.from_rows(species, rows, np.asarray(xyz), occ, B, N.DS_SCATTER_DOYLETURNER, dev)
+        rng = np.random.default_rng(3)
+        n = 1 << 20
+        hkl = torch.from_numpy(rng.integers(-25, 26, (n, 3)).astype(np.float64)).to(dev)
+        s_ = torch.linalg.norm(hkl, dim=1) / (2 * 4.1)
+        F = torch.empty((n, 2), dtype=torch.float64, device=dev)
+        st = torch.zeros(1, dtype=torch.int32, device=dev)
+        lib = N.load_library()
+        for _ in range(2):
+            N.check(lib.ds_family_structure_factors(packed.cstruct(), N.ptr(hkl), N.ptr(s_), n, N.ptr(F), N.ptr(st),
+                                                    N.stream_handle()), "families")
+        N.check_device_status(st, "families")
+        out.update(families=n, orbit_positions=len(species))
+    elif args.case == "legacy":
+        # the legacy leg's 12-atom P1 sphere table at r = 2.0 and 8192 Euler triples
+        from diffsims_gb300.diffraction_generator import DiffractionGenerator, euler_rzxz_quaternions, structure_base
+        from diffsims_gb300.sim_utils import PackedAtoms
+        rng = np.random.default_rng(31)
+        els = list(rng.choice(["C", "O", "Si", "Fe"], 12))
+        xyz, occ = rng.random((12, 3)), rng.uniform(0.6, 1.0, 12)
+        recip = np.ascontiguousarray(np.linalg.inv(structure_base(ds.Lattice(6.3, 7.1, 8.2, 84.0, 97.0, 103.0))).T)
+        atoms = PackedAtoms(els, xyz, occ, np.zeros(12), "lobato", dev)
+        q = euler_rzxz_quaternions(np.random.default_rng(7).uniform(-180, 180, (8192, 3)))
+        q[:, 1:] *= -1
+        quats = torch.from_numpy(q).to(dev)
+        settings = DiffractionGenerator(200)._gen.settings(1e-2)
+        for _ in range(2):
+            tab = PhaseTable.sphere(recip, atoms, 2.0, device=dev)
+            sp = simulate_phase(tab, quats, settings, 2.0, SpotBuffers(dev))
+        out.update(patterns=8192, spots=sp.total, n_hkl=tab.n)
     torch.cuda.synchronize()
     print(json.dumps(out))
 
@@ -894,7 +952,7 @@ def main():
     ap.add_argument("--skip-batch", action="store_true", help="leave out the batched-phases leg")
     ap.add_argument("--skip-families", action="store_true", help="leave out the per-family structure-factor leg")
     ap.add_argument("--skip-legacy", action="store_true", help="leave out the legacy calculate_ed_data leg")
-    ap.add_argument("--case", default=None, choices=["raster", "adjoint", "batch"],
+    ap.add_argument("--case", default=None, choices=["raster", "adjoint", "batch", "families", "legacy"],
                     help="run one small profiling case instead of the benchmark")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--out-dir", default=None)
