@@ -9,9 +9,12 @@ import numpy as np
 import torch
 
 from . import _native as N
-from .crystal import Phase, Rotation, quaternions_of
-from .engine import PhaseBatch, PhaseTable, SimSettings, SpotBuffers, simulate_phase, simulate_phase_streamed
+from .crystal import Phase, Rotation, lattice_params, quaternions_of, structure_of
+from .engine import (PhaseBatch, PhaseTable, SimSettings, SpotBuffers, reciprocal_basis, simulate_phase,
+                     simulate_phase_streamed)
+from .simulation1d import Simulation1D
 from .simulation2d import Simulation2D
+from .structure_factor import _space_group_operations
 from .sim_utils import get_electron_wavelength
 
 _SHAPE_NAMES = ("linear", "atanc", "sinc", "sin2c", "lorentzian")
@@ -28,6 +31,60 @@ def _shape_name(model):
     if name in _SHAPE_NAMES + ("binary",) and mod.endswith("shape_factor_models"):
         return name
     return None
+
+
+# ------------------------------------------------------------ 1-D profiles
+def point_group_rotations(space_group) -> np.ndarray:
+    """Distinct rotation parts R (fractional basis, integer, improper ones
+    included) of a space group's operations -- the point group that acts on
+    Miller indices as h -> h R.  ``None`` or 1 gives the identity alone."""
+    ops = _space_group_operations(space_group)
+    return np.unique(np.array([np.rint(R).astype(np.int64) for R, _ in ops]), axis=0)
+
+
+def symmetry_families(hkl, recip, rotations):
+    """One representative per family of symmetry-equivalent indices, as
+    ReciprocalLatticeVector.unique(use_symmetry=True)
+    (diffsims/crystallography/reciprocal_lattice_vector.py:1531-1548): every
+    vector's orbit {h R} in Cartesian coordinates rounded to 6 decimals, its
+    rows sorted by (z, y, x), the distinct orbits in ascending order of those
+    sorted rows, reversed; each family is represented by its first member in
+    the input order.  Returns (rows of ``hkl``, multiplicities = orbit sizes).
+    ``hkl`` (n, 3) integers, ``recip`` rows a*, b*, c*, ``rotations`` (m, 3, 3)."""
+    hkl = np.asarray(hkl, dtype=np.int64).reshape(-1, 3)
+    n = hkl.shape[0]
+    if n == 0:
+        return np.zeros(0, dtype=np.int64), np.zeros(0)
+    orbit = np.einsum("ni,oij->noj", hkl, np.asarray(rotations, dtype=np.int64))
+    data = (orbit.astype(np.float64) @ np.asarray(recip, dtype=np.float64)).round(6)
+    # per orbit: rows ordered by z, then y, then x (three stable sorts)
+    for col in (0, 1, 2):
+        order = np.argsort(data[:, :, col], axis=1, kind="stable")
+        data = np.take_along_axis(data, order[:, :, None], axis=1)
+        orbit = np.take_along_axis(orbit, order[:, :, None], axis=1)
+    _, idx = np.unique(data.reshape(n, -1), axis=0, return_index=True)
+    reps = idx[::-1]
+    mult = np.array([len({tuple(r) for r in orbit[i].tolist()}) for i in reps], dtype=np.float64)
+    return reps, mult
+
+
+def _min_dspacing_rows(phase, min_dspacing, scattering_params, debye_waller_factors):
+    """hkl rows of ReciprocalLatticeVector.from_min_dspacing (GPU enumeration),
+    their |g| and FP64 |F|^2 (GPU structure factors)."""
+    N.load_library()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    table = PhaseTable(phase, 1.0 / min_dspacing, False, scattering_params, debye_waller_factors, form="fp64",
+                       device=dev)
+    if table.n == 0:
+        return np.zeros((0, 3), dtype=np.int64), np.zeros(0), np.zeros(0)
+    torch.cuda.current_stream().synchronize()
+    return (table.hkl_host().astype(np.int64), np.sqrt(table.g2.cpu().numpy()),
+            table.F2d[:table.n].cpu().numpy())
+
+
+def _is_hexagonal(lattice) -> bool:
+    return bool(np.allclose(lattice_params(lattice)[3:], [90, 90, 120]))
+
 
 
 class SimulationGenerator:
@@ -152,3 +209,29 @@ class SimulationGenerator:
         if single_phase:
             return Simulation2D(phases[0], spots, rots[0], self, reciprocal_radius)
         return Simulation2D(phases, spots, rots, self, reciprocal_radius)
+
+    def calculate_diffraction1d(self, phase, reciprocal_radius: float = 1.0, minimum_intensity: float = 1e-3,
+                                 debye_waller_factors: dict = None):
+        """1-D profile of one phase (diffsims/generators/simulation_generator.py:261-317):
+        the hkl set of ``from_min_dspacing`` with its default 0.7 Angstrom (as the
+        reference, ``reciprocal_radius`` is only stored in the result), one
+        vector per family of the phase's point group (``symmetry_families``),
+        intensities multiplicity x |F|^2 on the GPU, scaled so the largest is
+        100, peaks above ``minimum_intensity`` kept; hkil indices for hexagonal
+        lattices.  The point group comes from ``phase.space_group`` (a diffpy
+        ``SpaceGroup``, operations with ``R`` and ``t``, ``(R, t)`` pairs, or
+        ``None`` for P1)."""
+        hkl, gspacing, F2 = _min_dspacing_rows(phase, 0.7, self.scattering_params, debye_waller_factors)
+        structure = structure_of(phase)
+        reps, mult = symmetry_families(hkl, reciprocal_basis(structure.lattice),
+                                       point_group_rotations(getattr(phase, "space_group", None)))
+        hkl_r = hkl[reps].astype(np.float64)
+        g_vectors = gspacing[reps]
+        intensities = mult * F2[reps]
+        if _is_hexagonal(structure.lattice):
+            hkl_r = np.column_stack([hkl_r[:, 0], hkl_r[:, 1], -(hkl_r[:, 0] + hkl_r[:, 1]), hkl_r[:, 2]])
+        intensities = np.asarray(intensities) / max(intensities) * 100
+        mask = intensities > minimum_intensity
+        return Simulation1D(phase=phase, reciprocal_spacing=g_vectors[mask], intensities=intensities[mask],
+                            hkl=hkl_r[mask], reciprocal_radius=reciprocal_radius, wavelength=self.wavelength)
+

@@ -607,3 +607,48 @@ def polar_flatten(patterns, radial_axes=None, azimuthal_axes=None):
         r_t = np.array(r_t, dtype=int)
         t_t = np.array(t_t, dtype=int)
     return r_t, t_t, i_t
+
+
+# --------------------------------------------------------------------------
+# 1-D profiles: SimulationGenerator.calculate_diffraction1d
+# --------------------------------------------------------------------------
+def unique_with_symmetry(hkl, rbase, rotations):
+    """ReciprocalLatticeVector.unique(use_symmetry=True)
+    (diffsims/crystallography/reciprocal_lattice_vector.py:1531-1548), with
+    orix's point-group orbit of each vector taken as {h R} (R the rotation
+    parts of the space group, acting on Miller indices) and orix's
+    ``Vector3d.unique`` as order-preserving (the order from_min_dspacing
+    keeps): per vector the orbit's Cartesian coordinates rounded to 6
+    decimals, rows lexsorted (z, then y, then x), np.unique over the orbits,
+    reversed.  Returns (rows, orbit sizes)."""
+    hkl = np.asarray(hkl).reshape(-1, 3)
+    n = hkl.shape[0]
+    orbits = [hkl[i] @ np.asarray(rotations) for i in range(n)]  # (m, 3) per vector; row o = h R_o
+    data = np.array([(o @ rbase).round(6) for o in orbits])
+    data_sorted = np.zeros_like(data)
+    for i in range(n):
+        a = data[i]
+        data_sorted[i] = a[np.lexsort(a.T)]
+    _, idx = np.unique(data_sorted, return_index=True, axis=0)
+    reps = idx[::-1]
+    mult = np.array([len({tuple(r) for r in orbits[i].tolist()}) for i in reps], dtype=float)
+    return reps, mult
+
+
+def diffraction1d(crystal: "Crystal", rotations, scattering_params="lobato", minimum_intensity=1e-3):
+    """calculate_diffraction1d (diffsims/generators/simulation_generator.py:261-317):
+    from_min_dspacing at its default 0.7 Angstrom, families by
+    ``unique_with_symmetry``, I = multiplicity |F|^2 scaled to 100, kept above
+    ``minimum_intensity``; hkil for hexagonal cells.  Returns (|g|, I, indices)."""
+    rb = crystal.rbase
+    hkl = enumerate_hkl(rb, 0.7)
+    g = np.sqrt(g_squared(g_cartesian(hkl, rb)))
+    reps, mult = unique_with_symmetry(hkl, rb, rotations)
+    hr = hkl[reps].astype(float)
+    inten = kinematical_intensities(hr, g[reps], crystal.elements, crystal.xyz, crystal.occupancy, crystal.B,
+                                    scattering_params, prefactor=mult)
+    if np.allclose(crystal.lattice[3:], [90, 90, 120]):
+        hr = np.column_stack([hr[:, 0], hr[:, 1], -(hr[:, 0] + hr[:, 1]), hr[:, 2]])
+    inten = np.asarray(inten) / max(inten) * 100
+    keep = inten > minimum_intensity
+    return g[reps][keep], inten[keep], hr[keep]
