@@ -14,7 +14,7 @@ from .engine import (PhaseBatch, PhaseTable, SimSettings, SpotBuffers, reciproca
                      simulate_phase_streamed)
 from .simulation1d import Simulation1D
 from .simulation2d import Simulation2D
-from .structure_factor import _space_group_operations
+from .symmetry import point_group_rotations, symmetry_families  # noqa: F401  (public here too)
 from .sim_utils import get_electron_wavelength
 
 _SHAPE_NAMES = ("linear", "atanc", "sinc", "sin2c", "lorentzian")
@@ -34,40 +34,6 @@ def _shape_name(model):
 
 
 # ------------------------------------------------------------ 1-D profiles
-def point_group_rotations(space_group) -> np.ndarray:
-    """Distinct rotation parts R (fractional basis, integer, improper ones
-    included) of a space group's operations -- the point group that acts on
-    Miller indices as h -> h R.  ``None`` or 1 gives the identity alone."""
-    ops = _space_group_operations(space_group)
-    return np.unique(np.array([np.rint(R).astype(np.int64) for R, _ in ops]), axis=0)
-
-
-def symmetry_families(hkl, recip, rotations):
-    """One representative per family of symmetry-equivalent indices, as
-    ReciprocalLatticeVector.unique(use_symmetry=True)
-    (diffsims/crystallography/reciprocal_lattice_vector.py:1531-1548): every
-    vector's orbit {h R} in Cartesian coordinates rounded to 6 decimals, its
-    rows sorted by (z, y, x), the distinct orbits in ascending order of those
-    sorted rows, reversed; each family is represented by its first member in
-    the input order.  Returns (rows of ``hkl``, multiplicities = orbit sizes).
-    ``hkl`` (n, 3) integers, ``recip`` rows a*, b*, c*, ``rotations`` (m, 3, 3)."""
-    hkl = np.asarray(hkl, dtype=np.int64).reshape(-1, 3)
-    n = hkl.shape[0]
-    if n == 0:
-        return np.zeros(0, dtype=np.int64), np.zeros(0)
-    orbit = np.einsum("ni,oij->noj", hkl, np.asarray(rotations, dtype=np.int64))
-    data = (orbit.astype(np.float64) @ np.asarray(recip, dtype=np.float64)).round(6)
-    # per orbit: rows ordered by z, then y, then x (three stable sorts)
-    for col in (0, 1, 2):
-        order = np.argsort(data[:, :, col], axis=1, kind="stable")
-        data = np.take_along_axis(data, order[:, :, None], axis=1)
-        orbit = np.take_along_axis(orbit, order[:, :, None], axis=1)
-    _, idx = np.unique(data.reshape(n, -1), axis=0, return_index=True)
-    reps = idx[::-1]
-    mult = np.array([len({tuple(r) for r in orbit[i].tolist()}) for i in reps], dtype=np.float64)
-    return reps, mult
-
-
 def _min_dspacing_rows(phase, min_dspacing, scattering_params, debye_waller_factors):
     """hkl rows of ReciprocalLatticeVector.from_min_dspacing (GPU enumeration),
     their |g| and FP64 |F|^2 (GPU structure factors)."""

@@ -30,6 +30,9 @@ from scipy.constants import c as _C, e as _E, h as _H, physical_constants
 
 from . import _native as N
 from .sim_utils import PackedAtoms, _TABLES
+from .crystal import sites_of
+from .engine import reciprocal_basis
+from .symmetry import _space_group_operations, expand_position, point_group_rotations, symmetry_families  # noqa: F401
 
 __all__ = [
     "get_doyleturner_atomic_scattering_factor",
@@ -40,6 +43,7 @@ __all__ = [
     "get_doyleturner_structure_factor",
     "get_kinematical_structure_factor",
     "get_refraction_corrected_wavelength",
+    "calculate_structure_factor",
 ]
 
 ELEMENTS = list(_TABLES["elements"])
@@ -79,42 +83,6 @@ def get_atomic_scattering_parameters(element, unit=None):
     factor = 1e-2 if (unit is not None and unit.lower() == "nm") else 1
     row = ATOMIC_SCATTERING_PARAMETERS_DOYLETURNER[_element_id(element) - 1]
     return row[:4] * factor, row[4:] * factor
-
-
-# --------------------------------------------------------- space groups
-def _space_group_operations(space_group):
-    if space_group is None or (isinstance(space_group, (int, np.integer)) and int(space_group) == 1):
-        return [(np.eye(3), np.zeros(3))]
-    if isinstance(space_group, (int, np.integer)):
-        raise NotImplementedError(
-            f"space group {int(space_group)} given by number: pass its operations (a diffpy SpaceGroup, an object "
-            "with iter_symops() / symop_list, or (R, t) pairs)")
-    if hasattr(space_group, "iter_symops"):
-        ops = list(space_group.iter_symops())
-    elif hasattr(space_group, "symop_list"):
-        ops = list(space_group.symop_list)
-    else:
-        ops = list(space_group)
-    out = []
-    for op in ops:
-        R, t = (op.R, op.t) if hasattr(op, "R") else op
-        out.append((np.asarray(R, dtype=np.float64).reshape(3, 3), np.asarray(t, dtype=np.float64).reshape(3)))
-    return out
-
-
-def expand_position(space_group, xyz, eps=1e-5):
-    """Distinct images ``R xyz + t`` of a fractional position, reduced into
-    [0, 1) (diffpy ``expandPosition(spacegroup, xyz)[0]``, called at
-    diffsims/structure_factor/structure_factor.py:94,162)."""
-    out = []
-    xyz = np.asarray(xyz, dtype=np.float64)
-    for R, t in _space_group_operations(space_group):
-        p = R @ xyz + t
-        p = p - np.floor(p)
-        if any(np.all(np.abs((p - q) - np.rint(p - q)) < eps) for q in out):
-            continue
-        out.append(p)
-    return np.array(out).reshape(-1, 3)
 
 
 def find_asymmetric_positions(positions, space_group):
@@ -274,3 +242,47 @@ def get_doyleturner_atomic_scattering_factor(atom, scattering_parameter, unit_ce
     """Doyle-Turner atomic scattering factor with occupancy and Debye-Waller
     factor (diffsims/structure_factor/atomic_scattering_factor.py:69-124)."""
     return _atom_factor(atom, scattering_parameter, N.DS_SCATTER_DOYLETURNER, float(unit_cell_volume))
+
+
+def _structure_factors_fp64(structure, hkl, g2, scattering_params):
+    """Complex F = sum_j f_j(g) occ_j exp(2 pi i h.x_j) (no Debye-Waller term)
+    of the given reflections: ds_structure_factors, FP64 form."""
+    lib = N.load_library()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    els, xyz, occ = sites_of(structure)
+    atoms = PackedAtoms(els, xyz, occ, np.zeros(len(els)), scattering_params, dev)
+    n = hkl.shape[0]
+    h = torch.as_tensor(np.ascontiguousarray(hkl, dtype=np.float64)).to(dev)
+    g = torch.as_tensor(np.ascontiguousarray(g2, dtype=np.float64)).to(dev)
+    F = torch.empty((max(n, 1), 2), dtype=torch.float64, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    N.check(lib.ds_structure_factors(atoms.cstruct(), None, N.ptr(h), N.ptr(g), n, N.DS_FORM_FP64, None, None,
+                                     N.ptr(F), None, 0, N.ptr(status), N.stream_handle()), "structure factors")
+    N.check_device_status(status, "structure factors")
+    F = F[:n].cpu().numpy()
+    return F[:, 0] + 1j * F[:, 1]
+
+
+def calculate_structure_factor(phase, hkl, scattering_params="xtables"):
+    """ReciprocalLatticeVector.calculate_structure_factor
+    (diffsims/crystallography/reciprocal_lattice_vector.py:647-720) for the
+    vectors ``hkl`` ((..., 3) integer Miller indices) of ``phase``: the
+    vectors are grouped into sets of symmetry-equivalent indices under the
+    phase's point group (``get_hkl_sets``, :766-820), the complex structure
+    factor of each set's first vector is computed on the GPU (FP64; the
+    formula of diffsims/utils/sim_utils.py:256-304 without Debye-Waller
+    factors, as the reference calls it) and given to every vector of the
+    set.  ``phase.structure`` must hold every atom of the cell (the
+    reference's ``sanitise_phase``).  Returns complex values of shape
+    ``hkl.shape[:-1]``."""
+    h = np.asarray(hkl, dtype=np.float64)
+    shape = h.shape[:-1]
+    h = h.reshape(-1, 3)
+    structure = phase.structure
+    recip = reciprocal_basis(structure.lattice)
+    reps, _, family = symmetry_families(np.rint(h).astype(np.int64), recip,
+                                        point_group_rotations(getattr(phase, "space_group", None)),
+                                        return_inverse=True)
+    g = h[reps] @ recip
+    F = _structure_factors_fp64(structure, h[reps], np.sum(g * g, axis=1), scattering_params)
+    return F[family].reshape(shape)

@@ -197,3 +197,36 @@ def test_entry_rejects_bad_arguments():
     with pytest.raises(NotImplementedError):
         get_kinematical_structure_factor(phase, [1, 1, 1], 0.2)
     assert get_kinematical_structure_factor(kat_phase("nickel"), np.zeros((0, 3)), np.zeros(0)).shape == (0,)
+
+
+def test_calculate_structure_factor_on_gpu():
+    """ReciprocalLatticeVector.calculate_structure_factor on the GPU: the
+    reference's doctest (Al, xtables and lobato) and table (Ni) values, and
+    the FP64 oracle for every set of a P6_3mc phase (1e-12 of the largest)."""
+    from diffsims_gb300.crystal import Atom, Lattice, Phase, Structure
+    from diffsims_gb300.structure_factor import calculate_structure_factor
+    from oracle import kinematic as ok
+    from tests.test_oracle_structure_factor import _al_phase, _ni_phase
+    F = calculate_structure_factor(_al_phase(), [[1, 1, 1], [2, 0, 0]])
+    np.testing.assert_allclose(F.real, [8.46881663, 7.04777513], rtol=1e-8)
+    F = calculate_structure_factor(_al_phase(), [[1, 1, 1], [2, 0, 0]], "lobato")
+    np.testing.assert_allclose(F.real, [8.44934816, 7.0387957], rtol=1e-8)
+    F = np.abs(calculate_structure_factor(_ni_phase(), [[1, 1, 1], [2, 0, 0]]))
+    assert [f"{v:.1f}" for v in F] == ["11.8", "10.4"]
+    atoms = [Atom("Si", [0, 0, 0]), Atom("Si", [1 / 3, 2 / 3, 0.5]), Atom("C", [0, 0, 0.188]),
+             Atom("C", [1 / 3, 2 / 3, 0.688])]
+    lat = (3.073, 3.073, 10.053, 90, 90, 120)
+    phase = Phase("sic", Structure(atoms, Lattice(*lat)), space_group=osf.space_group_operations(186))
+    rb = ok.reciprocal_base(ok.lattice_base(*lat))
+    hkl = ok.enumerate_hkl(rb, 0.8)
+    F = calculate_structure_factor(phase, hkl, "lobato")
+    rot = np.unique(np.array([np.rint(R).astype(int) for R, _ in osf.space_group_operations(186)]), axis=0)
+    key = [frozenset(tuple(r) for r in (h @ rot).tolist()) for h in hkl]
+    first = {}
+    for i, k in enumerate(key):
+        first.setdefault(k, i)
+    src = np.array([first[k] for k in key])
+    g = np.sqrt(ok.g_squared(ok.g_cartesian(hkl[src], rb)))
+    want = ok.structure_factor(hkl[src], g, [a.element for a in atoms], [a.xyz for a in atoms], [1.0] * 4,
+                               np.zeros(4), "lobato")
+    np.testing.assert_allclose(F, want, rtol=0, atol=1e-12 * np.max(np.abs(want)))

@@ -181,3 +181,72 @@ def test_host_element_table():
                                   osf.doyleturner_parameters("Fe", "nm")[0])
     with pytest.raises(KeyError):
         gsf.get_element_id_from_string("Xx")
+
+
+# --------------------------------- ReciprocalLatticeVector.calculate_structure_factor
+def _al_phase(sg=225):
+    from diffsims_gb300.crystal import Atom, Lattice, Phase, Structure
+    atoms = [Atom("Al", x) for x in ([0, 0, 0], [0, .5, .5], [.5, 0, .5], [.5, .5, 0])]
+    return Phase("al", Structure(atoms, Lattice(4.04, 4.04, 4.04)), space_group=osf.space_group_operations(sg))
+
+
+def _ni_phase():
+    from diffsims_gb300.crystal import Atom, Lattice, Phase, Structure
+    atoms = [Atom("Ni", x, Uisoequiv=0.006332) for x in ([0, 0, 0], [0, .5, .5], [.5, 0, .5], [.5, .5, 0])]
+    return Phase("nickel", Structure(atoms, Lattice(3.5236, 3.5236, 3.5236)),
+                 space_group=osf.space_group_operations(225))
+
+
+def _oracle_sf(monkeypatch):
+    from diffsims_gb300 import structure_factor as gsf
+    from oracle import kinematic as ok
+
+    def fp64(structure, hkl, g2, sp):
+        els = [a.element for a in structure]
+        xyz = [a.xyz for a in structure]
+        occ = [a.occupancy for a in structure]
+        return ok.structure_factor(hkl, np.sqrt(g2), els, xyz, occ, np.zeros(len(els)), sp)
+
+    monkeypatch.setattr(gsf, "_structure_factors_fp64", fp64)
+    return gsf
+
+
+def test_calculate_structure_factor_doctest(monkeypatch):
+    # diffsims/crystallography/reciprocal_lattice_vector.py:665-690 (Al, a = 4.04)
+    gsf = _oracle_sf(monkeypatch)
+    F = gsf.calculate_structure_factor(_al_phase(), [[1, 1, 1], [2, 0, 0]])
+    np.testing.assert_allclose(F.real, [8.46881663, 7.04777513], rtol=1e-8)
+    assert np.all(np.abs(F.imag) < 1e-12)
+    F = gsf.calculate_structure_factor(_al_phase(), [[1, 1, 1], [2, 0, 0]], "lobato")
+    np.testing.assert_allclose(F.real, [8.44934816, 7.0387957], rtol=1e-8)
+
+
+def test_calculate_structure_factor_table_kat(monkeypatch):
+    # diffsims/tests/crystallography/test_reciprocal_lattice_vector.py:330-338 (print_table)
+    gsf = _oracle_sf(monkeypatch)
+    F = np.abs(gsf.calculate_structure_factor(_ni_phase(), [[1, 1, 1], [2, 0, 0]]))
+    assert [f"{v:.1f}" for v in F] == ["11.8", "10.4"]
+    assert [f"{v:.1f}" for v in F ** 2] == ["140.0", "108.2"]
+    assert f"{(F ** 2 / (F ** 2).max() * 100)[1]:.1f}" == "77.3"
+
+
+def test_calculate_structure_factor_sets(monkeypatch):
+    """Every vector gets the value of its set's first vector (get_hkl_sets):
+    in a non-centrosymmetric, non-symmorphic group (P6_3mc) equivalent
+    reflections can differ in phase, and the reference copies the first."""
+    from diffsims_gb300.crystal import Atom, Lattice, Phase, Structure
+    gsf = _oracle_sf(monkeypatch)
+    atoms = [Atom("Si", [0, 0, 0]), Atom("Si", [1 / 3, 2 / 3, 0.5]), Atom("C", [0, 0, 0.188]),
+             Atom("C", [1 / 3, 2 / 3, 0.688])]
+    phase = Phase("sic", Structure(atoms, Lattice(3.073, 3.073, 10.053, 90, 90, 120)),
+                  space_group=osf.space_group_operations(186))
+    hkl = np.array([[1, 0, 1], [0, 1, 1], [-1, 0, 1], [1, 0, -1], [0, 0, 4], [1, 1, 0], [-1, -1, 0], [1, 0, 1]])
+    F = gsf.calculate_structure_factor(phase, hkl.reshape(2, 4, 3))
+    assert F.shape == (2, 4)
+    F = F.reshape(-1)
+    rot = np.unique(np.array([np.rint(R).astype(int) for R, _ in osf.space_group_operations(186)]), axis=0)
+    orbit = [{tuple(r) for r in (h @ rot).tolist()} for h in hkl]
+    for i in range(len(hkl)):
+        first = next(j for j in range(len(hkl)) if tuple(hkl[i]) in orbit[j])
+        assert F[i] == F[first]
+    assert F[0] == F[2]  # (-1, 0, 1) is in the set of (1, 0, 1) and copies its value
