@@ -57,7 +57,14 @@ class Lattice:
         return np.linalg.inv(self.base).T
 
 
+def _check_cell(a, b, c, alpha, beta, gamma):
+    p = np.array([a, b, c, alpha, beta, gamma], dtype=np.float64)
+    if not (np.all(np.isfinite(p)) and np.all(p[:3] > 0) and np.all((p[3:] > 0) & (p[3:] < 180))):
+        raise ValueError(f"invalid lattice: a={a} b={b} c={c} alpha={alpha} beta={beta} gamma={gamma}")
+
+
 def lattice_base(a, b, c, alpha, beta, gamma) -> np.ndarray:
+    _check_cell(a, b, c, alpha, beta, gamma)
     al, be, ga = np.deg2rad([alpha, beta, gamma])
     ca, cb, cg, sg = np.cos(al), np.cos(be), np.cos(ga), np.sin(ga)
     cx = c * cb
@@ -74,6 +81,7 @@ def diffpy_base(a, b, c, alpha, beta, gamma) -> np.ndarray:
     ``DiffractionGenerator``: c along z, b in the yz-plane (so a* is along x).
     Built from the cell geometry: b = b (0, sin alpha, cos alpha); a_z from
     a.c, a_y from a.b, a_x > 0 from |a|."""
+    _check_cell(a, b, c, alpha, beta, gamma)
     al, be, ga = np.deg2rad([alpha, beta, gamma])
     bv = np.array([0.0, b * math.sin(al), b * math.cos(al)])
     az = a * math.cos(be)

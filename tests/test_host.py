@@ -151,3 +151,76 @@ def test_precession_tight_quadrature_agrees_with_reference_quadrature():
         a = ok.sf_precession_integral_tight(s, r, np.deg2rad(1.0), m, 0.015)
         b = ok.sf_precession_integral(s, r, np.deg2rad(1.0), ok.ALL_SHAPE_MODELS[m], 0.015)
         np.testing.assert_allclose(a, b, rtol=1e-7, atol=1e-9)
+
+
+# ---------------------------------------------------------------- failures on the host
+def test_degenerate_and_non_finite_inputs_raise():
+    """Bad cells and rotations are rejected on the host before any launch."""
+    from diffsims_gb300.crystal import Rotation, diffpy_base, lattice_base
+    for bad in [(4.0, 4.0, 4.0, 90, 90, 180), (4.0, 4.0, float("nan"), 90, 90, 90), (1, 1, 1, 10, 170, 90)]:
+        with pytest.raises(ValueError):
+            lattice_base(*bad)
+        with pytest.raises(ValueError):
+            diffpy_base(*bad)
+    for q in ([0, 0, 0, 0], [1, float("nan"), 0, 0], [float("inf"), 0, 0, 0]):
+        with pytest.raises(ValueError):
+            Rotation(q)
+
+
+def test_unknown_element_warns_with_zero_coefficients():
+    """diffsims/utils/sim_utils.py:213-219: a warning and zero scattering
+    coefficients (the packing runs on the host; a CPU tensor suffices)."""
+    import torch
+    from diffsims_gb300.sim_utils import PackedAtoms
+    with pytest.warns(UserWarning, match="Xx"):
+        a = PackedAtoms(["Fe", "Xx2+"], np.zeros((2, 3)), [1.0, 1.0], [0.0, 0.0], "lobato", torch.device("cpu"))
+    coeffs = a.coeffs.numpy().reshape(-1, 10)
+    assert np.any(coeffs[0] != 0) and np.all(coeffs[1] == 0)
+    with pytest.raises(NotImplementedError):
+        PackedAtoms(["Fe"], np.zeros((1, 3)), [1.0], [0.0], "waasmaier", torch.device("cpu"))
+
+
+def test_new_entries_reject_bad_arguments_before_any_launch(lib):
+    """Argument errors come back as DS_ERR_INVALID_ARGUMENT with a message,
+    checked before any CUDA call (so this runs without a GPU)."""
+    from diffsims_gb300 import _native as N
+    r = (ctypes.c_double * 9)(*([0.25, 0, 0, 0, 0.25, 0, 0, 0, 0.25]))
+    hm = (ctypes.c_int32 * 3)(2, 2, 2)
+    fake = ctypes.c_void_p(4096)  # never dereferenced: validation fails first
+    assert lib.ds_enumerate_sphere(r, hm, -1.0, fake, fake, 125, fake, fake, 1 << 20, fake, None) == N.DS_ERR_INVALID_ARGUMENT
+    assert "radius" in lib.ds_last_error().decode()
+    assert lib.ds_enumerate_sphere(r, hm, 1.0, fake, fake, 124, fake, fake, 1 << 20, fake, None) == N.DS_ERR_INVALID_ARGUMENT
+    assert "capacity" in lib.ds_last_error().decode()
+    neg = (ctypes.c_int32 * 3)(2, -1, 2)
+    assert lib.ds_enumerate_sphere(r, neg, 1.0, fake, fake, 125, fake, fake, 1 << 20, fake, None) == N.DS_ERR_INVALID_ARGUMENT
+    atoms = N.ds_atoms(1, 1, 4096, 4096, N.DS_SCATTER["lobato"], 0)
+    assert lib.ds_family_structure_factors(atoms, fake, fake, 4, fake, fake, None) == N.DS_ERR_INVALID_ARGUMENT
+    assert "kind" in lib.ds_last_error().decode()
+    atoms = N.ds_atoms(1, 40, 4096, 4096, N.DS_SCATTER_DOYLETURNER, 0)
+    assert lib.ds_family_structure_factors(atoms, fake, fake, 4, fake, fake, None) == N.DS_ERR_INVALID_ARGUMENT
+    atoms = N.ds_atoms(1, 1, 4096 + 8, 4096, N.DS_SCATTER_KINEMATICAL, 0)
+    assert lib.ds_family_structure_factors(atoms, fake, fake, 4, fake, fake, None) == N.DS_ERR_INVALID_ARGUMENT
+    assert "aligned" in lib.ds_last_error().decode()
+    atoms = N.ds_atoms(1, 1, 4096, 4096, N.DS_SCATTER_KINEMATICAL, 0)
+    assert lib.ds_family_structure_factors(atoms, None, fake, 4, fake, fake, None) == N.DS_ERR_INVALID_ARGUMENT
+    assert lib.ds_family_structure_factors(atoms, fake, fake, -1, fake, fake, None) == N.DS_ERR_INVALID_ARGUMENT
+
+
+@pytest.mark.skipif(__import__("torch").cuda.is_available(), reason="checks the behaviour without a CUDA device")
+def test_compute_calls_fail_loudly_without_a_gpu():
+    """No CPU fallback: every compute entry of the package raises."""
+    import diffsims_gb300 as ds
+    from diffsims_gb300 import _native as N
+    from diffsims_gb300 import structure_factor as gsf
+    al = ds.Phase("Al", ds.Structure([ds.Atom("Al", [0, 0, 0])], ds.Lattice(4.05, 4.05, 4.05)))
+    calls = [
+        lambda: ds.SimulationGenerator(200).calculate_diffraction2d(al, ds.Rotation.identity()),
+        lambda: ds.SimulationGenerator(200).calculate_diffraction1d(al),
+        lambda: ds.get_kinematical_intensities(al.structure, [[1, 1, 1]], [0.4]),
+        lambda: ds.DiffractionGenerator(200).calculate_ed_data(al.structure, 1.0),
+        lambda: gsf.get_kinematical_structure_factor(al, [1, 1, 1], 0.2),
+        lambda: gsf.calculate_structure_factor(al, [[1, 1, 1]]),
+    ]
+    for call in calls:
+        with pytest.raises(N.NativeError):
+            call()
