@@ -10,6 +10,8 @@ loop of SimulationGenerator.calculate_diffraction2d
 from __future__ import annotations
 
 import ctypes as C
+import json
+import os
 from dataclasses import dataclass
 
 import numpy as np
@@ -726,16 +728,50 @@ class Autotuner:
     smaller tiles so their bitmap fits shared memory) and the per-CTA
     candidate staging (screened reflections held per tile before the ordered
     writes).  Remembers the choice per problem class (phases, orientations
-    and table sizes in powers of two, shape model, precession, form)."""
+    and table sizes in powers of two, shape model, precession, form); with a
+    ``path`` (or the environment variable ``DS_AUTOTUNE_CACHE``) the choices
+    also persist in a JSON file keyed by GPU name, so a later process on the
+    same kind of GPU skips the timing runs."""
 
     TILES = (4, 8, 16, 32)
     STAGE_PER_ORIENT = (384, 1536, 4096)  # staging capacity = tile x this
     CANDIDATES = TILES
 
-    def __init__(self, repeats=3):
+    def __init__(self, repeats=3, path=None):
         self.repeats = repeats
         self.cache = {}
         self.timings = {}
+        self.path = path
+
+    @staticmethod
+    def _key_str(k) -> str:
+        return "|".join(str(v) for v in k)
+
+    def _load(self) -> dict:
+        try:
+            with open(self.path) as f:
+                data = json.load(f)
+            return data if isinstance(data, dict) else {}
+        except (OSError, ValueError):
+            return {}
+
+    def lookup(self, device_name: str, k):
+        """A stored (orient_tile, stage_cap) for this GPU and problem class, or None."""
+        if not self.path:
+            return None
+        v = self._load().get(device_name, {}).get(self._key_str(k))
+        return (int(v[0]), int(v[1])) if isinstance(v, list) and len(v) == 2 else None
+
+    def store(self, device_name: str, k, choice):
+        """Add one choice to the file (read, update, write a temporary file, rename)."""
+        if not self.path:
+            return
+        data = self._load()
+        data.setdefault(device_name, {})[self._key_str(k)] = [int(choice[0]), int(choice[1])]
+        tmp = f"{self.path}.{os.getpid()}.tmp"
+        with open(tmp, "w") as f:
+            json.dump(data, f, indent=1, sort_keys=True)
+        os.replace(tmp, self.path)
 
     @staticmethod
     def key(batch: "PhaseBatch"):
@@ -749,6 +785,11 @@ class Autotuner:
         k = self.key(batch)
         if k in self.cache:
             return self.cache[k]
+        device_name = torch.cuda.get_device_name(batch.device) if self.path else None
+        stored = self.lookup(device_name, k) if self.path else None
+        if stored is not None:
+            self.cache[k] = stored
+            return stored
         lib = N.load_library()
         fp64 = batch.settings.form == "fp64"
         integ = batch.settings.precession_mode == N.DS_PRECESSION_INTEGRAL
@@ -780,6 +821,8 @@ class Autotuner:
             best = (4, 0)
         self.cache[k] = best
         self.timings[k] = times
+        if self.path and times:
+            self.store(device_name, k, best)
         return best
 
     def tile_for(self, batch: "PhaseBatch") -> int:
@@ -788,7 +831,7 @@ class Autotuner:
         return tile
 
 
-AUTOTUNER = Autotuner()
+AUTOTUNER = Autotuner(path=os.environ.get("DS_AUTOTUNE_CACHE") or None)
 
 
 def simulate_batch(tables, quats, settings: SimSettings, radius: float, orient_tile=None):

@@ -224,3 +224,26 @@ def test_compute_calls_fail_loudly_without_a_gpu():
     for call in calls:
         with pytest.raises(N.NativeError):
             call()
+
+
+def test_autotuner_disk_cache(tmp_path, monkeypatch):
+    """Tile choices persist per GPU name and problem class; without a path
+    nothing is read or written."""
+    from diffsims_gb300.engine import Autotuner
+    k = (32, 20, 17, "sinc", 0, "mixed")
+    mem = Autotuner()
+    assert mem.lookup("GB300", k) is None
+    mem.store("GB300", k, (16, 6144))  # no path: a no-op
+    assert not list(tmp_path.iterdir())
+    path = tmp_path / "tiles.json"
+    a = Autotuner(path=str(path))
+    assert a.lookup("GB300", k) is None
+    a.store("GB300", k, (32, 12288))
+    a.store("GB300", (1, 2, 3, "linear", 2, "fp64"), (8, 3072))
+    a.store("Other GPU", k, (8, 3072))
+    b = Autotuner(path=str(path))
+    assert b.lookup("GB300", k) == (32, 12288)
+    assert b.lookup("Other GPU", k) == (8, 3072)
+    assert b.lookup("GB300", (1, 2, 3, "linear", 2, "fp64")) == (8, 3072)
+    path.write_text("not json")
+    assert Autotuner(path=str(path)).lookup("GB300", k) is None  # a damaged file is ignored
