@@ -225,7 +225,7 @@ def run_gpu(args):
     import torch
     import diffsims_gb300 as ds
     from diffsims_gb300 import _native as N
-    from diffsims_gb300.engine import PhaseTable, SpotBuffers, simulate_phase, estimate_spots
+    from diffsims_gb300.engine import PhaseTable, SpotBuffers, simulate_phase
 
     lib = N.load_library()
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -14,7 +14,7 @@ from .engine import (PhaseBatch, PhaseTable, SimSettings, SpotBuffers, reciproca
                      simulate_phase_streamed)
 from .simulation1d import Simulation1D
 from .simulation2d import Simulation2D
-from .symmetry import point_group_rotations, symmetry_families  # noqa: F401  (public here too)
+from .symmetry import point_group_rotations, symmetry_families
 from .sim_utils import get_electron_wavelength
 
 _SHAPE_NAMES = ("linear", "atanc", "sinc", "sin2c", "lorentzian")

@@ -32,7 +32,7 @@ from . import _native as N
 from .sim_utils import PackedAtoms, _TABLES
 from .crystal import sites_of
 from .engine import reciprocal_basis
-from .symmetry import _space_group_operations, expand_position, point_group_rotations, symmetry_families  # noqa: F401
+from .symmetry import expand_position, point_group_rotations, symmetry_families
 
 __all__ = [
     "get_doyleturner_atomic_scattering_factor",
