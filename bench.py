@@ -537,6 +537,24 @@ def run_batch(args, torch, dev):
             "config": {k: v for k, v in W.items()}}
 
 
+def pm3m_operations():
+    """The 48 operations (R, 0) of Pm-3m: the closure of a 4-fold about z, a
+    3-fold about [111] and the inversion (the per-family leg's input)."""
+    gens = [np.array([[0, -1, 0], [1, 0, 0], [0, 0, 1]]), np.array([[0, 0, 1], [1, 0, 0], [0, 1, 0]]), -np.eye(3, dtype=int)]
+    group = {tuple(np.eye(3, dtype=int).ravel())}
+    frontier = [np.eye(3, dtype=int)]
+    while frontier:
+        new = []
+        for R in frontier:
+            for G in gens:
+                P = G @ R
+                if tuple(P.ravel()) not in group:
+                    group.add(tuple(P.ravel()))
+                    new.append(P)
+        frontier = new
+    return [(np.array(k, dtype=np.float64).reshape(3, 3), np.zeros(3)) for k in sorted(group)]
+
+
 def run_families(args, torch, dev):
     """Per-family structure factors (diffsims/structure_factor/structure_factor.py:103-185):
     2^20 Doyle-Turner families at 200 kV of a mixed site at a general
@@ -545,9 +563,8 @@ def run_families(args, torch, dev):
     from diffsims_gb300 import _native as N
     from diffsims_gb300 import structure_factor as gsf
     from diffsims_gb300.crystal import Atom, Lattice, Phase, Structure
-    from oracle import structure_factor_families as osf
     lib = N.load_library()
-    ops = osf.space_group_operations(221)
+    ops = pm3m_operations()
     atoms = [Atom("Fe", [0.11, 0.23, 0.37], 0.6, 0.005), Atom("Ni", [0.11, 0.23, 0.37], 0.4, 0.009),
              Atom("O", [0.5, 0.5, 0.5], 1.0, 0.011)]
     phase = Phase(structure=Structure(atoms, Lattice(4.1, 4.1, 4.1)), space_group=ops)
@@ -599,6 +616,7 @@ def run_families(args, torch, dev):
         if i >= args.warmup:
             t_e2e.append(time.perf_counter() - t0)
     # the oracle's per-family loop (the reference's algorithm) on one core, a bounded sample
+    from oracle import structure_factor_families as osf
     atoms_o = [(a.element, a.xyz, a.occupancy, a.Bisoequiv) for a in atoms]
     n_cpu = 2000
     t0 = time.perf_counter()
@@ -838,9 +856,8 @@ def run_case(args):
         # the per-family leg's 2^20 Doyle-Turner families (96 orbit positions), two launches
         from diffsims_gb300 import structure_factor as gsf
         from diffsims_gb300.sim_utils import PackedAtoms
-        from oracle import structure_factor_families as osf
         atoms = [ds.Atom("Fe", [0.11, 0.23, 0.37], 0.6, 0.005), ds.Atom("Ni", [0.11, 0.23, 0.37], 0.4, 0.009)]
-        sites = gsf._asymmetric_sites(atoms, osf.space_group_operations(221))
+        sites = gsf._asymmetric_sites(atoms, pm3m_operations())
         species, rows, xyz, occ, B = [], [], [], [], []
         for k, (z, positions, o, biso) in enumerate(sites):
             rows.append(gsf._coeff_row(z, N.DS_SCATTER_DOYLETURNER, 4.1 ** 3))
