@@ -99,6 +99,45 @@ def uniform_quaternions(n, seed=0):
     return q
 
 
+BATCH_ELEMENTS = ["C", "N", "O", "Al", "Si", "Ti", "Fe", "Cu"]
+
+
+def batch_phase_specs(seed=BATCH_WORKLOAD["seed"], n_phases=BATCH_WORKLOAD["n_phases"]):
+    """The uneven phases of the batched workload, in draw order: per phase
+    (lattice (a, b, c, alpha, beta, gamma), elements, fractional xyz, B,
+    orientation count, orientation seed)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_phases):
+        lat = tuple(rng.uniform(3, 20, 3)) + tuple(rng.uniform(80, 100, 3))
+        n_a = int(rng.integers(1, 501))
+        els = list(rng.choice(BATCH_ELEMENTS, n_a))
+        xyz = rng.random((n_a, 3))
+        B = rng.uniform(0.3, 1.5, n_a)
+        out.append((lat, els, xyz, B, int(rng.integers(1000, 50001)), 1000 + k))
+    return out
+
+
+def library_phase_specs(seed=LIBRARY_WORKLOAD["seed"]):
+    """The template library's three phases: per phase (name, lattice,
+    elements, fractional xyz, B); Al FCC, Fe BCC, and a 60-atom P1 cell."""
+    rng = np.random.default_rng(seed)
+    lat = tuple(rng.uniform(6, 10, 3)) + tuple(rng.uniform(70, 110, 3))
+    p1_els = list(rng.choice(["C", "N", "O", "Si", "Fe"], 60))
+    p1_xyz = rng.random((60, 3))
+    p1_B = rng.uniform(0.3, 1.5, 60)
+    return [("Al", (4.05, 4.05, 4.05, 90, 90, 90), ["Al"] * 4,
+             np.array([[0, 0, 0], [0, .5, .5], [.5, 0, .5], [.5, .5, 0]], dtype=np.float64), np.full(4, 0.5)),
+            ("Fe", (2.87, 2.87, 2.87, 90, 90, 90), ["Fe"] * 2, np.array([[0, 0, 0], [.5, .5, .5]], dtype=np.float64),
+             np.full(2, 0.35)),
+            ("P1", lat, p1_els, p1_xyz, p1_B)]
+
+
+def phase_of(name, lat, els, xyz):
+    import diffsims_gb300 as ds
+    return ds.Phase(name, ds.Structure([ds.Atom(e, x) for e, x in zip(els, xyz)], ds.Lattice(*lat)))
+
+
 # --------------------------------------------------------------------- CPU
 def _cpu_worker(args):
     """Reference CPU path (oracle restatement) on a slice of orientations."""
@@ -129,6 +168,48 @@ def cpu_reference_rate(n_sample, cores, seed=0):
         spots = sum(pool.map(_cpu_worker, args))
         dt = time.perf_counter() - t0
     return n_sample / dt, dt, spots
+
+
+def _cpu_phase_worker(args):
+    """The oracle's per-orientation path (the reference's algorithm) over a
+    slice of one phase's orientations; optionally each pattern rasterised by
+    the reference's recipe.  Returns the spot count."""
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    import warnings
+    from oracle import kinematic as ok
+    lat, els, xyz, B, q, params, raster = args
+    cr = ok.Crystal(lat, els, xyz, B=B)
+    p = ok.SimParams(**params)
+    table = ok.phase_table(cr, p)
+    n = 0
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        for R in ok.quaternion_to_matrix(q):
+            pat = ok.simulate_orientation(cr, p, table, R)
+            n += pat.hkl.shape[0]
+            if raster is not None:
+                ok.diffraction_pattern(pat.xyz, pat.intensity, raster["shape"], sigma=raster["sigma"],
+                                       calibration=raster["calibration"])
+    return n
+
+
+def cpu_phases_rate(jobs, cores):
+    """patterns/s of the oracle over ``jobs`` (each: lat, els, xyz, B,
+    quaternions, SimParams keywords, raster settings or None), every job's
+    orientations split over ``cores`` spawned workers."""
+    tasks = []
+    for lat, els, xyz, B, q, params, raster in jobs:
+        for part in np.array_split(q, max(1, min(cores, len(q)))):
+            if len(part):
+                tasks.append((lat, els, xyz, B, part, params, raster))
+    n_pat = sum(len(t[4]) for t in tasks)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        pool.map(_cpu_phase_worker, [t[:4] + (t[4][:1],) + t[5:] for t in tasks[:cores]])  # warm the workers
+        t0 = time.perf_counter()
+        spots = sum(pool.map(_cpu_phase_worker, tasks, chunksize=1))
+        dt = time.perf_counter() - t0
+    return n_pat / dt, dt, n_pat, spots
 
 
 # --------------------------------------------------------------- clocks
@@ -201,6 +282,19 @@ def fp32_peak_tflops(torch, lib, N):
         ms = e0.elapsed_time(e1)
         best = max(best, blocks * 256 * iters * 256 / (ms * 1e-3) / 1e12)
     return best
+
+
+def _hbm_peak():
+    """(GB/s, source) of the HBM copy bandwidth: MEASURED_PEAKS.json when
+    present, else the fallback figure."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            v = json.load(f).get("hbm_gbs")
+        if v:
+            return float(v), "MEASURED_PEAKS.json"
+    except (OSError, ValueError):
+        pass
+    return 6800.0, "fallback"
 
 
 def rank_shard(n_per_rank, seed, rank):
@@ -303,7 +397,7 @@ def run_gpu(args):
 
     # ---- end to end through the public API with host buffers
     rot_host = ds.Rotation(q_host)
-    e2e_ms = []
+    e2e_ms, e2e_split = [], []
     h2d = q_host.nbytes
     d2h = 0
     for it in range(args.warmup + args.steps):
@@ -311,14 +405,25 @@ def run_gpu(args):
         t0 = time.perf_counter()
         sim = gen.calculate_diffraction2d(phase, rot_host, reciprocal_radius=r,
                                           max_excitation_error=WORKLOAD["max_excitation_error"],
-                                          debye_waller_factors=list(B))
+                                          debye_waller_factors=list(B), timing=True)
         sp = sim.spots(0)
         sp.host(pinned=True)
         dt = time.perf_counter() - t0
         if it >= args.warmup:
             e2e_ms.append(dt * 1e3)
+            e2e_split.append(sp.timings())
         d2h = sp.nbytes()
+        del sim, sp
     e2e_value = n_o / (statistics.mean(e2e_ms) * 1e-3)
+    breakdown = {k: statistics.mean(t[k] for t in e2e_split) for k in e2e_split[0] if k != "chunks"}
+    breakdown["chunks"] = e2e_split[0].get("chunks")
+    breakdown["d2h_floor_ms_at_copy_rate"] = d2h / (breakdown["copy_span_ms"] * 1e-3) / 1e9 if breakdown.get(
+        "copy_span_ms") else None
+    breakdown["pinned_pool_bytes"] = gen._host_pool.allocated_bytes
+    breakdown["note"] = ("host ms per call: table (enumeration + structure factors, one count read), quaternion "
+                         "upload, launch set-up, waits for chunk counts, pinned-pool allocation (0 once warm), "
+                         "the wait in host() and its offsets fix-up; device ms from CUDA events: the chunks' span "
+                         "and the copies' span; d2h_floor_ms_at_copy_rate is the copy rate in GB/s")
 
     # ---- roofline of the dominant kernel (FP32 issue-bound screen)
     peak32 = fp32_peak_tflops(torch, lib, N)
@@ -326,34 +431,49 @@ def run_gpu(args):
     flops = 10.0 * n_o * n_h  # algorithmic FP32 FLOP per (orientation, row) pair
     achieved = flops / (kms * 1e-3) / 1e12
     bytes_alg = total_spots * 20 + (n_o + 1) * 8 + n_o * 32 + n_h * 32
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except OSError:
-        pass
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    hbm_peak, hbm_src = _hbm_peak()
     # DRAM bytes of one launch: the per-spot figure of the ncu capture in
     # profiles/simulate_kernel_p1_8192.md (8192 orientations of this workload)
     # scaled by the spots of this launch
     traffic = DRAM_BYTES_PER_SPOT * total_spots
 
-    # ---- FP64 comparator form on a subset, and the error of the mixed form against it
-    n_cmp = min(args.fp64_orientations, n_o)
-    q_cmp = q_dev[:n_cmp].contiguous()
+    # ---- the all-FP64 GPU form on the same 100k orientations (tables built
+    # outside the timed launches; the table builds timed on their own)
     t64 = PhaseTable(phase, r, True, "lobato", list(B), form="fp64", device=dev)
     s64 = gen.settings(WORKLOAD["max_excitation_error"], form="fp64")
-    b64 = SpotBuffers(dev, with_excitation_error=True)
-    simulate_phase(t64, q_cmp, s64, r, b64)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(st)
-    t64.build()
-    ref64 = simulate_phase(t64, q_cmp, s64, r, b64)
-    e1.record(st)
-    e1.synchronize()
-    fp64_rate = n_cmp / (e0.elapsed_time(e1) * 1e-3)
+    b64 = SpotBuffers(dev)
+    simulate_phase(t64, q_dev, s64, r, b64)  # sizes the outputs
+
+    def ev_time(fn, reps):
+        out = []
+        for _ in range(reps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            fn()
+            e1.record(st)
+            e1.synchronize()
+            out.append(e0.elapsed_time(e1))
+        return statistics.mean(out)
+
+    reps64 = max(1, min(args.steps, 3))
+    fp64_kernel_ms = ev_time(lambda: simulate_phase(t64, q_dev, s64, r, b64, sync=False), reps64)
+    fp64_table_ms = ev_time(t64.build, reps64)
+    mixed_table_ms = ev_time(table.build, reps64)
+    fp64_rate = n_o / (fp64_kernel_ms * 1e-3)
+    # error of the mixed form against the FP64 form on a subset (per pair, with excitation errors)
+    n_cmp = min(args.fp64_orientations, n_o)
+    q_cmp = q_dev[:n_cmp].contiguous()
+    b64s = SpotBuffers(dev, with_excitation_error=True)
+    ref64 = simulate_phase(t64, q_cmp, s64, r, b64s)
     mixed = simulate_phase(table, q_cmp, settings, r, SpotBuffers(dev, with_excitation_error=True))
     err = compare_forms(mixed, ref64, table, q_host[:n_cmp], settings)
+    # both forms against the FP64 oracle on the first orientations (the checker; untimed)
+    err_oracle = None
+    if not args.no_oracle_check:
+        err_oracle = oracle_errors(lat, els, xyz, B, q_host[:args.oracle_orientations],
+                                   {"mixed": host_csr_first(table, q_dev, settings, r, args.oracle_orientations),
+                                    "fp64": host_csr_first(t64, q_dev, s64, r, args.oracle_orientations)})
 
     grad = None if args.skip_grad else run_grad(args, torch, dev)
     batched = None if args.skip_batch else run_batch(args, torch, dev)
@@ -377,16 +497,21 @@ def run_gpu(args):
                        l2="256 MB buffer written between timed steps", form="mixed"),
         "spots_per_s": total_spots / (ms * 1e-3),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "ms_per_step": statistics.mean(e2e_ms), "ranks": 1},
+                "ms_per_step": statistics.mean(e2e_ms), "ranks": 1, "breakdown": breakdown},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
                      "frac": achieved / peak32, "traffic": traffic, "kernel": "simulate_kernel",
                      "kernel_ms": kms, "peak_source": "measured by bench.py FMA probe (ds_probe_fp32_fma)",
                      "hbm": {"achieved_gbs": bytes_alg / (kms * 1e-3) / 1e9, "peak_gbs": hbm_peak,
                              "frac": bytes_alg / (kms * 1e-3) / 1e9 / hbm_peak,
-                             "peak_source": "MEASURED_PEAKS.json" if peaks else "fallback"}},
-        "fp64_form": {"value": fp64_rate, "unit": UNIT, "orientations": n_cmp,
-                      "mixed_over_fp64": (n_o / (ms * 1e-3)) / fp64_rate},
+                             "peak_source": hbm_src}},
+        "fp64_form": {"value": fp64_rate, "unit": UNIT, "orientations": n_o, "kernel_ms": fp64_kernel_ms,
+                      "table_ms": fp64_table_ms, "mixed_kernel_ms": kms, "mixed_table_ms": mixed_table_ms,
+                      "mixed_over_fp64": fp64_kernel_ms / kms,
+                      "mixed_over_fp64_with_tables": (fp64_kernel_ms + fp64_table_ms) / (kms + mixed_table_ms),
+                      "note": "both forms on the same orientations with their tables resident; table builds "
+                              "(enumeration + structure factors) timed separately"},
         "error_vs_fp64_form": err,
+        "error_vs_oracle": err_oracle,
         "grad": grad,
         "batched_phases": batched,
         "template_library": library,
@@ -412,13 +537,14 @@ def cone_quaternions(n, deg, seed):
     return np.c_[np.cos(th / 2), np.sin(th / 2)[:, None] * ax]
 
 
-def run_grad(args, torch, dev):
-    """Gradient step of the differentiation workload: forward (tables,
-    spots, loss) and forward + adjoint, timed with the device synchronised on
-    both sides (the forward reads the row and spot counts on the host)."""
-    import diffsims_gb300 as ds
-    from diffsims_gb300.autograd import (SpotModel, compose_axis_angle, reciprocal_basis, simulate_intensities,
-                                         spot_loss)
+def grad_problem(n_orient=None):
+    """The differentiation workload's parameters and target perturbations, in
+    draw order: orthorhombic 7.1/9.3/12.4 cell, 64 atoms (O, Si, Fe), B in
+    [0.3, 1.5], cone orientations q0 (5 deg about [001]); the target has
+    fractional coordinates + N(0, 0.01), B x (1 + N(0, 0.1)), occupancy x
+    U(0.9, 1), lattice lengths + 0.2 % and orientations turned by 0.2 deg
+    about random axes (``target_rotvec``).  ``n_orient`` keeps the first
+    orientations of the full set."""
     W = GRAD_WORKLOAD
     rng = np.random.default_rng(W["seed"])
     n_a, n_o = W["n_atoms"], W["n_orientations"]
@@ -426,74 +552,217 @@ def run_grad(args, torch, dev):
     lat = np.array([7.1, 9.3, 12.4, 90.0, 90.0, 90.0])
     xyz, B, occ = rng.random((n_a, 3)), rng.uniform(0.3, 1.5, n_a), np.ones(n_a)
     q0 = cone_quaternions(n_o, W["cone_deg"], W["seed"] + 1)
-    gen = ds.SimulationGenerator(W["accelerating_voltage"], "lobato", W["precession_angle"], W["shape_factor_model"],
-                                 W["approximate_precession"])
-    model = SpotModel(els, gen, W["reciprocal_radius"], W["max_excitation_error"])
-    T = lambda a: torch.as_tensor(np.asarray(a, dtype=np.float64), device=dev)
     ax = rng.standard_normal((n_o, 3))
     ax *= np.radians(0.2) / np.linalg.norm(ax, axis=1, keepdims=True)
-    with torch.no_grad():
-        tq = compose_axis_angle(T(q0), T(ax))
-        target = simulate_intensities(model, T(xyz + rng.normal(0, 0.01, xyz.shape)),
-                                      T(B * (1 + rng.normal(0, 0.1, n_a))), T(occ * rng.uniform(0.9, 1.0, n_a)),
-                                      reciprocal_basis(torch.as_tensor(lat * [1.002, 1.002, 1.002, 1, 1, 1])), tq)
+    out = dict(elements=els, lattice=lat, xyz=xyz, B=B, occ=occ, q0=q0, target_rotvec=ax,
+               target_xyz=xyz + rng.normal(0, 0.01, xyz.shape), target_B=B * (1 + rng.normal(0, 0.1, n_a)),
+               target_occ=occ * rng.uniform(0.9, 1.0, n_a), target_lattice=lat * [1.002, 1.002, 1.002, 1, 1, 1])
+    if n_orient is not None:
+        out["q0"], out["target_rotvec"] = q0[:n_orient], ax[:n_orient]
+    return out
+
+
+def run_grad(args, torch, dev):
+    """Gradient step of the differentiation workload: forward (tables,
+    spots, loss) and forward + adjoint, timed with the device synchronised on
+    both sides (the forward reads the row and spot counts on the host); for
+    the rotation average (the workload's sinc with 1 deg precession) and for
+    the reference's default ``approximate_precession=True``
+    (lorentzian_precession).  The rotation-average gradients are checked
+    against autograd through the FP64 transcription of the reference
+    formulas on the same spots (every component), and that transcription
+    is timed on the host cores on a bounded sample."""
+    import diffsims_gb300 as ds
+    from diffsims_gb300.autograd import (SpotModel, compose_axis_angle, reciprocal_basis, simulate_intensities,
+                                         spot_loss)
+    W = GRAD_WORKLOAD
+    G = grad_problem()
+    els, lat, xyz, B, occ, q0 = G["elements"], G["lattice"], G["xyz"], G["B"], G["occ"], G["q0"]
+    n_o = q0.shape[0]
+    T = lambda a: torch.as_tensor(np.asarray(a, dtype=np.float64), device=dev)
     q0t = T(q0)
-    # parameters resident where they live in a refinement loop: per-atom and
-    # per-orientation values on the device, the six lattice parameters on the
-    # host (the forward reads the reciprocal basis on the host)
-    ps = [T(xyz), T(B), T(occ), torch.as_tensor(lat, dtype=torch.float64),
-          torch.zeros((n_o, 3), dtype=torch.float64, device=dev)]
 
-    def forward(grad):
-        for t in ps:
-            t.requires_grad_(grad)
-            t.grad = None
-        sim = simulate_intensities(model, ps[0], ps[1], ps[2], reciprocal_basis(ps[3]), compose_axis_angle(q0t, ps[4]))
-        L = spot_loss(sim, target)
-        if grad:
-            L.backward()
-        return L, sim, ps
+    def leg(approximate):
+        gen = ds.SimulationGenerator(W["accelerating_voltage"], "lobato", W["precession_angle"],
+                                     W["shape_factor_model"], approximate)
+        model = SpotModel(els, gen, W["reciprocal_radius"], W["max_excitation_error"])
+        with torch.no_grad():
+            tq = compose_axis_angle(q0t, T(G["target_rotvec"]))
+            target = simulate_intensities(model, T(G["target_xyz"]), T(G["target_B"]), T(G["target_occ"]),
+                                          reciprocal_basis(torch.as_tensor(G["target_lattice"])), tq)
+        # parameters resident where they live in a refinement loop: per-atom and
+        # per-orientation values on the device, the six lattice parameters on the
+        # host (the forward reads the reciprocal basis on the host)
+        ps = [T(xyz), T(B), T(occ), torch.as_tensor(lat, dtype=torch.float64),
+              torch.zeros((n_o, 3), dtype=torch.float64, device=dev)]
 
-    def timed(grad):
-        out = []
-        for it in range(args.warmup + args.steps):
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            L, sim, ps_ = forward(grad)
-            torch.cuda.synchronize()
-            if it >= args.warmup:
-                out.append((time.perf_counter() - t0) * 1e3)
-        return statistics.mean(out), L, sim, ps_
+        def forward(grad):
+            for t in ps:
+                t.requires_grad_(grad)
+                t.grad = None
+            sim = simulate_intensities(model, ps[0], ps[1], ps[2], reciprocal_basis(ps[3]),
+                                       compose_axis_angle(q0t, ps[4]))
+            L = spot_loss(sim, target)
+            if grad:
+                L.backward()
+            return L, sim
 
-    fwd_ms, L, sim, _ = timed(False)
-    grad_ms, _, _, ps = timed(True)
-    gnorm = {n: float(torch.linalg.norm(t.grad)) for n, t in zip(("xyz", "B", "occupancy", "lattice", "axis_angle"), ps)}
-    return {"ms_per_step": grad_ms, "forward_ms": fwd_ms, "grad_over_forward": grad_ms / fwd_ms,
-            "unit": "ms", "loss": float(L), "spots": int(sim.intensity.shape[0]), "gradient_norms": gnorm,
+        def timed(grad):
+            out = []
+            for it in range(args.warmup + args.steps):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                L, sim = forward(grad)
+                torch.cuda.synchronize()
+                if it >= args.warmup:
+                    out.append((time.perf_counter() - t0) * 1e3)
+            return statistics.mean(out), L, sim
+
+        fwd_ms, L, _ = timed(False)
+        grad_ms, Lg, sim = timed(True)
+        return dict(gen=gen, model=model, target=target, ps=ps, fwd_ms=fwd_ms, grad_ms=grad_ms, loss=float(L),
+                    sim=sim, loss_grad=float(Lg.detach()))
+
+    main = leg(W["approximate_precession"])
+    approx = leg(True)
+    names = ("xyz", "B", "occupancy", "lattice", "axis_angle")
+    g_gpu = {n: t.grad.detach().cpu().numpy() for n, t in zip(names, main["ps"])}
+    gnorm = {n: float(np.linalg.norm(v)) for n, v in g_gpu.items()}
+    check = None if args.no_oracle_check else grad_check(torch, dev, main, els, q0t, names)
+    cpu = None if args.no_cpu_baseline else grad_cpu_baseline(torch, main, els, q0, n_o)
+    return {"ms_per_step": main["grad_ms"], "forward_ms": main["fwd_ms"],
+            "grad_over_forward": main["grad_ms"] / main["fwd_ms"], "unit": "ms", "loss": main["loss"],
+            "spots": int(main["sim"].intensity.shape[0]), "gradient_norms": gnorm,
+            "approximate_precession_true": {"ms_per_step": approx["grad_ms"], "forward_ms": approx["fwd_ms"],
+                                            "grad_over_forward": approx["grad_ms"] / approx["fwd_ms"],
+                                            "spots": int(approx["sim"].intensity.shape[0])},
+            "error_vs_fp64_autograd": check, "cpu_baseline": cpu,
             "config": {k: v for k, v in W.items()}, "dtype": "f32 forward with f64 phase; f64 adjoint"}
+
+
+def _reference_grads(torch, sim, target, ps, els, q0t, p, upstream=None, chunk=131072):
+    """Autograd through the FP64 transcription of the reference formulas on
+    the spots of ``sim`` (orientation and hkl fixed), in chunks of spots:
+    the gradient of the loss (in the returned leaves' ``.grad``), its value,
+    and, with ``upstream`` (dL/dI per spot), the vector-Jacobian product
+    upstream . dI/dparams (a list per parameter group)."""
+    from oracle import autograd_reference as ar
+    loss = ar.MatchedLoss(sim.offsets, sim.hkl, target.intensity, target.offsets, target.hkl)
+    dev = q0t.device
+    counts = sim.offsets[1:] - sim.offsets[:-1]
+    orient = torch.repeat_interleave(torch.arange(counts.shape[0], device=counts.device), counts).to(dev)
+    hkl = sim.hkl.to(dev)
+    leaves = [t.detach().clone().requires_grad_() for t in ps]
+    recip = ar.reciprocal_basis_torch(leaves[3])
+    quats = ar.compose_axis_angle_torch(q0t[:counts.shape[0]], leaves[4])
+    n = int(hkl.shape[0])
+    total = 0.0
+    vjp = [torch.zeros_like(t) for t in leaves] if upstream is not None else None
+    for a in range(0, max(n, 1), chunk):
+        b = min(n, a + chunk)
+        I = ar.spot_intensities(leaves[0], leaves[1], leaves[2], recip, quats, els, "lobato", orient[a:b], hkl[a:b], p)
+        if upstream is not None:
+            for acc, g in zip(vjp, torch.autograd.grad(I, leaves, upstream[a:b].to(I.device), retain_graph=True)):
+                acc += g
+        La = loss(I, a)
+        La.backward(retain_graph=True)
+        total += float(La.detach())
+    return leaves, total, vjp
+
+
+def _grad_params(W, approximate):
+    from oracle import kinematic as ok
+    return ok.SimParams(accelerating_voltage=W["accelerating_voltage"], reciprocal_radius=W["reciprocal_radius"],
+                        max_excitation_error=W["max_excitation_error"], shape_factor_model=W["shape_factor_model"],
+                        precession_angle=W["precession_angle"], approximate_precession=approximate)
+
+
+def grad_check(torch, dev, main, els, q0t, names):
+    """Errors of the workload's GPU gradients against the FP64 transcription
+    of the reference formulas on the same spots (the checker; untimed):
+
+    * ``adjoint``: the hand-written adjoint alone -- the GPU's and the
+      transcription's vector-Jacobian products with the same upstream
+      dL/dI = 2 (I - T) (the GPU forward's intensities);
+    * ``loss_gradient``: the whole chain -- the GPU gradient of the loss
+      (FP32 forward intensities in the residual I - T) against autograd of
+      the FP64 loss.
+    Per group: every component relative to itself with floors, and the
+    group's norm-wise relative error."""
+    import warnings
+    from diffsims_gb300.autograd import compose_axis_angle, reciprocal_basis, simulate_intensities, spot_loss
+    from oracle import autograd_reference as ar
+    W = GRAD_WORKLOAD
+    t0 = time.perf_counter()
+    model, target = main["model"], main["target"]
+    ps = [t.detach().clone().requires_grad_() for t in main["ps"]]
+    sim = simulate_intensities(model, ps[0], ps[1], ps[2], reciprocal_basis(ps[3]), compose_axis_angle(q0t, ps[4]))
+    loss = ar.MatchedLoss(sim.offsets, sim.hkl, target.intensity, target.offsets, target.hkl)
+    gI = 2.0 * (sim.intensity.detach() - loss.target_per_spot)
+    g_adj = torch.autograd.grad(sim.intensity, ps, gI, retain_graph=True)
+    L = spot_loss(sim, target)
+    g_full = torch.autograd.grad(L, ps)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        leaves, L_ref, vjp = _reference_grads(torch, sim, target, ps, els, q0t,
+                                              _grad_params(W, W["approximate_precession"]), upstream=gI)
+    npy = lambda ts: {n: t.detach().cpu().numpy() for n, t in zip(names, ts)}
+    adj = ar.gradient_errors(npy(g_adj), npy(vjp))
+    full = ar.gradient_errors(npy(g_full), npy([t.grad for t in leaves]))
+    return {"adjoint": adj, "loss_gradient": full,
+            "adjoint_max_norm_rel": max(v["norm_rel"] for v in adj.values()),
+            "loss_gradient_max_norm_rel": max(v["norm_rel"] for v in full.values()),
+            "loss_rel_error": abs(float(L.detach()) - L_ref) / abs(L_ref), "spots": int(sim.intensity.shape[0]),
+            "reference": "autograd through the FP64 torch transcription (oracle/autograd_reference.py), same spots",
+            "seconds": time.perf_counter() - t0}
+
+
+def grad_cpu_baseline(torch, main, els, q0, n_o, n_sample=64):
+    """The FP64 transcription's forward + backward on the host cores (torch
+    threads) for the spots of the first ``n_sample`` orientations, scaled to
+    the workload's orientations: ms per gradient step."""
+    import warnings
+    W = GRAD_WORKLOAD
+    sim = main["sim"]
+    off = sim.offsets.cpu()
+    m = int(off[n_sample])
+
+    class Sub:
+        pass
+    sub, tgt = Sub(), Sub()
+    sub.offsets, sub.hkl = off[:n_sample + 1].clone(), sim.hkl[:m].cpu()
+    toff = main["target"].offsets.cpu()
+    tm = int(toff[n_sample])
+    tgt.offsets, tgt.hkl, tgt.intensity = toff[:n_sample + 1].clone(), main["target"].hkl[:tm].cpu(), \
+        main["target"].intensity[:tm].detach().cpu()
+    ps = [t.detach().cpu() if i != 4 else t.detach()[:n_sample].cpu() for i, t in enumerate(main["ps"])]
+    q0c = torch.as_tensor(q0[:n_sample], dtype=torch.float64)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        _reference_grads(torch, sub, tgt, ps, els, q0c, _grad_params(W, W["approximate_precession"]))  # warm
+        t0 = time.perf_counter()
+        _reference_grads(torch, sub, tgt, ps, els, q0c, _grad_params(W, W["approximate_precession"]))
+        dt = time.perf_counter() - t0
+    return {"value": dt * 1e3 * n_o / n_sample, "unit": "ms", "cores": torch.get_num_threads(), "kind": "port",
+            "sample": f"forward + backward of the FP64 torch transcription of the reference formulas on the "
+                      f"{m} spots of the first {n_sample} orientations ({dt:.2f} s), scaled by {n_o}/{n_sample}"}
 
 
 def run_batch(args, torch, dev):
     """Batched uneven phases: every phase's orientations in one persistent
     launch (CUDA graph replay), against the same phases launched one by one."""
     import diffsims_gb300 as ds
+    from diffsims_gb300 import _native as N
     from diffsims_gb300.engine import AUTOTUNER, Autotuner, PhaseBatch, PhaseTable, SpotBuffers, simulate_phase
     W = BATCH_WORKLOAD
-    rng = np.random.default_rng(W["seed"])
-    zs = ["C", "N", "O", "Al", "Si", "Ti", "Fe", "Cu"]
     gen = ds.SimulationGenerator(W["accelerating_voltage"], "lobato", shape_factor_model=W["shape_factor_model"])
     settings = gen.settings(W["max_excitation_error"])
     r = W["reciprocal_radius"]
     tables, qs = [], []
     t_tab = time.perf_counter()
-    for k in range(W["n_phases"]):
-        lat = tuple(rng.uniform(3, 20, 3)) + tuple(rng.uniform(80, 100, 3))
-        n_a = int(rng.integers(1, 501))
-        els = list(rng.choice(zs, n_a))
-        ph = ds.Phase(f"p{k}", ds.Structure([ds.Atom(e, x) for e, x in zip(els, rng.random((n_a, 3)))],
-                                            ds.Lattice(*lat)))
-        tables.append(PhaseTable(ph, r, True, "lobato", list(rng.uniform(0.3, 1.5, n_a)), device=dev))
-        qs.append(torch.from_numpy(uniform_quaternions(int(rng.integers(1000, 50001)), 1000 + k)).to(dev))
+    for k, (lat, els, xyz, B, n_q, q_seed) in enumerate(batch_phase_specs()):
+        tables.append(PhaseTable(phase_of(f"p{k}", lat, els, xyz), r, True, "lobato", list(B), device=dev))
+        qs.append(torch.from_numpy(uniform_quaternions(n_q, q_seed)).to(dev))
     torch.cuda.synchronize()
     table_s = time.perf_counter() - t_tab
     n_pat = sum(int(q.shape[0]) for q in qs)
@@ -526,6 +795,28 @@ def run_batch(args, torch, dev):
     for t, q, b in zip(tables, qs, bufs):
         simulate_phase(t, q, settings, r, b)  # size the buffers
     seq_ms = timed(lambda: [simulate_phase(t, q, settings, r, b, sync=False) for t, q, b in zip(tables, qs, bufs)])
+    # roofline: FP32 screen over every (orientation, row) pair, and the bytes written
+    peak32 = fp32_peak_tflops(torch, N.load_library(), N)
+    pairs = sum(int(q.shape[0]) * t.n for t, q in zip(tables, qs))
+    flops = 10.0 * pairs / (graph_ms * 1e-3) / 1e12
+    bytes_alg = n_spots * 20 + (n_pat + 1) * 8 + n_pat * 32 + sum(t.n for t in tables) * 28
+    hbm_peak = _hbm_peak()[0]
+    roof = {"bound": "fp32", "achieved": flops, "peak": peak32, "unit": "TFLOP/s", "frac": flops / peak32,
+            "pairs": pairs, "kernel": "simulate_batch_kernel", "kernel_ms": graph_ms,
+            "peak_source": "measured by bench.py FMA probe (ds_probe_fp32_fma)",
+            "hbm": {"achieved_gbs": bytes_alg / (graph_ms * 1e-3) / 1e9, "peak_gbs": hbm_peak,
+                    "frac": bytes_alg / (graph_ms * 1e-3) / 1e9 / hbm_peak}}
+    cpu = None
+    if not args.no_cpu_baseline:
+        params = dict(accelerating_voltage=W["accelerating_voltage"], reciprocal_radius=r,
+                      max_excitation_error=W["max_excitation_error"], shape_factor_model=W["shape_factor_model"])
+        jobs = [(lat, els, xyz, Bv, uniform_quaternions(n_q, q_seed)[:max(1, n_q // 256)], params, None)
+                for lat, els, xyz, Bv, n_q, q_seed in batch_phase_specs()]
+        cores = os.cpu_count() or 1
+        rate, dt, n_s, _ = cpu_phases_rate(jobs, cores)
+        cpu = {"value": rate, "unit": "patterns/s", "cores": cores, "kind": "port",
+               "sample": f"the first 1/256 of every phase's orientations ({n_s} patterns, {dt:.1f} s), FP64 numpy "
+                         f"restatement of the reference path, {cores} spawned processes"}
     return {"metric": "orientation patterns/s (32 uneven phases, one launch)", "value": n_pat / (graph_ms * 1e-3),
             "unit": "patterns/s", "ms_per_step": graph_ms, "patterns_per_step": n_pat, "spots_per_step": int(n_spots),
             "per_phase_launches_ms": seq_ms, "speedup_over_per_phase_launches": seq_ms / graph_ms,
@@ -533,7 +824,7 @@ def run_batch(args, torch, dev):
             "autotuner_ms": AUTOTUNER.timings.get(key),
             "n_hkl_range": [min(t.n for t in tables), max(t.n for t in tables)],
             "orientations_range": [min(int(q.shape[0]) for q in qs), max(int(q.shape[0]) for q in qs)],
-            "table_build_s": table_s, "launches_per_step": len(tables) + 2,
+            "table_build_s": table_s, "launches_per_step": len(tables) + 2, "roofline": roof, "cpu_baseline": cpu,
             "config": {k: v for k, v in W.items()}}
 
 
@@ -703,72 +994,91 @@ def run_legacy(args, torch, dev):
 
 def run_library(args, torch, dev, hbm_peak):
     """Template-library throughput: three phases simulated and rasterised in
-    8192-orientation chunks through one reused detector buffer."""
+    8192-orientation chunks through one reused detector buffer; with the
+    rotation average (the workload's linear with 0.5 deg precession) and with
+    the reference's default ``approximate_precession=True``."""
     import diffsims_gb300 as ds
+    from diffsims_gb300 import _native as N
     from diffsims_gb300.engine import PhaseTable, RasterBuffers, RasterSettings, SpotBuffers, rasterize, simulate_phase
     W = LIBRARY_WORKLOAD
-    rng = np.random.default_rng(W["seed"])
-    al = ds.Phase("Al", ds.Structure([ds.Atom("Al", x) for x in [[0, 0, 0], [0, .5, .5], [.5, 0, .5], [.5, .5, 0]]],
-                                     ds.Lattice(4.05, 4.05, 4.05, 90, 90, 90)))
-    fe = ds.Phase("Fe", ds.Structure([ds.Atom("Fe", x) for x in [[0, 0, 0], [.5, .5, .5]]],
-                                     ds.Lattice(2.87, 2.87, 2.87, 90, 90, 90)))
-    lat = tuple(rng.uniform(6, 10, 3)) + tuple(rng.uniform(70, 110, 3))
-    p1_els = list(rng.choice(["C", "N", "O", "Si", "Fe"], 60))
-    p1 = ds.Phase("P1", ds.Structure([ds.Atom(e, x) for e, x in zip(p1_els, rng.random((60, 3)))], ds.Lattice(*lat)))
-    dws = [[0.5] * 4, [0.35] * 2, list(rng.uniform(0.3, 1.5, 60))]
-    gen = ds.SimulationGenerator(W["accelerating_voltage"], "lobato", W["precession_angle"], W["shape_factor_model"],
-                                 W["approximate_precession"])
-    settings = gen.settings(W["max_excitation_error"])
+    specs = library_phase_specs()
+    phases = [phase_of(nm, lat, els, xyz) for nm, lat, els, xyz, _ in specs]
+    dws = [list(B) for *_, B in specs]
     r = W["reciprocal_radius"]
     n_o, chunk = W["n_orientations"], W["chunk"]
     H, Wd = W["shape"]
     qs = [torch.from_numpy(uniform_quaternions(n_o, 100 + i)).to(dev) for i in range(3)]
-    tables = [PhaseTable(ph, r, True, "lobato", dw, device=dev) for ph, dw in zip((al, fe, p1), dws)]
+    tables = [PhaseTable(ph, r, True, "lobato", dw, device=dev) for ph, dw in zip(phases, dws)]
     bufs = [SpotBuffers(dev) for _ in range(3)]
     rs = RasterSettings((H, Wd), sigma=W["sigma"], calibration=W["calibration"])
     rb = RasterBuffers(dev)
     img = torch.empty((chunk, H, Wd), dtype=torch.float32, device=dev)
     st = torch.cuda.current_stream()
-
-    def step(time_raster):
-        spots = [simulate_phase(t, q, settings, r, b) for t, q, b in zip(tables, qs, bufs)]
-        maxes = [int((s.offsets[1:] - s.offsets[:-1]).max().item()) for s in spots]
-        ras_ms = 0.0
-        for s, m in zip(spots, maxes):
-            for a in range(0, n_o, chunk):
-                b = min(a + chunk, n_o)
-                if time_raster:
-                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                    e0.record(st)
-                rasterize(s, rs, a, b, out=img[:b - a], max_spots=m, buffers=rb, sync=False)
-                if time_raster:
-                    e1.record(st)
-                    e1.synchronize()
-                    ras_ms += e0.elapsed_time(e1)
-        return spots, ras_ms
-
-    for _ in range(args.warmup):
-        step(False)
-    torch.cuda.synchronize()
-    ms = []
-    for _ in range(args.steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        spots, _ = step(False)
-        torch.cuda.synchronize()
-        ms.append((time.perf_counter() - t0) * 1e3)
-    _, ras_ms = step(True)
-    from diffsims_gb300 import _native as N
-    N.check_device_status(rb.status, "rasterize")
     n_pat = 3 * n_o
     bytes_img = n_pat * H * Wd * 4
-    ras_gbs = bytes_img / (ras_ms * 1e-3) / 1e9
-    return {"metric": "orientation patterns/s (simulated and rasterised)", "value": n_pat / (statistics.mean(ms) * 1e-3),
-            "unit": "patterns/s", "ms_per_step": statistics.mean(ms), "patterns_per_step": n_pat,
-            "spots_per_step": int(sum(s.total for s in spots)), "n_hkl": [t.n for t in tables],
-            "raster": {"ms": ras_ms, "achieved_gbs": ras_gbs, "peak_gbs": hbm_peak, "frac": ras_gbs / hbm_peak,
-                       "bytes_written": bytes_img, "launches": 3 * ((n_o + chunk - 1) // chunk),
-                       "note": "CUDA events around each chunk's launch; bytes = images written"},
+
+    def measure(approximate):
+        gen = ds.SimulationGenerator(W["accelerating_voltage"], "lobato", W["precession_angle"],
+                                     W["shape_factor_model"], approximate)
+        settings = gen.settings(W["max_excitation_error"])
+
+        def step(time_raster):
+            spots = [simulate_phase(t, q, settings, r, b) for t, q, b in zip(tables, qs, bufs)]
+            maxes = [int((s.offsets[1:] - s.offsets[:-1]).max().item()) for s in spots]
+            ras_ms = 0.0
+            for s, m in zip(spots, maxes):
+                for a in range(0, n_o, chunk):
+                    b = min(a + chunk, n_o)
+                    if time_raster:
+                        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                        e0.record(st)
+                    rasterize(s, rs, a, b, out=img[:b - a], max_spots=m, buffers=rb, sync=False)
+                    if time_raster:
+                        e1.record(st)
+                        e1.synchronize()
+                        ras_ms += e0.elapsed_time(e1)
+            return spots, ras_ms
+
+        for _ in range(args.warmup):
+            step(False)
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            spots, _ = step(False)
+            torch.cuda.synchronize()
+            ms.append((time.perf_counter() - t0) * 1e3)
+        _, ras_ms = step(True)
+        N.check_device_status(rb.status, "rasterize")
+        ras_gbs = bytes_img / (ras_ms * 1e-3) / 1e9
+        return {"value": n_pat / (statistics.mean(ms) * 1e-3), "ms_per_step": statistics.mean(ms),
+                "spots_per_step": int(sum(s.total for s in spots)),
+                "raster": {"ms": ras_ms, "achieved_gbs": ras_gbs, "peak_gbs": hbm_peak, "frac": ras_gbs / hbm_peak,
+                           "bytes_written": bytes_img, "launches": 3 * ((n_o + chunk - 1) // chunk),
+                           "note": "CUDA events around each chunk's launch; bytes = images written"}}
+
+    main = measure(W["approximate_precession"])
+    approx = measure(True)
+    cpu = None
+    if not args.no_cpu_baseline:
+        params = dict(accelerating_voltage=W["accelerating_voltage"], reciprocal_radius=r,
+                      max_excitation_error=W["max_excitation_error"], shape_factor_model=W["shape_factor_model"],
+                      precession_angle=W["precession_angle"], approximate_precession=W["approximate_precession"])
+        raster = {"shape": W["shape"], "sigma": W["sigma"], "calibration": W["calibration"]}
+        n_cpu = args.library_cpu_sample
+        jobs = [(lat, els, xyz, Bv, uniform_quaternions(n_o, 100 + i)[:n_cpu], params, raster)
+                for i, (_, lat, els, xyz, Bv) in enumerate(specs)]
+        cores = os.cpu_count() or 1
+        rate, dt, n_s, _ = cpu_phases_rate(jobs, cores)
+        cpu = {"value": rate, "unit": "patterns/s", "cores": cores, "kind": "port",
+               "sample": f"the first {n_cpu} orientations of each phase ({n_s} patterns, {dt:.1f} s): FP64 numpy "
+                         f"restatement of the reference path (scipy quad rotation average) and its rasteriser "
+                         f"(scipy gaussian_filter), {cores} spawned processes"}
+    return {"metric": "orientation patterns/s (simulated and rasterised)", "value": main["value"],
+            "unit": "patterns/s", "ms_per_step": main["ms_per_step"], "patterns_per_step": n_pat,
+            "spots_per_step": main["spots_per_step"], "n_hkl": [t.n for t in tables], "raster": main["raster"],
+            "approximate_precession_true": approx, "cpu_baseline": cpu,
             "config": {k: (list(v) if isinstance(v, tuple) else v) for k, v in W.items()}}
 
 
@@ -786,13 +1096,10 @@ def run_case(args):
     if args.case == "raster":
         # the template library's 60-atom P1 phase, 2048 patterns, two rasterisations
         W = LIBRARY_WORKLOAD
-        rng = np.random.default_rng(W["seed"])
-        lat = tuple(rng.uniform(6, 10, 3)) + tuple(rng.uniform(70, 110, 3))
-        els = list(rng.choice(["C", "N", "O", "Si", "Fe"], 60))
-        p1 = ds.Phase("P1", ds.Structure([ds.Atom(e, x) for e, x in zip(els, rng.random((60, 3)))], ds.Lattice(*lat)))
+        nm, lat, els, xyz, B = library_phase_specs()[2]
         gen = ds.SimulationGenerator(W["accelerating_voltage"], "lobato", W["precession_angle"],
                                      W["shape_factor_model"], W["approximate_precession"])
-        tab = PhaseTable(p1, W["reciprocal_radius"], True, "lobato", list(rng.uniform(0.3, 1.5, 60)), device=dev)
+        tab = PhaseTable(phase_of(nm, lat, els, xyz), W["reciprocal_radius"], True, "lobato", list(B), device=dev)
         q = torch.from_numpy(uniform_quaternions(2048, 1)).to(dev)
         sp = simulate_phase(tab, q, gen.settings(W["max_excitation_error"]), W["reciprocal_radius"], SpotBuffers(dev))
         img = torch.empty((2048,) + tuple(W["shape"]), dtype=torch.float32, device=dev)
@@ -835,19 +1142,12 @@ def run_case(args):
     elif args.case == "batch":
         # the 32 uneven phases with 1/16 of their orientations, one batched launch (tile 16)
         W = BATCH_WORKLOAD
-        rng = np.random.default_rng(W["seed"])
-        zs = ["C", "N", "O", "Al", "Si", "Ti", "Fe", "Cu"]
         gen = ds.SimulationGenerator(W["accelerating_voltage"], "lobato", shape_factor_model=W["shape_factor_model"])
         tables, qs = [], []
-        for k in range(W["n_phases"]):
-            lat = tuple(rng.uniform(3, 20, 3)) + tuple(rng.uniform(80, 100, 3))
-            n_a = int(rng.integers(1, 501))
-            els = list(rng.choice(zs, n_a))
-            ph = ds.Phase(f"p{k}", ds.Structure([ds.Atom(e, x) for e, x in zip(els, rng.random((n_a, 3)))],
-                                                ds.Lattice(*lat)))
-            tables.append(PhaseTable(ph, W["reciprocal_radius"], True, "lobato", list(rng.uniform(0.3, 1.5, n_a)),
-                                     device=dev))
-            qs.append(torch.from_numpy(uniform_quaternions(int(rng.integers(1000, 50001)) // 16, 1000 + k)).to(dev))
+        for k, (lat, els, xyz, B, n_q, q_seed) in enumerate(batch_phase_specs()):
+            tables.append(PhaseTable(phase_of(f"p{k}", lat, els, xyz), W["reciprocal_radius"], True, "lobato",
+                                     list(B), device=dev))
+            qs.append(torch.from_numpy(uniform_quaternions(n_q // 16, q_seed)).to(dev))
         batch = PhaseBatch(tables, qs, gen.settings(W["max_excitation_error"]), W["reciprocal_radius"], orient_tile=16)
         batch.run()
         batch.run()
@@ -895,6 +1195,39 @@ def run_case(args):
         out.update(patterns=8192, spots=sp.total, n_hkl=tab.n)
     torch.cuda.synchronize()
     print(json.dumps(out))
+
+
+def host_csr_first(table, q_dev, settings, r, n):
+    """Host CSR (offsets, rows, xyzi, s) of the first ``n`` orientations, run
+    on their own with excitation errors."""
+    from diffsims_gb300.engine import SpotBuffers, simulate_phase
+    sp = simulate_phase(table, q_dev[:n].contiguous(), settings, r, SpotBuffers(table.device, with_excitation_error=True))
+    return (sp.offsets.cpu().numpy(), sp.hkl_index.cpu().numpy(), sp.xyzi.cpu().numpy(),
+            sp.excitation_error.cpu().numpy())
+
+
+def oracle_errors(lat, els, xyz, B, q, runs):
+    """Errors of GPU results (``runs``: name -> host CSR of the orientations
+    ``q``) against the FP64 oracle, computed in spawned worker processes:
+    max relative intensity error, max |s| error, max position error (per
+    |g|), cutoff flips within 1e-9 1/Angstrom, FP64 round-off spots of
+    systematic absences, and differences neither explains."""
+    from oracle import compare as oc
+    from oracle import kinematic as ok
+    crystal = ok.Crystal(lat, els, xyz, B=B)
+    p = ok.SimParams(accelerating_voltage=WORKLOAD["accelerating_voltage"], reciprocal_radius=WORKLOAD["reciprocal_radius"],
+                     max_excitation_error=WORKLOAD["max_excitation_error"],
+                     shape_factor_model=WORKLOAD["shape_factor_model"])
+    t0 = time.perf_counter()
+    ref = oc.simulate_parallel(crystal, q, p)
+    out = {"orientations": int(len(q)), "oracle_s": time.perf_counter() - t0}
+    for name, (off, idx, xyzi, s) in runs.items():
+        st = oc.spot_errors(off, idx, xyzi, s, crystal, q, p, ref)
+        out[name] = {"max_rel_intensity": st["max_rel_I"], "max_abs_excitation_error": st["max_abs_s"],
+                     "max_rel_position": st["max_abs_pos"], "flips_within_1e-9": st["boundary_flips"],
+                     "max_flip_distance": st["max_flip_distance"], "noise_spots": st["noise_spots"],
+                     "unexplained": len(st["unexplained"]), "spots": st["spots"], "ordered": st["ordered"]}
+    return out
 
 
 def compare_forms(mixed, ref, table, q_host, settings):
@@ -964,6 +1297,11 @@ def main():
     ap.add_argument("--orientations", type=int, default=WORKLOAD["n_orientations"])
     ap.add_argument("--fp64-orientations", type=int, default=4096)
     ap.add_argument("--cpu-sample", type=int, default=16384)
+    ap.add_argument("--library-cpu-sample", type=int, default=512,
+                    help="orientations per phase of the template library's CPU baseline")
+    ap.add_argument("--oracle-orientations", type=int, default=2048,
+                    help="orientations of the headline workload checked against the FP64 oracle")
+    ap.add_argument("--no-oracle-check", action="store_true", help="leave out the error report against the oracle")
     ap.add_argument("--skip-grad", action="store_true", help="leave out the gradient-step leg")
     ap.add_argument("--skip-library", action="store_true", help="leave out the template-library leg")
     ap.add_argument("--skip-batch", action="store_true", help="leave out the batched-phases leg")
@@ -973,7 +1311,7 @@ def main():
                     help="run one small profiling case instead of the benchmark")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--out-dir", default=None)
-    ap.add_argument("--screen", default="auto", choices=["auto", "rows", "lines"],
+    ap.add_argument("--screen", default="auto", choices=["auto", "rows", "lines", "bricks"],
                     help="candidate screen of the orientation kernel (results are identical)")
     ap.add_argument("--device-only", action="store_true",
                     help="time only the device-resident step (for profiling); no e2e, FP64 form or CPU legs")

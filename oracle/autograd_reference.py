@@ -92,15 +92,23 @@ def _rotation_average(name, s0, a, w, n):
     h = ok.precession_breakpoint_step(name, w, n)
     x, wt = (torch.as_tensor(v, dtype=torch.float64, device=s0.device) for v in _GL16)
     s0d, ad = s0.detach().cpu().numpy(), a.detach().cpu().numpy()
-    cut_lists = []
-    for i in range(s0.shape[0]):
-        cuts = [0.0, math.pi]
-        if h > 0 and ad[i] > 0:
-            ks = np.arange(np.ceil((s0d[i] - ad[i]) / h), np.floor((s0d[i] + ad[i]) / h) + 1)
-            cuts += np.arccos(np.clip((ks * h - s0d[i]) / ad[i], -1, 1)).tolist()
-        cut_lists.append(np.unique(cuts))
-    m = max((len(c) for c in cut_lists), default=2)
-    cuts = np.array([np.concatenate([c, np.full(m - len(c), math.pi)]) for c in cut_lists]).reshape(-1, m)
+    n_sp = s0d.shape[0]
+    # cut angles of every spot at once: acos((k h - s0) / a) for the grid
+    # points k h inside [s0 - a, s0 + a], padded with pi (empty pieces)
+    if h > 0 and n_sp:
+        pos = ad > 0
+        safe_a = np.where(pos, ad, 1.0)
+        k_lo = np.where(pos, np.ceil((s0d - ad) / h), 0.0)
+        k_hi = np.where(pos, np.floor((s0d + ad) / h), -1.0)
+        cnt = np.maximum(k_hi - k_lo + 1, 0).astype(np.int64)
+        width = int(cnt.max(initial=0))
+        ks = k_lo[:, None] + np.arange(width)[None, :]
+        ang = np.arccos(np.clip((ks * h - s0d[:, None]) / safe_a[:, None], -1, 1))
+        ang = np.where(np.arange(width)[None, :] < cnt[:, None], ang, math.pi)
+    else:
+        ang = np.zeros((n_sp, 0))
+    cuts = np.concatenate([np.zeros((n_sp, 1)), ang, np.full((n_sp, 1), math.pi)], axis=1)
+    cuts.sort(axis=1)
     ct = torch.as_tensor(cuts, dtype=torch.float64, device=s0.device)
     mid, half = 0.5 * (ct[:, 1:] + ct[:, :-1]), 0.5 * (ct[:, 1:] - ct[:, :-1])   # (spots, pieces)
     t = mid[:, :, None] + half[:, :, None] * x                                     # (spots, pieces, 16)
@@ -150,3 +158,72 @@ def spot_intensities(xyz, B, occ, recip, quats, elements, scattering_params, spo
     re = (amp * torch.cos(ph)).sum(-1)
     im = (amp * torch.sin(ph)).sum(-1)
     return shf * (re * re + im * im)
+
+
+class MatchedLoss:
+    """L(I) = sum of squared intensity differences over the union of two
+    spot sets matched by (orientation, hkl), a spot missing on one side
+    counting with intensity 0 (the loss of the differentiation workload).
+    The match is made once on the host with a dictionary (equal keys -- the
+    two direct-beam rows -- pair up in order), so FP64 finite differences can
+    re-evaluate the loss of a fixed spot set cheaply."""
+
+    def __init__(self, offsets, hkl, target_I, target_offsets, target_hkl):
+        def keys(off, h):
+            off = np.asarray(off.detach().cpu() if torch.is_tensor(off) else off, dtype=np.int64)
+            h = np.asarray(h.detach().cpu() if torch.is_tensor(h) else h, dtype=np.int64)
+            o = np.repeat(np.arange(off.shape[0] - 1), np.diff(off))
+            return list(zip(o.tolist(), map(tuple, h.tolist())))
+        ks, kt = keys(offsets, hkl), keys(target_offsets, target_hkl)
+        pos_t = {}
+        for i, k in enumerate(kt):
+            pos_t.setdefault(k, []).append(i)
+        match_s, match_t = [], []
+        for i, k in enumerate(ks):
+            js = pos_t.get(k)
+            if js:
+                match_s.append(i)
+                match_t.append(js.pop(0))
+        T = target_I.detach().to(torch.float64)
+        dev = T.device
+        ms = torch.as_tensor(match_s, dtype=torch.int64, device=dev)
+        mt = torch.as_tensor(match_t, dtype=torch.int64, device=dev)
+        # per simulated spot: its matched target intensity, or 0
+        self.target_per_spot = torch.zeros(len(ks), dtype=torch.float64, device=dev)
+        self.target_per_spot[ms] = T[mt]
+        unmatched_t = torch.ones(T.shape[0], dtype=torch.bool, device=dev)
+        unmatched_t[mt] = False
+        self.constant = (T[unmatched_t] ** 2).sum()
+
+    def __call__(self, I, start=0):
+        """The loss of the simulated spots ``start:start + len(I)``; the
+        unmatched targets' constant is added to the chunk that starts at 0,
+        so the chunks' losses (and gradients) add up to the whole."""
+        d = I - self.target_per_spot[start:start + I.shape[0]].to(I.device)
+        out = (d * d).sum()
+        return out + self.constant.to(I.device) if start == 0 else out
+
+
+def gradient_errors(got, want, floor=1e-4, floors=(1e-6, 1e-4, 1e-2)):
+    """Per parameter group (dict name -> array):
+
+    * ``max_rel``: the largest |got - want| / max(|want|, floor x max|want|)
+      -- every component relative to itself, components below ``floor`` of
+      the group's largest measured against that floor;
+    * ``max_rel_at_floor``: the same for each of ``floors``;
+    * ``norm_rel``: ||got - want|| / ||want|| over the group;
+    * ``below_floor``: components below ``floor`` of the group's largest."""
+    out = {}
+    for name in want:
+        a = np.asarray(got[name], dtype=np.float64).reshape(-1)
+        b = np.asarray(want[name], dtype=np.float64).reshape(-1)
+        scale = float(np.abs(b).max()) if b.size else 0.0
+
+        def rel(fl):
+            den = np.maximum(np.abs(b), fl * scale) if scale > 0 else np.ones_like(b)
+            return float((np.abs(a - b) / den).max()) if b.size else 0.0
+        nb = float(np.linalg.norm(b))
+        out[name] = {"max_rel": rel(floor), "max_rel_at_floor": {f"{fl:g}": rel(fl) for fl in floors},
+                     "norm_rel": float(np.linalg.norm(a - b)) / nb if nb > 0 else 0.0,
+                     "components": int(b.size), "below_floor": int((np.abs(b) < floor * scale).sum())}
+    return out

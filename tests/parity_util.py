@@ -5,6 +5,7 @@ import warnings
 
 import numpy as np
 
+from oracle import compare as oc
 from oracle import kinematic as ok
 
 
@@ -34,79 +35,20 @@ def gpu_run(crystal, quats, p: ok.SimParams, form="mixed", orient_tile=0, with_s
     return spots, table
 
 
-def _boundary_distance(p, k0, s, z, r):
-    """Distance of one (orientation, row) pair from the selection boundary,
-    in the same units as the excitation error."""
-    eps = p.max_excitation_error
-    phi = np.deg2rad(abs(p.precession_angle))
-    if phi == 0:
-        return abs(abs(s) - eps)
-    Pz, Pt = k0 * np.cos(phi), k0 * np.sin(phi)
-    with np.errstate(invalid="ignore"):
-        zup = Pz - np.sqrt(k0 ** 2 - (r + Pt) ** 2)
-        zdo = Pz - np.sqrt(k0 ** 2 - (r - Pt) ** 2)
-    return min(abs(zup - (z - eps)), abs((z + eps) - zdo))
-
-
 def compare(spots, crystal, quats, p: ok.SimParams, rtol=1e-5, flip_window=1e-9, ref=None):
-    """Statistics of the GPU spots against the oracle; raises on any
-    difference not explained by a cutoff flip within ``flip_window``."""
-    with warnings.catch_warnings():
-        warnings.simplefilter("ignore")
-        ref = ref if ref is not None else ok.simulate(crystal, quats, p, return_s=True)
-    table = ok.phase_table(crystal, p)
-    Rs = ok.quaternion_to_matrix(quats)
-    k0 = 1 / ok.electron_wavelength(p.accelerating_voltage)
-    off = spots.offsets.cpu().numpy()
-    idx = spots.hkl_index.cpu().numpy().astype(np.int64)
-    xyzi = spots.xyzi.cpu().numpy().astype(np.float64)
+    """Statistics of the GPU spots against the oracle (``oracle.compare.spot_errors``);
+    raises on any difference not explained by a cutoff flip within
+    ``flip_window`` or by FP64 round-off of a systematic absence, on
+    intensities beyond ``rtol`` relative and on positions beyond 1e-5 |g|."""
+    if ref is None:
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            ref = ok.simulate(crystal, quats, p, return_s=True)
     s_gpu = spots.excitation_error.cpu().numpy() if spots.excitation_error is not None else None
-    g = table[2]
-    stats = dict(patterns=len(ref), spots=int(off[-1]), boundary_flips=0, noise_spots=0, max_rel_I=0.0,
-                 max_abs_pos=0.0, max_abs_s=0.0, max_flip_distance=0.0)
-    # the largest |F|^2 the structure can have: (sum_j occ_j f_j(0))^2
-    f2_scale = float(ok.kinematical_intensities([[0, 0, 0]], [0.0], crystal.elements, crystal.xyz,
-                                                crystal.occupancy, np.zeros(len(crystal.elements)),
-                                                p.scattering_params)[0]) or 1.0
-    assert off.shape[0] == len(ref) + 1 and off[0] == 0 and np.all(np.diff(off) >= 0)
-    for i, r in enumerate(ref):
-        a, b = off[i], off[i + 1]
-        gi = idx[a:b]
-        assert np.all(np.diff(gi) > 0), f"orientation {i}: spots not in table order"
-        common, ia, ib = np.intersect1d(gi, r.index, return_indices=True)
-        for j in np.setxor1d(gi, r.index):
-            if j in r.index:
-                # a spot the reference keeps only through FP64 round-off: a
-                # systematic absence (|F|^2 ~ 1e-32 of the strongest possible)
-                # kept because every spot of this pattern is one, so the
-                # 1e-20 * max mask compares noise with noise.  The CUDA path
-                # computes those |F|^2 as exact zeros and drops them.
-                I_ref = r.intensity[np.searchsorted(r.index, j)]
-                if I_ref <= 1e-24 * f2_scale:
-                    stats["noise_spots"] += 1
-                    continue
-            rot, s_all = ok.excitation_errors(crystal, p, table, Rs[i])
-            rr = np.hypot(rot[j, 0], rot[j, 1])
-            dist = _boundary_distance(p, k0, s_all[j], rot[j, 2], rr)
-            if dist < flip_window:
-                stats["boundary_flips"] += 1
-                stats["max_flip_distance"] = max(stats["max_flip_distance"], dist)
-                continue
-            raise AssertionError(f"orientation {i}: row {j} hkl {table[0][j]} differs (in gpu: {j in gi}), "
-                                 f"boundary distance {dist:.3e}")
-        Ig, Ir = xyzi[a:b][ia, 3], r.intensity[ib]
-        den = np.maximum(np.abs(Ir), 1e-300)
-        rel = np.abs(Ig - Ir) / den
-        rel = np.where((Ir == 0) & (Ig == 0), 0.0, rel)
-        noise = (Ir <= 1e-24 * f2_scale) & (Ig <= 1e-24 * f2_scale)  # round-off on both sides
-        stats["noise_spots"] += int(noise.sum())
-        rel = np.where(noise, 0.0, rel)
-        if rel.size:
-            stats["max_rel_I"] = max(stats["max_rel_I"], float(rel.max()))
-            pos = np.abs(xyzi[a:b][ia, :3] - r.xyz[ib]).max(axis=1) / np.maximum(g[common], 1e-3)
-            stats["max_abs_pos"] = max(stats["max_abs_pos"], float(pos.max()))
-            if s_gpu is not None:
-                stats["max_abs_s"] = max(stats["max_abs_s"], float(np.abs(s_gpu[a:b][ia] - r.excitation_error[ib]).max()))
+    stats = oc.spot_errors(spots.offsets.cpu().numpy(), spots.hkl_index.cpu().numpy(),
+                           spots.xyzi.cpu().numpy(), s_gpu, crystal, quats, p, ref, flip_window)
+    assert not stats["unexplained"], f"spots differ beyond the cutoff window: {stats}"
+    assert stats["ordered"], "spots not in table order"
     assert stats["max_rel_I"] <= rtol, stats
     assert stats["max_abs_pos"] <= 1e-5, stats
     return stats
