@@ -12,6 +12,8 @@ from __future__ import annotations
 import ctypes as C
 import json
 import os
+import time
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -329,6 +331,65 @@ def simulate_phase(table: PhaseTable, quats: torch.Tensor, settings: SimSettings
     raise N.NativeError("simulate: output capacity still exceeded after resizing")
 
 
+class HostSpotPool:
+    """Page-locked host arrays for streamed results, kept across calls.
+
+    Allocating (pinning) gigabytes of host memory costs far more than the
+    copies that fill it, so a generator keeps the sets it has made and hands
+    one out again once the result that used it has been garbage-collected
+    (each set remembers its owner through a weak reference).  A caller that
+    keeps every result alive gets a new set per call; one that drops the
+    previous result (the usual loop) alternates between two.  The numpy
+    arrays a result's ``host()`` returns guard the set too: while any of
+    them (or a view of one) lives, the set is not handed out again.  At most
+    ``max_sets`` idle sets are kept."""
+
+    def __init__(self, max_sets=2, headroom=1.25):
+        self.max_sets = int(max_sets)
+        self.headroom = float(headroom)
+        # [offsets int64, hkl_index int32, xyzi float32 (n, 4), owner weakref or None, guards]
+        self._sets = []
+        self.allocated_bytes = 0
+
+    @staticmethod
+    def _free(s):
+        return (s[3] is None or s[3]() is None) and all(g() is None for g in s[4])
+
+    def acquire(self, n_orient, n_spots):
+        """A free set with room for ``n_orient`` orientations and ``n_spots``
+        spots (the smallest that fits), or a new one."""
+        fits = [s for s in self._sets if self._free(s) and s[0].shape[0] >= n_orient + 1 and s[1].shape[0] >= n_spots]
+        if fits:
+            s = min(fits, key=lambda s: s[1].shape[0])
+            s[3] = None
+            s[4] = []
+            return s
+        idle = [s for s in self._sets if self._free(s)]
+        while idle and len(idle) >= self.max_sets:  # drop the smallest idle sets first
+            victim = min(idle, key=lambda s: s[1].shape[0])
+            idle.remove(victim)
+            self._sets.remove(victim)
+        n_o = int((n_orient + 1) * self.headroom) + 1
+        n_s = max(int(n_spots * self.headroom), 1024)
+        s = [torch.empty(n_o, dtype=torch.int64, pin_memory=True),
+             torch.empty(n_s, dtype=torch.int32, pin_memory=True),
+             torch.empty((n_s, 4), dtype=torch.float32, pin_memory=True), None, []]
+        self.allocated_bytes += n_o * 8 + n_s * 20
+        self._sets.append(s)
+        return s
+
+    def bind(self, s, owner):
+        s[3] = weakref.ref(owner)
+
+    @staticmethod
+    def guard(s, array):
+        """Keep set ``s`` from reuse while ``array`` (a numpy view of it) or
+        any view derived from it lives: numpy views share the base object,
+        here the tensor alias that ``Tensor.numpy()`` creates."""
+        base = array.base if array.base is not None else array
+        s[4].append(weakref.ref(base))
+
+
 class StreamedSpots(PhaseSpots):
     """Spots of one phase simulated in orientation chunks, each chunk's CSR
     copied to page-locked host memory on a side stream while the later
@@ -338,19 +399,21 @@ class StreamedSpots(PhaseSpots):
 
     ``host()`` waits for the copies in flight.  The device CSR (``offsets``
     is global; ``hkl_index``, ``xyzi``, ``excitation_error``) is assembled
-    from the chunks' regions on first access."""
+    from the chunks' regions on first access.  ``timings()`` gives the time
+    split of the call once the copies are done."""
 
-    def __init__(self, table, chunks, regions, host_bufs, done, total):
+    def __init__(self, table, chunks, regions, host_bufs, done, total, timing=None):
         self.table = table
         self._chunks = chunks        # per chunk: (first orientation, chunk offsets on the device, spot base)
         self._regions = regions      # per chunk: (idx, xyzi, s, n_spots)
-        self._host_bufs = host_bufs  # page-locked (offsets, hkl_index, xyzi)
+        self._host_bufs = host_bufs  # page-locked (offsets, hkl_index, xyzi) (pool set)
         self._done = done            # event after the last copy
         self.total = total
         self._n = sum(c[1].shape[0] - 1 for c in chunks)
         self._host = None
         self._dev = None
         self._off = None
+        self._timing = timing or {}
 
     @property
     def n_orient(self):
@@ -388,18 +451,41 @@ class StreamedSpots(PhaseSpots):
 
     def host(self, pinned=False):
         if self._host is None:
+            t0 = time.perf_counter()
             self._done.synchronize()
-            off, idx, xyzi = self._host_bufs
-            off = off.numpy()
+            t1 = time.perf_counter()
+            hb = self._host_bufs
+            off = hb[0][:self._n + 1].numpy()
             for a, o, base in self._chunks:  # chunk-relative offsets made global
                 off[a:a + o.shape[0] - 1] += base
             off[self._n] = self.total
-            self._host = (off, idx[:self.total].numpy(), xyzi[:self.total].numpy())
+            self._host = (off, hb[1][:self.total].numpy(), hb[2][:self.total].numpy())
+            for arr in self._host:
+                HostSpotPool.guard(hb, arr)
+            self._timing["host_wait_ms"] = (t1 - t0) * 1e3
+            self._timing["host_wrap_ms"] = (time.perf_counter() - t1) * 1e3
         return self._host
+
+    def timings(self):
+        """Time split of the call (milliseconds), complete after ``host()``:
+        host set-up before the first launch, host time blocked on chunk
+        counts, pinned-memory allocation, the chunks' device span (first
+        launch to last chunk end) and the copies' span (first copy to the
+        last), the wait in ``host()`` and the offsets fix-up."""
+        t = dict(self._timing)
+        ev = t.pop("_events", None)
+        if ev is not None:
+            self._done.synchronize()
+            k0, k1, c0 = ev
+            t["kernel_span_ms"] = k0.elapsed_time(k1)
+            t["copy_span_ms"] = c0.elapsed_time(self._done) if c0 is not None else 0.0
+            t["first_copy_after_launch_ms"] = k0.elapsed_time(c0) if c0 is not None else 0.0
+        return t
 
 
 def simulate_phase_streamed(table: PhaseTable, quats: torch.Tensor, settings: SimSettings, radius: float,
-                            chunk=32768, first_chunk=2048, with_excitation_error=False) -> StreamedSpots:
+                            chunk=32768, first_chunk=2048, with_excitation_error=False,
+                            host_pool: HostSpotPool | None = None, timing=False) -> StreamedSpots:
     """``simulate_phase`` for a result wanted on the host: the orientations
     run in chunks on the current stream, each into its own device region,
     and each chunk's spots are copied to page-locked host memory on a side
@@ -407,12 +493,17 @@ def simulate_phase_streamed(table: PhaseTable, quats: torch.Tensor, settings: Si
     Chunk sizes double from ``first_chunk`` up to ``chunk``: the copies
     start early, and the copy of a chunk (at about twice the kernel's time
     per orientation) overlaps the next, twice larger, chunk.  A chunk whose
-    spots overflow its region is re-run alone with the exact size."""
+    spots overflow its region is re-run alone with the exact size.  The host
+    arrays come from ``host_pool`` (reused across calls) or are allocated;
+    they are sized from the first chunk's spot count.  With ``timing`` the
+    result records CUDA events for ``StreamedSpots.timings``."""
+    t_start = time.perf_counter()
     lib = N.load_library()
     dev = table.device
     n = int(quats.shape[0])
     comp = torch.cuda.current_stream(dev)
     copy = torch.cuda.Stream(dev)
+    host_pool = host_pool or HostSpotPool(max_sets=0)
     bounds = [0]
     size = max(1, min(first_chunk, chunk))
     while bounds[-1] < n:
@@ -434,6 +525,12 @@ def simulate_phase_streamed(table: PhaseTable, quats: torch.Tensor, settings: Si
     chunk_off = [torch.empty(b - a + 1, dtype=torch.int64, device=dev) for a, b in zip(bounds[:-1], bounds[1:])]
     sf_status_h = torch.empty(1, dtype=torch.int32, pin_memory=True)
     sf_status_h.copy_(table._status, non_blocking=True)  # read after the first chunk, without a stall
+    k_start = k_end = c_start = None
+    if timing:
+        k_start = torch.cuda.Event(enable_timing=True)
+        k_end = torch.cuda.Event(enable_timing=True)
+        c_start = torch.cuda.Event(enable_timing=True)
+        k_start.record(comp)
 
     def launch(k, cap):
         a, b = bounds[k], bounds[k + 1]
@@ -446,23 +543,25 @@ def simulate_phase_streamed(table: PhaseTable, quats: torch.Tensor, settings: Si
                                 sbytes, N.ptr(status[k:]), N.stream_handle(comp)), "simulate")
         totals_h[k:k + 1].copy_(totals[k:k + 1], non_blocking=True)
         status_h[k:k + 1].copy_(status[k:k + 1], non_blocking=True)
-        ev = torch.cuda.Event()
+        ev = torch.cuda.Event(enable_timing=timing)
         ev.record(comp)
         return [idx, xyzi, s, ev]
 
     caps = [max(1024, (b - a) * per * 5 // 4) for a, b in zip(bounds[:-1], bounds[1:])]
     regions = [launch(k, caps[k]) for k in range(min(2, n_chunks))]
-    host_cap = sum(caps)
-    h_idx = torch.empty(host_cap, dtype=torch.int32, pin_memory=True)
-    h_xyzi = torch.empty((host_cap, 4), dtype=torch.float32, pin_memory=True)
-    h_off = torch.empty(n + 1, dtype=torch.int64, pin_memory=True)
+    t_launched = time.perf_counter()
+    wait_s = alloc_s = 0.0
+    hb = None
+    h_off = h_idx = h_xyzi = None
     base = 0
     out_regions, chunks = [], []
     for k in range(n_chunks):
         if k + 2 < n_chunks:
             regions.append(launch(k + 2, caps[k + 2]))  # two chunks queued ahead of the copies
         idx, xyzi, s, ev = regions[k]
+        tw = time.perf_counter()
         ev.synchronize()
+        wait_s += time.perf_counter() - tw
         v = N.check_status_value(int(status_h[k]), "simulate", allow=N.DS_ERR_CAPACITY)
         if k == 0:
             N.check_status_value(int(sf_status_h[0]), "structure_factors")
@@ -473,20 +572,33 @@ def simulate_phase_streamed(table: PhaseTable, quats: torch.Tensor, settings: Si
             ev.synchronize()
             N.check_status_value(int(status_h[k]), "simulate")
             cnt = int(totals_h[k])
-        if base + cnt > h_idx.shape[0]:
-            # the host arrays outgrew the estimate: grow them (waits for the copies so far)
-            copy.synchronize()
-            grow = max(base + cnt, h_idx.shape[0] * 3 // 2)
-            ni = torch.empty(grow, dtype=torch.int32, pin_memory=True)
-            nx = torch.empty((grow, 4), dtype=torch.float32, pin_memory=True)
-            ni[:base].copy_(h_idx[:base])
-            nx[:base].copy_(h_xyzi[:base])
-            h_idx, h_xyzi = ni, nx
         a, b = bounds[k], bounds[k + 1]
+        if hb is None:
+            # host arrays sized from the first chunk's spots per orientation
+            need = int(np.ceil(cnt / max(b - a, 1) * n * 1.1)) + 4096
+            ta = time.perf_counter()
+            hb = host_pool.acquire(n, need)
+            alloc_s += time.perf_counter() - ta
+            h_off, h_idx, h_xyzi = hb[0], hb[1], hb[2]
+        if base + cnt > h_idx.shape[0]:
+            # the host arrays outgrew the estimate: a larger set (waits for the copies so far)
+            copy.synchronize()
+            ta = time.perf_counter()
+            nb = host_pool.acquire(n, max(base + cnt, h_idx.shape[0] * 3 // 2))
+            alloc_s += time.perf_counter() - ta
+            nb[0][:a].copy_(h_off[:a])
+            nb[1][:base].copy_(h_idx[:base])
+            nb[2][:base].copy_(h_xyzi[:base])
+            hb[3] = None
+            hb[4] = []
+            hb = nb
+            h_off, h_idx, h_xyzi = hb[0], hb[1], hb[2]
         copy.wait_event(ev)
         # copies only on the side stream: a kernel there would wait for an
         # SM behind the persistent simulation kernel, and the copies behind it
         with torch.cuda.stream(copy):
+            if k == 0 and c_start is not None:
+                c_start.record(copy)
             if b > a:
                 h_off[a:b].copy_(chunk_off[k][:b - a], non_blocking=True)
             if cnt:
@@ -495,14 +607,22 @@ def simulate_phase_streamed(table: PhaseTable, quats: torch.Tensor, settings: Si
         out_regions.append((idx, xyzi, s, cnt))
         chunks.append((a, chunk_off[k], base))
         base += cnt
-    done = torch.cuda.Event()
+    done = torch.cuda.Event(enable_timing=timing)
     done.record(copy)
+    if k_end is not None:
+        k_end.record(comp)
     # the chunk buffers were read on the copy stream as well
     for r in out_regions + [(c, None, None, 0) for c in chunk_off]:
         for x in r[:3]:
             if x is not None:
                 x.record_stream(copy)
-    return StreamedSpots(table, chunks, out_regions, (h_off, h_idx, h_xyzi), done, base)
+    rec = {"launch_ms": (t_launched - t_start) * 1e3, "chunk_wait_ms": wait_s * 1e3, "pinned_alloc_ms": alloc_s * 1e3,
+           "streamed_call_ms": (time.perf_counter() - t_start) * 1e3, "chunks": n_chunks}
+    if timing:
+        rec["_events"] = (k_start, k_end, c_start)
+    res = StreamedSpots(table, chunks, out_regions, hb, done, base, rec)
+    host_pool.bind(hb, res)
+    return res
 
 
 @dataclass

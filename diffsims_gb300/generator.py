@@ -3,6 +3,7 @@ diffsims/generators/simulation_generator.py (``calculate_diffraction2d``)
 running on the CUDA library."""
 from __future__ import annotations
 
+import time
 from typing import Sequence, Union
 
 import numpy as np
@@ -10,10 +11,11 @@ import torch
 
 from . import _native as N
 from .crystal import Phase, Rotation, lattice_params, quaternions_of, structure_of
-from .engine import (PhaseBatch, PhaseTable, SimSettings, SpotBuffers, reciprocal_basis, simulate_phase,
+from .engine import (HostSpotPool, PhaseBatch, PhaseTable, SimSettings, SpotBuffers, reciprocal_basis, simulate_phase,
                      simulate_phase_streamed)
 from .simulation1d import Simulation1D
 from .simulation2d import Simulation2D
+from . import interop
 from .symmetry import point_group_rotations, symmetry_families
 from .sim_utils import get_electron_wavelength
 
@@ -46,6 +48,16 @@ def _min_dspacing_rows(phase, min_dspacing, scattering_params, debye_waller_fact
     torch.cuda.current_stream().synchronize()
     return (table.hkl_host().astype(np.int64), np.sqrt(table.g2.cpu().numpy()),
             table.F2d[:table.n].cpu().numpy())
+
+
+def _caller_rotations(caller_rotation, rots, single_phase):
+    """The caller's rotation objects for a reference-type result (orix
+    ``Rotation``); the identity as an orix ``Rotation`` when none was given."""
+    if caller_rotation is None:
+        from orix.quaternion import Rotation as OrixRotation
+        ident = OrixRotation.identity()
+        return ident if single_phase else [ident] * len(rots)
+    return caller_rotation
 
 
 def _is_hexagonal(lattice) -> bool:
@@ -93,7 +105,7 @@ class SimulationGenerator:
             raise NotImplementedError(
                 "The scattering parameters `{}` is not implemented. See documentation for available "
                 "implementations.".format(scattering_params))
-        self._buffers = {}
+        self._host_pool = HostSpotPool()  # page-locked result arrays reused across calls
 
     def __repr__(self):
         return (f"SimulationGenerator(accelerating_voltage={self.accelerating_voltage}, "
@@ -129,7 +141,8 @@ class SimulationGenerator:
                                 reciprocal_radius: float = 1.0, with_direct_beam: bool = True,
                                 max_excitation_error: float = 1e-2, shape_factor_width: float = None,
                                 debye_waller_factors: dict = None, show_progressbar: bool = False,
-                                form: str = "mixed", orient_tile: int = 0, stream_to_host: bool = True):
+                                form: str = "mixed", orient_tile: int = 0, stream_to_host: bool = True,
+                                timing: bool = False, result: str = "auto"):
         """Spot patterns of one or more phases, each under its own rotations.
 
         Arguments as diffsims/generators/simulation_generator.py:134-146;
@@ -141,8 +154,22 @@ class SimulationGenerator:
         phase runs in orientation chunks whose spots are copied to
         page-locked host memory while later chunks compute; ``False`` keeps
         the spots on the device only (for device-side consumers such as
-        ``get_diffraction_patterns``).  Returns ``Simulation2D``.
+        ``get_diffraction_patterns``); the page-locked host arrays are kept
+        by the generator and reused once a previous result is released.
+        With ``timing`` (single phase, streamed) the result's
+        ``spots(0).timings()`` gives the call's time split.  ``result``:
+        'native' returns this library's ``Simulation2D``; 'reference' the
+        reference package's own ``Simulation2D`` with ``DiffractingVector``
+        coordinates built per pattern on first read
+        (``interop.to_reference_simulation``; needs diffsims, orix and
+        diffpy); 'auto' (default) the reference's types when that package is
+        importable and the phases are not this library's ``Phase`` objects,
+        else the native one.
         """
+        t_call = time.perf_counter()
+        if result not in ("auto", "native", "reference"):
+            raise ValueError("result must be 'auto', 'native' or 'reference'")
+        caller_rotation = rotation
         if rotation is None:
             rotation = Rotation.from_euler((0, 0, 0), degrees=True)
         single_phase = not isinstance(phase, (list, tuple))
@@ -157,14 +184,23 @@ class SimulationGenerator:
         dev = torch.device("cuda", torch.cuda.current_device())
         settings = self.settings(max_excitation_error, shape_factor_width, form, orient_tile)
         rots, tables, qs = [], [], []
+        t_table = t_upload = 0.0
         for p, r in zip(phases, rotations):
             rot = r if isinstance(r, Rotation) else Rotation(quaternions_of(r))
+            t0 = time.perf_counter()
             tables.append(PhaseTable(p, reciprocal_radius, with_direct_beam, self.scattering_params,
                                      debye_waller_factors, form=form, device=dev))
+            t1 = time.perf_counter()
             qs.append(torch.from_numpy(quaternions_of(rot)).to(dev))
+            t_upload += time.perf_counter() - t1
+            t_table += t1 - t0
             rots.append(rot)
         if len(tables) == 1 and stream_to_host:
-            spots = [simulate_phase_streamed(tables[0], qs[0], settings, reciprocal_radius)]
+            sp = simulate_phase_streamed(tables[0], qs[0], settings, reciprocal_radius, host_pool=self._host_pool,
+                                         timing=timing)
+            sp._timing.update(table_ms=t_table * 1e3, upload_ms=t_upload * 1e3,
+                              before_stream_ms=(time.perf_counter() - t_call) * 1e3 - sp._timing["streamed_call_ms"])
+            spots = [sp]
         elif len(tables) == 1:
             spots = [simulate_phase(tables[0], qs[0], settings, reciprocal_radius, buffers=SpotBuffers(dev))]
         else:
@@ -173,8 +209,14 @@ class SimulationGenerator:
             tile = min(int(orient_tile), 16 if form == "mixed" else 8) if orient_tile else 0
             spots = PhaseBatch(tables, qs, settings, reciprocal_radius, orient_tile=tile).run().spots()
         if single_phase:
-            return Simulation2D(phases[0], spots, rots[0], self, reciprocal_radius)
-        return Simulation2D(phases, spots, rots, self, reciprocal_radius)
+            native = Simulation2D(phases[0], spots, rots[0], self, reciprocal_radius)
+        else:
+            native = Simulation2D(phases, spots, rots, self, reciprocal_radius)
+        if result == "native" or (result == "auto" and (interop.cached_reference_classes() is None or
+                                                        all(isinstance(p, Phase) for p in phases))):
+            return native
+        user_rot = _caller_rotations(caller_rotation, rots, single_phase)
+        return interop.to_reference_simulation(native, phases[0] if single_phase else phases, user_rot)
 
     def calculate_diffraction1d(self, phase, reciprocal_radius: float = 1.0, minimum_intensity: float = 1e-3,
                                  debye_waller_factors: dict = None):
