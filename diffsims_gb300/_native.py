@@ -31,7 +31,7 @@ DS_SCATTER = {"lobato": 0, "xtables": 1, None: 2}
 DS_SCATTER_KINEMATICAL = 3
 DS_SCATTER_DOYLETURNER = 4
 DS_SHAPE = {"linear": 0, "atanc": 1, "sinc": 2, "sin2c": 3, "lorentzian": 4, "binary": 5}
-DS_SCREEN = {"auto": 0, "rows": 1, "lines": 2}
+DS_SCREEN = {"auto": 0, "rows": 1, "lines": 2, "bricks": 3}
 DS_PRECESSION_NONE = 0
 DS_PRECESSION_LORENTZIAN = 1
 DS_PRECESSION_INTEGRAL = 2
@@ -43,7 +43,7 @@ EXPORTED_SYMBOLS = (
     "ds_simulate_batch", "ds_rasterize_scratch_bytes", "ds_rasterize",
     "ds_simulate_backward_scratch_bytes", "ds_simulate_backward", "ds_structure_factors_backward_scratch_bytes",
     "ds_axis_angle_compose", "ds_axis_angle_compose_backward", "ds_polar_flatten", "ds_structure_factors_backward",
-    "ds_probe_fp32_fma", "ds_last_error", "ds_version",
+    "ds_probe_fp32_fma", "ds_set_wait_limits", "ds_probe_wait_timeout", "ds_last_error", "ds_version",
 )
 
 
@@ -143,6 +143,8 @@ def load_library(require_cuda: bool = True):
             lib.ds_polar_flatten.argtypes = [vp, vp, i64, i64, vp, i64, vp, i64, vp, vp, vp, vp]
             lib.ds_axis_angle_compose_backward.argtypes = [vp, vp, i64, vp, vp, vp]
             lib.ds_probe_fp32_fma.argtypes = [i64, i32, vp, vp]
+            lib.ds_set_wait_limits.argtypes = [i64, i64]
+            lib.ds_probe_wait_timeout.argtypes = [i64, vp, sz, vp, vp, vp]
             lib.ds_last_error.restype = C.c_char_p
             lib.ds_version.restype = C.c_char_p
             for name in ("ds_box_extent", "ds_enumerate_hkl", "ds_structure_factors", "ds_kinematical_intensities",
@@ -150,7 +152,7 @@ def load_library(require_cuda: bool = True):
                          "ds_simulate", "ds_simulate_batch", "ds_rasterize", "ds_simulate_backward",
                          "ds_structure_factors_backward",
                          "ds_axis_angle_compose", "ds_axis_angle_compose_backward", "ds_polar_flatten",
-                         "ds_probe_fp32_fma"):
+                         "ds_probe_fp32_fma", "ds_set_wait_limits", "ds_probe_wait_timeout"):
                 getattr(lib, name).restype = C.c_int32
             _lib = lib
     if require_cuda and not torch.cuda.is_available():
@@ -183,6 +185,15 @@ def check_status_value(v: int, what: str, allow=0) -> int:
     if bad:
         raise NativeError(f"{what}: device status {v}")
     return v
+
+
+def set_wait_limits(lookback_polls: int = 0, mbarrier_polls: int = 0):
+    """Polls before the kernels' bounded waits give up (DS_ERR_TIMEOUT) for
+    launches set up from now on: the decoupled look-back's wait for an
+    earlier tile and the structure-factor kernels' wait for a staging copy.
+    0 restores the defaults (2^24 and 2^22 polls)."""
+    check(load_library(require_cuda=False).ds_set_wait_limits(int(lookback_polls), int(mbarrier_polls)),
+          "set_wait_limits")
 
 
 def ptr(t: torch.Tensor | None):

@@ -480,6 +480,7 @@ extern "C" ds_status ds_simulate_backward(const ds_sim_params *p, const ds_phase
                                           double *grad_quats, double *grad_recip, void *scratch, size_t scratch_bytes,
                                           int32_t *status, void *stream) {
     clear_error();
+    DS_NVTX_RANGE("ds_simulate_backward");
     DS_REQUIRE(p && t, "ds_simulate_backward: null pointer");
     DS_REQUIRE(n_orient >= 0, "ds_simulate_backward: n_orient < 0");
     DS_REQUIRE(p->k0 > 0 && isfinite(p->k0), "ds_simulate_backward: k0 must be finite and > 0");
@@ -560,6 +561,7 @@ extern "C" ds_status ds_structure_factors_backward(const ds_atoms *atoms, const 
                                                    double *grad_atoms, double *grad_recip, void *scratch,
                                                    size_t scratch_bytes, void *stream) {
     clear_error();
+    DS_NVTX_RANGE("ds_structure_factors_backward");
     DS_REQUIRE(atoms && recip, "ds_structure_factors_backward: null pointer");
     DS_REQUIRE(n >= 0, "ds_structure_factors_backward: n < 0");
     DS_REQUIRE(atoms->n_atoms >= 0 && atoms->n_species >= 0 && atoms->n_species <= 32,
@@ -596,6 +598,7 @@ extern "C" ds_status ds_structure_factors_backward(const ds_atoms *atoms, const 
 extern "C" ds_status ds_axis_angle_compose(const double *q0, const double *rotvec, int64_t n, double *quats_out,
                                            void *stream) {
     clear_error();
+    DS_NVTX_RANGE("ds_axis_angle_compose");
     DS_REQUIRE(n >= 0, "ds_axis_angle_compose: n < 0");
     if (n == 0) return DS_OK;
     DS_REQUIRE(q0 && rotvec && quats_out, "ds_axis_angle_compose: null array");
@@ -606,6 +609,7 @@ extern "C" ds_status ds_axis_angle_compose(const double *q0, const double *rotve
 extern "C" ds_status ds_axis_angle_compose_backward(const double *q0, const double *rotvec, int64_t n,
                                                     const double *grad_quats, double *grad_rotvec, void *stream) {
     clear_error();
+    DS_NVTX_RANGE("ds_axis_angle_compose_backward");
     DS_REQUIRE(n >= 0, "ds_axis_angle_compose_backward: n < 0");
     if (n == 0) return DS_OK;
     DS_REQUIRE(q0 && rotvec && grad_quats && grad_rotvec, "ds_axis_angle_compose_backward: null array");

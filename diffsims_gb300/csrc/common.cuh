@@ -7,9 +7,24 @@
 
 #include <string>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "diffsims_gb300.h"
 
 namespace ds {
+
+// An NVTX range over the host work of one C entry (argument checks, plans,
+// the enqueued launches), named after the entry: profilers (Nsight Systems,
+// ncu's NVTX filters) show each call on the host timeline beside its
+// kernels.  Without a profiler attached a push / pop is a check of a null
+// callback.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+#define DS_NVTX_RANGE(name) ::ds::NvtxRange ds_nvtx_range_(name)
 
 // ----------------------------------------------------------------------------
 // host-side error reporting (thread-local last message)
@@ -107,11 +122,17 @@ __host__ __device__ inline void split_double(double x, float &hi, float &lo) {
 constexpr unsigned long long LB_FLAG_AGG = 1ull << 62;
 constexpr unsigned long long LB_FLAG_INC = 2ull << 62;
 constexpr unsigned long long LB_VALUE_MASK = (1ull << 62) - 1;
-constexpr long long LB_SPIN_LIMIT = 1ll << 24;  // polls (with backoff) before giving up
+constexpr long long LB_SPIN_LIMIT = 1ll << 24;  // polls (with backoff) before giving up (default)
+
+// Process-wide wait limits read when a launch is set up (ds_set_wait_limits;
+// 0 = the defaults above and below).
+long long wait_limit_lookback();
+long long wait_limit_mbarrier();
 
 struct LookbackScratch {
     unsigned long long *ticket;  // one word, zeroed before launch
     unsigned long long *state;   // n_tiles words, zeroed before launch
+    long long spin_limit;        // polls before a wait gives up
 };
 
 inline size_t lookback_scratch_bytes(long long n_tiles) {
@@ -119,7 +140,7 @@ inline size_t lookback_scratch_bytes(long long n_tiles) {
 }
 inline LookbackScratch lookback_scratch(void *base) {
     auto *p = reinterpret_cast<unsigned long long *>(base);
-    return {p, p + 32};
+    return {p, p + 32, wait_limit_lookback()};
 }
 
 // A state word carries its flag and value together and no other data is
@@ -153,7 +174,7 @@ __device__ inline long long lookback_resolve(LookbackScratch lb, long long tile,
         unsigned long long s = lb_load(lb.state + idx);
         unsigned long long flag = s & ~LB_VALUE_MASK;
         if (flag == 0ull) {
-            if (++spins > LB_SPIN_LIMIT) {
+            if (++spins > lb.spin_limit) {
                 atomicOr(status, DS_ERR_TIMEOUT);
                 return -1;
             }
@@ -209,15 +230,19 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-constexpr long long MBAR_SPIN_LIMIT = 1ll << 22;
-// Bounded wait for phase `parity`; on timeout flags DS_ERR_TIMEOUT and waits a
-// second, longer bounded time so that no copy is left writing this CTA's
-// shared memory after it returns.  Returns false on timeout.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int32_t *status) {
-    for (long long i = 0; i < MBAR_SPIN_LIMIT; ++i)
+constexpr long long MBAR_SPIN_LIMIT = 1ll << 22;  // default polls of the first wait
+// Bounded wait for phase `parity` (`limit` polls); on timeout flags
+// DS_ERR_TIMEOUT and waits a second bounded time (`drain` polls; by default
+// the long fixed one, whatever `limit` is) so that no copy this CTA issued is
+// left writing its shared memory after it returns.  A caller that issued no
+// copy on the barrier may pass a short `drain`.  Returns false on timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int32_t *status,
+                                                  long long limit = MBAR_SPIN_LIMIT,
+                                                  long long drain = 16 * MBAR_SPIN_LIMIT) {
+    for (long long i = 0; i < limit; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     atomicOr(status, DS_ERR_TIMEOUT);
-    for (long long i = 0; i < 16 * MBAR_SPIN_LIMIT; ++i)
+    for (long long i = 0; i < drain; ++i)
         if (mbar_try_wait(bar, parity)) break;
     return false;
 }

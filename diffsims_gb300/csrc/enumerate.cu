@@ -180,6 +180,7 @@ extern "C" ds_status ds_enumerate_hkl(const double recip[9], const int32_t hmax[
                                       int64_t *count_out, void *scratch, size_t scratch_bytes,
                                       int32_t *status, void *stream) {
     clear_error();
+    DS_NVTX_RANGE("ds_enumerate_hkl");
     DS_REQUIRE(recip && hmax && hkl_out && g2_out && count_out && scratch && status,
                "ds_enumerate_hkl: null pointer");
     DS_REQUIRE(hmax[0] >= 0 && hmax[1] >= 0 && hmax[2] >= 0, "ds_enumerate_hkl: negative box");
@@ -206,6 +207,7 @@ extern "C" ds_status ds_enumerate_sphere(const double recip[9], const int32_t hm
                                          int32_t *hkl_out, double *g2_out, int64_t capacity, int64_t *count_out,
                                          void *scratch, size_t scratch_bytes, int32_t *status, void *stream) {
     clear_error();
+    DS_NVTX_RANGE("ds_enumerate_sphere");
     DS_REQUIRE(recip && hmax && hkl_out && g2_out && count_out && scratch && status,
                "ds_enumerate_sphere: null pointer");
     DS_REQUIRE(hmax[0] >= 0 && hmax[1] >= 0 && hmax[2] >= 0, "ds_enumerate_sphere: negative box");

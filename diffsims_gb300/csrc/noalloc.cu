@@ -21,11 +21,11 @@
 //   different streams, or from different host threads without ordering) race
 //   on it.  Calls on one stream are ordered and safe.  Every call clears the
 //   parts that must start at zero (look-back tile states, line counters).
-// * the first call on a device looks up the array's device address with
-//   cudaGetSymbolAddress (once per device, with that device current); make
-//   that first call before any stream capture.
-#include <mutex>
-
+// * every call looks the array's device address up with
+//   cudaGetSymbolAddress, with the caller's device current (a host-side
+//   lookup once the library's device code is loaded on that device), so the
+//   address is never stale, also across a cudaDeviceReset.  The first call on
+//   a device loads that device code: make it before any stream capture.
 #include "common.cuh"
 
 namespace ds {
@@ -33,24 +33,16 @@ namespace ds {
 constexpr size_t DS_NOALLOC_SCRATCH_BYTES = 64ull << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[DS_NOALLOC_SCRATCH_BYTES];
 
-constexpr int NOALLOC_MAX_DEVICES = 64;
-static void *g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {nullptr};
-static std::mutex g_noalloc_mutex;
+ds_status simulate_scratch_plan(const ds_sim_params *p, const ds_phase_table *t, long long n_orient,
+                                size_t *total, long long *stage_cap, size_t *per_stage);
 
 // Device address of the static scratch on the current device (host code may
 // not use the symbol itself as a device pointer).
 static ds_status noalloc_scratch(void **out) {
-    int dev = 0;
-    DS_CUDA_TRY(cudaGetDevice(&dev));
-    DS_REQUIRE(dev >= 0 && dev < NOALLOC_MAX_DEVICES, "ds_simulate_noalloc: device index out of range");
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (g_noalloc_ptr[dev] == nullptr) {
-        void *p = nullptr;
-        DS_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-        DS_REQUIRE(p != nullptr, "ds_simulate_noalloc: no device address for the static scratch");
-        g_noalloc_ptr[dev] = p;
-    }
-    *out = g_noalloc_ptr[dev];
+    void *p = nullptr;
+    DS_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    DS_REQUIRE(p != nullptr, "ds_simulate_noalloc: no device address for the static scratch");
+    *out = p;
     return DS_OK;
 }
 
@@ -61,33 +53,37 @@ using namespace ds;
 extern "C" ds_status ds_simulate_noalloc(const ds_sim_params *p, const ds_phase_table *t, const double *quats,
                                          int64_t n_orient, ds_spots *out, int32_t *status, void *stream) {
     clear_error();
+    DS_NVTX_RANGE("ds_simulate_noalloc");
     DS_REQUIRE(p && t && out && status, "ds_simulate_noalloc: null pointer");
     DS_REQUIRE(p->stage_cap >= 0, "ds_simulate_noalloc: stage_cap < 0");
     void *scratch = nullptr;
     ds_status st = noalloc_scratch(&scratch);
     if (st) return st;
-    // Fit the scratch into the static array: shrink the candidate staging
-    // (halving; 1 leaves every orientation on the bitmap fallback) until the
-    // plan fits, else reject.
+    if (n_orient <= 0)  // nothing to plan: ds_simulate only writes the empty CSR (or rejects n_orient < 0)
+        return ds_simulate(p, t, quats, n_orient, out, scratch, DS_NOALLOC_SCRATCH_BYTES, status, stream);
+    // Fit the scratch into the static array.  Only the per-CTA candidate
+    // staging depends on the staging capacity, linearly: take the largest
+    // capacity that fits (1 leaves every orientation on the bitmap fallback),
+    // then check it with a second plan.
     ds_sim_params q = *p;
-    long long cap = q.stage_cap > 0 ? q.stage_cap : 24576;
-    size_t need = 0;
-    for (;;) {
-        q.stage_cap = (int32_t)cap;
-        need = ds_simulate_scratch_bytes(&q, t, n_orient);
-        if (n_orient > 0 && need == 0) {
-            // the plan itself failed (e.g. a table too large for one tile)
-            set_error("ds_simulate_noalloc: no launch plan for these sizes");
-            return DS_ERR_INVALID_ARGUMENT;
-        }
-        if (need <= DS_NOALLOC_SCRATCH_BYTES) break;
-        if (cap == 1) {
-            set_error("ds_simulate_noalloc: this problem needs " + std::to_string(need) +
+    size_t total = 0, per = 0;
+    long long cap = 0;
+    st = simulate_scratch_plan(&q, t, n_orient, &total, &cap, &per);
+    if (st) return st;  // the plan's own status and message
+    if (total > DS_NOALLOC_SCRATCH_BYTES) {
+        const size_t slack = 512;  // alignment of the two staging arrays
+        const size_t fixed = total - per * (size_t)cap;
+        if (fixed + per + slack > DS_NOALLOC_SCRATCH_BYTES) {
+            set_error("ds_simulate_noalloc: this problem needs at least " + std::to_string(fixed + per) +
                       " bytes of scratch; the static scratch holds " + std::to_string(DS_NOALLOC_SCRATCH_BYTES) +
                       " bytes (use ds_simulate with a caller-owned scratch buffer)");
             return DS_ERR_INVALID_ARGUMENT;
         }
-        cap = cap > 64 ? cap / 2 : 1;
+        const long long fit = (long long)((DS_NOALLOC_SCRATCH_BYTES - fixed - slack) / per);
+        q.stage_cap = (int32_t)(fit < cap ? fit : cap);
+        st = simulate_scratch_plan(&q, t, n_orient, &total, &cap, &per);
+        if (st) return st;
+        DS_REQUIRE(total <= DS_NOALLOC_SCRATCH_BYTES, "ds_simulate_noalloc: staging plan does not fit the static scratch");
     }
     return ds_simulate(&q, t, quats, n_orient, out, scratch, DS_NOALLOC_SCRATCH_BYTES, status, stream);
 }

@@ -87,6 +87,7 @@ extern "C" ds_status ds_polar_flatten(const int64_t *offsets, const float *xyzi,
                                       const double *azimuthal_axes, int64_t n_azimuthal, double *r_out,
                                       double *theta_out, double *intensity_out, void *stream) {
     clear_error();
+    DS_NVTX_RANGE("ds_polar_flatten");
     DS_REQUIRE(n_patterns >= 0 && max_spots >= 0, "ds_polar_flatten: negative size");
     DS_REQUIRE((radial_axes == nullptr) == (azimuthal_axes == nullptr),
                "ds_polar_flatten: give both axes or neither");

@@ -883,6 +883,7 @@ extern "C" ds_status ds_rasterize(const ds_raster_params *p, const int64_t *offs
                                   int64_t n_patterns, int64_t max_spots, float *out, void *scratch,
                                   size_t scratch_bytes, int32_t *status, void *stream) {
     clear_error();
+    DS_NVTX_RANGE("ds_rasterize");
     ds_status st = raster_validate(p);
     if (st) return st;
     DS_REQUIRE(status, "ds_rasterize: null status");

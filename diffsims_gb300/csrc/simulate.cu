@@ -1,5 +1,7 @@
 // A4-A7 host side: launch plan, scratch layout and the ds_simulate entry
 // point of the orientation kernel (device code in simulate_kernel.cuh).
+#include <algorithm>
+
 #include "simulate_kernel.cuh"
 
 namespace ds {
@@ -113,16 +115,238 @@ lines_kernel(SimConst c, const int32_t *__restrict__ hkl, LineP *__restrict__ li
 
 static inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+// ---------------------------------------------------------------- bricks ----
+// Rows per block (atomic counts).
+__global__ void brick_count_kernel(BrickGeom G, const int32_t *__restrict__ hkl, long long n, int32_t *cnt) {
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    atomicAdd(&cnt[brick_block(G, hkl[3 * j], hkl[3 * j + 1], hkl[3 * j + 2])], 1);
+}
+
+// One block: each block of rows becomes ceil(count / 32) bricks of 32 slots;
+// first[blk] = its first brick (exclusive scan), bblk[brick] = its block,
+// meta[0] = number of bricks.
+constexpr int BRICK_SCAN_THREADS = 1024;
+__global__ void __launch_bounds__(BRICK_SCAN_THREADS)
+brick_scan_kernel(int nblk, const int32_t *__restrict__ cnt, int32_t *first, int32_t *bblk, int32_t *meta) {
+    __shared__ int s_part[BRICK_SCAN_THREADS / 32];
+    __shared__ int s_carry;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) s_carry = 0;
+    __syncthreads();
+    for (int i0 = 0; i0 < nblk; i0 += BRICK_SCAN_THREADS) {
+        const int i = i0 + tid;
+        const int v = i < nblk ? (cnt[i] + 31) / 32 : 0;
+        const int iv = warp_inclusive_scan(v, lane);
+        if (lane == 31) s_part[warp] = iv;
+        __syncthreads();
+        if (warp == 0) {
+            const int a = s_part[lane];
+            s_part[lane] = warp_inclusive_scan(a, lane) - a;
+        }
+        __syncthreads();
+        const int f = s_carry + s_part[warp] + iv - v;
+        if (i < nblk) {
+            first[i] = f;
+            for (int k = 0; k < v; ++k) bblk[f + k] = i;
+        }
+        __syncthreads();
+        if (tid == BRICK_SCAN_THREADS - 1) s_carry = f + v;
+        __syncthreads();
+    }
+    if (tid == 0) meta[0] = s_carry;
+}
+
+// Rows into the slots of their block's bricks, with copies of their screen
+// data (the order inside a block is immaterial: the screen sets bits at the
+// rows' table positions).
+__global__ void brick_fill_kernel(BrickGeom G, const int32_t *__restrict__ hkl, long long n,
+                                  const int32_t *__restrict__ first, int32_t *fill, const float4 *__restrict__ scr,
+                                  const float *__restrict__ zh, int32_t *bperm, float4 *bscr, float *bzh) {
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int blk = brick_block(G, hkl[3 * j], hkl[3 * j + 1], hkl[3 * j + 2]);
+    const long long slot = 32ll * first[blk] + atomicAdd(&fill[blk], 1);
+    bperm[slot] = (int32_t)j;
+    bscr[slot] = scr[j];
+    bzh[slot] = zh[j];
+}
+
+// One warp per brick: the empty slots filled (row -1, z_half -1: never
+// passes), the band [lo, hi] of the rows' z-intervals (the prep's FP32
+// values, as the row test uses them) and the block centre.
+__global__ void brick_bounds_kernel(BrickGeom G, const int32_t *__restrict__ bblk, const int32_t *__restrict__ first,
+                                    const int32_t *__restrict__ cnt, const int32_t *__restrict__ meta, int32_t *bperm,
+                                    float4 *bscr, float *bzh, float4 *brec, float *bhalf) {
+    const int lane = threadIdx.x & 31;
+    const long long b = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (b >= meta[0]) return;
+    const int blk = bblk[b];
+    const int in_brick = min(32, cnt[blk] - 32 * (int)(b - first[blk]));
+    const long long slot = 32 * b + lane;
+    float lo = INFINITY, hi = -INFINITY;
+    if (lane < in_brick) {
+        const float zm = -bscr[slot].w, w = bzh[slot];
+        lo = zm - w;
+        hi = zm + w;
+    } else {
+        bperm[slot] = -1;
+        bscr[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+        bzh[slot] = -1.f;
+    }
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(FULL_MASK, lo, d));
+        hi = fmaxf(hi, __shfl_xor_sync(FULL_MASK, hi, d));
+    }
+    if (lane == 0) {
+        const int bz = blk % G.nbz, by = (blk / G.nbz) % G.nby, bx = blk / (G.nbz * G.nby);
+        const float hc = (float)(bx * G.bh - G.hmax[0]) + 0.5f * (float)(G.bh - 1);
+        const float kc = (float)(by * G.bk - G.hmax[1]) + 0.5f * (float)(G.bk - 1);
+        const float lc = (float)(bz * G.bl - G.hmax[2]) + 0.5f * (float)(G.bl - 1);
+        brec[b] = make_float4(hc, kc, lc, -0.5f * (lo + hi));
+        bhalf[b] = 0.5f * (hi - lo) + G.rho_margin;
+    }
+}
+
+BrickGeom brick_geometry(const double recip[9], const int32_t hmax[3], int O, double reach) {
+    // cost per row and tile ~ (C0 + O C1 pass) / P for bricks of P rows, the
+    // pass rate ~ the share of a ball of radius R within rho + reach of a
+    // plane through its centre: 1.5 (rho + reach) / R
+    double len[3], R = 0.0;
+    for (int i = 0; i < 3; ++i) {
+        len[i] = sqrt(recip[3 * i] * recip[3 * i] + recip[3 * i + 1] * recip[3 * i + 1] +
+                      recip[3 * i + 2] * recip[3 * i + 2]);
+        R = fmax(R, len[i] * (double)(hmax[i] > 0 ? hmax[i] : 1));
+    }
+    const double C0 = 12.0, C1 = 11.0;
+    BrickGeom G{};
+    double best = 1e300, best_rho = 0.0;
+    for (int bh = 1; bh <= 8; ++bh)
+        for (int bk = 1; bk <= 8; ++bk)
+            for (int bl = 1; bl <= 8; ++bl) {
+                const int P = bh * bk * bl;
+                if (P > 32) continue;
+                double rho = 0.0;  // the largest corner of the block, |B*^T (d_h, d_k, d_l)|
+                for (int sh = -1; sh <= 1; sh += 2)
+                    for (int sk = -1; sk <= 1; sk += 2)
+                        for (int sl = -1; sl <= 1; sl += 2) {
+                            const double d[3] = {0.5 * sh * (bh - 1), 0.5 * sk * (bk - 1), 0.5 * sl * (bl - 1)};
+                            double v2 = 0.0;
+                            for (int x = 0; x < 3; ++x) {
+                                const double v = d[0] * recip[x] + d[1] * recip[3 + x] + d[2] * recip[6 + x];
+                                v2 += v * v;
+                            }
+                            rho = fmax(rho, sqrt(v2));
+                        }
+                const double pass = fmin(1.0, 1.5 * (rho + reach) / fmax(R, 1e-12));
+                const double cost = (C0 + (double)O * C1 * pass) / (double)P;
+                if (cost < best) {
+                    best = cost;
+                    best_rho = rho;
+                    G.bh = bh; G.bk = bk; G.bl = bl;
+                }
+            }
+    for (int i = 0; i < 3; ++i) G.hmax[i] = hmax[i] > 0 ? hmax[i] : 0;
+    G.nbx = (2 * G.hmax[0] + G.bh) / G.bh;
+    G.nby = (2 * G.hmax[1] + G.bk) / G.bk;
+    G.nbz = (2 * G.hmax[2] + G.bl) / G.bl;
+    // margin over the FP32 rounding of the brick and row tests (~1e-6 at
+    // |g| of a few 1/Angstrom) and of the band's ends
+    G.rho_margin = (float)(best_rho * (1.0 + 1e-5) + 1e-4);
+    return G;
+}
+
+static inline long long brick_blocks(const BrickGeom &G) { return (long long)G.nbx * G.nby * G.nbz; }
+// bricks at most: one per non-empty block plus one per 32 rows
+static inline long long brick_max(const BrickGeom &G, long long n_hkl) {
+    return std::min(brick_blocks(G), n_hkl) + n_hkl / 32 + 1;
+}
+
+size_t brick_scratch_bytes(const BrickGeom &G, long long n_hkl) {
+    const long long nblk = brick_blocks(G), nb = brick_max(G, n_hkl);
+    size_t o = 0;
+    o += align_up((size_t)nblk * 4, 256) * 2;        // counts, fill (zeroed)
+    o += align_up(16, 256);                          // meta (zeroed)
+    o += align_up((size_t)nblk * 4, 256);            // first brick of each block
+    o += align_up((size_t)nb * 4, 256);              // brick -> block
+    o += align_up((size_t)nb * 32 * 4, 256);         // slot rows
+    o += align_up((size_t)nb * 32 * sizeof(float4), 256);
+    o += align_up((size_t)nb * 32 * 4, 256);         // slot z_half
+    o += align_up((size_t)nb * sizeof(float4), 256);
+    o += align_up((size_t)nb * 4, 256);              // half widths
+    return o;
+}
+
+ds_status launch_brick_build(const BrickGeom &G, const int32_t *hkl, long long n_hkl, const float4 *scr,
+                             const float *zh, void *scratch, TableP &T, cudaStream_t s) {
+    const long long nblk = brick_blocks(G), nb = brick_max(G, n_hkl);
+    DS_REQUIRE(nblk > 0 && nblk < (1ll << 30) && nb < (1ll << 26), "brick screen: block grid out of range");
+    unsigned char *b = reinterpret_cast<unsigned char *>(scratch);
+    size_t o = 0;
+    int32_t *cnt = reinterpret_cast<int32_t *>(b + o); o += align_up((size_t)nblk * 4, 256);
+    int32_t *fill = reinterpret_cast<int32_t *>(b + o); o += align_up((size_t)nblk * 4, 256);
+    int32_t *meta = reinterpret_cast<int32_t *>(b + o); o += align_up(16, 256);
+    const size_t zero_bytes = o;
+    int32_t *first = reinterpret_cast<int32_t *>(b + o); o += align_up((size_t)nblk * 4, 256);
+    int32_t *bblk = reinterpret_cast<int32_t *>(b + o); o += align_up((size_t)nb * 4, 256);
+    int32_t *bperm = reinterpret_cast<int32_t *>(b + o); o += align_up((size_t)nb * 32 * 4, 256);
+    float4 *bscr = reinterpret_cast<float4 *>(b + o); o += align_up((size_t)nb * 32 * sizeof(float4), 256);
+    float *bzh = reinterpret_cast<float *>(b + o); o += align_up((size_t)nb * 32 * 4, 256);
+    float4 *brec = reinterpret_cast<float4 *>(b + o); o += align_up((size_t)nb * sizeof(float4), 256);
+    float *bhalf = reinterpret_cast<float *>(b + o);
+    DS_CUDA_TRY(cudaMemsetAsync(b, 0, zero_bytes, s));
+    if (n_hkl > 0) {
+        const unsigned g = (unsigned)((n_hkl + 255) / 256);
+        brick_count_kernel<<<g, 256, 0, s>>>(G, hkl, n_hkl, cnt);
+        ds_status st = check_launch("brick_count_kernel");
+        if (st) return st;
+        brick_scan_kernel<<<1, BRICK_SCAN_THREADS, 0, s>>>((int)nblk, cnt, first, bblk, meta);
+        st = check_launch("brick_scan_kernel");
+        if (st) return st;
+        brick_fill_kernel<<<g, 256, 0, s>>>(G, hkl, n_hkl, first, fill, scr, zh, bperm, bscr, bzh);
+        st = check_launch("brick_fill_kernel");
+        if (st) return st;
+        brick_bounds_kernel<<<(unsigned)((nb * 32 + 255) / 256), 256, 0, s>>>(G, bblk, first, cnt, meta, bperm, bscr,
+                                                                           bzh, brec, bhalf);
+        st = check_launch("brick_bounds_kernel");
+        if (st) return st;
+    }
+    T.bperm = bperm;
+    T.bscr = bscr;
+    T.bzh = bzh;
+    T.brec = brec;
+    T.bhalf = bhalf;
+    T.bmeta = meta;
+    return DS_OK;
+}
+
 constexpr long long STAGE_CAP = 24576;  // staged candidates per pipeline slot (20 bytes each)
 
 struct SimPlan {
     int O, W, Ws;
     long long n_tiles, grid, stage_cap;
-    int line_mode;
+    int line_mode, brick_mode;
     long long line_tiles;
-    size_t off_lb, off_scr, off_zh, off_g2, off_sidx, off_sI, off_lines, off_lmeta, off_llb, total;
+    BrickGeom bricks;
+    size_t off_lb, off_scr, off_zh, off_g2, off_sidx, off_sI, off_lines, off_lmeta, off_llb, off_bricks, total;
     size_t smem;
 };
+
+// Half-thickness of the selection band about the Ewald sphere (1/Angstrom),
+// for the brick shape's cost model: s_max, widened by how far the precessing
+// sphere strays at the table's largest |g|.
+double selection_reach(const ds_sim_params *p, const ds_phase_table *t) {
+    double reach = p->max_excitation_error;
+    if (p->precession_mode != DS_PRECESSION_NONE) {
+        double R = 0.0;
+        for (int i = 0; i < 3; ++i)
+            R = fmax(R, sqrt(t->recip[3 * i] * t->recip[3 * i] + t->recip[3 * i + 1] * t->recip[3 * i + 1] +
+                             t->recip[3 * i + 2] * t->recip[3 * i + 2]) * (double)t->hmax[i]);
+        reach += R * sin(p->precession_angle) + p->k0 * (1.0 - cos(p->precession_angle));
+    }
+    return reach;
+}
 
 static int pick_O(const ds_sim_params *p, long long n_hkl, long long n_orient) {
     long long W = (n_hkl + 31) / 32;
@@ -167,6 +391,7 @@ static ds_status make_plan(const ds_sim_params *p, const ds_phase_table *t, long
     // interval arithmetic costs about what the row tests do.
     P.line_mode = (p->form == DS_FORM_MIXED && p->precession_mode == DS_PRECESSION_NONE &&
                    p->screen == DS_SCREEN_LINES && t->n_hkl > 0) ? 1 : 0;
+    P.brick_mode = (p->form == DS_FORM_MIXED && !P.line_mode && t->n_hkl > 0 && p->screen == DS_SCREEN_BRICKS) ? 1 : 0;
     P.line_tiles = (t->n_hkl + LN_TILE - 1) / LN_TILE;
     P.O = pick_O(p, t->n_hkl, n_orient);
     if (p->form == DS_FORM_FP64 && P.O > 16) P.O = 16;
@@ -206,6 +431,12 @@ static ds_status make_plan(const ds_sim_params *p, const ds_phase_table *t, long
     o = align_up(o, 256);
     P.off_lmeta = o; o += 256;
     P.off_llb = o; o += P.line_mode ? lookback_scratch_bytes(P.line_tiles) : 0;
+    o = align_up(o, 256);
+    P.off_bricks = o;
+    if (P.brick_mode) {
+        P.bricks = brick_geometry(t->recip, t->hmax, P.O, selection_reach(p, t));
+        o += brick_scratch_bytes(P.bricks, t->n_hkl);
+    }
     P.total = align_up(o, 256);
     return DS_OK;
 }
@@ -228,6 +459,22 @@ static ds_status launch_sim(const void *kern, SimConst c, TableP T, const double
     return check_launch("simulate_kernel");
 }
 
+// Scratch of ds_simulate for one problem, with make_plan's own status and
+// message on failure: the bytes at the staging capacity of p (or the
+// default), the staging capacity the plan uses, and the bytes one more unit
+// of staging capacity adds (two slots of (row, I) per CTA).
+ds_status simulate_scratch_plan(const ds_sim_params *p, const ds_phase_table *t, long long n_orient,
+                                size_t *total, long long *stage_cap, size_t *per_stage) {
+    DS_REQUIRE(p && t && total && stage_cap && per_stage, "simulate_scratch_plan: null pointer");
+    SimPlan P;
+    ds_status st = make_plan(p, t, n_orient, P);
+    if (st) return st;
+    *total = P.total;
+    *stage_cap = P.stage_cap;
+    *per_stage = (size_t)(2 * P.grid) * (sizeof(int32_t) + sizeof(float));
+    return DS_OK;
+}
+
 }  // namespace ds
 
 using namespace ds;
@@ -243,6 +490,7 @@ extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t
                                  int64_t n_orient, ds_spots *out, void *scratch, size_t scratch_bytes,
                                  int32_t *status, void *stream) {
     clear_error();
+    DS_NVTX_RANGE("ds_simulate");
     DS_REQUIRE(p && t && out && status, "ds_simulate: null pointer");
     DS_REQUIRE(n_orient >= 0, "ds_simulate: n_orient < 0");
     DS_REQUIRE(t->n_hkl >= 0 && t->n_hkl < (1ll << 31), "ds_simulate: n_hkl out of range");
@@ -293,6 +541,14 @@ extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t
     }
     T.lines = reinterpret_cast<const LineP *>(sb + P.off_lines);
     T.line_meta = reinterpret_cast<const int *>(sb + P.off_lmeta);
+    T.bperm = T.bmeta = nullptr;
+    T.bscr = T.brec = nullptr;
+    T.bzh = T.bhalf = nullptr;
+    c.brick_mode = P.brick_mode;
+    if (P.brick_mode) {
+        ds_status st = launch_brick_build(P.bricks, t->hkl, t->n_hkl, T.scr, T.zh, sb + P.off_bricks, T, s);
+        if (st) return st;
+    }
     if (P.line_mode) {
         DS_CUDA_TRY(cudaMemsetAsync(sb + P.off_lmeta, 0x7f, 256, s));  // [1] = no 000 row yet (0x7f7f7f7f)
         DS_CUDA_TRY(cudaMemsetAsync(sb + P.off_llb, 0, lookback_scratch_bytes(P.line_tiles), s));

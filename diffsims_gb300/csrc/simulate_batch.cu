@@ -36,11 +36,13 @@ static inline size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 constexpr long long BATCH_STAGE_CAP = 24576;
 
 struct BatchPlan {
-    int O, Ws_max, grid;
+    int O, Ws_max, grid, brick_mode;
     int Op[SIM_BATCH_MAX];
     long long n_tiles, n_orient, stage_cap;
     size_t smem, off_lb, off_sidx, off_sI, total;
-    size_t off_prep[SIM_BATCH_MAX];  // per phase: scr, zh, g2dd
+    size_t off_prep[SIM_BATCH_MAX];    // per phase: scr, zh, g2dd
+    size_t off_bricks[SIM_BATCH_MAX];  // per phase: the brick screen's arrays
+    BrickGeom bricks[SIM_BATCH_MAX];
 };
 
 static ds_status batch_plan(const ds_sim_params *p, const ds_batch_phase *ph, int n, BatchPlan &P) {
@@ -94,6 +96,15 @@ static ds_status batch_plan(const ds_sim_params *p, const ds_batch_phase *ph, in
         const size_t nh = (size_t)ph[i].table.n_hkl;
         o += align256(nh * sizeof(float4)) + align256(nh * sizeof(float)) + align256(nh * sizeof(float2));
     }
+    P.brick_mode = (p->form == DS_FORM_MIXED && p->screen == DS_SCREEN_BRICKS) ? 1 : 0;
+    for (int i = 0; i < n; ++i) {
+        o = align256(o);
+        P.off_bricks[i] = o;
+        if (P.brick_mode && ph[i].table.n_hkl > 0) {
+            P.bricks[i] = brick_geometry(ph[i].table.recip, ph[i].table.hmax, P.Op[i], selection_reach(p, &ph[i].table));
+            o += brick_scratch_bytes(P.bricks[i], ph[i].table.n_hkl);
+        }
+    }
     o = align256(o);
     P.off_sidx = o; o += (size_t)(2 * P.grid * P.stage_cap) * sizeof(int32_t);
     o = align256(o);
@@ -127,6 +138,7 @@ extern "C" ds_status ds_simulate_batch(const ds_sim_params *p, const ds_batch_ph
                                        ds_spots *out, void *scratch, size_t scratch_bytes, int32_t *status,
                                        void *stream) {
     clear_error();
+    DS_NVTX_RANGE("ds_simulate_batch");
     DS_REQUIRE(p && phases && out && status, "ds_simulate_batch: null pointer");
     {
         ds_status vs = validate_params(p, "ds_simulate_batch");
@@ -159,6 +171,7 @@ extern "C" ds_status ds_simulate_batch(const ds_sim_params *p, const ds_batch_ph
     c.n_tiles = P.n_tiles;
     c.capacity = out->capacity;
     c.line_mode = 0;
+    c.brick_mode = P.brick_mode;
 
     PhaseBatch B;
     B.n = n_phases;
@@ -183,6 +196,9 @@ extern "C" ds_status ds_simulate_batch(const ds_sim_params *p, const ds_batch_ph
         d.T.F2d = t->F2d;
         d.T.lines = nullptr;
         d.T.line_meta = nullptr;
+        d.T.bperm = d.T.bmeta = nullptr;
+        d.T.bscr = d.T.brec = nullptr;
+        d.T.bzh = d.T.bhalf = nullptr;
         d.quats = phases[i].quats;
         for (int k = 0; k < 9; ++k) d.recip[k] = cp.recip[k];
         for (int k = 0; k < 3; ++k) d.hmax[k] = cp.hmax[k];
@@ -198,6 +214,10 @@ extern "C" ds_status ds_simulate_batch(const ds_sim_params *p, const ds_batch_ph
         orient0 += no;
         st = launch_sim_prep(cp, t->hkl, t->g2, scr, zh, g2dd, nh, s);
         if (st) return st;
+        if (P.brick_mode && nh > 0) {
+            st = launch_brick_build(P.bricks[i], t->hkl, nh, scr, zh, sb + P.off_bricks[i], d.T, s);
+            if (st) return st;
+        }
     }
     DS_CUDA_TRY(cudaMemsetAsync(sb + P.off_lb, 0, lookback_scratch_bytes(P.n_tiles), s));
     LookbackScratch lb = lookback_scratch(sb + P.off_lb);

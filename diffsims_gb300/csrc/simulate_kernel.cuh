@@ -63,6 +63,7 @@ struct SimConst {
     int W, Ws;
     int hmax[3];
     int line_mode;                  // phase 1 by per-(orientation, line) intervals
+    int brick_mode;                 // phase 1 by bricks (then rows of passing bricks)
     double alpha0, alpha1, beta0, beta1, csq;  // z_a = alpha0 + alpha1 g^2, z_b = beta0 + beta1 g^2, |c*|^2
     float a2f, b2f;                 // -alpha1 |c*|^2, -beta1 |c*|^2
     float inv_a2f, inv_b2f;
@@ -352,7 +353,41 @@ struct TableP {
     const double *F2d;
     const LineP *lines;   // line screen: per-line constants
     const int *line_meta; // [0] lines, [1] first trailing 000 row
+    // brick screen: brick b holds up to 32 rows in slots [32 b, 32 b + 32):
+    // their table rows bperm (-1: an empty slot), screen data bscr and bzh
+    // (copies of scr and zh); brec[b] = (h, k, l of its block's centre,
+    // -middle of its rows' z band), bhalf[b] = half width of that band plus
+    // the block's radius; bmeta[0] = number of bricks
+    const int32_t *bperm;
+    const float4 *bscr;
+    const float *bzh;
+    const float4 *brec;
+    const float *bhalf;
+    const int32_t *bmeta;
 };
+
+// ------------------------------------------------------------- bricks ----
+// The rows grouped into blocks of bh x bk x bl consecutive (h, k, l) of the
+// table's index box.  A block's rows lie within rho (its corner radius,
+// 1/Angstrom) of its centre g_c, and every row's z-interval [z_mid - z_half,
+// z_mid + z_half] lies in the block's band [lo, hi]; with z = n . g and |n| =
+// 1, a row can pass the per-row test only if |n . g_c - (lo + hi)/2| <
+// (hi - lo)/2 + rho.  That test, widened by a rounding margin, is the brick
+// test: rows of bricks that fail it are not tested.
+struct BrickGeom {
+    int bh, bk, bl;      // block edge in h, k, l
+    int nbx, nby, nbz;   // blocks along h, k, l
+    int hmax[3];
+    float rho_margin;    // corner radius + rounding margin (1/Angstrom)
+};
+__host__ __device__ __forceinline__ int brick_block(const BrickGeom &G, int h, int k, int l) {
+    // rows are within the box |h| <= hmax (the table's contract); clamped so
+    // that a table breaking it cannot index outside the block arrays
+    const int bx = min(max((h + G.hmax[0]) / G.bh, 0), G.nbx - 1);
+    const int by = min(max((k + G.hmax[1]) / G.bk, 0), G.nby - 1);
+    const int bz = min(max((l + G.hmax[2]) / G.bl, 0), G.nbz - 1);
+    return (bx * G.nby + by) * G.nbz + bz;
+}
 
 // One candidate's table data, loaded ahead of its evaluation.
 struct SpotIn {
@@ -809,6 +844,62 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
                     const int o = i / n_zero;
                     const long long j = zero_start + i % n_zero;
                     atomicOr(&bitmap[o * Ws + (int)(j >> 5)], 1u << (int)(j & 31));
+                }
+            } else if (FORM == DS_FORM_MIXED && c.brick_mode) {
+                // bricks: one test per (brick, orientation) with the lanes over
+                // the tile's orientations; the brick's rows (lanes) are then
+                // tested, exactly as the row screen tests them, for each
+                // orientation the brick passes, and their bits or-ed into a
+                // zeroed bitmap (the phase's OP rows) at their table positions.
+                // A warp's bricks are b = warp + 8 i; the header and rows of the
+                // next two are in flight while one is screened.
+                uint4 *bm4 = reinterpret_cast<uint4 *>(bitmap);
+                for (int i = tid; i < (OP * Ws + 3) / 4; i += SIM_THREADS) bm4[i] = make_uint4(0u, 0u, 0u, 0u);
+                float b0 = 0.f, b1 = 0.f, b2 = 0.f;
+                if (lane < n_valid) {
+                    const float4 m4 = sop[lane].mz;
+                    b0 = m4.x; b1 = m4.y; b2 = m4.z;
+                }
+                __syncthreads();
+                const int nb = n_hkl > 0 ? T.bmeta[0] : 0;  // a phase without rows has no bricks
+                struct BrickIn {
+                    float4 h, e;
+                    float hw, zh;
+                    int j;
+                };
+                auto load_brick = [&](int b) {
+                    BrickIn in;
+                    in.h = make_float4(0.f, 0.f, 0.f, 0.f);
+                    in.e = in.h;
+                    in.hw = -1.f;
+                    in.zh = -1.f;
+                    in.j = -1;
+                    if (b < nb) {
+                        const long long slot = 32ll * b + lane;
+                        in.h = T.brec[b];
+                        in.hw = T.bhalf[b];
+                        in.j = T.bperm[slot];
+                        in.e = T.bscr[slot];
+                        in.zh = T.bzh[slot];
+                    }
+                    return in;
+                };
+                BrickIn n0 = load_brick(warp), n1 = load_brick(warp + SIM_WARPS);
+                for (int b = warp; b < nb; b += SIM_WARPS) {
+                    const BrickIn cur = n0;
+                    n0 = n1;
+                    n1 = load_brick(b + 2 * SIM_WARPS);
+                    const float zb = fmaf(b0, cur.h.x, fmaf(b1, cur.h.y, fmaf(b2, cur.h.z, cur.h.w)));
+                    unsigned todo = __ballot_sync(FULL_MASK, lane < n_valid && fabsf(zb) < cur.hw);
+                    while (todo) {
+                        const int o = __ffs(todo) - 1;
+                        todo &= todo - 1u;
+                        const float4 m4 = sop[o].mz;
+                        const float z = fmaf(m4.x, cur.e.x, fmaf(m4.y, cur.e.y, fmaf(m4.z, cur.e.z, cur.e.w)));
+                        // the row screen's test: the sign of |z| - z_half
+                        if (cur.j >= 0 && (__float_as_uint(fabsf(z) - cur.zh) >> 31))
+                            atomicOr(&bitmap[o * Ws + (cur.j >> 5)], 1u << (cur.j & 31));
+                    }
                 }
             } else if (FORM == DS_FORM_FP64) {
                 for (int wc = warp; wc < W; wc += SIM_WARPS) {
@@ -1337,6 +1428,7 @@ inline void fill_const(const ds_sim_params *p, const ds_phase_table *t, SimConst
     c.Ws = c.W | 1;
     c.n_orient = 0;
     c.line_mode = 0;
+    c.brick_mode = 0;
     c.n_tiles = 0;
     c.capacity = 0;
 }
@@ -1344,6 +1436,18 @@ inline void fill_const(const ds_sim_params *p, const ds_phase_table *t, SimConst
 // sim_prep_kernel launcher (simulate.cu): the screen arrays of one table.
 ds_status launch_sim_prep(const SimConst &c, const int32_t *hkl, const double *g2, float4 *scr, float *zh, float2 *g2dd,
                           long long n_hkl, cudaStream_t s);
+
+// Brick screen (simulate.cu).  brick_geometry picks the block shape for a
+// table (recip rows a*, b*, c*; hmax) and a tile of O orientations, whose
+// selection band reaches `reach` (1/Angstrom) off the Ewald sphere;
+// brick_scratch_bytes is the scratch the bricks of n rows take;
+// launch_brick_build fills the brick arrays of T from the table rows and the
+// prep's screen arrays (after launch_sim_prep, on the same stream).
+BrickGeom brick_geometry(const double recip[9], const int32_t hmax[3], int O, double reach);
+double selection_reach(const ds_sim_params *p, const ds_phase_table *t);
+size_t brick_scratch_bytes(const BrickGeom &G, long long n_hkl);
+ds_status launch_brick_build(const BrickGeom &G, const int32_t *hkl, long long n_hkl, const float4 *scr,
+                             const float *zh, void *scratch, TableP &T, cudaStream_t s);
 
 // ------------------------------------------------------------- host side ----
 

@@ -33,6 +33,7 @@ struct SfConst {
     int n_atoms, n_species, kind, has_hkl_i;
     int g_is_spacing;  // g2 holds |g| (square it) -- the get_kinematical_intensities entry
     int _pad;
+    long long mbar_limit;  // polls of the staging wait before it gives up
 };
 
 struct SfSmem {
@@ -105,7 +106,8 @@ __device__ inline void sf_prologue(const SfConst &c, const ds_atoms &A, unsigned
 // Copy atoms [start, start+cnt) into shared memory with one TMA bulk copy;
 // every thread waits on the barrier (bounded).  Returns false on timeout.
 __device__ inline bool sf_stage_chunk(const ds_atoms &A, unsigned char *smem, const SfSmem &L, int start,
-                                      int cnt, uint32_t &parity, int32_t *status, bool want_float) {
+                                      int cnt, uint32_t &parity, int32_t *status, bool want_float,
+                                      long long limit) {
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L.bar);
     ds_atom *sa = reinterpret_cast<ds_atom *>(smem + L.atoms);
     if (threadIdx.x == 0) {
@@ -113,7 +115,7 @@ __device__ inline bool sf_stage_chunk(const ds_atoms &A, unsigned char *smem, co
         mbar_arrive_expect_tx(bar, bytes);
         tma_bulk_g2s(sa, A.atoms + start, bytes, bar);
     }
-    bool ok = mbar_wait_bounded(bar, parity, status);
+    bool ok = mbar_wait_bounded(bar, parity, status, limit);
     parity ^= 1u;
     if (want_float) {
         float *occf = reinterpret_cast<float *>(smem + L.occf);
@@ -164,7 +166,7 @@ sf_mixed_kernel(SfConst c, ds_atoms A, const int32_t *__restrict__ hkl_i, const 
     uint32_t parity = 0;
     for (int start = 0; start < c.n_atoms; start += chunk_cap) {
         int cnt = min(chunk_cap, c.n_atoms - start);
-        if (!sf_stage_chunk(A, smem, Ls, start, cnt, parity, status, true)) return;
+        if (!sf_stage_chunk(A, smem, Ls, start, cnt, parity, status, true, c.mbar_limit)) return;
         if (active) {
             for (int i = sub; i < cnt; i += L) {
                 const ds_atom &a = sa[i];
@@ -247,7 +249,7 @@ sf_fp64_kernel(SfConst c, ds_atoms A, const int32_t *__restrict__ hkl_i, const d
         int sp_prev = -1;
         for (int start = 0; start < c.n_atoms; start += chunk_cap) {
             int cnt = min(chunk_cap, c.n_atoms - start);
-            if (!sf_stage_chunk(A, smem, Ls, start, cnt, parity, status, false)) return;
+            if (!sf_stage_chunk(A, smem, Ls, start, cnt, parity, status, false, c.mbar_limit)) return;
             if (active) {
                 for (int i = sub; i < cnt; i += L) {
                     const ds_atom &a = sa[i];
@@ -350,6 +352,7 @@ extern "C" ds_status ds_structure_factors(const ds_atoms *atoms, const int32_t *
                                           double *F, void *scratch, size_t scratch_bytes, int32_t *status,
                                           void *stream) {
     clear_error();
+    DS_NVTX_RANGE("ds_structure_factors");
     ds_status st = validate_atoms(atoms);
     if (st) return st;
     DS_REQUIRE((hkl_i != nullptr) != (hkl_d != nullptr), "ds_structure_factors: give exactly one of hkl_i, hkl_d");
@@ -358,7 +361,7 @@ extern "C" ds_status ds_structure_factors(const ds_atoms *atoms, const int32_t *
     DS_REQUIRE(form == DS_FORM_MIXED || form == DS_FORM_FP64, "ds_structure_factors: bad form");
     if (n == 0) return DS_OK;
     cudaStream_t s = (cudaStream_t)stream;
-    SfConst c{n, atoms->n_atoms, atoms->n_species, atoms->kind, hkl_i != nullptr, 0, 0};
+    SfConst c{n, atoms->n_atoms, atoms->n_species, atoms->kind, hkl_i != nullptr, 0, 0, wait_limit_mbarrier()};
     if (form == DS_FORM_FP64)
         return launch_fp64(c, *atoms, hkl_i, hkl_d, g2, nullptr, F2, F2d, F, nullptr, nullptr, n, status, s);
     DS_REQUIRE(scratch && scratch_bytes >= ds_structure_factor_scratch_bytes(n, atoms->n_atoms),
@@ -381,6 +384,7 @@ extern "C" ds_status ds_family_structure_factors(const ds_atoms *atoms, const do
                                                  const double *scattering_parameter, int64_t n, double *F,
                                                  int32_t *status, void *stream) {
     clear_error();
+    DS_NVTX_RANGE("ds_family_structure_factors");
     DS_REQUIRE(atoms && atoms->atoms && atoms->coeffs, "ds_family_structure_factors: null atoms");
     DS_REQUIRE(atoms->n_atoms >= 1, "ds_family_structure_factors: n_atoms must be >= 1");
     DS_REQUIRE(atoms->n_species >= 1 && atoms->n_species <= SF_MAX_SPECIES,
@@ -392,7 +396,7 @@ extern "C" ds_status ds_family_structure_factors(const ds_atoms *atoms, const do
     if (n == 0) return DS_OK;
     DS_REQUIRE(hkl_d && scattering_parameter && F && status, "ds_family_structure_factors: null pointer");
     // g_is_spacing squares the per-reflection input: the kernel sees s^2
-    SfConst c{n, atoms->n_atoms, atoms->n_species, atoms->kind, 0, 1, 0};
+    SfConst c{n, atoms->n_atoms, atoms->n_species, atoms->kind, 0, 1, 0, wait_limit_mbarrier()};
     return launch_fp64(c, *atoms, nullptr, hkl_d, scattering_parameter, nullptr, nullptr, nullptr, F, nullptr,
                        nullptr, n, status, (cudaStream_t)stream);
 }
@@ -401,12 +405,13 @@ extern "C" ds_status ds_kinematical_intensities(const ds_atoms *atoms, const dou
                                                 const double *prefactor, int64_t n, double *out, void * /*scratch*/,
                                                 size_t /*scratch_bytes*/, int32_t *status, void *stream) {
     clear_error();
+    DS_NVTX_RANGE("ds_kinematical_intensities");
     ds_status st = validate_atoms(atoms);
     if (st) return st;
     DS_REQUIRE(hkl_d && g_spacing && out && status, "ds_kinematical_intensities: null pointer");
     DS_REQUIRE(n >= 0, "ds_kinematical_intensities: n < 0");
     if (n == 0) return DS_OK;
-    SfConst c{n, atoms->n_atoms, atoms->n_species, atoms->kind, 0, 1, 0};
+    SfConst c{n, atoms->n_atoms, atoms->n_species, atoms->kind, 0, 1, 0, wait_limit_mbarrier()};
     return launch_fp64(c, *atoms, nullptr, hkl_d, g_spacing, prefactor, nullptr, out, nullptr, nullptr, nullptr, n,
                        status, (cudaStream_t)stream);
 }

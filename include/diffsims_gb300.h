@@ -48,10 +48,14 @@ enum { DS_SCATTER_LOBATO = 0, DS_SCATTER_XTABLES = 1, DS_SCATTER_NONE = 2,
 enum { DS_SHAPE_LINEAR = 0, DS_SHAPE_ATANC = 1, DS_SHAPE_SINC = 2, DS_SHAPE_SIN2C = 3,
        DS_SHAPE_LORENTZIAN = 4, DS_SHAPE_BINARY = 5 };
 
-/* candidate screen of ds_simulate: per-(orientation, hkl line) intervals or a
- * test per (orientation, row); both keep a superset of the selected spots,
- * the exact selection follows, so the results are identical */
-enum { DS_SCREEN_AUTO = 0, DS_SCREEN_ROWS = 1, DS_SCREEN_LINES = 2 };
+/* candidate screen of ds_simulate: a test per (orientation, row); per-
+ * (orientation, hkl line) intervals; or bricks -- the rows grouped into
+ * compact blocks of hkl, each block tested once per orientation and its rows
+ * only where the block passes (the same per-row test, so the same rows are
+ * kept).  All keep a superset of the selected spots and the exact selection
+ * follows, so the results are identical.  AUTO: rows (the fastest measured
+ * on the large single-phase workload). */
+enum { DS_SCREEN_AUTO = 0, DS_SCREEN_ROWS = 1, DS_SCREEN_LINES = 2, DS_SCREEN_BRICKS = 3 };
 
 /* precession handling (diffsims/generators/simulation_generator.py:363-411) */
 enum { DS_PRECESSION_NONE = 0,
@@ -238,9 +242,12 @@ ds_status ds_simulate_batch(const ds_sim_params *p, const ds_batch_phase *phases
  * library instead of a caller buffer; inputs and outputs are still the
  * caller's.  Sizes whose scratch does not fit (after shrinking the candidate
  * staging) return DS_ERR_INVALID_ARGUMENT.  All calls share the array: calls
- * that overlap on the GPU race (one stream is safe).  The first call on a
- * device looks the array up (cudaGetSymbolAddress): make it before any stream
- * capture.  Allocates nothing. */
+ * that overlap on the GPU race (one stream is safe).  Every call looks the
+ * array's address up (cudaGetSymbolAddress, the caller's device current), so
+ * a device reset between calls is safe; the first call on a device loads the
+ * library's device code: make it before any stream capture.  A problem the
+ * library cannot plan returns the plan's own status and message.  Allocates
+ * nothing. */
 ds_status ds_simulate_noalloc(const ds_sim_params *p, const ds_phase_table *t, const double *quats,
                               int64_t n_orient, ds_spots *out, int32_t *status, void *stream);
 
@@ -336,6 +343,24 @@ ds_status ds_structure_factors_backward(const ds_atoms *atoms, const int32_t *hk
  * blocks*256 floats.  FLOPs = blocks * 256 * iters * 256.  Used to measure the
  * FP32 roofline denominator. */
 ds_status ds_probe_fp32_fma(int64_t iters, int32_t blocks, float *out, void *stream);
+
+/* Bounded device waits (no counterpart in the reference, which has no device
+ * code on this path).  Every spin of the kernels gives up after a number of
+ * polls, sets DS_ERR_TIMEOUT in the status word and returns: the decoupled
+ * look-back's wait for an earlier tile (default 2^24 polls with backoff) and
+ * the structure-factor kernels' wait for a staging copy (default 2^22 polls;
+ * after a timeout they still wait, bounded, for their own copy to land).
+ * ds_set_wait_limits sets both first-wait limits for launches set up
+ * afterwards, process-wide; values <= 0 restore the defaults. */
+ds_status ds_set_wait_limits(int64_t lookback_polls, int64_t mbarrier_polls);
+
+/* Runs the two kinds of bounded wait on flags nothing ever sets (a look-back
+ * predecessor that never publishes; an mbarrier nobody arrives on, with no
+ * copy issued), each limited to `polls` (1..2^20): both give up, DS_ERR_TIMEOUT
+ * is set in *status, and out[0] = -1 (look-back prefix), out[1] = 0 (barrier
+ * not completed).  scratch: >= 272 bytes (cleared here). */
+ds_status ds_probe_wait_timeout(int64_t polls, void *scratch, size_t scratch_bytes, int64_t *out,
+                                int32_t *status, void *stream);
 
 /* Last host-side error message of the calling thread ("" if none). */
 const char *ds_last_error(void);

@@ -154,3 +154,27 @@ def test_calculate_diffraction2d_phases_in_one_launch():
         for a, b in zip(multi.coordinates[k], one.coordinates):
             assert np.array_equal(a.data, b.data) and np.array_equal(a.intensity, b.intensity)
             assert np.array_equal(a.hkl, b.hkl)
+
+
+@pytest.mark.parametrize("tile", [4, 16, 32])
+def test_batch_brick_screen_matches_row_screen(tile):
+    """The batched launch with every phase on the brick screen (its own
+    bricks per phase) against the row screen, bit for bit, including a phase
+    whose candidate table is empty."""
+    import torch
+    from diffsims_gb300.engine import PhaseBatch, PhaseTable
+    dev = torch.device("cuda", 0)
+    p = ok.SimParams(accelerating_voltage=200, reciprocal_radius=1.2, max_excitation_error=0.015,
+                     shape_factor_model="sinc")
+    tables, qs = _phase_set(torch, dev, p, SPECS)
+    empty = random_cell(7, 3, edges=(3, 4))
+    tables.append(PhaseTable(pu.to_phase(empty), 0.05, False, "lobato", list(empty.B), device=dev))
+    qs.append(torch.as_tensor(ok.random_quaternions(25, seed=8)).to(dev))
+    assert tables[-1].n == 0
+    out = {}
+    for screen in ("rows", "bricks"):
+        settings = pu.generator_for(p).settings(p.max_excitation_error)
+        settings.screen = screen
+        out[screen] = PhaseBatch(tables, qs, settings, p.reciprocal_radius, orient_tile=tile).run().spots()
+    for a, b in zip(out["rows"], out["bricks"]):
+        _same(a, b)

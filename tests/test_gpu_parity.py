@@ -333,9 +333,9 @@ def test_staging_fallback_agrees(stage_cap):
     ("p1", random_p1(30, 17), 1.5, 0.02), ("al", al_fcc(), 1.0, 0.01), ("long_c", random_p1(8, 19, edges=(4, 20)), 1.8, 0.02),
     ("graphite", graphite(), 1.6768, 0.1), ("si_big", si_crystal(), 3.0, 0.01)])
 def test_line_screen_matches_row_screen(name, crystal, r, eps):
-    """The per-(orientation, hkl line) interval screen and the per-row screen
-    keep different supersets; after the exact selection the spots agree bit
-    for bit."""
+    """The per-(orientation, hkl line) interval screen, the brick screen and
+    the per-row screen keep different supersets (bricks: the same rows);
+    after the exact selection the spots agree bit for bit."""
     import torch
     from diffsims_gb300.engine import PhaseTable, SpotBuffers, simulate_phase
     dev = torch.device("cuda", 0)
@@ -346,16 +346,51 @@ def test_line_screen_matches_row_screen(name, crystal, r, eps):
     table = PhaseTable(pu.to_phase(crystal), r, True, "lobato", list(crystal.B), device=dev)
     qd = torch.as_tensor(q).to(dev)
     res = {}
-    for screen in ("rows", "lines"):
+    for screen in ("rows", "lines", "bricks"):
         st = gen.settings(eps)
         st.screen = screen
         res[screen] = simulate_phase(table, qd, st, r, SpotBuffers(dev, with_excitation_error=True))
-    a, b = res["rows"], res["lines"]
-    assert a.total == b.total
+    a = res["rows"]
+    for other in ("lines", "bricks"):
+        b = res[other]
+        assert a.total == b.total, other
+        assert np.array_equal(a.offsets.cpu().numpy(), b.offsets.cpu().numpy()), other
+        assert np.array_equal(a.hkl_index.cpu().numpy(), b.hkl_index.cpu().numpy()), other
+        assert np.array_equal(a.xyzi.cpu().numpy(), b.xyzi.cpu().numpy()), other
+        assert np.array_equal(a.excitation_error.cpu().numpy(), b.excitation_error.cpu().numpy()), other
+    pu.compare(res["bricks"], crystal, q, p)
+
+
+@pytest.mark.parametrize("kw", [dict(precession_angle=0.5), dict(precession_angle=1.0, approximate_precession=False,
+                                                                 shape_factor_model="sinc"),
+                                dict(shape_factor_model="sinc", with_direct_beam=False)])
+@pytest.mark.parametrize("tile", [0, 4, 32])
+def test_brick_screen_matches_row_screen(kw, tile):
+    """Bricks against rows with precession (the widened band), without the
+    direct beam, and for several orientation tiles: bit for bit."""
+    import torch
+    from diffsims_gb300.engine import PhaseTable, SpotBuffers, simulate_phase
+    dev = torch.device("cuda", 0)
+    crystal = random_p1(60, 23)
+    base = dict(accelerating_voltage=200, shape_factor_model="lorentzian", reciprocal_radius=1.6,
+                max_excitation_error=0.015)
+    base.update(kw)
+    p = ok.SimParams(**base)
+    gen = pu.generator_for(p)
+    table = PhaseTable(pu.to_phase(crystal), p.reciprocal_radius, p.with_direct_beam, "lobato", list(crystal.B),
+                       device=dev)
+    q = ok.random_quaternions(700, seed=12)
+    qd = torch.as_tensor(q).to(dev)
+    res = {}
+    for screen in ("rows", "bricks"):
+        st = gen.settings(p.max_excitation_error, orient_tile=tile)
+        st.screen = screen
+        res[screen] = simulate_phase(table, qd, st, p.reciprocal_radius, SpotBuffers(dev))
+    a, b = res["rows"], res["bricks"]
+    assert a.total == b.total and a.total > 1000
     assert np.array_equal(a.offsets.cpu().numpy(), b.offsets.cpu().numpy())
     assert np.array_equal(a.hkl_index.cpu().numpy(), b.hkl_index.cpu().numpy())
     assert np.array_equal(a.xyzi.cpu().numpy(), b.xyzi.cpu().numpy())
-    pu.compare(b, crystal, q, p)
 
 
 def test_capacity_overflow_is_retried():
@@ -373,7 +408,7 @@ def test_capacity_overflow_is_retried():
     pu.compare(spots, crystal, q, p)
 
 
-@pytest.mark.parametrize("screen", ["lines", "rows"])
+@pytest.mark.parametrize("screen", ["lines", "rows", "bricks"])
 def test_empty_table_and_no_direct_beam(screen):
     """A radius below the first reflection and no direct beam: an empty
     candidate table, empty patterns; and small tables without 000 rows."""

@@ -247,3 +247,18 @@ def test_autotuner_disk_cache(tmp_path, monkeypatch):
     assert b.lookup("GB300", (1, 2, 3, "linear", 2, "fp64")) == (8, 3072)
     path.write_text("not json")
     assert Autotuner(path=str(path)).lookup("GB300", k) is None  # a damaged file is ignored
+
+
+def test_wait_limit_entries_reject_bad_arguments(lib):
+    """ds_probe_wait_timeout validates its arguments before any CUDA call;
+    ds_set_wait_limits accepts any value (<= 0 restores the defaults)."""
+    from diffsims_gb300 import _native as N
+    fake = ctypes.c_void_p(4096)
+    assert lib.ds_probe_wait_timeout(0, fake, 512, fake, fake, None) == N.DS_ERR_INVALID_ARGUMENT
+    assert "polls" in lib.ds_last_error().decode()
+    assert lib.ds_probe_wait_timeout(1 << 21, fake, 512, fake, fake, None) == N.DS_ERR_INVALID_ARGUMENT
+    assert lib.ds_probe_wait_timeout(100, fake, 16, fake, fake, None) == N.DS_ERR_INVALID_ARGUMENT
+    assert "scratch" in lib.ds_last_error().decode()
+    assert lib.ds_probe_wait_timeout(100, None, 512, fake, fake, None) == N.DS_ERR_INVALID_ARGUMENT
+    assert lib.ds_set_wait_limits(5, 7) == N.DS_OK
+    assert lib.ds_set_wait_limits(0, -1) == N.DS_OK

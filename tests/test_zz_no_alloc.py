@@ -92,3 +92,22 @@ def test_noalloc_rejects_oversized_problem(lib):
                                  N.stream_handle())
     assert rc == N.DS_ERR_INVALID_ARGUMENT
     assert "static scratch" in lib.ds_last_error().decode()
+
+
+def test_noalloc_reports_the_plans_own_error(lib):
+    """A candidate table too large for one orientation tile: the entry point
+    returns the launch plan's own status and message (not a generic one).
+    The table's arrays are null, so nothing could launch even if planning
+    passed (ds_simulate rejects missing arrays before any launch)."""
+    import torch
+    from diffsims_gb300 import _native as N
+    dev = torch.device("cuda", 0)
+    p = ok.SimParams(accelerating_voltage=200, reciprocal_radius=1.0)
+    settings = pu.generator_for(p).settings(0.01)
+    t = N.ds_phase_table()
+    t.n_hkl = 1 << 30
+    out = N.ds_spots(None, None, None, 0, None, None)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    rc = lib.ds_simulate_noalloc(settings.cstruct(), t, None, 1000, out, status.data_ptr(), N.stream_handle())
+    assert rc == N.DS_ERR_INVALID_ARGUMENT
+    assert "too large for one orientation tile" in lib.ds_last_error().decode()
