@@ -19,52 +19,47 @@ import numpy as np
 
 class StructureLibrary:
     """Phase identifiers -> (structure, list of Euler triples in degrees,
-    rotating z-x-z)."""
+    rotating z-x-z); ``struct_lib`` maps each identifier to that pair."""
 
     def __init__(self, identifiers, structures, orientations):
-        if len(identifiers) != len(structures):
-            raise ValueError("Number of identifiers ({}) and structures ({}) must be the same.".format(
-                len(identifiers), len(structures)))
-        if len(identifiers) != len(orientations):
-            raise ValueError("Number of identifiers ({}) and orientations ({}) must be the same.".format(
-                len(identifiers), len(orientations)))
+        for what, seq in (("structures", structures), ("orientations", orientations)):
+            if len(seq) != len(identifiers):
+                raise ValueError(f"Number of identifiers ({len(identifiers)}) and {what} ({len(seq)}) "
+                                 f"must be the same.")
         self.identifiers = identifiers
         self.structures = structures
         self.orientations = orientations
-        self.struct_lib = dict()
-        for ident, struct, ori in zip(identifiers, structures, orientations):
-            self.struct_lib[ident] = (struct, ori)
+        self.struct_lib = dict(zip(identifiers, zip(structures, orientations)))
 
     @classmethod
     def from_orientation_lists(cls, identifiers, structures, orientations):
         return cls(identifiers, structures, orientations)
 
     def get_library_size(self, to_print=False):
-        """Total number of orientations (a one-entry list counts as one)."""
-        size_library = 0
-        for i in range(len(self.orientations)):
-            size_library += 1 if len(self.orientations[i]) == 1 else len(self.orientations[i])
-            if to_print:
-                print(self.identifiers[i], "has", len(self.orientations[i]), "number of entries.")
-        return size_library
+        """Number of orientations over all phases."""
+        if to_print:
+            for ident, ori in zip(self.identifiers, self.orientations):
+                print(ident, "has", len(ori), "number of entries.")
+        return int(sum(len(ori) for ori in self.orientations))
 
 
 def load_DiffractionLibrary(filename, safety=False):
     """Load a pickled library; ``safety`` must acknowledge that unpickling
     runs code from the file."""
-    if safety:
-        with open(filename, "rb") as handle:
-            return pickle.load(handle)
-    raise RuntimeError("Unpickling is risky, turn safety to True if you trust the author of this content")
+    if not safety:
+        raise RuntimeError("Unpickling is risky, turn safety to True if you trust the author of this content")
+    with open(filename, "rb") as handle:
+        return pickle.load(handle)
 
 
 def _get_library_entry_from_angles(library, phase, angles):
-    """Index of the first orientation within 1e-2 (sum of absolute angle
-    differences, degrees) of ``angles``."""
-    for orientation_index, orientation in enumerate(library[phase]["orientations"]):
-        if np.sum(np.abs(np.subtract(orientation, angles))) < 1e-2:
-            return orientation_index
-    raise ValueError("It appears that no library entry lies with 1e-2 of the target angle")
+    """Index of the first orientation of ``phase`` whose Euler triple is
+    within 1e-2 of ``angles`` (sum of absolute differences, degrees)."""
+    table = np.asarray(library[phase]["orientations"], dtype=np.float64).reshape(-1, 3)
+    hits = np.flatnonzero(np.abs(table - np.asarray(angles, dtype=np.float64)).sum(axis=1) < 1e-2)
+    if hits.size == 0:
+        raise ValueError("It appears that no library entry lies with 1e-2 of the target angle")
+    return int(hits[0])
 
 
 class DiffractionLibrary(dict):
@@ -80,20 +75,17 @@ class DiffractionLibrary(dict):
         self.with_direct_beam = False
 
     def get_library_entry(self, phase=None, angle=None):
-        if phase is not None:
-            phase_entry = self[phase]
-            orientation_index = _get_library_entry_from_angles(self, phase, angle) if angle is not None else 0
-        elif angle is not None:
+        """The simulation, intensities, pixel coordinates and intensity norm
+        of one entry: the orientation nearest ``angle`` of ``phase``, or the
+        first orientation of ``phase`` (of the first phase when none is
+        given; an ``angle`` needs a ``phase``)."""
+        if phase is None and angle is not None:
             raise ValueError("To select a certain angle you must first specify a phase")
-        else:
-            phase_entry = next(iter(self.values()))
-            orientation_index = 0
-        return {
-            "Sim": phase_entry["simulations"][orientation_index],
-            "intensities": phase_entry["intensities"][orientation_index],
-            "pixel_coords": phase_entry["pixel_coords"][orientation_index],
-            "pattern_norm": np.linalg.norm(phase_entry["intensities"][orientation_index]),
-        }
+        entry = self[phase] if phase is not None else next(iter(self.values()))
+        k = _get_library_entry_from_angles(self, phase, angle) if angle is not None else 0
+        inten = entry["intensities"][k]
+        return {"Sim": entry["simulations"][k], "intensities": inten, "pixel_coords": entry["pixel_coords"][k],
+                "pattern_norm": np.linalg.norm(inten)}
 
     def pickle_library(self, filename):
         with open(filename, "wb") as handle:

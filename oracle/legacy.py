@@ -190,3 +190,57 @@ def calculate_profile_data(lattice: DiffpyLattice, elements, xyz, occupancy, dw,
             y.append(v[0])
             hk.append(k)
     return x, np.asarray(y) / max(y) * 100, hk
+
+
+def transformed_coordinates(coords, angle, center=(0, 0), mirrored=False):
+    """In-plane turn of spot coordinates, the reference's operation order:
+    theta = m atan2(y, x) + deg2rad(angle), r = |(x, y)|,
+    (r cos theta + cx, r sin theta + cy).  Follows
+    diffsims/sims/diffraction_simulation.py:199-215."""
+    out = np.array(coords, dtype=np.float64, copy=True)
+    x, y = out[:, 0], out[:, 1]
+    theta = (-1 if mirrored else 1) * np.arctan2(y, x) + np.deg2rad(angle)
+    rd = np.sqrt(x ** 2 + y ** 2)
+    out[:, 0] = rd * np.cos(theta) + center[0]
+    out[:, 1] = rd * np.sin(theta) + center[1]
+    return out
+
+
+def legacy_diffraction_pattern(calibrated_xy, intensities, shape=(512, 512), sigma=10, direct_beam_position=None,
+                               in_plane_angle=0, mirrored=False):
+    """DiffractionSimulation.get_diffraction_pattern: pixel positions, the
+    in-frame spots truncated to int (last write wins), scipy
+    ``gaussian_filter`` (via add_shot_and_point_spread without noise) and
+    the division by the maximum; zeros when no spot is in the frame.
+    Follows diffsims/sims/diffraction_simulation.py:296-354 and
+    diffsims/pattern/detector_functions.py:64-80,109-141."""
+    from scipy import ndimage as ndi
+    if direct_beam_position is None:
+        direct_beam_position = (shape[1] // 2, shape[0] // 2)
+    c = transformed_coordinates(calibrated_xy, in_plane_angle, direct_beam_position, mirrored)
+    inf = (c[:, 0] >= 0) & (c[:, 0] < shape[1]) & (c[:, 1] >= 0) & (c[:, 1] < shape[0])
+    sc = c[inf].astype(int)
+    si = np.asarray(intensities)[inf]
+    pattern = np.zeros(shape)
+    if si.shape[0] == 0:
+        return pattern
+    pattern[sc[:, 0], sc[:, 1]] = si
+    pattern = ndi.gaussian_filter(pattern.T, sigma)
+    return np.divide(pattern, np.max(pattern))
+
+
+def legacy_mask(calibrated_xy, intensities, shape, radius=6.0, negative=True, radius_function=None,
+                direct_beam_position=None, in_plane_angle=0, mirrored=False):
+    """DiffractionSimulation.get_as_mask: a mask filled with ``negative``
+    and discs (X - x)^2 + (Y - y)^2 < r^2 set to ``not negative``.  Follows
+    diffsims/sims/diffraction_simulation.py:235-294 and
+    diffsims/utils/mask_utils.py:24-28,64-116."""
+    r = radius if radius_function is None else radius_function(np.asarray(intensities))
+    if direct_beam_position is None:
+        direct_beam_position = (shape[1] // 2, shape[0] // 2)
+    c = transformed_coordinates(calibrated_xy, in_plane_angle, direct_beam_position, mirrored)
+    mask = np.full(shape, negative, dtype=bool)
+    X, Y = np.meshgrid(np.arange(shape[1]), np.arange(shape[0]))
+    for (x, y), rr in zip(c[:, :2], r * np.ones(c.shape[0])):
+        mask[(X - x) ** 2 + (Y - y) ** 2 < rr ** 2] = not negative
+    return mask

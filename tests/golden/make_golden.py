@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this folder from the reference itself.
 
-Runs only where a diffsims checkout is available (default
-``/root/reference``); the fixtures it writes are committed so the tests never
+Runs only where a diffsims checkout is available (its path is the one
+required argument); the fixtures it writes are committed so the tests never
 need the reference.  What it does:
 
 * copies the reference's golden detector image
@@ -104,7 +104,7 @@ def structures():
     return out
 
 
-def main(ref_root="/root/reference"):
+def main(ref_root):
     su, sfm = load_reference(ref_root)
     old = np.load(pathlib.Path(ref_root) / "diffsims/tests/generators/old_simulation.npy")
     np.save(HERE / "graphite_pattern_128.npy", old)
@@ -246,7 +246,7 @@ def load_reference_structure_factor(ref_root):
     return asp, asf, ssf
 
 
-def main_structure_factor(ref_root="/root/reference"):
+def main_structure_factor(ref_root):
     asp, asf, ssf = load_reference_structure_factor(ref_root)
     rng = np.random.default_rng(29)
     g = {}
@@ -376,7 +376,7 @@ def profile_cases():
             ("p1", 1.2, {}), ("p1", 1.6, {"scattering_params": "xtables"})]
 
 
-def main_legacy(ref_root="/root/reference"):
+def main_legacy(ref_root):
     from oracle import legacy as ol
     dg = load_reference_legacy(ref_root)
     g = {}
@@ -406,6 +406,8 @@ def main_legacy(ref_root="/root/reference"):
 
 
 if __name__ == "__main__":
-    main(*sys.argv[1:])
-    main_structure_factor(*sys.argv[1:])
-    main_legacy(*sys.argv[1:])
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py /path/to/diffsims-checkout")
+    main(sys.argv[1])
+    main_structure_factor(sys.argv[1])
+    main_legacy(sys.argv[1])

@@ -14,9 +14,13 @@ element symbol -> five (a_i, b_i) pairs, and
 98 rows of a1-a4, b1-b4 in 1/Angstrom^2.  This script copies the numbers
 verbatim into JSON so the library and the GPU host never need the reference.
 
-Usage (needs a checkout of the reference)::
+Usage (needs a checkout of the reference; its path is the one argument)::
 
-    python diffsims_gb300/data/make_tables.py /path/to/diffsims-checkout
+    python tests/golden/make_tables.py /path/to/diffsims-checkout
+
+It writes ``diffsims_gb300/data/scattering_params.json``, the package's data
+file (committed), and lives beside the test fixtures' generator because it is
+a one-off build step, not part of the package.
 """
 import importlib.util
 import json
@@ -45,11 +49,13 @@ def main(ref_root):
         "doyleturner": [list(map(float, row)) for row in dt.ATOMIC_SCATTERING_PARAMETERS_DOYLETURNER],
         "elements": list(dt.ELEMENTS),
     }
-    dst = pathlib.Path(__file__).with_name("scattering_params.json")
+    dst = pathlib.Path(__file__).resolve().parents[2] / "diffsims_gb300" / "data" / "scattering_params.json"
     dst.write_text(json.dumps(out, sort_keys=True, separators=(",", ":")))
     print(f"wrote {dst} ({len(out['lobato'])} lobato, {len(out['xtables'])} xtables, "
           f"{len(out['doyleturner'])} doyle-turner)")
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_tables.py /path/to/diffsims-checkout")
+    main(sys.argv[1])

@@ -59,7 +59,7 @@ def excitation_error_of(i, hkl):
 
 
 def compare(i, sim, coords, idx, inten, rtol=1e-5, atol_rel=0.0):
-    got = {tuple(h): k for k, h in enumerate(sim._indices)}
+    got = {tuple(h): k for k, h in enumerate(sim._hkl)}
     want = {tuple(h): k for k, h in enumerate(idx)}
     flips = 0
     scale = np.max(inten) if inten.size else 1.0
@@ -75,10 +75,10 @@ def compare(i, sim, coords, idx, inten, rtol=1e-5, atol_rel=0.0):
     assert order == sorted(order)
     a = np.array([got[h] for h in common], dtype=int)
     b = np.array([want[h] for h in common], dtype=int)
-    Ig, Ir = sim._intensities[a], inten[b]
+    Ig, Ir = sim._I[a], inten[b]
     np.testing.assert_allclose(Ig, Ir, rtol=rtol, atol=max(1e-24 * scale, atol_rel * scale))
     gn = np.maximum(np.linalg.norm(coords[b], axis=1), 1e-3)
-    assert np.all(np.abs(sim._coordinates[a] - coords[b]).max(axis=1) <= 1e-5 * gn)
+    assert np.all(np.abs(sim._xyz[a] - coords[b]).max(axis=1) <= 1e-5 * gn)
     return flips
 
 
@@ -216,3 +216,36 @@ def test_profiles_match_reference_fixtures(ref, j):
     assert list(prof.hkls) == list(ref[f"profile{j}_hkls"])
     np.testing.assert_allclose(prof.magnitudes, ref[f"profile{j}_magnitudes"], rtol=1e-13)
     np.testing.assert_allclose(prof.intensities, ref[f"profile{j}_intensities"], rtol=1e-9, atol=1e-9)
+
+
+@pytest.mark.parametrize("kw", [dict(), dict(in_plane_angle=30.0), dict(mirrored=True, sigma=2.0),
+                                dict(shape=(200, 200), direct_beam_position=(80, 120), sigma=3.0)])
+def test_legacy_drawing_methods_match_reference_recipe(kw):
+    """DiffractionSimulation.get_diffraction_pattern (GPU rasteriser) and
+    get_as_mask against the reference's recipes restated in the oracle
+    (diffsims/sims/diffraction_simulation.py:235-354).  Patterns with a spot
+    within 1e-4 px of a pixel edge (float32 positions may truncate the other
+    way) are left out and counted."""
+    compared = 0
+    for case in (1, 3, 4, 9):
+        sim = run_case(case)
+        sim.calibration = 0.01
+        shape = kw.get("shape", (512, 512))
+        args = {k: v for k, v in kw.items() if k != "shape"}
+        dbp = args.get("direct_beam_position") or (shape[1] // 2, shape[0] // 2)
+        pos = ol.transformed_coordinates(sim.calibrated_coordinates, args.get("in_plane_angle", 0), dbp,
+                                         args.get("mirrored", False))
+        fr = pos[:, :2] - np.floor(pos[:, :2])
+        if np.any(((fr < 1e-4) | (fr > 1 - 1e-4)) & (np.abs(sim.calibrated_coordinates) > 0)):
+            continue
+        got = sim.get_diffraction_pattern(shape, **args)
+        want = ol.legacy_diffraction_pattern(sim.calibrated_coordinates, sim.intensities, shape, **args)
+        np.testing.assert_allclose(got, want, rtol=0, atol=2e-6 * max(np.abs(want).max(), 1e-300))
+        margs = {k: v for k, v in args.items() if k != "sigma"}
+        for negative, rf in ((True, None), (False, np.sqrt)):
+            m = sim.get_as_mask(shape, radius=4.5, negative=negative, radius_function=rf, **margs)
+            mw = ol.legacy_mask(sim.calibrated_coordinates, sim.intensities, shape, radius=4.5, negative=negative,
+                                radius_function=rf, **margs)
+            assert np.array_equal(m, mw)
+        compared += 1
+    assert compared >= 1

@@ -167,3 +167,19 @@ def test_oracle_profiles_match_reference_fixtures(ref, j):
     assert list(h) == list(ref[f"profile{j}_hkls"])
     np.testing.assert_allclose(x, ref[f"profile{j}_magnitudes"], rtol=1e-14)
     np.testing.assert_allclose(y, ref[f"profile{j}_intensities"], rtol=1e-12, atol=1e-11)
+
+
+@pytest.mark.parametrize("angle, mirrored, center", [(0, False, (0, 0)), (33.0, False, (5, -2)),
+                                                     (-120.5, True, (256, 256)), (90, True, (0, 0))])
+def test_diffraction_simulation_transform_matches_reference_order(angle, mirrored, center):
+    """The container's in-plane turn (complex form) against the reference's
+    atan2 / sqrt / cos / sin order (oracle restatement): equal to round-off."""
+    from diffsims_gb300.diffraction_simulation import DiffractionSimulation
+    rng = np.random.default_rng(5)
+    c = rng.normal(0, 1, (50, 3))
+    sim = DiffractionSimulation(c, intensities=rng.random(50), with_direct_beam=True)
+    sim.calibration = 0.02
+    for units, src in (("real", c), ("pixel", c[:, :2] / 0.02)):
+        got = sim._get_transformed_coordinates(angle, center, mirrored, units=units)
+        want = ol.transformed_coordinates(src, angle, center, mirrored)
+        np.testing.assert_allclose(got[:, :2], want[:, :2], rtol=0, atol=1e-12 * max(1.0, np.abs(want).max()))
