@@ -43,7 +43,8 @@ EXPORTED_SYMBOLS = (
     "ds_simulate_batch", "ds_rasterize_scratch_bytes", "ds_rasterize",
     "ds_simulate_backward_scratch_bytes", "ds_simulate_backward", "ds_structure_factors_backward_scratch_bytes",
     "ds_axis_angle_compose", "ds_axis_angle_compose_backward", "ds_polar_flatten", "ds_structure_factors_backward",
-    "ds_probe_fp32_fma", "ds_set_wait_limits", "ds_probe_wait_timeout", "ds_last_error", "ds_version",
+    "ds_probe_fp32_fma", "ds_set_wait_limits", "ds_probe_wait_timeout", "ds_apply_shape_factors_scratch_bytes",
+    "ds_apply_shape_factors", "ds_last_error", "ds_version",
 )
 
 
@@ -144,6 +145,9 @@ def load_library(require_cuda: bool = True):
             lib.ds_axis_angle_compose_backward.argtypes = [vp, vp, i64, vp, vp, vp]
             lib.ds_probe_fp32_fma.argtypes = [i64, i32, vp, vp]
             lib.ds_set_wait_limits.argtypes = [i64, i64]
+            lib.ds_apply_shape_factors_scratch_bytes.argtypes = [i64]
+            lib.ds_apply_shape_factors_scratch_bytes.restype = sz
+            lib.ds_apply_shape_factors.argtypes = [vp, vp, vp, vp, vp, i64, dp, C.POINTER(ds_spots), vp, sz, vp, vp]
             lib.ds_probe_wait_timeout.argtypes = [i64, vp, sz, vp, vp, vp]
             lib.ds_last_error.restype = C.c_char_p
             lib.ds_version.restype = C.c_char_p
@@ -152,7 +156,8 @@ def load_library(require_cuda: bool = True):
                          "ds_simulate", "ds_simulate_batch", "ds_rasterize", "ds_simulate_backward",
                          "ds_structure_factors_backward",
                          "ds_axis_angle_compose", "ds_axis_angle_compose_backward", "ds_polar_flatten",
-                         "ds_probe_fp32_fma", "ds_set_wait_limits", "ds_probe_wait_timeout"):
+                         "ds_probe_fp32_fma", "ds_set_wait_limits", "ds_probe_wait_timeout",
+                         "ds_apply_shape_factors"):
                 getattr(lib, name).restype = C.c_int32
             _lib = lib
     if require_cuda and not torch.cuda.is_available():

@@ -150,6 +150,9 @@ class SpotModel:
         self.elements = list(elements)
         self._atoms = PackedAtoms(self.elements, np.zeros((n, 3)), np.ones(n), np.zeros(n),
                                   generator.scattering_params, dev)
+        if getattr(generator, "_custom_shape", None) is not None:
+            raise NotImplementedError("gradients are available for the built-in shape-factor models only "
+                                      "(a function of the caller's has no adjoint kernel)")
         self.settings = generator.settings(max_excitation_error, shape_factor_width, form)
         self.reciprocal_radius = float(reciprocal_radius)
         self.with_direct_beam = bool(with_direct_beam)

@@ -20,7 +20,7 @@ import torch
 from . import _native as N
 from .crystal import Lattice, diffpy_base, lattice_params, sites_of
 from .diffraction_simulation import DiffractionSimulation, ProfileSimulation
-from .engine import PhaseTable, simulate_phase
+from .engine import PhaseTable, custom_shape_spots, simulate_phase
 from .generator import SimulationGenerator
 from .sim_utils import PackedAtoms, debye_waller_per_atom, get_electron_wavelength, get_kinematical_intensities
 
@@ -97,7 +97,13 @@ class DiffractionGenerator:
         q[:, 1:] *= -1
         quats = torch.from_numpy(np.ascontiguousarray(q)).to(dev)
         settings = self._gen.settings(max_excitation_error, shape_factor_width, form)
-        spots = simulate_phase(table, quats, settings, reciprocal_radius)
+        if self._gen._custom_shape is not None and settings.precession_mode != N.DS_PRECESSION_LORENTZIAN:
+            # a shape-factor function of the caller's: evaluated on the host
+            # between the selection and the finishing kernel
+            spots = custom_shape_spots(table, quats, settings, reciprocal_radius, self._gen._custom_shape,
+                                       self.shape_factor_kwargs)
+        else:
+            spots = simulate_phase(table, quats, settings, reciprocal_radius)
         off, idx, xyzi = spots.host(pinned=True)
         # one gather and one cast for all patterns; each simulation holds views
         hkl = table.hkl_host()[idx].astype(np.float64) if spots.total else np.zeros((0, 3))

@@ -625,6 +625,70 @@ def simulate_phase_streamed(table: PhaseTable, quats: torch.Tensor, settings: Si
     return res
 
 
+def apply_shape_factors(spots: PhaseSpots, F2: torch.Tensor, shape_factors: torch.Tensor, minimum_intensity: float,
+                        stream=None) -> PhaseSpots:
+    """The spots of ``spots`` (one phase, the model switched off) finished
+    with per-spot shape factors ``shape_factors`` (float64): I = sf |F|^2,
+    the per-pattern mask I > max I * minimum_intensity and ordered
+    compaction (``ds_apply_shape_factors``)."""
+    lib = N.load_library()
+    dev = spots.offsets.device
+    n = spots.n_orient
+    total_in = int(spots.total)
+    sf = shape_factors.to(dev, torch.float64).contiguous()
+    if sf.numel() != total_in:
+        raise ValueError(f"{sf.numel()} shape factors for {total_in} spots")
+    nbytes = lib.ds_apply_shape_factors_scratch_bytes(n)
+    scratch = torch.empty(max(int(nbytes), 16), dtype=torch.uint8, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    total = torch.zeros(1, dtype=torch.int64, device=dev)
+    offsets = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    cap = max(total_in, 1)
+    idx = torch.empty(cap, dtype=torch.int32, device=dev)
+    xyzi = torch.empty((cap, 4), dtype=torch.float32, device=dev)
+    xin = spots.xyzi if total_in else torch.zeros((1, 4), dtype=torch.float32, device=dev)
+    iin = spots.hkl_index if total_in else torch.zeros(1, dtype=torch.int32, device=dev)
+    out = N.ds_spots(offsets.data_ptr(), idx.data_ptr(), xyzi.data_ptr(), cap, total.data_ptr(), None)
+    N.check(lib.ds_apply_shape_factors(N.ptr(spots.offsets), N.ptr(iin), N.ptr(xin), N.ptr(sf) if total_in else None,
+                                       N.ptr(F2), n, float(minimum_intensity), out, N.ptr(scratch), scratch.numel(),
+                                       N.ptr(status), N.stream_handle(stream)), "apply_shape_factors")
+    N.check_device_status(status, "apply_shape_factors")
+    return PhaseSpots(spots.table, offsets, idx, xyzi, int(total.item()))
+
+
+def custom_shape_spots(table: PhaseTable, quats: torch.Tensor, settings: SimSettings, radius: float, model,
+                       kwargs: dict) -> PhaseSpots:
+    """One phase's spots with a shape-factor function of the caller's
+    (diffsims/generators/simulation_generator.py:387-411): the orientation
+    kernel selects the spots with the model switched off and returns their
+    excitation errors; ``model(s, width, **kwargs)`` is evaluated on each
+    pattern's array on the host (with precession and
+    ``approximate_precession=False``, its average over the precession circle,
+    (1/2 pi) int_0^2pi model(s + r phi cos t) dt by adaptive quadrature per
+    spot, diffsims/utils/shape_factor_models.py:222-268); the kernel
+    ``ds_apply_shape_factors`` finishes the intensities, the mask and the
+    compaction."""
+    select = SimSettings(**{**settings.__dict__, "shape_model": "binary", "minimum_intensity": -1.0})
+    first = simulate_phase(table, quats, select, radius, SpotBuffers(table.device, with_excitation_error=True))
+    off, _, xyzi = first.host()
+    s_all = first.excitation_error.cpu().numpy() if first.total else np.zeros(0)
+    w = settings.shape_width
+    sf = np.zeros(first.total, dtype=np.float64)
+    phi = settings.precession_angle_rad
+    if settings.precession_mode == N.DS_PRECESSION_INTEGRAL:
+        from scipy.integrate import quad
+        r_all = np.hypot(xyzi[:, 0].astype(np.float64), xyzi[:, 1].astype(np.float64))
+        for k in range(first.total):
+            s0, a = float(s_all[k]), float(r_all[k]) * phi
+            sf[k] = quad(lambda t: model(s0 + a * np.cos(t), w, **kwargs), 0, 2 * np.pi)[0] / (2 * np.pi)
+    else:
+        for i in range(first.n_orient):
+            a, b = int(off[i]), int(off[i + 1])
+            if b > a:
+                sf[a:b] = np.broadcast_to(np.asarray(model(s_all[a:b], w, **kwargs), dtype=np.float64), (b - a,))
+    return apply_shape_factors(first, table.F2, torch.from_numpy(sf), settings.minimum_intensity)
+
+
 @dataclass
 class RasterSettings:
     """Arguments of Simulation2D.get_diffraction_pattern

@@ -11,8 +11,8 @@ import torch
 
 from . import _native as N
 from .crystal import Phase, Rotation, lattice_params, quaternions_of, structure_of
-from .engine import (HostSpotPool, PhaseBatch, PhaseTable, SimSettings, SpotBuffers, reciprocal_basis, simulate_phase,
-                     simulate_phase_streamed)
+from .engine import (HostSpotPool, PhaseBatch, PhaseTable, SimSettings, SpotBuffers, custom_shape_spots,
+                     reciprocal_basis, simulate_phase, simulate_phase_streamed)
 from .simulation1d import Simulation1D
 from .simulation2d import Simulation2D
 from . import interop
@@ -87,17 +87,16 @@ class SimulationGenerator:
                 raise NotImplementedError(
                     f"{shape_factor_model} is not a recognized shape factor model, choose from: "
                     f"{_SHAPE_NAMES} or provide your own function.")
-            self.shape_factor_model = shape_factor_model
-        else:
-            if _shape_name(shape_factor_model) is None:
-                raise NotImplementedError(
-                    "custom shape factor callables cannot run inside the CUDA kernels; use one of "
-                    f"{_SHAPE_NAMES + ('binary',)} (by name or as diffsims.utils.shape_factor_models functions)")
-            self.shape_factor_model = shape_factor_model
+        elif not callable(shape_factor_model):
+            raise NotImplementedError(f"{shape_factor_model} is neither a shape factor model name nor a function")
+        self.shape_factor_model = shape_factor_model
         self.minimum_intensity = minimum_intensity
         self.shape_factor_kwargs = kwargs
+        # a function of the caller's (not one of the reference's models) runs
+        # on the host between two kernel launches (engine.custom_shape_spots)
+        self._custom_shape = None if _shape_name(shape_factor_model) is not None else shape_factor_model
         unknown = set(kwargs) - {"minima_number"}
-        if unknown:
+        if unknown and self._custom_shape is None:
             raise TypeError(f"unexpected shape factor keyword arguments: {sorted(unknown)}")
         if scattering_params in ["lobato", "xtables", None]:
             self.scattering_params = scattering_params
@@ -130,8 +129,9 @@ class SimulationGenerator:
         else:
             mode = N.DS_PRECESSION_INTEGRAL
         width = max_excitation_error if shape_factor_width is None else shape_factor_width
+        kernel_model = "binary" if self._custom_shape is not None else _shape_name(self.shape_factor_model)
         return SimSettings(k0=1.0 / lam, max_excitation_error=float(max_excitation_error), shape_width=float(width),
-                           shape_model=_shape_name(self.shape_factor_model), precession_angle_rad=phi,
+                           shape_model=kernel_model, precession_angle_rad=phi,
                            precession_mode=mode, minimum_intensity=float(self.minimum_intensity),
                            minima_number=float(self.shape_factor_kwargs.get("minima_number", 5)), form=form,
                            orient_tile=orient_tile)
@@ -195,7 +195,14 @@ class SimulationGenerator:
             t_upload += time.perf_counter() - t1
             t_table += t1 - t0
             rots.append(rot)
-        if len(tables) == 1 and stream_to_host:
+        custom = self._custom_shape is not None and settings.precession_mode != N.DS_PRECESSION_LORENTZIAN
+        if custom:
+            # the caller's function on the host between the selection and the
+            # finishing kernel (lorentzian_precession ignores the model, as in
+            # the reference, and stays on the plain path)
+            spots = [custom_shape_spots(t, q, settings, reciprocal_radius, self._custom_shape,
+                                        self.shape_factor_kwargs) for t, q in zip(tables, qs)]
+        elif len(tables) == 1 and stream_to_host:
             sp = simulate_phase_streamed(tables[0], qs[0], settings, reciprocal_radius, host_pool=self._host_pool,
                                          timing=timing)
             sp._timing.update(table_ms=t_table * 1e3, upload_ms=t_upload * 1e3,

@@ -251,6 +251,24 @@ ds_status ds_simulate_batch(const ds_sim_params *p, const ds_batch_phase *phases
 ds_status ds_simulate_noalloc(const ds_sim_params *p, const ds_phase_table *t, const double *quats,
                               int64_t n_orient, ds_spots *out, int32_t *status, void *stream);
 
+/* Custom shape factors: the last step of calculate_diffraction2d with a
+ * shape-factor function of the caller's
+ * (diffsims/generators/simulation_generator.py:117-120,387-411), which
+ * cannot run in a kernel.  The spots come from ds_simulate with the model
+ * switched off (DS_SHAPE_BINARY, minimum_intensity < 0: every selected row,
+ * its excitation error requested); the caller evaluates its function on
+ * them; this call finishes each pattern: I = shape_factors[k] * F2[row]
+ * (FP64 product), keeps I > max(pattern I) * minimum_intensity (:237-240)
+ * and compacts the kept spots in order into out (x, y, z copied, I
+ * replaced).  offsets_in / hkl_index_in / xyzi_in: the first call's CSR;
+ * shape_factors: one per input spot; F2: the table's |F|^2 (mixed form).
+ * Capacity overflow as ds_simulate.  scratch: ds_apply_shape_factors_scratch_bytes. */
+size_t ds_apply_shape_factors_scratch_bytes(int64_t n_patterns);
+ds_status ds_apply_shape_factors(const int64_t *offsets_in, const int32_t *hkl_index_in, const float *xyzi_in,
+                                 const double *shape_factors, const float *F2, int64_t n_patterns,
+                                 double minimum_intensity, ds_spots *out, void *scratch, size_t scratch_bytes,
+                                 int32_t *status, void *stream);
+
 /* ------------------------------------------------------------------------ */
 /* Detector images of spot patterns.  Replaces Simulation2D.get_diffraction_pattern
  * (diffsims/simulations/simulation2d.py:357-442) with

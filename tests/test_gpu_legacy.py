@@ -115,9 +115,9 @@ def test_many_rotations_in_one_launch():
     assert len(many) == 64
     for k in (0, 17, 63):
         one = gen.calculate_ed_data(st, 1.5, rotation=eul[k])
-        np.testing.assert_array_equal(one._indices, many[k]._indices)
-        np.testing.assert_array_equal(one._intensities, many[k]._intensities)
-        np.testing.assert_array_equal(one._coordinates, many[k]._coordinates)
+        np.testing.assert_array_equal(one._hkl, many[k]._hkl)
+        np.testing.assert_array_equal(one._I, many[k]._I)
+        np.testing.assert_array_equal(one._xyz, many[k]._xyz)
 
 
 def test_sphere_enumeration_matches_oracle():

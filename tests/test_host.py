@@ -262,3 +262,40 @@ def test_wait_limit_entries_reject_bad_arguments(lib):
     assert lib.ds_probe_wait_timeout(100, None, 512, fake, fake, None) == N.DS_ERR_INVALID_ARGUMENT
     assert lib.ds_set_wait_limits(5, 7) == N.DS_OK
     assert lib.ds_set_wait_limits(0, -1) == N.DS_OK
+
+
+def test_custom_shape_functions_are_accepted():
+    """A shape-factor function of the caller's (diffsims/generators/simulation_generator.py:117-120)
+    is kept with its keyword arguments; the kernels then run with the model
+    switched off (the function is applied between two launches); the
+    reference's own model functions still map to their names."""
+    import diffsims_gb300 as ds
+
+    def local_excite(excitation_error, maximum_excitation_error, t):
+        return (np.sin(t) * excitation_error) / maximum_excitation_error
+
+    g = ds.SimulationGenerator(300, shape_factor_model=local_excite, t=0.2)
+    assert g.shape_factor_model is local_excite and g.shape_factor_kwargs == {"t": 0.2}
+    assert g._custom_shape is local_excite and g.settings().shape_model == "binary"
+    with pytest.raises(TypeError):
+        ds.SimulationGenerator(300, shape_factor_model="sinc", t=0.2)
+    with pytest.raises(NotImplementedError):
+        ds.SimulationGenerator(300, shape_factor_model=3.0)
+    from diffsims_gb300.autograd import SpotModel
+    with pytest.raises(NotImplementedError):
+        SpotModel(["Si"], g, device="cpu")
+
+
+def test_apply_shape_factors_rejects_bad_arguments(lib):
+    from diffsims_gb300 import _native as N
+    fake = ctypes.c_void_p(4096)
+    out = N.ds_spots(4096, 4096, 4096, 10, 4096, None)
+    assert lib.ds_apply_shape_factors(fake, fake, fake, fake, fake, -1, 1e-20, out, fake, 1 << 20, fake,
+                                      None) == N.DS_ERR_INVALID_ARGUMENT
+    assert lib.ds_apply_shape_factors(fake, fake, fake, fake, fake, 5, float("nan"), out, fake, 1 << 20, fake,
+                                      None) == N.DS_ERR_INVALID_ARGUMENT
+    assert "finite" in lib.ds_last_error().decode()
+    assert lib.ds_apply_shape_factors(fake, fake, fake, fake, fake, 5, 1e-20, out, fake, 8, fake,
+                                      None) == N.DS_ERR_INVALID_ARGUMENT
+    assert "scratch" in lib.ds_last_error().decode()
+    assert lib.ds_apply_shape_factors_scratch_bytes(100) >= 100 * 8
