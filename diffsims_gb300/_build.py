@@ -18,6 +18,7 @@ CSRC = PKG / "csrc"
 INCLUDE = PKG.parent / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libdiffsims_gb300.so"
+LIB_DEBUG = PKG / "libdiffsims_gb300_debug.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -33,17 +34,24 @@ def _flags(extra=()):
                    "-I", str(INCLUDE), "--expt-relaxed-constexpr", *extra]
 
 
-def build(verbose: bool = False, ptxas_verbose: bool = False, force: bool = False) -> pathlib.Path:
+def build(verbose: bool = False, ptxas_verbose: bool = False, force: bool = False,
+          debug: bool = False) -> pathlib.Path:
+    """Compile csrc/*.cu and link the library; ``debug`` builds the
+    bounds-checked variant (-DDS_DEBUG_BOUNDS) as libdiffsims_gb300_debug.so."""
+    lib = LIB_DEBUG if debug else LIB
+    objdir = BUILD / "debug" if debug else BUILD
     sources = sorted(CSRC.glob("*.cu"))
     deps = sources + sorted(CSRC.glob("*.cuh")) + [INCLUDE / "diffsims_gb300.h", pathlib.Path(__file__)]
-    if not force and LIB.exists() and LIB.stat().st_mtime > max(p.stat().st_mtime for p in deps):
-        return LIB
-    BUILD.mkdir(exist_ok=True)
+    if not force and lib.exists() and lib.stat().st_mtime > max(p.stat().st_mtime for p in deps):
+        return lib
+    objdir.mkdir(parents=True, exist_ok=True)
     nvcc = nvcc_path()
     extra = ["-Xptxas", "-v"] if ptxas_verbose else []
+    if debug:
+        extra.append("-DDS_DEBUG_BOUNDS")
 
     def compile_one(src: pathlib.Path):
-        obj = BUILD / (src.stem + ".o")
+        obj = objdir / (src.stem + ".o")
         cmd = [nvcc, *_flags(extra), "-c", str(src), "-o", str(obj)]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
@@ -56,16 +64,16 @@ def build(verbose: bool = False, ptxas_verbose: bool = False, force: bool = Fals
         for obj, log in results:
             if log.strip():
                 print(f"--- {obj.name}\n{log}", file=sys.stderr)
-    tmp = LIB.with_suffix(".so.tmp")
+    tmp = lib.with_suffix(".so.tmp")
     # the CUDA runtime is linked statically (nvcc's default): no libcudart.so
     # lookup at load time, on either machine
     cmd = [nvcc, *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *[str(o) for o, _ in results]]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(verbose=True, ptxas_verbose="-v" in sys.argv, force="-f" in sys.argv))
+    print(build(verbose=True, ptxas_verbose="-v" in sys.argv, force="-f" in sys.argv, debug="--debug" in sys.argv))

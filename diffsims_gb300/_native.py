@@ -6,12 +6,19 @@ present, every compute entry raises.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import pathlib
 import threading
 
 import torch
 
-_LIB_PATH = pathlib.Path(__file__).resolve().parent / "libdiffsims_gb300.so"
+# DIFFSIMS_GB300_DEBUG_BOUNDS=1 loads the bounds-checked build
+# (libdiffsims_gb300_debug.so, kernels compiled with -DDS_DEBUG_BOUNDS: every
+# checked index outside its array sets DS_ERR_BOUNDS in the status word and
+# the access is skipped); `python -m diffsims_gb300._build --debug` builds it.
+DEBUG_BOUNDS = os.environ.get("DIFFSIMS_GB300_DEBUG_BOUNDS", "") == "1"
+_LIB_PATH = pathlib.Path(__file__).resolve().parent / (
+    "libdiffsims_gb300_debug.so" if DEBUG_BOUNDS else "libdiffsims_gb300.so")
 _lock = threading.Lock()
 _lib = None
 
@@ -23,6 +30,7 @@ DS_ERR_CAPACITY = 4
 DS_ERR_TIMEOUT = 8
 DS_ERR_UNSUPPORTED = 16
 DS_ERR_NONFINITE = 32
+DS_ERR_BOUNDS = 64
 
 DS_FORM_MIXED = 0
 DS_FORM_FP64 = 1
@@ -187,6 +195,8 @@ def check_status_value(v: int, what: str, allow=0) -> int:
         raise NativeError(f"{what}: a bounded device wait timed out (status {v})")
     if bad & DS_ERR_NONFINITE:
         raise ValueError(f"{what}: non-finite input (status {v})")
+    if bad & DS_ERR_BOUNDS:
+        raise NativeError(f"{what}: an index check of the bounds-checked build failed (status {v})")
     if bad:
         raise NativeError(f"{what}: device status {v}")
     return v

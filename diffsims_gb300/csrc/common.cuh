@@ -49,6 +49,22 @@ void clear_error();
         }                                                                          \
     } while (0)
 
+// Bounds-checked builds (-DDS_DEBUG_BOUNDS; the library is then built as
+// libdiffsims_gb300_debug.so): DS_IN_BOUNDS(i, n, status) is false, and
+// DS_ERR_BOUNDS is or-ed into the kernel's status word, when the index i lies
+// outside [0, n); the caller skips the access.  Normal builds compile every
+// check to `true`.
+#ifdef DS_DEBUG_BOUNDS
+__device__ __forceinline__ bool debug_in_bounds(long long i, long long n, int32_t *status) {
+    if (i >= 0 && i < n) return true;
+    atomicOr(status, DS_ERR_BOUNDS);
+    return false;
+}
+#define DS_IN_BOUNDS(i, n, status) ::ds::debug_in_bounds((long long)(i), (long long)(n), (status))
+#else
+#define DS_IN_BOUNDS(i, n, status) true
+#endif
+
 inline ds_status check_launch(const char *what) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {

@@ -625,9 +625,11 @@ raster_fast_kernel(const RasterConst c, const int64_t *__restrict__ off, const f
             const int X = A.sx[k], Y = A.sy[k];
             const float am = A.amp[k];
             const int ylo = max(0, Y - c.R), yhi = min(H, Y + c.R + 1);
-            for (int y = ylo; y < yhi; ++y)
-                A.ent[A.rstart[y] + atomicAdd(&A.rfill[y], 1)] =
-                    make_int2(__float_as_int(am * reflect_weight(c, y, Y, H)), (X << 16) | k);
+            for (int y = ylo; y < yhi; ++y) {
+                const int slot = A.rstart[y] + atomicAdd(&A.rfill[y], 1);
+                if (DS_IN_BOUNDS(slot, (long long)c.NS * P, status))
+                    A.ent[slot] = make_int2(__float_as_int(am * reflect_weight(c, y, Y, H)), (X << 16) | k);
+            }
         }
         __syncthreads();
         for (int y = tid; y < H; y += RAS_THREADS) {
@@ -796,9 +798,462 @@ raster_fast_kernel(const RasterConst c, const int64_t *__restrict__ off, const f
     }
 }
 
+// ----------------------------------------------------------- slice mode ----
+// Fast mode when the filter footprints and the per-pattern tables fit in
+// shared memory (every detector up to a few thousand pixels wide).  The image
+// is cut into slices of SH whole rows; warp w owns slices w, w + 8, ... and
+// builds each one in a private shared-memory buffer, so no two warps ever
+// touch the same pixel.  Each slice has the list of spots whose footprint
+// reaches it, in ascending spot order; the warp takes the spots in that order
+// and spreads a spot's footprint pixels (row, column pairs) over all 32 lanes,
+// one fused multiply-add per pair.  A pair step never holds the same pixel
+// twice, and the spots of one pixel are added in spot order: the image is
+// deterministic, and equal across calls that split the patterns differently.
+// Normalised images take two passes over the slices: the first finds the
+// maximum (the running maximum of the updates when no amplitude is negative:
+// the partial sums of non-negative terms never exceed their final value), the
+// second rebuilds each slice and stores it scaled.  Global memory sees only the
+// spot records and the image, written once.
+#ifndef DS_RAS_SLICE_TARGET
+#define DS_RAS_SLICE_TARGET (55 * 1024)  // shared bytes per CTA: four CTAs per SM
+#endif
+constexpr int RAS_SLICE_TARGET = DS_RAS_SLICE_TARGET;
+static_assert(RAS_WARPS == 8, "slice ownership (s mod 8) assumes eight warps per CTA");
+
+struct SliceGeom {
+    int SH;      // rows per slice
+    int Ws;      // buffer row stride in floats: >= W, a multiple of 4, = 4 ceil(P / 4) mod 32
+    int nsl;     // slices per image
+    int span;    // most slices one footprint reaches
+    int P;       // footprint width 2R + 1
+    unsigned mP; // ceil(2^32 / P): j / P = umulhi(j, mP) for j < P^2 (P odd, P^3 < 2^32)
+    int wt2;     // the P x P product table is in shared memory (P <= 31)
+};
+
+struct SliceArena {
+    float *buf;          // RAS_WARPS x SH x Ws
+    int *key, *slot, *hkey, *hidx;
+    int *sxy;            // X | Y << 15 | (footprint crosses an image edge) << 30
+    float *amp;
+    int *scnt, *sstart, *sfill;  // nsl + 1 each
+    int *sent;           // slice entries (spot indices), CSR by sstart
+    float *wt, *wt2;     // 1-D weights w[|d|], d = 0..R; products w[|dy - R|] w[|dx - R|]
+    int *misc;
+    float *wmax;
+};
+
+__host__ __device__ inline int slice_stride(int W, int P) {
+    const int want = (4 * ((P + 3) / 4)) & 31;  // consecutive rows start 4 ceil(P / 4) banks apart
+    return W + (((want - W) % 32) + 32) % 32;
+}
+
+__host__ __device__ inline size_t slice_arena_bytes(int NS, int T, int R, const SliceGeom &g) {
+    size_t o = ras_align((size_t)RAS_WARPS * g.SH * g.Ws * 4);
+    o += ras_align((size_t)NS * 4) * 2;              // key, slot
+    o += ras_align((size_t)T * 4) * 2;               // hkey, hidx
+    o += ras_align((size_t)NS * 4) * 2;              // sxy, amp
+    o += ras_align((size_t)(g.nsl + 1) * 4) * 3;     // scnt, sstart, sfill
+    o += ras_align((size_t)NS * g.span * 4);         // sent
+    o += ras_align((size_t)(R + 1) * 4);
+    o += ras_align(g.wt2 ? (size_t)g.P * g.P * 4 : 0);
+    o += ras_align(64 * 4) + ras_align(RAS_WARPS * 4);
+    return o;
+}
+
+__device__ inline SliceArena carve_slice(unsigned char *base, int NS, int T, int R, const SliceGeom &g) {
+    SliceArena A;
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        unsigned char *p = base + o;
+        o += ras_align(bytes);
+        return p;
+    };
+    A.buf = (float *)take((size_t)RAS_WARPS * g.SH * g.Ws * 4);
+    A.key = (int *)take((size_t)NS * 4);
+    A.slot = (int *)take((size_t)NS * 4);
+    A.hkey = (int *)take((size_t)T * 4);
+    A.hidx = (int *)take((size_t)T * 4);
+    A.sxy = (int *)take((size_t)NS * 4);
+    A.amp = (float *)take((size_t)NS * 4);
+    A.scnt = (int *)take((size_t)(g.nsl + 1) * 4);
+    A.sstart = (int *)take((size_t)(g.nsl + 1) * 4);
+    A.sfill = (int *)take((size_t)(g.nsl + 1) * 4);
+    A.sent = (int *)take((size_t)NS * g.span * 4);
+    A.wt = (float *)take((size_t)(R + 1) * 4);
+    A.wt2 = (float *)take(g.wt2 ? (size_t)g.P * g.P * 4 : 0);
+    A.misc = (int *)take(64 * 4);
+    A.wmax = (float *)take(RAS_WARPS * 4);
+    return A;
+}
+
+// reflect_weight with the weights in shared memory
+__device__ inline float reflect_weight_s(const float *wt, int R, int x, int P, int n) {
+    float v = 0.f;
+    if (R < n) {
+        const int d = abs(x - P);
+        if (d <= R) v += wt[d];
+        const int m1 = x + P + 1;
+        if (m1 <= R) v += wt[m1];
+        const int m2 = 2 * n - 1 - P - x;
+        if (m2 <= R) v += wt[m2];
+        return v;
+    }
+    const int per = 2 * n;
+    for (int fam = 0; fam < 2; ++fam) {
+        const int base = fam == 0 ? P : -P - 1;
+        const int k0 = (int)floor((double)(x - R - base) / per);
+        for (int k = k0;; ++k) {
+            const int q = base + k * per;
+            if (q > x + R) break;
+            if (q >= x - R) v += wt[abs(q - x)];
+        }
+    }
+    return v;
+}
+
+// Adds the spots of slice rows [ys, ye) (entries e0..e1) into the warp's
+// buffer; with TRACK, `run` takes the maximum of every updated value.
+template <bool TRACK>
+__device__ inline void slice_splat(const RasterConst &c, const SliceGeom &g, const SliceArena &A, int ys, int ye,
+                                   int e0, int e1, float *buf, int lane, float &run, int32_t *status) {
+    const int R = c.R, P = g.P, Ws = g.Ws;
+    for (int e = e0; e < e1; ++e) {
+        const int k = A.sent[e];
+        const int v = A.sxy[k];
+        const int X = v & 0x7fff, Y = (v >> 15) & 0x7fff;
+        const float a = A.amp[k];
+        const int y0 = max(Y - R, ys), y1 = min(Y + R + 1, ye);
+        if (!(v >> 30)) {
+            // interior: pairs j = dy P + dx of the full footprint, rows y0..y1 only
+            const int jb = (y0 - (Y - R)) * P, je = (y1 - (Y - R)) * P;
+            const int corner = (Y - R - ys) * Ws + (X - R);  // footprint corner, relative to the slice (may be < 0)
+            for (int j0 = jb; j0 < je; j0 += 32) {
+                const int j = j0 + lane;
+                if (j < je) {
+                    const int dy = P == 1 ? j : (int)__umulhi((unsigned)j, g.mP);
+                    const int dx = j - dy * P;
+                    const float w = g.wt2 ? A.wt2[j] : A.wt[abs(dy - R)] * A.wt[abs(dx - R)];
+                    if (!DS_IN_BOUNDS(corner + dy * Ws + dx, (ye - ys) * Ws, status)) continue;
+                    float *q = buf + (corner + dy * Ws + dx);
+                    const float nv = fmaf(a, w, *q);
+                    *q = nv;
+                    if (TRACK) run = fmaxf(run, nv);
+                }
+            }
+        } else {
+            // the footprint crosses an image edge: the clipped box, mirrored weights
+            const int xl = max(0, X - R), xh = min(c.W, X + R + 1), nx = xh - xl;
+            const int np = (y1 - y0) * nx;
+            for (int j0 = 0; j0 < np; j0 += 32) {
+                const int j = j0 + lane;
+                if (j < np) {
+                    const int dy = j / nx, dx = j - dy * nx;
+                    const int y = y0 + dy, x = xl + dx;
+                    const float w = reflect_weight_s(A.wt, R, y, Y, c.H) * reflect_weight_s(A.wt, R, x, X, c.W);
+                    if (!DS_IN_BOUNDS((y - ys) * Ws + x, (ye - ys) * Ws, status)) continue;
+                    float *q = buf + (y - ys) * Ws + x;
+                    const float nv = fmaf(a, w, *q);
+                    *q = nv;
+                    if (TRACK) run = fmaxf(run, nv);
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+__device__ inline void slice_zero(float *buf, int n_floats, int lane) {
+    float4 *b4 = reinterpret_cast<float4 *>(buf);
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int i = lane; i < n_floats / 4; i += 32) b4[i] = z;
+    __syncwarp();
+}
+
+// pattern / max in float32: mode 0 multiplies by the reciprocal (max * (1 / max)
+// == 1 exactly), mode 1 also returns 1 for the maximum itself, mode 2 divides
+// (a maximum of zero, infinity or NaN, as numpy does)
+__device__ __forceinline__ float slice_scale(float u, int mode, float mx, float inv) {
+    if (mode == 0) return u * inv;
+    if (mode == 1) return u == mx ? 1.f : u * inv;
+    return u / mx;
+}
+
+constexpr int SLICE_FLAG_NEG = 1, SLICE_FLAG_NAN = 2;
+
+template <bool VEC>
+__global__ void __launch_bounds__(RAS_THREADS, 4)
+raster_slice_kernel(const RasterConst c, const SliceGeom g, const int64_t *__restrict__ off,
+                    const float4 *__restrict__ xyzi, long long n_patterns, float *__restrict__ out, int32_t *status) {
+    extern __shared__ __align__(16) unsigned char ras_smem[];
+    const int R = c.R, P = g.P, SH = g.SH, nsl = g.nsl;
+    const SliceArena A = carve_slice(ras_smem, c.NS, c.T, R, g);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int H = c.H, W = c.W;
+    const size_t img = (size_t)H * W;
+    float *buf = A.buf + (size_t)warp * SH * g.Ws;
+    const unsigned lt = (1u << lane) - 1u;
+
+    for (int i = tid; i <= R; i += RAS_THREADS) A.wt[i] = c.wt[i];
+    if (g.wt2)
+        for (int j = tid; j < P * P; j += RAS_THREADS) {
+            const int dy = j / P, dx = j - dy * P;
+            A.wt2[j] = c.wt[abs(dy - R)] * c.wt[abs(dx - R)];
+        }
+
+    for (long long p = blockIdx.x; p < n_patterns; p += gridDim.x) {
+        const long long a0 = off[p];
+        const long long n_ll = off[p + 1] - a0;
+        if (n_ll > c.NS || n_ll < 0) {
+            if (tid == 0) atomicOr(status, DS_ERR_CAPACITY);
+            continue;
+        }
+        const int n = (int)n_ll;
+        int Tp = 64;
+        while (Tp < n + n / 2) Tp <<= 1;
+        const int tbits = __ffs(Tp) - 1;
+        for (int t = tid; t < Tp; t += RAS_THREADS) {
+            A.hkey[t] = -1;
+            A.hidx[t] = -1;
+        }
+        for (int s = tid; s <= nsl; s += RAS_THREADS) {
+            A.scnt[s] = 0;
+            A.sfill[s] = 0;
+        }
+        if (tid == 0) {
+            A.misc[RAS_WARPS] = 0;      // in-frame spots
+            A.misc[RAS_WARPS + 1] = 0;  // amplitude flags
+            A.misc[RAS_WARPS + 2] = 0;  // largest non-negative amplitude (float bits)
+        }
+        __syncthreads();  // also orders the weight tables before their first use
+
+        // ---- pixel coordinates, frame test, last write wins per pixel
+        int my_in = 0;
+        for (int i = tid; i < n; i += RAS_THREADS) {
+            const float4 e = xyzi[a0 + i];
+            double X, Y;
+            pixel_xy(c, e, X, Y);
+            int key = -1, sl = -1;
+            if (in_frame(c, X, Y)) {
+                ++my_in;
+                key = (int)Y * W + (int)X;
+                unsigned h = ((unsigned)key * 2654435761u) >> (32 - tbits);
+                for (int t = 0; t < Tp; ++t) {
+                    const int prev = atomicCAS(&A.hkey[h], -1, key);
+                    if (prev == -1 || prev == key) {
+                        atomicMax(&A.hidx[h], i);
+                        sl = (int)h;
+                        break;
+                    }
+                    h = (h + 1) & (unsigned)(Tp - 1);
+                }
+                if (sl < 0) key = -1;
+            }
+            A.key[i] = key;
+            A.slot[i] = sl;
+        }
+        my_in = __reduce_add_sync(FULL_MASK, my_in);
+        if (lane == 0 && my_in) atomicAdd(&A.misc[RAS_WARPS], my_in);
+        __syncthreads();
+        const int n_in = A.misc[RAS_WARPS];
+
+        // ---- ordered compaction, slice counts, amplitude flags
+        int n_alive = 0;
+        for (int c0 = 0; c0 < n; c0 += RAS_THREADS) {
+            const int i = c0 + tid;
+            bool alive = false;
+            if (i < n && A.key[i] >= 0) alive = A.hidx[A.slot[i]] == i;
+            const unsigned bal = __ballot_sync(FULL_MASK, alive);
+            if (lane == 0) A.misc[warp] = __popc(bal);
+            __syncthreads();
+            int wbase = 0, tot = 0;
+            for (int w = 0; w < RAS_WARPS; ++w) {
+                const int v = A.misc[w];
+                if (w < warp) wbase += v;
+                tot += v;
+            }
+            if (alive) {
+                const int k = n_alive + wbase + __popc(bal & lt);
+                const int key = A.key[i];
+                const int X = key % W, Y = key / W;
+                const float am = xyzi[a0 + i].w;
+                const bool edge = X - R < 0 || X + R >= W || Y - R < 0 || Y + R >= H;
+                A.sxy[k] = X | (Y << 15) | ((int)edge << 30);
+                A.amp[k] = am;
+                if (!(am >= 0.f)) atomicOr(&A.misc[RAS_WARPS + 1], am != am ? SLICE_FLAG_NAN : SLICE_FLAG_NEG);
+                else atomicMax(&A.misc[RAS_WARPS + 2], __float_as_int(am));  // non-negative floats order as ints
+                const int s0 = max(0, Y - R) / SH, s1 = min(H - 1, Y + R) / SH;
+                for (int s = s0; s <= s1; ++s) atomicAdd(&A.scnt[s], 1);
+            }
+            n_alive += tot;
+            __syncthreads();
+        }
+        const int aflags = A.misc[RAS_WARPS + 1];
+
+        // ---- slice starts: exclusive scan of the counts over nsl + 1 entries
+        {
+            const int per = (nsl + 1 + RAS_THREADS - 1) / RAS_THREADS;
+            const int s0 = tid * per, s1 = min(nsl + 1, s0 + per);
+            int sum = 0;
+            for (int s = s0; s < s1; ++s) sum += A.scnt[s];
+            const int inc = warp_inclusive_scan(sum, lane);
+            if (lane == 31) A.misc[warp] = inc;
+            __syncthreads();
+            int run = inc - sum;
+            for (int w = 0; w < warp; ++w) run += A.misc[w];
+            for (int s = s0; s < s1; ++s) {
+                A.sstart[s] = run;
+                run += A.scnt[s];
+            }
+            __syncthreads();
+        }
+
+        // ---- slice entries in spot order: warp w fills its own slices, 32 spots
+        // at a time; within a slice the lanes take consecutive places by lane
+        for (int k0 = 0; k0 < n_alive; k0 += 32) {
+            const int k = k0 + lane;
+            int t0 = 1 << 30, t1 = -(1 << 30);
+            if (k < n_alive) {
+                const int Y = (A.sxy[k] >> 15) & 0x7fff;
+                const int s0 = max(0, Y - R) / SH, s1 = min(H - 1, Y + R) / SH;
+                const int f = s0 + ((warp - s0) & 7), l = s1 - ((s1 - warp) & 7);  // owned slices in [s0, s1]
+                t0 = (f - warp) >> 3;
+                t1 = (l - warp) >> 3;
+            }
+            const int tmin = __reduce_min_sync(FULL_MASK, t0), tmax = __reduce_max_sync(FULL_MASK, t1);
+            for (int t = tmin; t <= tmax; ++t) {
+                const bool act = t0 <= t && t <= t1;
+                const unsigned bal = __ballot_sync(FULL_MASK, act);
+                if (!bal) continue;
+                const int s = warp + 8 * t;
+                const int base = A.sstart[s] + A.sfill[s];
+                if (act && DS_IN_BOUNDS(base + __popc(bal & lt), (long long)c.NS * g.span, status))
+                    A.sent[base + __popc(bal & lt)] = k;
+                __syncwarp();
+                if (lane == 0) A.sfill[s] += __popc(bal);
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+
+        // ---- the maximum (normalise).  Without negative amplitudes only the
+        // slices that can hold it are built: the centre pixel of the strongest
+        // spot is at least lower = a_max w0^2 (its other terms are >= 0, and a
+        // rounded non-negative sum never falls below a term), and no pixel of
+        // a slice exceeds its bound U = sum of a_k times the spot's largest
+        // weight (w0^2 inside the image; at an edge each axis adds at most
+        // three mirrored taps, or the whole filter, 1, when R >= the side),
+        // widened by 0.1 % for rounding.  A slice with U < lower is skipped.
+        const bool norm = c.normalize && n_in > 0;
+        float mx = 1.f;
+        if (norm) {
+            const bool readback = (aflags & SLICE_FLAG_NEG) != 0;
+            const float w00 = A.wt[0] * A.wt[0];  // the product table's centre entry
+            const float lower = __int_as_float(A.misc[RAS_WARPS + 2]) * w00;
+            const float wedge = (R < H && R < W) ? 9.f * w00 : 1.f;
+            float run = -INFINITY;
+            bool any_empty = false;
+            for (int s = warp; s < nsl; s += RAS_WARPS) {
+                const int e0 = A.sstart[s], e1 = A.sstart[s + 1];
+                if (e0 == e1) {
+                    any_empty = true;
+                    continue;
+                }
+                if (!readback) {
+                    float U = 0.f;
+                    for (int e = e0 + lane; e < e1; e += 32) {
+                        const int k = A.sent[e];
+                        U += A.amp[k] * ((A.sxy[k] >> 30) ? wedge : w00);
+                    }
+#pragma unroll
+                    for (int d = 16; d >= 1; d >>= 1) U += __shfl_xor_sync(FULL_MASK, U, d);
+                    if (U * 1.001f < lower) continue;
+                }
+                const int ys = s * SH, ye = min(H, ys + SH);
+                slice_zero(buf, (ye - ys) * g.Ws, lane);
+                if (readback) {
+                    slice_splat<false>(c, g, A, ys, ye, e0, e1, buf, lane, run, status);
+                    for (int r = 0; r < ye - ys; ++r)
+                        for (int x = lane; x < W; x += 32) run = fmaxf(run, buf[r * g.Ws + x]);
+                    __syncwarp();
+                } else {
+                    slice_splat<true>(c, g, A, ys, ye, e0, e1, buf, lane, run, status);
+                }
+            }
+            // without negative amplitudes every pixel is >= 0, uncovered ones 0
+            if (any_empty || !readback) run = fmaxf(run, 0.f);
+#pragma unroll
+            for (int d = 16; d >= 1; d >>= 1) run = fmaxf(run, __shfl_xor_sync(FULL_MASK, run, d));
+            if (lane == 0) A.wmax[warp] = run;
+            __syncthreads();
+            mx = A.wmax[0];
+            for (int w = 1; w < RAS_WARPS; ++w) mx = fmaxf(mx, A.wmax[w]);
+            if (aflags & SLICE_FLAG_NAN) mx = NAN;  // numpy's max propagates NaN
+        }
+        const float inv = 1.f / mx;
+        const int mode = !norm ? 0 : !(mx > 0.f && mx < INFINITY) ? 2 : mx * inv == 1.f ? 0 : 1;
+        const float sc_inv = norm ? inv : 1.f;
+        const float zero_val = norm ? 0.f / mx : 0.f;
+
+        // ---- the image, slice by slice
+        float *dst0 = out + (size_t)p * img;
+        for (int s = warp; s < nsl; s += RAS_WARPS) {
+            const int ys = s * SH, ye = min(H, ys + SH);
+            float *dst = dst0 + (size_t)ys * W;
+            const int e0 = A.sstart[s], e1 = A.sstart[s + 1];
+            if (e0 == e1) {
+                const int nf = (ye - ys) * W;
+                if (VEC) {
+                    const float4 z = make_float4(zero_val, zero_val, zero_val, zero_val);
+                    for (int i = lane; i < nf / 4; i += 32) st_cs(reinterpret_cast<float4 *>(dst) + i, z);
+                } else {
+                    for (int i = lane; i < nf; i += 32) st_cs1(dst + i, zero_val);
+                }
+                continue;
+            }
+            slice_zero(buf, (ye - ys) * g.Ws, lane);
+            float unused = 0.f;
+            slice_splat<false>(c, g, A, ys, ye, e0, e1, buf, lane, unused, status);
+            for (int r = 0; r < ye - ys; ++r) {
+                const float *src = buf + r * g.Ws;
+                float *row = dst + (size_t)r * W;
+                if (VEC) {
+                    for (int x = 4 * lane; x < W; x += 128) {
+                        const float4 u = *reinterpret_cast<const float4 *>(src + x);
+                        st_cs(reinterpret_cast<float4 *>(row + x),
+                              make_float4(slice_scale(u.x, mode, mx, sc_inv), slice_scale(u.y, mode, mx, sc_inv),
+                                          slice_scale(u.z, mode, mx, sc_inv), slice_scale(u.w, mode, mx, sc_inv)));
+                    }
+                } else {
+                    for (int x = lane; x < W; x += 32) st_cs1(row + x, slice_scale(src[x], mode, mx, sc_inv));
+                }
+            }
+            __syncwarp();
+        }
+        __syncthreads();  // the arena is reused by the next pattern
+    }
+}
+
+static bool slice_geometry(const ds_raster_params *p, int NS, int T, int R, SliceGeom &g, size_t &bytes) {
+    const int H = p->height, W = p->width, P = 2 * R + 1;
+    if (!p->fast || W >= (1 << 15) || H >= (1 << 15)) return false;
+    for (int SH : {8, 4, 2, 1}) {
+        g.SH = SH;
+        g.P = P;
+        g.Ws = slice_stride(W, P);
+        g.nsl = (H + SH - 1) / SH;
+        g.span = std::min(g.nsl, (P - 1 + SH - 1) / SH + 1);
+        g.mP = P > 1 ? (unsigned)((0x100000000ull + P - 1) / P) : 0u;
+        g.wt2 = P <= 31 ? 1 : 0;
+        bytes = slice_arena_bytes(NS, T, R, g);
+        if (bytes <= (size_t)RAS_SLICE_TARGET || (SH == 1 && bytes <= RAS_SMEM_LIMIT)) return true;
+    }
+    return false;
+}
+
 struct RasterPlan {
     int NS, T, grid;
-    bool one_pass;
+    bool one_pass, slice;
+    SliceGeom g;
     size_t arena, smem, scratch;
 };
 
@@ -820,13 +1275,27 @@ static ds_status raster_plan(const ds_raster_params *p, int64_t max_spots, Raste
     while (fast ? T < NS + NS / 2 : T < 2 * NS) T <<= 1;  // the kernels' per-pattern hash sizes
     P.NS = NS;
     P.T = T;
+    int dev = 0, n_sm = 0;
+    DS_CUDA_TRY(cudaGetDevice(&dev));
+    DS_CUDA_TRY(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+    size_t slice_bytes = 0;
+    P.slice = slice_geometry(p, NS, T, filter_radius(p), P.g, slice_bytes);
+    if (P.slice) {
+        P.one_pass = false;
+        P.arena = P.smem = slice_bytes;
+        P.scratch = 0;
+        int per_sm = 0;
+        for (const void *k : {(const void *)raster_slice_kernel<true>, (const void *)raster_slice_kernel<false>})
+            DS_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem));
+        DS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, raster_slice_kernel<true>, RAS_THREADS,
+                                                                  P.smem));
+        P.grid = n_sm * std::max(1, per_sm);
+        return DS_OK;
+    }
     P.one_pass = fast && p->normalize && (p->width % 4) == 0 && fast_flag_bytes(p->height, p->width) <= RAS_FLAGS_MAX;
     P.arena = fast ? fast_arena_bytes(NS, T, p->height, 2 * filter_radius(p) + 1,
                                       P.one_pass ? fast_flag_bytes(p->height, p->width) : 0)
                    : raster_arena_bytes(NS, T, p->height);
-    int dev = 0, n_sm = 0;
-    DS_CUDA_TRY(cudaGetDevice(&dev));
-    DS_CUDA_TRY(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
     if (P.arena <= RAS_SMEM_LIMIT) {
         P.smem = P.arena;
         P.scratch = 0;
@@ -940,6 +1409,13 @@ extern "C" ds_status ds_rasterize(const ds_raster_params *p, const int64_t *offs
     const float4 *x4 = reinterpret_cast<const float4 *>(xyzi);
     size_t arena = P.arena;
     long long np = n_patterns;
+    if (P.slice) {
+        SliceGeom geo = P.g;
+        void *sargs[] = {&c, &geo, const_cast<int64_t **>(&offsets), const_cast<float4 **>(&x4), &np, &out, &status};
+        const void *kern = vec ? (const void *)raster_slice_kernel<true> : (const void *)raster_slice_kernel<false>;
+        DS_CUDA_TRY(cudaLaunchKernel(kern, dim3(grid), dim3(RAS_THREADS), sargs, P.smem, s));
+        return check_launch("raster_slice_kernel");
+    }
     void *args[] = {&c, const_cast<int64_t **>(&offsets), const_cast<float4 **>(&x4), &np, &out, &g, &arena, &status};
     const void *kern = vec ? raster_kernel_ptr<true>(c.fast != 0) : raster_kernel_ptr<false>(c.fast != 0);
     DS_CUDA_TRY(cudaLaunchKernel(kern, dim3(grid), dim3(RAS_THREADS), args, P.smem, s));

@@ -897,7 +897,8 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
                         const float4 m4 = sop[o].mz;
                         const float z = fmaf(m4.x, cur.e.x, fmaf(m4.y, cur.e.y, fmaf(m4.z, cur.e.z, cur.e.w)));
                         // the row screen's test: the sign of |z| - z_half
-                        if (cur.j >= 0 && (__float_as_uint(fabsf(z) - cur.zh) >> 31))
+                        if (cur.j >= 0 && (__float_as_uint(fabsf(z) - cur.zh) >> 31) &&
+                            DS_IN_BOUNDS(o * Ws + (cur.j >> 5), OP * Ws, status))
                             atomicOr(&bitmap[o * Ws + (cur.j >> 5)], 1u << (cur.j & 31));
                     }
                 }
@@ -915,7 +916,7 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
                         const uint32_t b = __ballot_sync(FULL_MASK, hit);
                         if (lane == o) myword = b;
                     }
-                    if (lane < OP) bitmap[lane * Ws + wc] = myword;
+                    if (lane < OP && DS_IN_BOUNDS(lane * Ws + wc, O * Ws, status)) bitmap[lane * Ws + wc] = myword;
                 }
             } else {
                 constexpr bool MREG = O <= 16;  // as in the line screen
@@ -979,7 +980,8 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
 #pragma unroll
                         for (int k = 0; k < CH; ++k) {
                             const int wck = wc + k * SIM_WARPS;
-                            if (lane < OPC && wck < W) bitmap[(OPC - 1 - lane) * Ws + wck] = bits[k];
+                            if (lane < OPC && wck < W && DS_IN_BOUNDS((OPC - 1 - lane) * Ws + wck, O * Ws, status))
+                                bitmap[(OPC - 1 - lane) * Ws + wck] = bits[k];
                         }
                     }
                 };
@@ -1041,7 +1043,7 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
                         row, w0, w1, lane, wqueue,
                         [&](long long j, bool v) {
                             SpotIn in;
-                            if (v) in = load_spot<FORM>(T, j);
+                            if (v && DS_IN_BOUNDS(j, n_hkl, status)) in = load_spot<FORM>(T, j);
                             return in;
                         },
                         [&](long long j, int rk, const SpotIn &in) {
@@ -1049,8 +1051,10 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
                             double sv;
                             bool sel = eval_in<FORM, INTEG>(c, op, in, I, z, sv);
                             if (sel && I == 0.f && all_zero_drop) sel = false;
-                            my_idx[base + rk] = (int32_t)j;
-                            my_I[base + rk] = sel ? I : -1.f;
+                            if (DS_IN_BOUNDS(base + rk, stg.cap, status)) {
+                                my_idx[base + rk] = (int32_t)j;
+                                my_I[base + rk] = sel ? I : -1.f;
+                            }
                             if (sel) {
                                 ++lcnt;
                                 lmax = fmaxf(lmax, I);
@@ -1231,7 +1235,7 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
                             const int r = r0 + 32 * b + lane;
                             II[b] = -1.f;
                             jj[b] = 0;
-                            if (r < cc) {
+                            if (r < cc && DS_IN_BOUNDS(base + r, stg.cap, status)) {
                                 II[b] = b_I[base + r];
                                 jj[b] = b_idx[base + r];
                             }
@@ -1240,7 +1244,7 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
 #pragma unroll
                         for (int b = 0; b < 4; ++b) {
                             ee[b] = make_float4(0.f, 0.f, 0.f, 0.f);
-                            if (!(II[b] < 0.f)) ee[b] = T.scr[jj[b]];
+                            if (!(II[b] < 0.f) && DS_IN_BOUNDS(jj[b], PNH(bbuf), status)) ee[b] = T.scr[jj[b]];
                         }
 #pragma unroll
                         for (int b = 0; b < 4; ++b) {

@@ -31,7 +31,10 @@ enum {
     DS_ERR_CAPACITY = 4,      /* device word bit: output capacity exceeded   */
     DS_ERR_TIMEOUT = 8,       /* device word bit: a bounded wait gave up     */
     DS_ERR_UNSUPPORTED = 16,
-    DS_ERR_NONFINITE = 32     /* device word bit: non-finite input met       */
+    DS_ERR_NONFINITE = 32,    /* device word bit: non-finite input met       */
+    DS_ERR_BOUNDS = 64        /* device word bit, bounds-checked builds only
+                                 (-DDS_DEBUG_BOUNDS): an index check failed
+                                 and the access was skipped                  */
 };
 
 /* arithmetic form of a call */

@@ -299,3 +299,27 @@ def test_apply_shape_factors_rejects_bad_arguments(lib):
                                       None) == N.DS_ERR_INVALID_ARGUMENT
     assert "scratch" in lib.ds_last_error().decode()
     assert lib.ds_apply_shape_factors_scratch_bytes(100) >= 100 * 8
+
+
+def test_status_bits_mirror_the_header_and_decode():
+    """Every DS_ERR_* of include/diffsims_gb300.h has its value in _native,
+    and the device-word bits raise their own errors (DS_ERR_BOUNDS comes from
+    the bounds-checked build only)."""
+    from diffsims_gb300 import _native as N
+    text = (ROOT / "include" / "diffsims_gb300.h").read_text()
+    found = dict((k, int(v)) for k, v in re.findall(r"\b(DS_ERR_[A-Z_]+)\s*=\s*(\d+)", text))
+    assert found and found["DS_ERR_BOUNDS"] == 64
+    for k, v in found.items():
+        assert getattr(N, k) == v, k
+    assert N.check_status_value(0, "x") == 0
+    assert N.check_status_value(N.DS_ERR_CAPACITY, "x", allow=N.DS_ERR_CAPACITY) == N.DS_ERR_CAPACITY
+    with pytest.raises(N.NativeError, match="bounds-checked"):
+        N.check_status_value(N.DS_ERR_BOUNDS, "x")
+    with pytest.raises(N.NativeError, match="timed out"):
+        N.check_status_value(N.DS_ERR_TIMEOUT | N.DS_ERR_BOUNDS, "x")
+
+
+def test_bounds_checked_build_is_a_separate_library():
+    from diffsims_gb300 import _build, _native as N
+    assert _build.LIB_DEBUG.name == "libdiffsims_gb300_debug.so" and _build.LIB_DEBUG != _build.LIB
+    assert N._LIB_PATH.name == ("libdiffsims_gb300_debug.so" if N.DEBUG_BOUNDS else "libdiffsims_gb300.so")
