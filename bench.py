@@ -284,6 +284,23 @@ def fp32_peak_tflops(torch, lib, N):
     return best
 
 
+def fp32_nominal_tflops(torch):
+    """Nominal FP32 FMA peak of this GPU: SMs x 128 FP32 lanes x 2 FLOP x the
+    maximum SM clock (2.07 GHz on GB300: 152 x 128 x 2 x 2.07e9 = 80.5
+    TFLOP/s), stated beside the measured figure."""
+    n_sm = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = 2070.0
+    try:
+        import subprocess
+        out = subprocess.run(["nvidia-smi", "--query-gpu=clocks.max.sm", "--format=csv,noheader,nounits", "-i", "0"],
+                             capture_output=True, text=True, timeout=20).stdout.strip().splitlines()
+        if out:
+            mhz = float(out[0])
+    except (OSError, ValueError, subprocess.SubprocessError):
+        pass
+    return {"tflops": n_sm * 128 * 2 * mhz * 1e6 / 1e12, "basis": f"{n_sm} SMs x 128 FP32 lanes x 2 FLOP x {mhz:.0f} MHz"}
+
+
 def _hbm_peak():
     """(GB/s, source) of the HBM copy bandwidth: MEASURED_PEAKS.json when
     present, else the fallback figure."""
@@ -501,6 +518,7 @@ def run_gpu(args):
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
                      "frac": achieved / peak32, "traffic": traffic, "kernel": "simulate_kernel",
                      "kernel_ms": kms, "peak_source": "measured by bench.py FMA probe (ds_probe_fp32_fma)",
+                     "peak_nominal": fp32_nominal_tflops(torch),
                      "hbm": {"achieved_gbs": bytes_alg / (kms * 1e-3) / 1e9, "peak_gbs": hbm_peak,
                              "frac": bytes_alg / (kms * 1e-3) / 1e9 / hbm_peak,
                              "peak_source": hbm_src}},
@@ -803,7 +821,7 @@ def run_batch(args, torch, dev):
     hbm_peak = _hbm_peak()[0]
     roof = {"bound": "fp32", "achieved": flops, "peak": peak32, "unit": "TFLOP/s", "frac": flops / peak32,
             "pairs": pairs, "kernel": "simulate_batch_kernel", "kernel_ms": graph_ms,
-            "peak_source": "measured by bench.py FMA probe (ds_probe_fp32_fma)",
+            "peak_source": "measured by bench.py FMA probe (ds_probe_fp32_fma)", "peak_nominal": fp32_nominal_tflops(torch),
             "hbm": {"achieved_gbs": bytes_alg / (graph_ms * 1e-3) / 1e9, "peak_gbs": hbm_peak,
                     "frac": bytes_alg / (graph_ms * 1e-3) / 1e9 / hbm_peak}}
     cpu = None
@@ -820,7 +838,7 @@ def run_batch(args, torch, dev):
     return {"metric": "orientation patterns/s (32 uneven phases, one launch)", "value": n_pat / (graph_ms * 1e-3),
             "unit": "patterns/s", "ms_per_step": graph_ms, "patterns_per_step": n_pat, "spots_per_step": int(n_spots),
             "per_phase_launches_ms": seq_ms, "speedup_over_per_phase_launches": seq_ms / graph_ms,
-            "orient_tile": batch.orient_tile, "stage_cap": batch.stage_cap,
+            "orient_tile": batch.orient_tile, "stage_cap": batch.stage_cap, "refine_parts": batch.refine_parts,
             "autotuner_ms": AUTOTUNER.timings.get(key),
             "n_hkl_range": [min(t.n for t in tables), max(t.n for t in tables)],
             "orientations_range": [min(int(q.shape[0]) for q in qs), max(int(q.shape[0]) for q in qs)],

@@ -70,7 +70,8 @@ class ds_sim_params(C.Structure):
     _fields_ = [("k0", C.c_double), ("max_excitation_error", C.c_double), ("shape_width", C.c_double),
                 ("precession_angle", C.c_double), ("minimum_intensity", C.c_double),
                 ("minima_number", C.c_double), ("shape_model", C.c_int32), ("precession_mode", C.c_int32),
-                ("form", C.c_int32), ("orient_tile", C.c_int32), ("stage_cap", C.c_int32), ("screen", C.c_int32)]
+                ("form", C.c_int32), ("orient_tile", C.c_int32), ("stage_cap", C.c_int32), ("screen", C.c_int32),
+                ("refine_parts", C.c_int32), ("_reserved", C.c_int32)]
 
 
 class ds_phase_table(C.Structure):
@@ -95,6 +96,7 @@ class ds_raster_params(C.Structure):
 
 
 assert C.sizeof(ds_atom) == 48
+assert C.sizeof(ds_sim_params) == 80
 
 
 class NativeError(RuntimeError):

@@ -522,6 +522,7 @@ extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t
     c.Ws = P.Ws;
     c.n_orient = n_orient;
     c.line_mode = P.line_mode;
+    c.parts_log2 = refine_parts_log2(p, P.O);
     c.n_tiles = P.n_tiles;
     c.capacity = out->capacity;
 

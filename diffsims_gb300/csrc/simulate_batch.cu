@@ -172,6 +172,7 @@ extern "C" ds_status ds_simulate_batch(const ds_sim_params *p, const ds_batch_ph
     c.capacity = out->capacity;
     c.line_mode = 0;
     c.brick_mode = P.brick_mode;
+    c.parts_log2 = refine_parts_log2(p, P.O);
 
     PhaseBatch B;
     B.n = n_phases;

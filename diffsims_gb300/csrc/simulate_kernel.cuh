@@ -45,11 +45,7 @@ constexpr float SIM_TAU_SF = 1e-6f;    // |s| this close to a zero of the shape 
 constexpr float SIM_TAU_PREC = 2e-7f;  // precession band margin below this -> FP64 decision
 constexpr float SIM_U_MAX = 0.01f;     // (r / k0)^2 above this -> FP64 (series not used)
 constexpr int SIM_MAX_O = 32;
-// tuning knobs (compile time): word ranges per orientation in the refine and
-// write passes, and chunks screened per step in phase 1
-#ifndef DS_SIM_PARTS
-#define DS_SIM_PARTS 2
-#endif
+// tuning knob (compile time): chunks screened per step in phase 1
 #ifndef DS_SIM_SCREEN_CHUNKS
 #define DS_SIM_SCREEN_CHUNKS 2
 #endif
@@ -71,6 +67,7 @@ struct SimConst {
     float int_step_f, mw_f;
     float int_tau;                  // precession average: FP32 result below this -> FP64
     int mask_on, zero_drop;         // thr > 0, thr >= 0 (the FP64 compares done once, on the host)
+    int parts_log2;                 // refine / write units: 2^parts_log2 word ranges per orientation (<= 8)
     float thr_up;                   // >= thr, with margin: FP32 pre-check of I <= max * thr
     long long n_hkl, n_orient, n_tiles, capacity;
 };
@@ -694,8 +691,9 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
     constexpr int ACC_STRIDE = acc_stride(O);
     constexpr int ACC_TILE_TOTAL = O * ACC_WORDS;
     // phases 2-3 run over units (orientation, part): NP word ranges per
-    // orientation, taken by warps from a shared counter for load balance
-    constexpr int NP = O >= 2 ? DS_SIM_PARTS : 8;
+    // orientation (reflections per unit: the table over NP), taken by warps
+    // from a shared counter for load balance; NP is a launch parameter
+    const int NPL = c.parts_log2, NP = 1 << NPL;
     const bool all_zero_drop = c.zero_drop != 0;
     const unsigned lanemask_lt = (1u << lane) - 1u;
     auto part_range = [&](int Wp, int p, int &w0, int &w1) {
@@ -992,7 +990,7 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
 
             // ---------------- candidate counts per unit and staging bases
             for (int u = warp; u < n_units; u += SIM_WARPS) {
-                const int o = u / NP, p = u % NP;
+                const int o = u >> NPL, p = u & (NP - 1);
                 int w0, w1;
                 part_range(W, p, w0, w1);
                 const uint32_t *row = bitmap + o * Ws;
@@ -1006,20 +1004,22 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
             if (warp == 0) {
                 // staging bases: the units in (orientation, part) order, the
                 // longest prefix that fits the staging is staged
-                constexpr int UPL = (O * NP + 31) / 32;  // units per lane
-                long long cc[UPL], sum = 0;
+                constexpr int UPL_MAX = (O * 8 + 31) / 32;  // units per lane at NP = 8
+                const int UPL = (O * NP + 31) / 32;
+                long long cc[UPL_MAX], sum = 0;
 #pragma unroll
-                for (int i = 0; i < UPL; ++i) {
+                for (int i = 0; i < UPL_MAX; ++i) {
                     const int u = lane * UPL + i;
-                    cc[i] = u < n_units ? (long long)acc[(u / NP) * ACC_WORDS + ACC_CCNT0 + u % NP] : 0ll;
+                    cc[i] = (i < UPL && u < n_units) ? (long long)acc[(u >> NPL) * ACC_WORDS + ACC_CCNT0 + (u & (NP - 1))]
+                                                     : 0ll;
                     sum += cc[i];
                 }
                 long long run = warp_exclusive_scan_ll(sum, lane);
 #pragma unroll
-                for (int i = 0; i < UPL; ++i) {
+                for (int i = 0; i < UPL_MAX; ++i) {
                     const int u = lane * UPL + i;
-                    if (u < n_units)
-                        acc[(u / NP) * ACC_WORDS + ACC_CBASE0 + u % NP] =
+                    if (i < UPL && u < n_units)
+                        acc[(u >> NPL) * ACC_WORDS + ACC_CBASE0 + (u & (NP - 1))] =
                             run + cc[i] <= stg.cap ? (unsigned long long)run : NO_STAGE;
                     run += cc[i];
                 }
@@ -1028,7 +1028,7 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
 
             // ---------------- phase 2: refine, intensities, per-orientation max
             for (int u = next_unit(0); u < n_units; u = next_unit(0)) {
-                const int o = u / NP, p = u % NP;
+                const int o = u >> NPL, p = u & (NP - 1);
                 int w0, w1;
                 part_range(W, p, w0, w1);
                 uint32_t *row = bitmap + o * Ws;
@@ -1119,7 +1119,7 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
             }
             if (need_mask) {
                 for (int u = next_unit(1); u < n_units; u = next_unit(1)) {
-                    const int o = u / NP, p = u % NP;
+                    const int o = u >> NPL, p = u & (NP - 1);
                     const float mx = __uint_as_float((unsigned)acc[o * ACC_WORDS + ACC_MAXI]);
                     const float mnp = __uint_as_float((unsigned)acc[o * ACC_WORDS + ACC_MINPOS]);
                     if (!((double)mnp <= (double)mx * c.thr)) continue;
@@ -1213,7 +1213,7 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
             for (int o = tid; o < bn_valid; o += SIM_THREADS)
                 offsets[bo_out + o] = prefix + (long long)bacc[o * ACC_WORDS + ACC_OFF];
             for (int u = next_unit(counter); u < bn_valid * NP; u = next_unit(counter)) {
-                const int o = u / NP, p = u % NP;
+                const int o = u >> NPL, p = u & (NP - 1);
                 int w0, w1;
                 part_range(W, p, w0, w1);
                 const uint32_t *row = bitmap + o * Ws;
@@ -1362,14 +1362,25 @@ inline ds_status validate_params(const ds_sim_params *p, const char *who) {
                    p->orient_tile == 8 || p->orient_tile == 16 || p->orient_tile == 32,
                w + ": orient_tile must be 0, 1, 2, 4, 8, 16 or 32");
     DS_REQUIRE(p->stage_cap >= 0, w + ": stage_cap < 0");
+    DS_REQUIRE(p->refine_parts == 0 || p->refine_parts == 1 || p->refine_parts == 2 || p->refine_parts == 4 ||
+                   p->refine_parts == 8,
+               w + ": refine_parts must be 0, 1, 2, 4 or 8");
     DS_REQUIRE(p->precession_mode == DS_PRECESSION_NONE || p->precession_angle > 0,
                w + ": precession mode needs a positive angle");
 
     return DS_OK;
 }
 
+// log2 of the refine / write units per orientation: the caller's choice, or
+// two per orientation (eight for single-orientation tiles, so the units still
+// fill the CTA's warps).
+inline int refine_parts_log2(const ds_sim_params *p, int O) {
+    const int parts = p->refine_parts > 0 ? p->refine_parts : (O >= 2 ? 2 : 8);
+    return parts >= 8 ? 3 : parts >= 4 ? 2 : parts >= 2 ? 1 : 0;
+}
+
 // The kernel constants of one phase; the per-launch fields (O, W, Ws,
-// n_orient, n_tiles, capacity, line_mode) are set by the caller.
+// n_orient, n_tiles, capacity, line_mode, parts_log2) are set by the caller.
 inline void fill_const(const ds_sim_params *p, const ds_phase_table *t, SimConst &c) {
     c.k0 = p->k0;
     c.eps = p->max_excitation_error;
@@ -1433,6 +1444,7 @@ inline void fill_const(const ds_sim_params *p, const ds_phase_table *t, SimConst
     c.n_orient = 0;
     c.line_mode = 0;
     c.brick_mode = 0;
+    c.parts_log2 = 1;
     c.n_tiles = 0;
     c.capacity = 0;
 }

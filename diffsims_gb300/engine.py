@@ -175,12 +175,13 @@ class SimSettings:
     orient_tile: int = 0
     stage_cap: int = 0
     screen: str = "auto"
+    refine_parts: int = 0   # word ranges per orientation in the refine / write passes (0: library choice)
 
     def cstruct(self) -> N.ds_sim_params:
         return N.ds_sim_params(self.k0, self.max_excitation_error, self.shape_width, self.precession_angle_rad,
                                self.minimum_intensity, self.minima_number, N.DS_SHAPE[self.shape_model],
                                self.precession_mode, FORMS[self.form], self.orient_tile, self.stage_cap,
-                               N.DS_SCREEN[self.screen])
+                               N.DS_SCREEN[self.screen], self.refine_parts, 0)
 
 
 class PhaseSpots:
@@ -805,6 +806,7 @@ class PhaseBatch:
                         for g in self.groups]
         self.graph = None
         self.stage_cap = int(settings.stage_cap)
+        self.refine_parts = int(settings.refine_parts)
         self.orient_tile = 0
         if orient_tile is None:
             orient_tile = (autotuner or AUTOTUNER).tile_for(self)
@@ -823,6 +825,8 @@ class PhaseBatch:
         p = self.settings.cstruct()
         p.orient_tile = int(self.orient_tile if orient_tile is None else orient_tile)
         p.stage_cap = int(self.stage_cap)
+        if self.refine_parts:
+            p.refine_parts = int(self.refine_parts)
         return p
 
     def _plan(self, capacity=None):
@@ -909,16 +913,20 @@ class Autotuner:
     """Picks the tile shape of a batched launch by timing the feasible
     candidates on the batch itself (CUDA events, best of a few launches):
     orientations per tile (the largest any phase may use; bigger tables get
-    smaller tiles so their bitmap fits shared memory) and the per-CTA
-    candidate staging (screened reflections held per tile before the ordered
-    writes).  Remembers the choice per problem class (phases, orientations
-    and table sizes in powers of two, shape model, precession, form); with a
-    ``path`` (or the environment variable ``DS_AUTOTUNE_CACHE``) the choices
-    also persist in a JSON file keyed by GPU name, so a later process on the
-    same kind of GPU skips the timing runs."""
+    smaller tiles so their bitmap fits shared memory), the per-CTA candidate
+    staging (screened reflections held per tile before the ordered writes),
+    then, at the best of those, the reflections per work unit of the refine
+    and write passes (each orientation's candidate bitmap cut into 1, 2, 4 or
+    8 word ranges that the CTA's warps take from a shared counter).
+    Remembers the choice per problem class (phases, orientations and table
+    sizes in powers of two, shape model, precession, form); with a ``path``
+    (or the environment variable ``DS_AUTOTUNE_CACHE``) the choices also
+    persist in a JSON file keyed by GPU name, so a later process on the same
+    kind of GPU skips the timing runs."""
 
     TILES = (4, 8, 16, 32)
     STAGE_PER_ORIENT = (384, 1536, 4096)  # staging capacity = tile x this
+    PARTS = (1, 2, 4, 8)                  # word ranges per orientation (refine / write units)
     CANDIDATES = TILES
 
     def __init__(self, repeats=3, path=None):
@@ -940,18 +948,22 @@ class Autotuner:
             return {}
 
     def lookup(self, device_name: str, k):
-        """A stored (orient_tile, stage_cap) for this GPU and problem class, or None."""
+        """A stored (orient_tile, stage_cap, refine_parts) for this GPU and
+        problem class, or None (entries without the parts read as 0: the
+        library's choice)."""
         if not self.path:
             return None
         v = self._load().get(device_name, {}).get(self._key_str(k))
-        return (int(v[0]), int(v[1])) if isinstance(v, list) and len(v) == 2 else None
+        if not isinstance(v, list) or len(v) not in (2, 3):
+            return None
+        return (int(v[0]), int(v[1]), int(v[2]) if len(v) == 3 else 0)
 
     def store(self, device_name: str, k, choice):
         """Add one choice to the file (read, update, write a temporary file, rename)."""
         if not self.path:
             return
         data = self._load()
-        data.setdefault(device_name, {})[self._key_str(k)] = [int(choice[0]), int(choice[1])]
+        data.setdefault(device_name, {})[self._key_str(k)] = [int(v) for v in choice]
         tmp = f"{self.path}.{os.getpid()}.tmp"
         with open(tmp, "w") as f:
             json.dump(data, f, indent=1, sort_keys=True)
@@ -965,7 +977,7 @@ class Autotuner:
                 s.shape_model, int(s.precession_mode), s.form)
 
     def tune(self, batch: "PhaseBatch"):
-        """(orient_tile, stage_cap) for this batch (cached per class)."""
+        """(orient_tile, stage_cap, refine_parts) for this batch (cached per class)."""
         k = self.key(batch)
         if k in self.cache:
             return self.cache[k]
@@ -979,30 +991,49 @@ class Autotuner:
         integ = batch.settings.precession_mode == N.DS_PRECESSION_INTEGRAL
         tiles = [c for c in self.TILES if c <= (8 if fp64 else 16 if integ else 32)]
         best, best_ms, times = None, None, {}
+
+        def trial(c, sc, parts):
+            batch.orient_tile, batch.stage_cap, batch.refine_parts = c, sc, parts
+            p = batch.cparams()
+            if any(lib.ds_simulate_batch_scratch_bytes(p, it, len(it)) == 0 for it in batch._items):
+                return None  # infeasible (tile does not fit shared memory)
+            try:
+                batch._plan()
+                batch.run()  # sizes the outputs, checks the status
+            except (ValueError, N.NativeError):
+                return None
+            ms = []
+            for _ in range(self.repeats):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                batch._launch()
+                e1.record()
+                e1.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            return min(ms)
+
         for c in tiles:
             for sc in (c * spo for spo in self.STAGE_PER_ORIENT):
-                batch.orient_tile, batch.stage_cap = c, sc
-                p = batch.cparams()
-                if any(lib.ds_simulate_batch_scratch_bytes(p, it, len(it)) == 0 for it in batch._items):
-                    continue  # infeasible (tile does not fit shared memory)
-                try:
-                    batch._plan()
-                    batch.run()  # sizes the outputs, checks the status
-                except (ValueError, N.NativeError):
+                t = trial(c, sc, 0)
+                if t is None:
                     continue
-                ms = []
-                for _ in range(self.repeats):
-                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                    e0.record()
-                    batch._launch()
-                    e1.record()
-                    e1.synchronize()
-                    ms.append(e0.elapsed_time(e1))
-                times[f"tile{c}_stage{sc}"] = min(ms)
-                if best_ms is None or min(ms) < best_ms:
-                    best, best_ms = (c, sc), min(ms)
+                times[f"tile{c}_stage{sc}"] = t
+                if best_ms is None or t < best_ms:
+                    best, best_ms = (c, sc, 0), t
+        if best is not None:
+            c, sc, _ = best
+            default_parts = 2 if c >= 2 else 8
+            for parts in self.PARTS:
+                if parts == default_parts:
+                    continue
+                t = trial(c, sc, parts)
+                if t is None:
+                    continue
+                times[f"tile{c}_stage{sc}_parts{parts}"] = t
+                if t < best_ms:
+                    best, best_ms = (c, sc, parts), t
         if best is None:
-            best = (4, 0)
+            best = (4, 0, 0)
         self.cache[k] = best
         self.timings[k] = times
         if self.path and times:
@@ -1010,8 +1041,9 @@ class Autotuner:
         return best
 
     def tile_for(self, batch: "PhaseBatch") -> int:
-        tile, stage = self.tune(batch)
+        tile, stage, parts = self.tune(batch)
         batch.stage_cap = stage
+        batch.refine_parts = parts
         return tile
 
 

@@ -172,6 +172,11 @@ typedef struct {
     int32_t orient_tile;         /* orientations per CTA (0 = library choice)       */
     int32_t stage_cap;           /* staged candidates per CTA (0 = library choice)  */
     int32_t screen;              /* DS_SCREEN_* (0 = library choice)                */
+    int32_t refine_parts;        /* reflections per work unit of the refine and
+                                    write passes: each orientation's candidate
+                                    bitmap is cut into this many word ranges
+                                    (1, 2, 4 or 8; 0 = library choice)            */
+    int32_t _reserved;           /* 0                                               */
 } ds_sim_params;
 
 /* One phase's candidate table (device arrays of n_hkl rows, in reference order). */

@@ -121,10 +121,37 @@ def test_autotuner_picks_and_caches():
     key = Autotuner.key(batch)
     assert batch.orient_tile in Autotuner.TILES
     assert batch.stage_cap in [batch.orient_tile * s for s in Autotuner.STAGE_PER_ORIENT]
-    assert tuner.cache[key] == (batch.orient_tile, batch.stage_cap) and tuner.timings[key]
+    assert batch.refine_parts in (0,) + Autotuner.PARTS
+    assert tuner.cache[key] == (batch.orient_tile, batch.stage_cap, batch.refine_parts) and tuner.timings[key]
+    assert any("_parts" in name for name in tuner.timings[key])  # the reflections-per-unit sweep ran
     batch.run()
     again = PhaseBatch(tables, qs, settings, p.reciprocal_radius, autotuner=tuner)
-    assert (again.orient_tile, again.stage_cap) == (batch.orient_tile, batch.stage_cap)
+    assert (again.orient_tile, again.stage_cap, again.refine_parts) == \
+        (batch.orient_tile, batch.stage_cap, batch.refine_parts)
+
+
+@pytest.mark.parametrize("parts", [1, 4, 8])
+def test_refine_parts_give_identical_spots(parts):
+    """The reflections per refine / write unit change the work split, not
+    the result: single-phase and batched launches equal the default split."""
+    import dataclasses
+    import torch
+    from diffsims_gb300.engine import PhaseBatch, SpotBuffers, simulate_phase
+    dev = torch.device("cuda", 0)
+    p = ok.SimParams(accelerating_voltage=200, reciprocal_radius=1.2, max_excitation_error=0.015,
+                     shape_factor_model="sinc")
+    settings = pu.generator_for(p).settings(p.max_excitation_error)
+    other = dataclasses.replace(settings, refine_parts=parts)
+    tables, qs = _phase_set(torch, dev, p, SPECS)
+    for t, q in zip(tables, qs):
+        a = simulate_phase(t, q, settings, p.reciprocal_radius, SpotBuffers(dev))
+        b = simulate_phase(t, q, other, p.reciprocal_radius, SpotBuffers(dev))
+        _same(a, b)
+    ba = PhaseBatch(tables, qs, settings, p.reciprocal_radius, orient_tile=8).run()
+    bb = PhaseBatch(tables, qs, other, p.reciprocal_radius, orient_tile=8).run()
+    assert bb.refine_parts == parts
+    for a, b in zip(ba.spots(), bb.spots()):
+        _same(a, b)
 
 
 def test_more_phases_than_one_launch_holds():

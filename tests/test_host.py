@@ -238,13 +238,19 @@ def test_autotuner_disk_cache(tmp_path, monkeypatch):
     path = tmp_path / "tiles.json"
     a = Autotuner(path=str(path))
     assert a.lookup("GB300", k) is None
-    a.store("GB300", k, (32, 12288))
-    a.store("GB300", (1, 2, 3, "linear", 2, "fp64"), (8, 3072))
-    a.store("Other GPU", k, (8, 3072))
+    a.store("GB300", k, (32, 12288, 4))
+    a.store("GB300", (1, 2, 3, "linear", 2, "fp64"), (8, 3072, 0))
+    a.store("Other GPU", k, (8, 3072, 1))
     b = Autotuner(path=str(path))
-    assert b.lookup("GB300", k) == (32, 12288)
-    assert b.lookup("Other GPU", k) == (8, 3072)
-    assert b.lookup("GB300", (1, 2, 3, "linear", 2, "fp64")) == (8, 3072)
+    assert b.lookup("GB300", k) == (32, 12288, 4)
+    assert b.lookup("Other GPU", k) == (8, 3072, 1)
+    assert b.lookup("GB300", (1, 2, 3, "linear", 2, "fp64")) == (8, 3072, 0)
+    # an entry written before the refine parts were tuned reads as the library's choice
+    import json
+    data = json.loads(path.read_text())
+    data["GB300"][Autotuner._key_str(k)] = [16, 6144]
+    path.write_text(json.dumps(data))
+    assert Autotuner(path=str(path)).lookup("GB300", k) == (16, 6144, 0)
     path.write_text("not json")
     assert Autotuner(path=str(path)).lookup("GB300", k) is None  # a damaged file is ignored
 
@@ -323,3 +329,23 @@ def test_bounds_checked_build_is_a_separate_library():
     from diffsims_gb300 import _build, _native as N
     assert _build.LIB_DEBUG.name == "libdiffsims_gb300_debug.so" and _build.LIB_DEBUG != _build.LIB
     assert N._LIB_PATH.name == ("libdiffsims_gb300_debug.so" if N.DEBUG_BOUNDS else "libdiffsims_gb300.so")
+
+
+def test_refine_parts_is_validated(lib):
+    """refine_parts (reflections per refine / write unit) travels in the
+    params struct; values other than 0, 1, 2, 4 and 8 are rejected with a
+    message before any CUDA call."""
+    import ctypes as C
+    from diffsims_gb300 import _native as N
+    from diffsims_gb300.engine import SimSettings
+    for parts in (0, 1, 2, 4, 8):
+        assert SimSettings(39.87, 0.02, 0.02, "lorentzian", refine_parts=parts).cstruct().refine_parts == parts
+    t = N.ds_phase_table()
+    t.n_hkl = 0
+    fake = C.c_void_p(16)
+    out = N.ds_spots(fake, fake, fake, 0, fake, None)
+    for parts in (3, 16, -1):
+        p = SimSettings(39.87, 0.02, 0.02, "lorentzian", refine_parts=parts).cstruct()
+        assert lib.ds_simulate(p, t, fake, 1, out, fake, 1 << 20, fake, None) == N.DS_ERR_INVALID_ARGUMENT
+        assert "refine_parts" in lib.ds_last_error().decode()
+        assert lib.ds_simulate_batch(p, None, 0, out, fake, 1 << 20, fake, None) == N.DS_ERR_INVALID_ARGUMENT
