@@ -107,7 +107,7 @@ def test_settings_mapping():
 def test_packed_atoms_layout():
     from diffsims_gb300 import _native as N
     assert ctypes.sizeof(N.ds_atom) == 48
-    assert ctypes.sizeof(N.ds_sim_params) == 6 * 8 + 6 * 4
+    assert ctypes.sizeof(N.ds_sim_params) == 6 * 8 + 8 * 4
     assert N.ds_phase_table.recip.offset % 8 == 0
 
 
