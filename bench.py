@@ -434,13 +434,15 @@ def run_gpu(args):
     e2e_value = n_o / (statistics.mean(e2e_ms) * 1e-3)
     breakdown = {k: statistics.mean(t[k] for t in e2e_split) for k in e2e_split[0] if k != "chunks"}
     breakdown["chunks"] = e2e_split[0].get("chunks")
-    breakdown["d2h_floor_ms_at_copy_rate"] = d2h / (breakdown["copy_span_ms"] * 1e-3) / 1e9 if breakdown.get(
+    breakdown["d2h_bytes"] = int(d2h)
+    breakdown["copy_span_gbs"] = d2h / (breakdown["copy_span_ms"] * 1e-3) / 1e9 if breakdown.get(
         "copy_span_ms") else None
     breakdown["pinned_pool_bytes"] = gen._host_pool.allocated_bytes
     breakdown["note"] = ("host ms per call: table (enumeration + structure factors, one count read), quaternion "
                          "upload, launch set-up, waits for chunk counts, pinned-pool allocation (0 once warm), "
                          "the wait in host() and its offsets fix-up; device ms from CUDA events: the chunks' span "
-                         "and the copies' span; d2h_floor_ms_at_copy_rate is the copy rate in GB/s")
+                         "and the copies' span; copy_span_gbs = the spots' bytes over the copies' span (the device-to-host "
+                         "rate the call achieved)")
 
     # ---- roofline of the dominant kernel (FP32 issue-bound screen)
     peak32 = fp32_peak_tflops(torch, lib, N)
