@@ -43,6 +43,7 @@ struct RasterConst {
     int one_pass;       // fast + normalise: build each covered row once (flags below)
     int NS, T;          // arena capacity in spots, hash slots (power of two >= 2 NS)
     double cal, cx, cy, ca, sa, mf, snap;
+    float icf, caf, saf, mff, cxf, cyf, snapf;  // FP32 copies (1 / cal rounded) for the cell pre-check
     double pref, exp_pref, clip;
     float wt[RAS_MAX_R + 1];  // fast: filter weights w[|d|], d = 0..R
 };
@@ -113,6 +114,34 @@ __device__ inline void pixel_xy(const RasterConst &c, float4 e, double &X, doubl
 
 __device__ inline bool in_frame(const RasterConst &c, double X, double Y) {
     return X >= 0.0 && X < (double)c.W && Y >= 0.0 && Y < (double)c.H;
+}
+
+// Whole-pixel cell (ix, iy) of one spot and the frame test, as pixel_xy and
+// in_frame give them in FP64 (fast mode needs nothing else).  The same
+// arithmetic in FP32 is within E = 4 * 2^-23 (|u| + |v| + |c| + |X|) + 1e-6 px
+// of the FP64 X (the rounding of 1 / cal, u, v, cos, sin and the two FMAs,
+// with a factor of two to spare); when both FP32 coordinates lie farther than
+// E plus the snap window from every pixel edge, their floors are the FP64
+// floors (and no snapping applies), else the FP64 path decides.  Non-finite
+// or huge coordinates fail the test and take the FP64 path.
+__device__ inline bool pixel_cell(const RasterConst &c, float4 e, int &ix, int &iy) {
+    const float u = e.x * c.icf, v = c.mff * (e.y * c.icf);
+    const float Xf = fmaf(u, c.caf, fmaf(-v, c.saf, c.cxf));
+    const float Yf = fmaf(v, c.caf, fmaf(u, c.saf, c.cyf));
+    const float ex = 4.77e-7f * (fabsf(u) + fabsf(v) + fabsf(c.cxf) + fabsf(Xf)) + 1e-6f + c.snapf;
+    const float ey = 4.77e-7f * (fabsf(u) + fabsf(v) + fabsf(c.cyf) + fabsf(Yf)) + 1e-6f + c.snapf;
+    const float fx = Xf - floorf(Xf), fy = Yf - floorf(Yf);
+    if (fx > ex && fx < 1.f - ex && fy > ey && fy < 1.f - ey) {
+        ix = (int)floorf(Xf);
+        iy = (int)floorf(Yf);
+        return ix >= 0 && ix < c.W && iy >= 0 && iy < c.H;
+    }
+    double X, Y;
+    pixel_xy(c, e, X, Y);
+    if (!in_frame(c, X, Y)) return false;
+    ix = (int)X;
+    iy = (int)Y;
+    return true;
 }
 
 // Sub-pixel mode: the clip radius of a spot (NaN: the spot is skipped),
@@ -545,12 +574,11 @@ raster_fast_kernel(const RasterConst c, const int64_t *__restrict__ off, const f
         int my_in = 0;
         for (int i = tid; i < n; i += RAS_THREADS) {
             const float4 e = xyzi[a0 + i];
-            double X, Y;
-            pixel_xy(c, e, X, Y);
+            int ix, iy;
             int key = -1, sl = -1;
-            if (in_frame(c, X, Y)) {
+            if (pixel_cell(c, e, ix, iy)) {
                 ++my_in;
-                key = (int)Y * W + (int)X;
+                key = iy * W + ix;
                 // open addressing; Tp >= 1.5 n slots, so a free slot is always found
                 unsigned h = ((unsigned)key * 2654435761u) >> (32 - tbits);
                 for (int t = 0; t < Tp; ++t) {
@@ -1030,12 +1058,11 @@ raster_slice_kernel(const RasterConst c, const SliceGeom g, const int64_t *__res
         int my_in = 0;
         for (int i = tid; i < n; i += RAS_THREADS) {
             const float4 e = xyzi[a0 + i];
-            double X, Y;
-            pixel_xy(c, e, X, Y);
+            int ix, iy;
             int key = -1, sl = -1;
-            if (in_frame(c, X, Y)) {
+            if (pixel_cell(c, e, ix, iy)) {
                 ++my_in;
-                key = (int)Y * W + (int)X;
+                key = iy * W + ix;
                 unsigned h = ((unsigned)key * 2654435761u) >> (32 - tbits);
                 for (int t = 0; t < Tp; ++t) {
                     const int prev = atomicCAS(&A.hkey[h], -1, key);
@@ -1384,6 +1411,13 @@ extern "C" ds_status ds_rasterize(const ds_raster_params *p, const int64_t *offs
     c.sa = sin(th);
     c.mf = p->mirrored ? -1.0 : 1.0;
     c.snap = p->pixel_snap;
+    c.icf = (float)(1.0 / c.cal);
+    c.caf = (float)c.ca;
+    c.saf = (float)c.sa;
+    c.mff = (float)c.mf;
+    c.cxf = (float)c.cx;
+    c.cyf = (float)c.cy;
+    c.snapf = (float)c.snap;
     c.clip = p->clip_threshold;
     c.pref = 1.0 / (2.0 * PI * p->sigma * p->sigma);
     c.exp_pref = -1.0 / (2.0 * p->sigma * p->sigma);

@@ -697,8 +697,8 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
     const bool all_zero_drop = c.zero_drop != 0;
     const unsigned lanemask_lt = (1u << lane) - 1u;
     auto part_range = [&](int Wp, int p, int &w0, int &w1) {
-        w0 = (int)(((long long)Wp * p) / NP);
-        w1 = (int)(((long long)Wp * (p + 1)) / NP);
+        w0 = (int)(((long long)Wp * p) >> NPL);
+        w1 = (int)(((long long)Wp * (p + 1)) >> NPL);
     };
     // the phase constants of pipeline buffer b (one phase without MULTI)
     auto PW = [&](int b) -> int { return MULTI ? s_ph[b].W : c.W; };

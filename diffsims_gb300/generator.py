@@ -105,6 +105,8 @@ class SimulationGenerator:
                 "The scattering parameters `{}` is not implemented. See documentation for available "
                 "implementations.".format(scattering_params))
         self._host_pool = HostSpotPool()  # page-locked result arrays reused across calls
+        self._qstage = None               # page-locked quaternion staging, reused across calls
+        self._qstage_done = None          # event after the last uploads out of the staging
 
     def __repr__(self):
         return (f"SimulationGenerator(accelerating_voltage={self.accelerating_voltage}, "
@@ -135,6 +137,29 @@ class SimulationGenerator:
                            precession_mode=mode, minimum_intensity=float(self.minimum_intensity),
                            minima_number=float(self.shape_factor_kwargs.get("minima_number", 5)), form=form,
                            orient_tile=orient_tile)
+
+    def _upload_quaternions(self, arrays, dev):
+        """Device copies of the (n, 4) quaternion arrays through one reusable
+        page-locked staging buffer: a host copy into it, then asynchronous
+        uploads on the current stream.  The next call waits for this call's
+        uploads (an event) before it overwrites the staging."""
+        total = sum(int(a.shape[0]) for a in arrays)
+        if self._qstage_done is not None:
+            self._qstage_done.synchronize()
+        if self._qstage is None or self._qstage.shape[0] < total:
+            self._qstage = torch.empty((max(total, 4096), 4), dtype=torch.float64, pin_memory=True)
+        out, off = [], 0
+        for a in arrays:
+            n = int(a.shape[0])
+            st = self._qstage[off:off + n]
+            st.numpy()[...] = a
+            d = torch.empty((n, 4), dtype=torch.float64, device=dev)
+            d.copy_(st, non_blocking=True)
+            out.append(d)
+            off += n
+        self._qstage_done = torch.cuda.Event()
+        self._qstage_done.record(torch.cuda.current_stream(dev))
+        return out
 
     def calculate_diffraction2d(self, phase: Union[Phase, Sequence[Phase]],
                                 rotation: Union[Rotation, Sequence[Rotation]] = None,
@@ -183,18 +208,20 @@ class SimulationGenerator:
         N.load_library()
         dev = torch.device("cuda", torch.cuda.current_device())
         settings = self.settings(max_excitation_error, shape_factor_width, form, orient_tile)
-        rots, tables, qs = [], [], []
-        t_table = t_upload = 0.0
-        for p, r in zip(phases, rotations):
-            rot = r if isinstance(r, Rotation) else Rotation(quaternions_of(r))
+        rots, tables = [], []
+        t_table = 0.0
+        t1 = time.perf_counter()
+        for r in rotations:
+            rots.append(r if isinstance(r, Rotation) else Rotation(quaternions_of(r)))
+        # the orientations go up first, asynchronously from page-locked staging:
+        # the copies run while the host builds the tables
+        qs = self._upload_quaternions([quaternions_of(rot) for rot in rots], dev)
+        t_upload = time.perf_counter() - t1
+        for p in phases:
             t0 = time.perf_counter()
             tables.append(PhaseTable(p, reciprocal_radius, with_direct_beam, self.scattering_params,
                                      debye_waller_factors, form=form, device=dev))
-            t1 = time.perf_counter()
-            qs.append(torch.from_numpy(quaternions_of(rot)).to(dev))
-            t_upload += time.perf_counter() - t1
-            t_table += t1 - t0
-            rots.append(rot)
+            t_table += time.perf_counter() - t0
         custom = self._custom_shape is not None and settings.precession_mode != N.DS_PRECESSION_LORENTZIAN
         if custom:
             # the caller's function on the host between the selection and the
