@@ -132,6 +132,37 @@ def test_reference_fast_vs_slow_kat():
     assert not np.allclose(_raster(spots, fast=True, **kw)[0], _raster(spots, fast=False, **kw)[0])
 
 
+def test_fast_mode_amplitude_cases():
+    """The slice rasteriser's normalisation paths against the oracle: a
+    dominant spot (the maximum pass builds only the slices that can hold the
+    maximum), negative amplitudes (every slice built and read back), a NaN
+    amplitude (numpy's max is NaN: a NaN image), equal amplitudes on an odd
+    width, and spots on every border row and column."""
+    rng = np.random.default_rng(17)
+    pats = []
+    xy = rng.uniform(-0.6, 0.6, size=(60, 2))
+    amp = rng.uniform(0.01, 1.0, 60)
+    amp[7] = 500.0
+    pats.append((np.c_[xy, np.zeros(60)], amp))                       # dominant spot
+    amp2 = amp.copy()
+    amp2[::3] *= -1
+    pats.append((np.c_[xy, np.zeros(60)], amp2))                      # negative amplitudes
+    amp3 = amp.copy()
+    amp3[11] = np.nan
+    pats.append((np.c_[xy, np.zeros(60)], amp3))                      # a NaN amplitude
+    pats.append((np.c_[xy, np.zeros(60)], np.ones(60)))               # equal amplitudes
+    edge = np.array([[-0.64, -0.64, 0], [0.63, 0.63, 0], [-0.64, 0.2, 0], [0.1, 0.63, 0], [0.0, -0.64, 0]])
+    pats.append((edge, np.array([1.0, 2.0, 3.0, 4.0, 5.0])))           # border rows and columns
+    spots = _spots_of(pats)
+    for kw in (dict(shape=(128, 128), sigma=1.0, calibration=0.01),
+               dict(shape=(97, 131), sigma=1.3, calibration=0.01),
+               dict(shape=(128, 128), sigma=2.0, calibration=0.01, normalize=False)):
+        got, want = _raster(spots, **kw), _oracle(spots, **kw)
+        _assert_images(got, want)
+    got = _raster(spots, shape=(128, 128), sigma=1.0, calibration=0.01)
+    assert np.all(np.isnan(got[2])) and got[0].max() == 1.0
+
+
 def test_many_spots_use_global_arena():
     """A pattern whose per-pattern arena exceeds shared memory (5000 spots)
     runs from the global scratch arena: same images."""
