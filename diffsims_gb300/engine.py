@@ -253,6 +253,35 @@ class PhaseSpots:
     def nbytes(self):
         return self.offsets.numel() * 8 + self.total * (4 + 16)
 
+    def select(self, index) -> "PhaseSpots":
+        """The patterns ``index`` (an int, a slice or an integer array) as a
+        new ``PhaseSpots``: their CSR rows gathered on the device, the table
+        shared."""
+        n = self.n_orient
+        pick = np.atleast_1d(np.arange(n)[index]).astype(np.int64)
+        dev = self.offsets.device
+        sel = torch.as_tensor(pick, device=dev)
+        starts = self.offsets[sel]
+        counts = self.offsets[sel + 1] - starts
+        off = torch.zeros(pick.shape[0] + 1, dtype=torch.int64, device=dev)
+        off[1:] = torch.cumsum(counts, 0)
+        total = int(off[-1].item())
+        which = torch.repeat_interleave(torch.arange(pick.shape[0], device=dev), counts)
+        src = starts[which] + (torch.arange(total, device=dev) - off[:-1][which])
+        s = None if self.excitation_error is None else self.excitation_error[src]
+        out = PhaseSpots(self.table, off, self.hkl_index[src], self.xyzi[src], total, s)
+        if self.table is None:
+            out._hkl_rows = self._hkl_rows
+        return out
+
+    def __deepcopy__(self, memo):
+        """Copies of the device arrays; the phase table (read-only) is shared."""
+        s = None if self.excitation_error is None else self.excitation_error.clone()
+        out = PhaseSpots(self.table, self.offsets.clone(), self.hkl_index.clone(), self.xyzi.clone(), self.total, s)
+        if self.table is None:
+            out._hkl_rows = self._hkl_rows.copy()
+        return out
+
 
 def _fetch_pinned(tensors):
     """Device -> page-locked host copies (torch's caching host allocator

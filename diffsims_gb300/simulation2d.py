@@ -3,12 +3,16 @@
 Mirror the parts of diffsims/simulations/simulation2d.py (``Simulation2D``,
 :109-764) and diffsims/crystallography/_diffracting_vector.py
 (``DiffractingVector``) that users of ``calculate_diffraction2d`` read: the
-phase x rotation nesting, iteration, per-pattern spot vectors with
-``data`` / ``intensity`` / ``hkl``, ``polar_flatten_simulations`` and
-``get_diffraction_pattern``.  Spots stay on the device in CSR form until a
-pattern is accessed; plotting is not provided.
+phase x rotation nesting, the ``iphase`` / ``irot`` selectors, the
+phase / rotation cursor and iteration, per-pattern spot vectors with
+``data`` / ``intensity`` / ``hkl``, in-plane transforms,
+``polar_flatten_simulations`` and ``get_diffraction_pattern``.  Spots stay
+on the device in CSR form until a pattern is accessed; plotting is not
+provided.
 """
 from __future__ import annotations
+
+import copy
 
 import numpy as np
 
@@ -123,6 +127,47 @@ class _PhaseCoordinates:
             yield self[i]
 
 
+class _PhaseSelector:
+    """``Simulation2D.iphase[item]``: the phases ``item`` (a name, an index
+    or a slice) as a new ``Simulation2D`` over the same device spots
+    (diffsims/simulations/simulation2d.py:43-73)."""
+
+    def __init__(self, sim):
+        self.sim = sim
+
+    def __getitem__(self, item):
+        sim = self.sim
+        if not sim._multi_phase:
+            raise ValueError("Only one phase in the simulation")
+        plist, rlist = list(sim.phases), list(sim.rotations)
+        if isinstance(item, str):
+            item = [getattr(p, "name", None) for p in plist].index(item)
+        elif not isinstance(item, (int, np.integer, slice)):
+            raise ValueError("Item must be a string or integer")
+        # an index gives a one-phase simulation, a slice a list of phases
+        return Simulation2D(plist[item], sim._spots[item], rlist[item], sim.simulation_generator,
+                            sim.reciprocal_radius)
+
+
+class _RotationSelector:
+    """``Simulation2D.irot[item]``: the rotations ``item`` of every phase as
+    a new ``Simulation2D`` (their spots gathered on the device;
+    diffsims/simulations/simulation2d.py:76-106)."""
+
+    def __init__(self, sim):
+        self.sim = sim
+
+    def __getitem__(self, item):
+        sim = self.sim
+        if sim.current_size == 1:
+            raise ValueError("Only one rotation in the simulation")
+        if not sim._multi_phase:
+            return Simulation2D(sim.phases, sim._spots[0].select(item), sim.rotations[item],
+                                sim.simulation_generator, sim.reciprocal_radius)
+        return Simulation2D(sim.phases, [s.select(item) for s in sim._spots], [r[item] for r in sim.rotations],
+                            sim.simulation_generator, sim.reciprocal_radius)
+
+
 class Simulation2D:
     """Result of ``SimulationGenerator.calculate_diffraction2d``.
 
@@ -200,6 +245,39 @@ class Simulation2D:
     def current_size(self):
         return len(self._coords[self.phase_index])
 
+    @property
+    def iphase(self):
+        return _PhaseSelector(self)
+
+    @property
+    def irot(self):
+        return _RotationSelector(self)
+
+    @property
+    def current_phase(self):
+        return self.phases[self.phase_index] if self._multi_phase else self.phases
+
+    def get_current_rotation_matrix(self):
+        """3 x 3 matrix of the current rotation (``phase_index``, ``rotation_index``)."""
+        rot = self.rotations[self.phase_index] if self._multi_phase else self.rotations
+        return np.array(rot.to_matrix()[self.rotation_index])
+
+    def deepcopy(self):
+        """A copy with its own spot arrays (the generator is shared)."""
+        return copy.deepcopy(self, {id(self.simulation_generator): self.simulation_generator})
+
+    def rotate_shift_coordinates(self, angle: float, center=(0, 0), mirrored: bool = False):
+        """The current pattern's spots turned in-plane by ``angle`` degrees
+        (after a mirror across x when ``mirrored``) and shifted by
+        ``center``: x + iy -> (x -/+ iy) e^{i angle} + c; z, intensities and
+        hkl unchanged (diffsims/simulations/simulation2d.py:261-311)."""
+        v = self.get_current_coordinates()
+        data = v.data.copy()
+        w = data[:, 0] + 1j * (-data[:, 1] if mirrored else data[:, 1])
+        w = w * np.exp(1j * np.deg2rad(angle)) + complex(center[0], center[1])
+        data[:, 0], data[:, 1] = w.real, w.imag
+        return DiffractingVector(v.phase, data, v.intensity, v.hkl, v.rotation)
+
     def get_simulation(self, item):
         """(rotation, phase index, DiffractingVector) of flat index ``item``."""
         counts = np.cumsum([len(c) for c in self._coords])
@@ -212,9 +290,23 @@ class Simulation2D:
         return self._coords[self.phase_index][self.rotation_index]
 
     def __iter__(self):
-        for c in self._coords:
-            for v in c:
-                yield v
+        """The patterns in order, phase by phase, through the phase / rotation
+        cursor as the reference iterates (the cursor is back at (0, 0) at
+        the end)."""
+        return self
+
+    def __next__(self):
+        if self.phase_index >= len(self._coords):
+            self.phase_index = 0
+            self.rotation_index = 0
+            raise StopIteration
+        v = self._coords[self.phase_index][self.rotation_index]
+        if self.rotation_index + 1 >= self.current_size:
+            self.rotation_index = 0
+            self.phase_index += 1
+        else:
+            self.rotation_index += 1
+        return v
 
     def __len__(self):
         return sum(len(c) for c in self._coords)
@@ -281,3 +373,6 @@ def _get_closest(array, values):
         np.fabs(values - array[np.maximum(idxs - 1, 0)]) < np.fabs(values - array[np.minimum(idxs, len(array) - 1)]))
     idxs[prev_closer] -= 1
     return idxs
+
+
+get_closest = _get_closest  # the reference's public name (simulation2d.py:767)

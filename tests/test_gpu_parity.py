@@ -446,3 +446,72 @@ def test_empty_and_single_orientation():
     q = ok.euler_to_quaternion([0, 0, 0])
     spots, _ = pu.gpu_run(crystal, q, p, "mixed")
     pu.compare(spots, crystal, q, p)
+
+
+def test_simulation2d_selectors_cursor_and_transforms():
+    """iphase / irot selections (diffsims/simulations/simulation2d.py:43-106),
+    the phase / rotation cursor and its iteration (:200-260), the current
+    phase and rotation matrix, deepcopy, the in-plane transform (:261-311)
+    and get_closest (:767-781) on a two-phase result."""
+    import diffsims_gb300 as ds
+    from diffsims_gb300.simulation2d import get_closest
+    gen = ds.SimulationGenerator(300)
+    si = pu.to_phase(si_crystal())
+    big = pu.to_phase(si_crystal(10))
+    big.name = "big"
+    r1 = ds.Rotation.from_euler([[0, 0, 0], [0.1, 0.1, 0.1], [0.3, 0.2, 0.1]])
+    r2 = ds.Rotation.from_euler([[0, 0, 0], [0.1, 0.1, 0.1], [0.2, 0.2, 0.2], [0.5, 0.1, 0.4]])
+    sim = gen.calculate_diffraction2d([si, big], rotation=[r1, r2], reciprocal_radius=1.0)
+
+    def same(a, b):
+        np.testing.assert_array_equal(a.data, b.data)
+        np.testing.assert_array_equal(a.intensity, b.intensity)
+        np.testing.assert_array_equal(a.hkl, b.hkl)
+
+    one = sim.iphase[0]
+    assert one.phases is si and len(one) == 3 and not one.has_multiple_phases
+    for i in range(3):
+        same(one.coordinates[i], sim.coordinates[0][i])
+    named = sim.iphase["big"]
+    assert named.phases is big and len(named) == 4
+    same(named.coordinates[3], sim.coordinates[1][3])
+    both = sim.iphase[0:2]
+    assert both.num_phases == 2 and len(both) == 7
+    with pytest.raises(ValueError):
+        one.iphase[0]
+    with pytest.raises(ValueError):
+        sim.iphase[1.5]
+    sub = sim.irot[1:3]
+    assert [len(c) for c in sub.coordinates] == [2, 2]
+    same(sub.coordinates[0][0], sim.coordinates[0][1])
+    same(sub.coordinates[1][1], sim.coordinates[1][2])
+    np.testing.assert_allclose(sub.rotations[1].data, r2.data[1:3], rtol=0, atol=1e-15)
+    single = one.irot[2]
+    same(single.coordinates, sim.coordinates[0][2])
+    with pytest.raises(ValueError):
+        single.irot[0]
+    # the cursor: iteration visits every pattern in order and ends at (0, 0)
+    seen = list(sim)
+    assert len(seen) == 7 and sim.phase_index == 0 and sim.rotation_index == 0
+    same(seen[4], sim.coordinates[1][1])
+    sim.phase_index, sim.rotation_index = 1, 2
+    assert sim.current_phase is big and sim.current_size == 4
+    np.testing.assert_allclose(sim.get_current_rotation_matrix(), r2.to_matrix()[2], rtol=0, atol=0)
+    same(sim.get_current_coordinates(), sim.coordinates[1][2])
+    # in-plane transform against the reference's polar form
+    v = sim.get_current_coordinates()
+    t = sim.rotate_shift_coordinates(30.0, center=(1.0, -2.0), mirrored=True)
+    x, y = v.data[:, 0], v.data[:, 1]
+    theta = -np.arctan2(y, x) + np.deg2rad(30.0)
+    rd = np.sqrt(x ** 2 + y ** 2)
+    np.testing.assert_allclose(t.data[:, 0], rd * np.cos(theta) + 1.0, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(t.data[:, 1], rd * np.sin(theta) - 2.0, rtol=0, atol=1e-12)
+    np.testing.assert_array_equal(t.data[:, 2], v.data[:, 2])
+    np.testing.assert_array_equal(t.intensity, v.intensity)
+    # deepcopy: its own spot arrays
+    d = sim.deepcopy()
+    assert d.simulation_generator is gen and d is not sim
+    d.spots(0).xyzi.zero_()
+    assert np.any(sim.spots(0).xyzi.cpu().numpy() != 0)
+    same(d.coordinates[1][3], sim.coordinates[1][3])
+    np.testing.assert_array_equal(get_closest([0.0, 1.0, 2.0, 3.0], np.array([0.4, 1.6, 5.0, -1.0])), [0, 2, 3, 0])
