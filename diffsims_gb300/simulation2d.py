@@ -76,6 +76,17 @@ class DiffractingVector:
     def gspacing(self):
         return np.linalg.norm(self.data, axis=1)
 
+    @property
+    def dspacing(self):
+        return 1.0 / self.gspacing
+
+    def calculate_structure_factor(self):
+        """Not available on spot vectors, as in the reference
+        (diffsims/crystallography/_diffracting_vector.py:180-184): the
+        intensities already hold |F|^2 times the shape factor."""
+        raise NotImplementedError("Structure factor calculation not implemented for DiffractionVector. "
+                                  "Use ReciprocalLatticeVector instead.")
+
     def __getitem__(self, key):
         if isinstance(key, (int, np.integer)):
             key = slice(key, key + 1 if key != -1 else None)
