@@ -69,7 +69,7 @@ __device__ inline float shape_base_f32(const C &c, float s) {
         }
         case DS_SHAPE_LORENTZIAN: {  // :154-180 = 1 / (1 + (pi s / w)^2)
             const float x = c.sigma_f * s;
-            return 1.f / fmaf(x, x, 1.f);
+            return __frcp_rn(fmaf(x, x, 1.f));  // the correctly rounded reciprocal: = 1.f / (...)
         }
         default:
             return 1.f;  // binary, :33-49
