@@ -349,3 +349,35 @@ def test_refine_parts_is_validated(lib):
         assert lib.ds_simulate(p, t, fake, 1, out, fake, 1 << 20, fake, None) == N.DS_ERR_INVALID_ARGUMENT
         assert "refine_parts" in lib.ds_last_error().decode()
         assert lib.ds_simulate_batch(p, None, 0, out, fake, 1 << 20, fake, None) == N.DS_ERR_INVALID_ARGUMENT
+
+
+def test_phase_spots_select_and_copy():
+    """PhaseSpots.select gathers whole patterns of the CSR (an index, a slice
+    or an array, in the given order) and deepcopy owns its arrays; checked
+    on CPU tensors against a direct numpy gather."""
+    import copy
+    import torch
+    from diffsims_gb300.engine import PhaseSpots
+    rng = np.random.default_rng(2)
+    counts = rng.integers(0, 5, 9)
+    off = np.zeros(10, dtype=np.int64)
+    off[1:] = np.cumsum(counts)
+    total = int(off[-1])
+    idx = rng.integers(0, 100, total).astype(np.int32)
+    xyzi = rng.random((total, 4)).astype(np.float32)
+    s = rng.random(total)
+    sp = PhaseSpots(None, torch.as_tensor(off), torch.as_tensor(idx), torch.as_tensor(xyzi), total, torch.as_tensor(s))
+    sp._hkl_rows = rng.integers(-5, 5, (100, 3)).astype(np.float64)
+    for pick in (3, slice(2, 7), slice(None, None, -2), np.array([8, 0, 0, 5])):
+        sel = sp.select(pick)
+        want = np.atleast_1d(np.arange(9)[pick])
+        assert sel.n_orient == len(want)
+        rows = np.concatenate([np.arange(off[i], off[i + 1]) for i in want]) if len(want) else np.zeros(0, int)
+        np.testing.assert_array_equal(sel.offsets.numpy(), np.r_[0, np.cumsum(counts[want])])
+        np.testing.assert_array_equal(sel.hkl_index.numpy(), idx[rows])
+        np.testing.assert_array_equal(sel.xyzi.numpy(), xyzi[rows])
+        np.testing.assert_array_equal(sel.excitation_error.numpy(), s[rows])
+        assert sel.total == len(rows) and sel._hkl_rows is sp._hkl_rows
+    c = copy.deepcopy(sp)
+    c.xyzi.zero_()
+    assert np.array_equal(sp.xyzi.numpy(), xyzi) and c.total == total
