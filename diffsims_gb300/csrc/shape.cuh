@@ -8,6 +8,7 @@
 //   float width_f, mw_f, mfac_f, sigma_f, phi_f, int_step_f;
 //     (mw = n / w, mfac = pi n / |w|, sigma = pi / w)
 #pragma once
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -247,6 +248,79 @@ __device__ __forceinline__ T shape_vd(const ShapeK<T> &K, T s, T &df) {
     }
 }
 
+// The linear model's rotation average in closed form (FP64):
+//   (1 / pi) int_0^pi max(0, 1 - |s0 + a cos t| / w) dt,  a > 0, w > 0.
+// On each of [0, w] and [-w, 0] the integrand is 1 -/+ (s0 + a cos t) / w
+// between the angles t(b) = acos((b - s0) / a) of the interval's ends, so the
+// integral is (1 -/+ s0 / w) dt -/+ (a / w) d(sin t).  Evaluated stably:
+// every angle is held as x or pi - x (x <= pi / 2) from the exactly summed
+// distance of b to the nearer end of [s0 - a, s0 + a] (t = 2 asin(sqrt(d /
+// 2a))), range ends are exactly 0 or pi, and a piece that ends where the
+// integrand vanishes (t_e at b = +/-w) is written about that angle:
+//   (a / w) [sin t_e (1 - cos D) +/- cos t_e (D - sin D)],  D its length,
+// with 1 - cos D = 2 sin^2(D / 2) and D - sin D by its Taylor series for
+// small D: no difference of nearly equal terms, so small averages (spots
+// that graze the support) keep their relative accuracy (~1e-14 against
+// 50-digit arithmetic, averages from 1e-19 to 1).
+struct PrecAngle {
+    double x;
+    bool top;     // t = x (near 0) or pi - x (near pi)
+    bool inside;  // b strictly inside (s0 - a, s0 + a)
+};
+
+__device__ __forceinline__ double d_minus_sin(double d) {
+    if (d < 0.25) {
+        const double d2 = d * d;
+        return d * d2 * (1.0 / 6 - d2 * (1.0 / 120 - d2 * (1.0 / 5040 - d2 * (1.0 / 362880 - d2 / 39916800.0))));
+    }
+    return d - sin(d);
+}
+
+__device__ inline double linear_precession_closed(double s0, double a, double w) {
+    const double PI = SHAPE_PI;
+    // s0 + a = hi + hl and s0 - a = lo + ll exactly (two-sum)
+    const double hi = s0 + a, hb = hi - s0, hl = (s0 - (hi - hb)) + (a - hb);
+    const double lo = s0 - a, lb = lo - s0, ll = (s0 - (lo - lb)) + (-a - lb);
+    auto angle = [&](double b) {
+        PrecAngle A;
+        const double dt = (hi - b) + hl;  // (s0 + a) - b
+        const double db = (b - lo) - ll;  // b - (s0 - a)
+        A.inside = dt > 0.0 && db > 0.0;
+        A.top = dt <= db;
+        A.x = A.inside ? 2.0 * asin(fmin(1.0, sqrt((A.top ? dt : db) / (2.0 * a)))) : 0.0;
+        return A;
+    };
+    auto diff = [&](const PrecAngle &A, const PrecAngle &B) {  // t(B) - t(A)
+        if (A.top && B.top) return B.x - A.x;
+        if (!A.top && !B.top) return A.x - B.x;
+        if (A.top) return (PI - B.x) - A.x;
+        return B.x - (PI - A.x);
+    };
+    const PrecAngle Tw = angle(w), T0 = angle(0.0), Tm = angle(-w);
+    double tot = 0.0;
+    double d = diff(Tw, T0);  // [0, w]: (w - s) / w
+    if (d > 0.0) {
+        if (Tw.inside) {
+            const double se = sin(Tw.x), ce = Tw.top ? cos(Tw.x) : -cos(Tw.x);
+            const double h = sin(0.5 * d);
+            tot += (a / w) * (se * 2.0 * h * h + ce * d_minus_sin(d));
+        } else {
+            tot += ((w - s0) / w) * d - (a / w) * (sin(T0.x) - sin(Tw.x));
+        }
+    }
+    d = diff(T0, Tm);  // [-w, 0]: (w + s) / w
+    if (d > 0.0) {
+        if (Tm.inside) {
+            const double se = sin(Tm.x), ce = Tm.top ? cos(Tm.x) : -cos(Tm.x);
+            const double h = sin(0.5 * d);
+            tot += (a / w) * (se * 2.0 * h * h - ce * d_minus_sin(d));
+        } else {
+            tot += ((w + s0) / w) * d + (a / w) * (sin(Tm.x) - sin(T0.x));
+        }
+    }
+    return tot / PI;
+}
+
 template <typename T, bool GRAD, int SHAPE, class C>
 __device__ __forceinline__ T precession_average_impl(const C &c, T s0h, T s0l, T a, T *ds0, T *da) {
     const T PI_T = (T)SHAPE_PI;
@@ -257,6 +331,9 @@ __device__ __forceinline__ T precession_average_impl(const C &c, T s0h, T s0l, T
         const T v = shape_vd<SHAPE, GRAD>(K, s0, dfd);
         if (GRAD) { *ds0 = dfd; *da = (T)0; }
         return v;
+    }
+    if constexpr (SHAPE == DS_SHAPE_LINEAR && !GRAD && std::is_same<T, double>::value) {
+        if (K.w > 0.0) return linear_precession_closed(s0, a, K.w);
     }
     const T h = (T)c.int_step;
     const T w = K.w;
