@@ -260,20 +260,32 @@ __device__ __forceinline__ T shape_vd(const ShapeK<T> &K, T s, T &df) {
 //   (a / w) [sin t_e (1 - cos D) +/- cos t_e (D - sin D)],  D its length,
 // with 1 - cos D = 2 sin^2(D / 2) and D - sin D by its Taylor series for
 // small D: no difference of nearly equal terms, so small averages (spots
-// that graze the support) keep their relative accuracy (~1e-14 against
-// 50-digit arithmetic, averages from 1e-19 to 1).
+// that graze the support) keep their relative accuracy (<= 1e-10 against
+// 50-digit arithmetic, averages from 1e-19 to 1).  Sines and cosines come
+// from the half-angle values q = sin(x / 2), p = cos(x / 2) of each angle,
+// so a call costs three FP64 asin and square roots.
 struct PrecAngle {
-    double x;
-    bool top;     // t = x (near 0) or pi - x (near pi)
+    double x;     // t = x (near 0) or pi - x (near pi), x = 2 asin(q) in [0, pi]
+    double q, p;  // sin(x / 2), cos(x / 2)
+    bool top;
     bool inside;  // b strictly inside (s0 - a, s0 + a)
 };
 
-__device__ __forceinline__ double d_minus_sin(double d) {
+// D - sin D, with sin D = 2 h cos(D / 2) from h = sin(D / 2)
+__device__ __forceinline__ double d_minus_sin(double d, double h) {
     if (d < 0.25) {
         const double d2 = d * d;
         return d * d2 * (1.0 / 6 - d2 * (1.0 / 120 - d2 * (1.0 / 5040 - d2 * (1.0 / 362880 - d2 / 39916800.0))));
     }
-    return d - sin(d);
+    return d - 2.0 * h * sqrt((1.0 - h) * (1.0 + h));
+}
+
+// sin and cos of the angle from its half-angle values: sin t = 2 q p,
+// cos t = 1 - 2 q^2 (negated for t = pi - x); no trigonometric call
+__device__ __forceinline__ void prec_sc(const PrecAngle &A, double &sn, double &cs) {
+    sn = 2.0 * A.q * A.p;
+    const double c = (1.0 - A.q) * (1.0 + A.q) - A.q * A.q;
+    cs = A.top ? c : -c;
 }
 
 __device__ inline double linear_precession_closed(double s0, double a, double w) {
@@ -287,35 +299,43 @@ __device__ inline double linear_precession_closed(double s0, double a, double w)
         const double db = (b - lo) - ll;  // b - (s0 - a)
         A.inside = dt > 0.0 && db > 0.0;
         A.top = dt <= db;
-        A.x = A.inside ? 2.0 * asin(fmin(1.0, sqrt((A.top ? dt : db) / (2.0 * a)))) : 0.0;
+        A.q = A.inside ? fmin(1.0, sqrt((A.top ? dt : db) / (2.0 * a))) : 0.0;
+        A.p = sqrt((1.0 - A.q) * (1.0 + A.q));
+        A.x = A.inside ? 2.0 * asin(A.q) : 0.0;
         return A;
     };
-    auto diff = [&](const PrecAngle &A, const PrecAngle &B) {  // t(B) - t(A)
+    // t(B) - t(A), and h = sin of its half from the half-angle values
+    auto diff = [&](const PrecAngle &A, const PrecAngle &B, double &h) {
+        const double sa = A.top ? A.q : A.p, ca = A.top ? A.p : A.q;  // sin, cos of t(A) / 2
+        const double sb = B.top ? B.q : B.p, cb = B.top ? B.p : B.q;
+        h = sb * ca - cb * sa;
         if (A.top && B.top) return B.x - A.x;
         if (!A.top && !B.top) return A.x - B.x;
         if (A.top) return (PI - B.x) - A.x;
         return B.x - (PI - A.x);
     };
     const PrecAngle Tw = angle(w), T0 = angle(0.0), Tm = angle(-w);
-    double tot = 0.0;
-    double d = diff(Tw, T0);  // [0, w]: (w - s) / w
+    double tot = 0.0, h, se, ce, s1, c1;
+    double d = diff(Tw, T0, h);  // [0, w]: (w - s) / w
     if (d > 0.0) {
         if (Tw.inside) {
-            const double se = sin(Tw.x), ce = Tw.top ? cos(Tw.x) : -cos(Tw.x);
-            const double h = sin(0.5 * d);
-            tot += (a / w) * (se * 2.0 * h * h + ce * d_minus_sin(d));
+            prec_sc(Tw, se, ce);
+            tot += (a / w) * (se * 2.0 * h * h + ce * d_minus_sin(d, h));
         } else {
-            tot += ((w - s0) / w) * d - (a / w) * (sin(T0.x) - sin(Tw.x));
+            prec_sc(T0, s1, c1);
+            prec_sc(Tw, se, ce);
+            tot += ((w - s0) / w) * d - (a / w) * (s1 - se);
         }
     }
-    d = diff(T0, Tm);  // [-w, 0]: (w + s) / w
+    d = diff(T0, Tm, h);  // [-w, 0]: (w + s) / w
     if (d > 0.0) {
         if (Tm.inside) {
-            const double se = sin(Tm.x), ce = Tm.top ? cos(Tm.x) : -cos(Tm.x);
-            const double h = sin(0.5 * d);
-            tot += (a / w) * (se * 2.0 * h * h - ce * d_minus_sin(d));
+            prec_sc(Tm, se, ce);
+            tot += (a / w) * (se * 2.0 * h * h - ce * d_minus_sin(d, h));
         } else {
-            tot += ((w + s0) / w) * d + (a / w) * (sin(Tm.x) - sin(T0.x));
+            prec_sc(Tm, se, ce);
+            prec_sc(T0, s1, c1);
+            tot += ((w + s0) / w) * d + (a / w) * (se - s1);
         }
     }
     return tot / PI;
