@@ -512,7 +512,7 @@ extern "C" ds_status ds_simulate_backward(const ds_sim_params *p, const ds_phase
     c.sigma_f = (float)(PI / c.width);
     c.phi_f = (float)c.phi;
     c.int_step_f = (float)c.int_step;
-    c.int_tau = precession_fp64_threshold(p->shape_model);
+    c.int_tau = precession_fp64_threshold_quadrature(p->shape_model);
     for (int i = 0; i < 9; ++i) c.recip[i] = t->recip[i];
     c.n_orient = n_orient;
     c.n_hkl = t->n_hkl;

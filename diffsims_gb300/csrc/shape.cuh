@@ -39,7 +39,15 @@ inline double precession_breakpoint_step(int shape, double width, double minima)
 // difference of O(1) terms near the band edge) 3e-5 at 1e-5..1e-4, 7e-6 at
 // 1e-3..1e-2, 2e-6 above; sin2c 8e-6 at 1e-3..1e-2, 5e-6 above; sinc 3e-6
 // above 1e-3; atanc and lorentzian ~1e-6 above 1e-4.
+// The forward kernels take the linear model's average from its FP32 closed
+// form (simulate_kernel.cuh), accurate to 7.4e-7 down to 1e-10: only
+// averages below that are redone in FP64.
+inline float precession_fp64_threshold_quadrature(int shape);
 inline float precession_fp64_threshold(int shape) {
+    return shape == DS_SHAPE_LINEAR ? 1e-10f : precession_fp64_threshold_quadrature(shape);
+}
+// FP32 quadrature (the adjoint kernels, and every model but linear forward)
+inline float precession_fp64_threshold_quadrature(int shape) {
     switch (shape) {
         case DS_SHAPE_LINEAR:
         case DS_SHAPE_SIN2C: return 1e-2f;
