@@ -856,6 +856,7 @@ struct SliceGeom {
     int P;       // footprint width 2R + 1
     unsigned mP; // ceil(2^32 / P): j / P = umulhi(j, mP) for j < P^2 (P odd, P^3 < 2^32)
     int wt2;     // the P x P product table is in shared memory (P <= 31)
+    int loff;    // per-lane pair offsets in shared memory (wt2 and SH P <= 128)
 };
 
 struct SliceArena {
@@ -864,8 +865,10 @@ struct SliceArena {
     int *sxy;            // X | Y << 15 | (footprint crosses an image edge) << 30
     float *amp;
     int *scnt, *sstart, *sfill;  // nsl + 1 each
+    float *sU;                   // nsl + 1: a bound on every pixel of the slice (the maximum pass)
     int *sent;           // slice entries (spot indices), CSR by sstart
     float *wt, *wt2;     // 1-D weights w[|d|], d = 0..R; products w[|dy - R|] w[|dx - R|]
+    int *loff;           // pair m -> (m / P) Ws + m % P, m < 128 (with g.loff)
     int *misc;
     float *wmax;
 };
@@ -880,10 +883,11 @@ __host__ __device__ inline size_t slice_arena_bytes(int NS, int T, int R, const 
     o += ras_align((size_t)NS * 4) * 2;              // key, slot
     o += ras_align((size_t)T * 4) * 2;               // hkey, hidx
     o += ras_align((size_t)NS * 4) * 2;              // sxy, amp
-    o += ras_align((size_t)(g.nsl + 1) * 4) * 3;     // scnt, sstart, sfill
+    o += ras_align((size_t)(g.nsl + 1) * 4) * 4;     // scnt, sstart, sfill, sU
     o += ras_align((size_t)NS * g.span * 4);         // sent
     o += ras_align((size_t)(R + 1) * 4);
     o += ras_align(g.wt2 ? (size_t)g.P * g.P * 4 : 0);
+    o += ras_align(g.loff ? (size_t)128 * 4 : 0);
     o += ras_align(64 * 4) + ras_align(RAS_WARPS * 4);
     return o;
 }
@@ -906,9 +910,11 @@ __device__ inline SliceArena carve_slice(unsigned char *base, int NS, int T, int
     A.scnt = (int *)take((size_t)(g.nsl + 1) * 4);
     A.sstart = (int *)take((size_t)(g.nsl + 1) * 4);
     A.sfill = (int *)take((size_t)(g.nsl + 1) * 4);
+    A.sU = (float *)take((size_t)(g.nsl + 1) * 4);
     A.sent = (int *)take((size_t)NS * g.span * 4);
     A.wt = (float *)take((size_t)(R + 1) * 4);
     A.wt2 = (float *)take(g.wt2 ? (size_t)g.P * g.P * 4 : 0);
+    A.loff = (int *)take(g.loff ? (size_t)128 * 4 : 0);
     A.misc = (int *)take(64 * 4);
     A.wmax = (float *)take(RAS_WARPS * 4);
     return A;
@@ -951,7 +957,24 @@ __device__ inline void slice_splat(const RasterConst &c, const SliceGeom &g, con
         const int X = v & 0x7fff, Y = (v >> 15) & 0x7fff;
         const float a = A.amp[k];
         const int y0 = max(Y - R, ys), y1 = min(Y + R + 1, ye);
-        if (!(v >> 30)) {
+        if (!(v >> 30) && g.loff) {
+            // interior, pairs m of the footprint's rows y0..y1: weight
+            // wt2[r0 P + m], buffer offset from the per-lane table
+            const int jb = (y0 - (Y - R)) * P, np = (y1 - y0) * P;
+            const int base = (y0 - ys) * Ws + (X - R);
+            for (int m0 = 0; m0 < np; m0 += 32) {
+                const int m = m0 + lane;
+                if (m < np) {
+                    const float w = A.wt2[jb + m];
+                    const int o = base + A.loff[m];
+                    if (!DS_IN_BOUNDS(o, (ye - ys) * Ws, status)) continue;
+                    float *q = buf + o;
+                    const float nv = fmaf(a, w, *q);
+                    *q = nv;
+                    if (TRACK) run = fmaxf(run, nv);
+                }
+            }
+        } else if (!(v >> 30)) {
             // interior: pairs j = dy P + dx of the full footprint, rows y0..y1 only
             const int jb = (y0 - (Y - R)) * P, je = (y1 - (Y - R)) * P;
             const int corner = (Y - R - ys) * Ws + (X - R);  // footprint corner, relative to the slice (may be < 0)
@@ -1022,6 +1045,13 @@ raster_slice_kernel(const RasterConst c, const SliceGeom g, const int64_t *__res
     const unsigned lt = (1u << lane) - 1u;
 
     for (int i = tid; i <= R; i += RAS_THREADS) A.wt[i] = c.wt[i];
+    // a spot's largest pixel weight: w0^2 inside the image; at an edge each
+    // axis adds at most three mirrored taps, or the whole filter (1) when
+    // R >= the side
+    const float w00 = c.wt[0] * c.wt[0];  // = the product table's centre entry
+    const float wedge = (R < H && R < W) ? 9.f * w00 : 1.f;
+    if (g.loff)
+        for (int m = tid; m < 128; m += RAS_THREADS) A.loff[m] = (m / P) * g.Ws + m % P;
     if (g.wt2)
         for (int j = tid; j < P * P; j += RAS_THREADS) {
             const int dy = j / P, dx = j - dy * P;
@@ -1046,6 +1076,7 @@ raster_slice_kernel(const RasterConst c, const SliceGeom g, const int64_t *__res
         for (int s = tid; s <= nsl; s += RAS_THREADS) {
             A.scnt[s] = 0;
             A.sfill[s] = 0;
+            A.sU[s] = 0.f;
         }
         if (tid == 0) {
             A.misc[RAS_WARPS] = 0;      // in-frame spots
@@ -1109,7 +1140,12 @@ raster_slice_kernel(const RasterConst c, const SliceGeom g, const int64_t *__res
                 if (!(am >= 0.f)) atomicOr(&A.misc[RAS_WARPS + 1], am != am ? SLICE_FLAG_NAN : SLICE_FLAG_NEG);
                 else atomicMax(&A.misc[RAS_WARPS + 2], __float_as_int(am));  // non-negative floats order as ints
                 const int s0 = max(0, Y - R) / SH, s1 = min(H - 1, Y + R) / SH;
-                for (int s = s0; s <= s1; ++s) atomicAdd(&A.scnt[s], 1);
+                // the slices' pixel bounds (in any order: a bound, widened below)
+                const float ub = am * (edge ? wedge : w00);
+                for (int s = s0; s <= s1; ++s) {
+                    atomicAdd(&A.scnt[s], 1);
+                    atomicAdd(&A.sU[s], ub);
+                }
             }
             n_alive += tot;
             __syncthreads();
@@ -1174,9 +1210,7 @@ raster_slice_kernel(const RasterConst c, const SliceGeom g, const int64_t *__res
         float mx = 1.f;
         if (norm) {
             const bool readback = (aflags & SLICE_FLAG_NEG) != 0;
-            const float w00 = A.wt[0] * A.wt[0];  // the product table's centre entry
             const float lower = __int_as_float(A.misc[RAS_WARPS + 2]) * w00;
-            const float wedge = (R < H && R < W) ? 9.f * w00 : 1.f;
             float run = -INFINITY;
             bool any_empty = false;
             for (int s = warp; s < nsl; s += RAS_WARPS) {
@@ -1185,16 +1219,9 @@ raster_slice_kernel(const RasterConst c, const SliceGeom g, const int64_t *__res
                     any_empty = true;
                     continue;
                 }
-                if (!readback) {
-                    float U = 0.f;
-                    for (int e = e0 + lane; e < e1; e += 32) {
-                        const int k = A.sent[e];
-                        U += A.amp[k] * ((A.sxy[k] >> 30) ? wedge : w00);
-                    }
-#pragma unroll
-                    for (int d = 16; d >= 1; d >>= 1) U += __shfl_xor_sync(FULL_MASK, U, d);
-                    if (U * 1.001f < lower) continue;
-                }
+                // the bound summed in compaction (atomics: any order; the 0.1 %
+                // covers its rounding up to ~1.6e4 spots per slice)
+                if (!readback && A.sU[s] * 1.001f < lower) continue;
                 const int ys = s * SH, ye = min(H, ys + SH);
                 slice_zero(buf, (ye - ys) * g.Ws, lane);
                 if (readback) {
@@ -1271,6 +1298,7 @@ static bool slice_geometry(const ds_raster_params *p, int NS, int T, int R, Slic
         g.span = std::min(g.nsl, (P - 1 + SH - 1) / SH + 1);
         g.mP = P > 1 ? (unsigned)((0x100000000ull + P - 1) / P) : 0u;
         g.wt2 = P <= 31 ? 1 : 0;
+        g.loff = (g.wt2 && SH * P <= 128) ? 1 : 0;
         bytes = slice_arena_bytes(NS, T, R, g);
         if (bytes <= (size_t)RAS_SLICE_TARGET || (SH == 1 && bytes <= RAS_SMEM_LIMIT)) return true;
     }
