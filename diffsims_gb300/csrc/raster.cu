@@ -1171,8 +1171,28 @@ raster_slice_kernel(const RasterConst c, const SliceGeom g, const int64_t *__res
         }
 
         // ---- slice entries in spot order: warp w fills its own slices, 32 spots
-        // at a time; within a slice the lanes take consecutive places by lane
-        for (int k0 = 0; k0 < n_alive; k0 += 32) {
+        // at a time; within a slice the lanes take consecutive places by lane.
+        // When a footprint spans at most 8 slices a spot has at most one slice
+        // of each warp: one match over the lanes' slices places them all.
+        for (int k0 = 0; g.span <= 8 && k0 < n_alive; k0 += 32) {
+            const int k = k0 + lane;
+            int s = -1;
+            if (k < n_alive) {
+                const int Y = (A.sxy[k] >> 15) & 0x7fff;
+                const int s0 = max(0, Y - R) / SH, s1 = min(H - 1, Y + R) / SH;
+                const int f = s0 + ((warp - s0) & 7);  // the warp's slice in [s0, s1], if any
+                if (f <= s1) s = f;
+            }
+            const unsigned grp = __match_any_sync(FULL_MASK, s);
+            if (s >= 0) {
+                const int place = A.sstart[s] + A.sfill[s] + __popc(grp & lt);
+                if (DS_IN_BOUNDS(place, (long long)c.NS * g.span, status)) A.sent[place] = k;
+            }
+            __syncwarp();
+            if (s >= 0 && (grp >> lane) == 1u) A.sfill[s] += __popc(grp);  // the group's last lane
+            __syncwarp();
+        }
+        for (int k0 = 0; g.span > 8 && k0 < n_alive; k0 += 32) {
             const int k = k0 + lane;
             int t0 = 1 << 30, t1 = -(1 << 30);
             if (k < n_alive) {
