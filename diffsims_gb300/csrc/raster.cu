@@ -25,6 +25,7 @@
 // the kernel is bound by HBM writes.
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -1023,9 +1024,10 @@ __device__ inline void slice_zero(float *buf, int n_floats, int lane) {
 // pattern / max in float32: mode 0 multiplies by the reciprocal (max * (1 / max)
 // == 1 exactly), mode 1 also returns 1 for the maximum itself, mode 2 divides
 // (a maximum of zero, infinity or NaN, as numpy does)
-__device__ __forceinline__ float slice_scale(float u, int mode, float mx, float inv) {
-    if (mode == 0) return u * inv;
-    if (mode == 1) return u == mx ? 1.f : u * inv;
+template <int MODE>
+__device__ __forceinline__ float slice_scale(float u, float mx, float inv) {
+    if (MODE == 0) return u * inv;
+    if (MODE == 1) return u == mx ? 1.f : u * inv;
     return u / mx;
 }
 
@@ -1052,6 +1054,9 @@ raster_slice_kernel(const RasterConst c, const SliceGeom g, const int64_t *__res
     const float wedge = (R < H && R < W) ? 9.f * w00 : 1.f;
     if (g.loff)
         for (int m = tid; m < 128; m += RAS_THREADS) A.loff[m] = (m / P) * g.Ws + m % P;
+    // every slice build starts from a zero buffer: zeroed here once, then
+    // cleaned by whoever used it (the read-back, or the maximum pass)
+    slice_zero(buf, SH * g.Ws, lane);
     if (g.wt2)
         for (int j = tid; j < P * P; j += RAS_THREADS) {
             const int dy = j / P, dx = j - dy * P;
@@ -1243,7 +1248,6 @@ raster_slice_kernel(const RasterConst c, const SliceGeom g, const int64_t *__res
                 // covers its rounding up to ~1.6e4 spots per slice)
                 if (!readback && A.sU[s] * 1.001f < lower) continue;
                 const int ys = s * SH, ye = min(H, ys + SH);
-                slice_zero(buf, (ye - ys) * g.Ws, lane);
                 if (readback) {
                     slice_splat<false>(c, g, A, ys, ye, e0, e1, buf, lane, run, status);
                     for (int r = 0; r < ye - ys; ++r)
@@ -1252,6 +1256,7 @@ raster_slice_kernel(const RasterConst c, const SliceGeom g, const int64_t *__res
                 } else {
                     slice_splat<true>(c, g, A, ys, ye, e0, e1, buf, lane, run, status);
                 }
+                slice_zero(buf, (ye - ys) * g.Ws, lane);  // clean for the next build
             }
             // without negative amplitudes every pixel is >= 0, uncovered ones 0
             if (any_empty || !readback) run = fmaxf(run, 0.f);
@@ -1284,23 +1289,36 @@ raster_slice_kernel(const RasterConst c, const SliceGeom g, const int64_t *__res
                 }
                 continue;
             }
-            slice_zero(buf, (ye - ys) * g.Ws, lane);
             float unused = 0.f;
             slice_splat<false>(c, g, A, ys, ye, e0, e1, buf, lane, unused, status);
-            for (int r = 0; r < ye - ys; ++r) {
-                const float *src = buf + r * g.Ws;
-                float *row = dst + (size_t)r * W;
-                if (VEC) {
-                    for (int x = 4 * lane; x < W; x += 128) {
-                        const float4 u = *reinterpret_cast<const float4 *>(src + x);
-                        st_cs(reinterpret_cast<float4 *>(row + x),
-                              make_float4(slice_scale(u.x, mode, mx, sc_inv), slice_scale(u.y, mode, mx, sc_inv),
-                                          slice_scale(u.z, mode, mx, sc_inv), slice_scale(u.w, mode, mx, sc_inv)));
+            // read back, scale, store; zeros written back leave the buffer clean
+            auto store_rows = [&](auto md) {
+                constexpr int MODE = decltype(md)::value;
+                for (int r = 0; r < ye - ys; ++r) {
+                    float *src = buf + r * g.Ws;
+                    float *row = dst + (size_t)r * W;
+                    if (VEC) {
+                        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+                        for (int x = 4 * lane; x < W; x += 128) {
+                            float4 *q = reinterpret_cast<float4 *>(src + x);
+                            const float4 u = *q;
+                            *q = z4;
+                            st_cs(reinterpret_cast<float4 *>(row + x),
+                                  make_float4(slice_scale<MODE>(u.x, mx, sc_inv), slice_scale<MODE>(u.y, mx, sc_inv),
+                                              slice_scale<MODE>(u.z, mx, sc_inv), slice_scale<MODE>(u.w, mx, sc_inv)));
+                        }
+                    } else {
+                        for (int x = lane; x < W; x += 32) {
+                            const float u = src[x];
+                            src[x] = 0.f;
+                            st_cs1(row + x, slice_scale<MODE>(u, mx, sc_inv));
+                        }
                     }
-                } else {
-                    for (int x = lane; x < W; x += 32) st_cs1(row + x, slice_scale(src[x], mode, mx, sc_inv));
                 }
-            }
+            };
+            if (mode == 0) store_rows(std::integral_constant<int, 0>{});
+            else if (mode == 1) store_rows(std::integral_constant<int, 1>{});
+            else store_rows(std::integral_constant<int, 2>{});
             __syncwarp();
         }
         __syncthreads();  // the arena is reused by the next pattern
