@@ -27,7 +27,12 @@ Arms:
                     against the oracle's per-family loop on one core),
                     "legacy_ed_data" (the legacy DiffractionGenerator:
                     100,000 Euler triples of one structure in one launch,
-                    against the oracle's per-orientation call on one core).
+                    against the oracle's per-orientation call on one core),
+                    "polar_templates" (polar_flatten_simulations of the
+                    headline's 100,000 patterns, unbinned and binned, HBM
+                    roofline, against the oracle's numpy restatement),
+                    "profiles_1d" (calculate_diffraction1d of the headline's
+                    200-atom cell, public call, against the oracle).
   --impl reference  the reference's CPU path restated in numpy (the FP64
                     oracle) on all host cores, a bounded sample per step.
 
@@ -499,6 +504,8 @@ def run_gpu(args):
     library = None if args.skip_library else run_library(args, torch, dev, hbm_peak)
     families = None if args.skip_families else run_families(args, torch, dev)
     legacy = None if args.skip_legacy else run_legacy(args, torch, dev)
+    polar = None if args.skip_polar else run_polar(args, torch, dev, hbm_peak, spots)
+    profiles = None if args.skip_profiles else run_profiles(args, torch, dev)
 
     cpu = None
     if not args.no_cpu_baseline:
@@ -537,6 +544,8 @@ def run_gpu(args):
         "template_library": library,
         "family_structure_factors": families,
         "legacy_ed_data": legacy,
+        "polar_templates": polar,
+        "profiles_1d": profiles,
         "cpu_baseline": cpu,
         "clocks": clocks,
         "gpu_launches": 5 * args.steps,
@@ -944,6 +953,87 @@ def run_families(args, torch, dev):
             "dtype": "f64"}
 
 
+def run_polar(args, torch, dev, hbm_peak, spots):
+    """Polar templates (Simulation2D.polar_flatten_simulations,
+    diffsims/simulations/simulation2d.py:313-355) of the headline leg's
+    100,000 patterns on the device: padded (r, theta, I) float64 arrays,
+    unbinned and binned to 256 radial x 360 azimuthal axes.  Bytes = the spot
+    records read (16 B) + the three arrays written (24 B per slot).  CPU
+    baseline: the oracle's numpy restatement on one core over a sample."""
+    from diffsims_gb300.engine import polar_flatten
+    from oracle import kinematic as ok
+    st = torch.cuda.current_stream()
+    n = spots.n_orient
+    m = int((spots.offsets[1:] - spots.offsets[:-1]).max().item())
+    rax = np.linspace(0.0, 2.0, 256)
+    aax = np.linspace(-np.pi, np.pi, 360)
+    out = {}
+    for name, kw in (("unbinned", {}), ("binned", dict(radial_axes=rax, azimuthal_axes=aax))):
+        for _ in range(args.warmup):
+            res = polar_flatten([spots], **kw)
+        del res
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            res = polar_flatten([spots], **kw)
+            e1.record(st)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            del res
+        t = statistics.median(ms)
+        nbytes = spots.total * 16 + 3 * n * m * 8
+        out[name] = {"ms": t, "patterns_per_s": n / (t * 1e-3), "achieved_gbs": nbytes / (t * 1e-3) / 1e9,
+                     "frac": nbytes / (t * 1e-3) / 1e9 / hbm_peak, "bytes": int(nbytes)}
+    off, _, xyzi = spots.host()
+    n_cpu = 2000
+    pats = [(xyzi[off[k]:off[k + 1], :3].astype(np.float64), xyzi[off[k]:off[k + 1], 3].astype(np.float64))
+            for k in range(n_cpu)]
+    t0 = time.perf_counter()
+    ok.polar_flatten(pats)
+    cpu_rate = n_cpu / (time.perf_counter() - t0)
+    return {"metric": "polar templates/s (padded r, theta, I)", "value": out["unbinned"]["patterns_per_s"],
+            "unit": "patterns/s", "patterns": n, "max_spots": m, "spots": int(spots.total), **out,
+            "roofline": {"bound": "hbm", "achieved": out["unbinned"]["achieved_gbs"], "peak": hbm_peak,
+                         "unit": "GB/s", "frac": out["unbinned"]["frac"]},
+            "cpu_baseline": {"value": cpu_rate, "unit": "patterns/s", "cores": 1, "kind": "port",
+                             "sample": f"{n_cpu} patterns of the same spots, the oracle's numpy polar_flatten"},
+            "note": "the launch plus its three float64 output allocations (the kernel writes the padding)"}
+
+
+def run_profiles(args, torch, dev):
+    """1-D profiles (SimulationGenerator.calculate_diffraction1d,
+    diffsims/generators/simulation_generator.py:261-317) of the headline's
+    200-atom P1 cell: the from_min_dspacing set at 0.7 Angstrom, enumeration
+    and FP64 structure factors on the GPU, families on the host; the public
+    call timed against the oracle's restatement (numpy, one core)."""
+    import diffsims_gb300 as ds
+    from oracle import kinematic as ok
+    lat, els, xyz, B = make_crystal(WORKLOAD["cell_seed"], WORKLOAD["n_atoms"])
+    phase = phase_of("P1", lat, els, xyz)
+    gen = ds.SimulationGenerator(WORKLOAD["accelerating_voltage"])
+    for _ in range(max(1, args.warmup)):
+        prof = gen.calculate_diffraction1d(phase, 1.0)
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(max(3, args.steps)):
+        t0 = time.perf_counter()
+        prof = gen.calculate_diffraction1d(phase, 1.0)
+        ts.append(time.perf_counter() - t0)
+    t = statistics.median(ts)
+    cr = ok.Crystal(lat, els, xyz)
+    t0 = time.perf_counter()
+    ok.diffraction1d(cr, np.eye(3, dtype=int)[None])
+    cpu_s = time.perf_counter() - t0
+    return {"metric": "1-D profiles/s (calculate_diffraction1d, 200-atom P1, d_min 0.7 A)", "value": 1.0 / t,
+            "unit": "profiles/s", "ms_per_call": t * 1e3, "peaks": int(len(prof.intensities)),
+            "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "profiles/s", "cores": 1, "kind": "port",
+                             "sample": "one profile, the oracle's numpy restatement (FP64 structure factors, "
+                                       "families)"},
+            "note": "public call: host families and result objects included"}
+
+
 def run_legacy(args, torch, dev):
     """Legacy DiffractionGenerator.calculate_ed_data
     (diffsims/generators/diffraction_generator.py:192-331): a 12-atom P1 cell
@@ -1327,6 +1417,8 @@ def main():
     ap.add_argument("--skip-batch", action="store_true", help="leave out the batched-phases leg")
     ap.add_argument("--skip-families", action="store_true", help="leave out the per-family structure-factor leg")
     ap.add_argument("--skip-legacy", action="store_true", help="leave out the legacy calculate_ed_data leg")
+    ap.add_argument("--skip-polar", action="store_true", help="leave out the polar-template leg")
+    ap.add_argument("--skip-profiles", action="store_true", help="leave out the 1-D profile leg")
     ap.add_argument("--case", default=None, choices=["raster", "adjoint", "batch", "families", "legacy"],
                     help="run one small profiling case instead of the benchmark")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -1097,9 +1097,10 @@ def polar_flatten(spots_list, radial_axes=None, azimuthal_axes=None):
     counts = [int(s.n_orient) for s in spots_list]
     maxes = [int((s.offsets[1:] - s.offsets[:-1]).max().item()) if s.n_orient else 0 for s in spots_list]
     n, m = sum(counts), max(maxes)
-    r = torch.zeros((n, m), dtype=torch.float64, device=dev)
-    t = torch.zeros((n, m), dtype=torch.float64, device=dev)
-    i = torch.zeros((n, m), dtype=torch.float64, device=dev)
+    # the kernel writes every slot of every pattern (zero padding included)
+    r = torch.empty((n, m), dtype=torch.float64, device=dev)
+    t = torch.empty((n, m), dtype=torch.float64, device=dev)
+    i = torch.empty((n, m), dtype=torch.float64, device=dev)
     binned = radial_axes is not None and azimuthal_axes is not None
     rax = torch.as_tensor(np.asarray(radial_axes, dtype=np.float64)).to(dev) if binned else None
     aax = torch.as_tensor(np.asarray(azimuthal_axes, dtype=np.float64)).to(dev) if binned else None
