@@ -1286,6 +1286,20 @@ def run_case(args):
                                                     N.stream_handle()), "families")
         N.check_device_status(st, "families")
         out.update(families=n, orbit_positions=len(species))
+    elif args.case == "polar":
+        # polar templates of 8192 headline orientations, unbinned then binned
+        from diffsims_gb300.engine import polar_flatten
+        lat, els, xyz, B = make_crystal(WORKLOAD["cell_seed"], WORKLOAD["n_atoms"])
+        gen = ds.SimulationGenerator(WORKLOAD["accelerating_voltage"], "lobato",
+                                     shape_factor_model=WORKLOAD["shape_factor_model"])
+        tab = PhaseTable(phase_of("P1", lat, els, xyz), WORKLOAD["reciprocal_radius"], True, "lobato", list(B),
+                         device=dev)
+        q = torch.from_numpy(uniform_quaternions(8192, WORKLOAD["orientation_seed"])).to(dev)
+        sp = simulate_phase(tab, q, gen.settings(WORKLOAD["max_excitation_error"]), WORKLOAD["reciprocal_radius"],
+                            SpotBuffers(dev))
+        polar_flatten([sp])
+        polar_flatten([sp], np.linspace(0.0, 2.0, 256), np.linspace(-np.pi, np.pi, 360))
+        out.update(patterns=8192, spots=sp.total)
     elif args.case == "legacy":
         # the legacy leg's 12-atom P1 sphere table at r = 2.0 and 8192 Euler triples
         from diffsims_gb300.diffraction_generator import DiffractionGenerator, euler_rzxz_quaternions, structure_base
@@ -1419,7 +1433,7 @@ def main():
     ap.add_argument("--skip-legacy", action="store_true", help="leave out the legacy calculate_ed_data leg")
     ap.add_argument("--skip-polar", action="store_true", help="leave out the polar-template leg")
     ap.add_argument("--skip-profiles", action="store_true", help="leave out the 1-D profile leg")
-    ap.add_argument("--case", default=None, choices=["raster", "adjoint", "batch", "families", "legacy"],
+    ap.add_argument("--case", default=None, choices=["raster", "adjoint", "batch", "families", "legacy", "polar"],
                     help="run one small profiling case instead of the benchmark")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--out-dir", default=None)
