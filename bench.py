@@ -359,6 +359,7 @@ def run_gpu(args):
     q_host = rank_shard(n_o, WORKLOAD["orientation_seed"], rank)
     gen = ds.SimulationGenerator(WORKLOAD["accelerating_voltage"], "lobato",
                                  shape_factor_model=WORKLOAD["shape_factor_model"])
+    gen.host_transfer = args.host_transfer
     r = WORKLOAD["reciprocal_radius"]
     settings = gen.settings(WORKLOAD["max_excitation_error"], form="mixed")
     settings.screen = args.screen
@@ -435,6 +436,7 @@ def run_gpu(args):
             e2e_ms.append(dt * 1e3)
             e2e_split.append(sp.timings())
         d2h = sp.nbytes()
+        transfer = "stores" if type(sp).__name__ == "HostSpots" else "copies"
         del sim, sp
     e2e_value = n_o / (statistics.mean(e2e_ms) * 1e-3)
     breakdown = {k: statistics.mean(t[k] for t in e2e_split) for k in e2e_split[0] if k != "chunks"}
@@ -443,11 +445,13 @@ def run_gpu(args):
     breakdown["copy_span_gbs"] = d2h / (breakdown["copy_span_ms"] * 1e-3) / 1e9 if breakdown.get(
         "copy_span_ms") else None
     breakdown["pinned_pool_bytes"] = gen._host_pool.allocated_bytes
+    breakdown["host_transfer"] = transfer
     breakdown["note"] = ("host ms per call: table (enumeration + structure factors, one count read), quaternion "
-                         "upload, launch set-up, waits for chunk counts, pinned-pool allocation (0 once warm), "
-                         "the wait in host() and its offsets fix-up; device ms from CUDA events: the chunks' span "
-                         "and the copies' span; copy_span_gbs = the spots' bytes over the copies' span (the device-to-host "
-                         "rate the call achieved)")
+                         "upload, launch set-up, waits for the kernel (chunk_wait_ms), pinned-pool allocation (0 once "
+                         "warm), the wrap in host(); device ms from CUDA events: the kernel's span and the transfer's "
+                         "span, the same span when the kernel stores the spots into page-locked host memory itself "
+                         "(host_transfer 'stores', one launch); copy_span_gbs = the spots' bytes over the transfer "
+                         "span (the device-to-host rate the call achieved)")
 
     # ---- roofline of the dominant kernel (FP32 issue-bound screen)
     peak32 = fp32_peak_tflops(torch, lib, N)
@@ -1431,6 +1435,9 @@ def main():
     ap.add_argument("--skip-batch", action="store_true", help="leave out the batched-phases leg")
     ap.add_argument("--skip-families", action="store_true", help="leave out the per-family structure-factor leg")
     ap.add_argument("--skip-legacy", action="store_true", help="leave out the legacy calculate_ed_data leg")
+    ap.add_argument("--host-transfer", default="copies", choices=["stores", "copies"],
+                    help="how the e2e leg's spots reach the host: chunked copies (default) or the kernel's own "
+                         "stores into page-locked memory")
     ap.add_argument("--skip-polar", action="store_true", help="leave out the polar-template leg")
     ap.add_argument("--skip-profiles", action="store_true", help="leave out the 1-D profile leg")
     ap.add_argument("--case", default=None, choices=["raster", "adjoint", "batch", "families", "legacy", "polar"],

@@ -52,7 +52,7 @@ EXPORTED_SYMBOLS = (
     "ds_simulate_backward_scratch_bytes", "ds_simulate_backward", "ds_structure_factors_backward_scratch_bytes",
     "ds_axis_angle_compose", "ds_axis_angle_compose_backward", "ds_polar_flatten", "ds_structure_factors_backward",
     "ds_probe_fp32_fma", "ds_set_wait_limits", "ds_probe_wait_timeout", "ds_apply_shape_factors_scratch_bytes",
-    "ds_apply_shape_factors", "ds_last_error", "ds_version",
+    "ds_apply_shape_factors", "ds_host_mapped", "ds_last_error", "ds_version",
 )
 
 
@@ -159,6 +159,7 @@ def load_library(require_cuda: bool = True):
             lib.ds_apply_shape_factors_scratch_bytes.restype = sz
             lib.ds_apply_shape_factors.argtypes = [vp, vp, vp, vp, vp, i64, dp, C.POINTER(ds_spots), vp, sz, vp, vp]
             lib.ds_probe_wait_timeout.argtypes = [i64, vp, sz, vp, vp, vp]
+            lib.ds_host_mapped.argtypes = [vp, C.POINTER(C.c_int32)]
             lib.ds_last_error.restype = C.c_char_p
             lib.ds_version.restype = C.c_char_p
             for name in ("ds_box_extent", "ds_enumerate_hkl", "ds_structure_factors", "ds_kinematical_intensities",
@@ -167,7 +168,7 @@ def load_library(require_cuda: bool = True):
                          "ds_structure_factors_backward",
                          "ds_axis_angle_compose", "ds_axis_angle_compose_backward", "ds_polar_flatten",
                          "ds_probe_fp32_fma", "ds_set_wait_limits", "ds_probe_wait_timeout",
-                         "ds_apply_shape_factors"):
+                         "ds_apply_shape_factors", "ds_host_mapped"):
                 getattr(lib, name).restype = C.c_int32
             _lib = lib
     if require_cuda and not torch.cuda.is_available():
@@ -202,6 +203,14 @@ def check_status_value(v: int, what: str, allow=0) -> int:
     if bad:
         raise NativeError(f"{what}: device status {v}")
     return v
+
+
+def host_mapped(ptr: int) -> bool:
+    """Whether host address ``ptr`` is page-locked memory that kernels address
+    at the same value (``ds_host_mapped``)."""
+    out = C.c_int32(0)
+    check(load_library().ds_host_mapped(C.c_void_p(int(ptr)), C.byref(out)), "host_mapped")
+    return bool(out.value)
 
 
 def set_wait_limits(lookback_polls: int = 0, mbarrier_polls: int = 0):

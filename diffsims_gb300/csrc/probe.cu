@@ -1,6 +1,8 @@
 // FP32 FMA throughput probe: the denominator of the FP32 roofline of the
 // screening kernel (no counterpart in the reference).  Each thread runs eight
 // independent FMA chains; the result is stored so nothing is optimised away.
+// Also the query whether a host buffer is addressable by kernels at its own
+// address (used to let the orientation kernel write its spots to the host).
 #include "common.cuh"
 
 namespace ds {
@@ -26,4 +28,18 @@ extern "C" ds_status ds_probe_fp32_fma(int64_t iters, int32_t blocks, float *out
     DS_REQUIRE(out && iters > 0 && blocks > 0, "ds_probe_fp32_fma: bad arguments");
     fma_probe_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(iters, out);
     return check_launch("fma_probe_kernel");
+}
+
+extern "C" ds_status ds_host_mapped(const void *ptr, int32_t *mapped) {
+    clear_error();
+    DS_REQUIRE(mapped, "ds_host_mapped: mapped is null");
+    *mapped = 0;
+    if (!ptr) return DS_OK;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        (void)cudaGetLastError();  // not known to the runtime: not mapped
+        return DS_OK;
+    }
+    *mapped = (a.type == cudaMemoryTypeHost && a.devicePointer == ptr) ? 1 : 0;
+    return DS_OK;
 }

@@ -377,9 +377,21 @@ class HostSpotPool:
     def __init__(self, max_sets=2, headroom=1.25):
         self.max_sets = int(max_sets)
         self.headroom = float(headroom)
-        # [offsets int64, hkl_index int32, xyzi float32 (n, 4), owner weakref or None, guards]
+        # [offsets int64, hkl_index int32, xyzi float32 (n, 4), owner weakref or None, guards
+        #  (, addressable by kernels)]
         self._sets = []
         self.allocated_bytes = 0
+        # spots per orientation of earlier calls, by (table rows, settings, radius):
+        # sizes the next call's arrays when the kernel writes into them directly
+        self.density = {}
+
+    @staticmethod
+    def mapped(s):
+        """Whether set ``s`` is addressable by kernels at its host addresses
+        (``ds_host_mapped``; asked once per set)."""
+        if len(s) < 6:
+            s.append(all(N.host_mapped(t.data_ptr()) for t in s[:3]))
+        return s[5]
 
     @staticmethod
     def _free(s):
@@ -651,6 +663,147 @@ def simulate_phase_streamed(table: PhaseTable, quats: torch.Tensor, settings: Si
     if timing:
         rec["_events"] = (k_start, k_end, c_start)
     res = StreamedSpots(table, chunks, out_regions, hb, done, base, rec)
+    host_pool.bind(hb, res)
+    return res
+
+
+class HostSpots(PhaseSpots):
+    """Spots of one phase that the orientation kernel stored straight into
+    page-locked host memory (``simulate_phase_to_host``).  ``host()`` returns
+    views of those arrays (complete when the call returns); the device CSR
+    (``offsets``, ``hkl_index``, ``xyzi``) is uploaded on first access.
+    ``timings()`` gives the time split of the call."""
+
+    def __init__(self, table, host_set, n_orient, total, timing=None):
+        self.table = table
+        self._set = host_set         # page-locked (offsets, hkl_index, xyzi) (pool set)
+        self._n = int(n_orient)
+        self.total = int(total)
+        self.excitation_error = None
+        self._host = None
+        self._dev = None
+        self._timing = timing or {}
+
+    @property
+    def n_orient(self):
+        return self._n
+
+    def _device_csr(self):
+        if self._dev is None:
+            hb, dev = self._set, self.table.device
+            self._dev = tuple(x.to(dev) for x in (hb[0][:self._n + 1], hb[1][:self.total], hb[2][:self.total]))
+        return self._dev
+
+    @property
+    def offsets(self):
+        return self._device_csr()[0]
+
+    @property
+    def hkl_index(self):
+        return self._device_csr()[1]
+
+    @property
+    def xyzi(self):
+        return self._device_csr()[2]
+
+    def host(self, pinned=False):
+        if self._host is None:
+            t0 = time.perf_counter()
+            hb = self._set
+            self._host = (hb[0][:self._n + 1].numpy(), hb[1][:self.total].numpy(), hb[2][:self.total].numpy())
+            for arr in self._host:
+                HostSpotPool.guard(hb, arr)
+            self._timing["host_wrap_ms"] = (time.perf_counter() - t0) * 1e3
+        return self._host
+
+    def nbytes(self):
+        return (self._n + 1) * 8 + self.total * (4 + 16)
+
+    def timings(self):
+        """Time split of the call (milliseconds): host set-up before the
+        launch, the host's wait for the kernel, page-locked allocation, and
+        the kernel's device time, which is also the transfer's (its stores
+        are the transfer; ``copy_span_ms`` repeats it)."""
+        t = dict(self._timing)
+        ev = t.pop("_events", None)
+        if ev is not None:
+            k0, k1 = ev
+            k1.synchronize()
+            t["kernel_span_ms"] = t["copy_span_ms"] = k0.elapsed_time(k1)
+            t["first_copy_after_launch_ms"] = 0.0
+        return t
+
+
+def simulate_phase_to_host(table: PhaseTable, quats: torch.Tensor, settings: SimSettings, radius: float,
+                           host_pool: HostSpotPool | None = None, timing=False) -> HostSpots | None:
+    """``simulate_phase`` for a result wanted on the host, as one launch whose
+    output arrays are page-locked host memory: the orientation kernel's own
+    coalesced stores carry the spots over the host link while it computes.
+    The link (about 190 GB/s against 20 bytes per spot) bounds the call; the
+    kernel's work hides under it entirely, with no device staging of the
+    spots and no separate copy.  The host arrays come from ``host_pool``,
+    sized from the spots per orientation of an earlier call with the same
+    table size and settings, else from ``estimate_spots``; a launch that
+    overflows them is re-run once with the exact size.  Returns None, having
+    launched nothing, when there are no orientations or the pool's memory is
+    not addressable by kernels (the caller then copies instead:
+    ``simulate_phase_streamed``).  Returns once the spots are on the host."""
+    t_start = time.perf_counter()
+    n = int(quats.shape[0])
+    if n == 0:
+        return None
+    lib = N.load_library()
+    dev = table.device
+    host_pool = host_pool or HostSpotPool(max_sets=0)
+    p = settings.cstruct()
+    t = table.cstruct()
+    sbytes = int(lib.ds_simulate_scratch_bytes(p, t, n))
+    key = (int(table.n), float(settings.max_excitation_error), float(settings.shape_width),
+           float(settings.precession_angle_rad), int(settings.precession_mode), float(radius))
+    per = host_pool.density.get(key)
+    need = int(n * per * 1.05) + 1024 if per is not None else n * estimate_spots(table, settings, radius)
+    scratch = torch.empty(max(sbytes, 16), dtype=torch.uint8, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    total = torch.zeros(1, dtype=torch.int64, device=dev)
+    comp = torch.cuda.current_stream(dev)
+    alloc_s = wait_s = 0.0
+    events = None
+    for attempt in range(2):
+        ta = time.perf_counter()
+        hb = host_pool.acquire(n, need)
+        alloc_s += time.perf_counter() - ta
+        if not host_pool.mapped(hb):
+            return None
+        if attempt:
+            status.zero_()
+        if timing:
+            events = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            events[0].record(comp)
+        out = N.ds_spots(hb[0].data_ptr(), hb[1].data_ptr(), hb[2].data_ptr(), int(hb[1].shape[0]),
+                         total.data_ptr(), None)
+        N.check(lib.ds_simulate(p, t, N.ptr(quats), n, out, N.ptr(scratch), sbytes, N.ptr(status),
+                                N.stream_handle(comp)), "simulate")
+        if timing:
+            events[1].record(comp)
+        tw = time.perf_counter()
+        if attempt == 0:
+            t_launched = tw
+        v = N.check_device_status(status, "simulate", allow=N.DS_ERR_CAPACITY)  # waits for the kernel
+        wait_s += time.perf_counter() - tw
+        N.check_device_status(table._status, "structure_factors")
+        cnt = int(total.item())
+        if not (v & N.DS_ERR_CAPACITY):
+            break
+        need = cnt
+    else:
+        raise N.NativeError("simulate: output capacity still exceeded after resizing")
+    host_pool.density[key] = cnt / n
+    rec = {"launch_ms": (t_launched - t_start) * 1e3, "chunk_wait_ms": wait_s * 1e3,
+           "pinned_alloc_ms": alloc_s * 1e3, "streamed_call_ms": (time.perf_counter() - t_start) * 1e3,
+           "chunks": 1, "host_wait_ms": 0.0}
+    if timing:
+        rec["_events"] = events
+    res = HostSpots(table, hb, n, cnt, rec)
     host_pool.bind(hb, res)
     return res
 

@@ -12,7 +12,7 @@ import torch
 from . import _native as N
 from .crystal import Phase, Rotation, lattice_params, quaternions_of, structure_of
 from .engine import (HostSpotPool, PhaseBatch, PhaseTable, SimSettings, SpotBuffers, custom_shape_spots,
-                     reciprocal_basis, simulate_phase, simulate_phase_streamed)
+                     reciprocal_basis, simulate_phase, simulate_phase_streamed, simulate_phase_to_host)
 from .simulation1d import Simulation1D
 from .simulation2d import Simulation2D
 from . import interop
@@ -105,6 +105,11 @@ class SimulationGenerator:
                 "The scattering parameters `{}` is not implemented. See documentation for available "
                 "implementations.".format(scattering_params))
         self._host_pool = HostSpotPool()  # page-locked result arrays reused across calls
+        # how a single phase's spots reach the host: "copies" (chunked copies
+        # overlapping the later chunks) or "stores" (the kernel writes them
+        # into page-locked host memory itself; measured slower on the headline
+        # workload: 154 against 180 GB/s over the host link)
+        self.host_transfer = "copies"
         self._qstage = None               # page-locked quaternion staging, reused across calls
         self._qstage_done = None          # event after the last uploads out of the staging
 
@@ -176,8 +181,12 @@ class SimulationGenerator:
         all-FP64 comparator).  ``show_progressbar`` is accepted and ignored
         (each phase is one kernel launch).  With ``stream_to_host`` (the
         default, as the results are normally read on the host) a single
-        phase runs in orientation chunks whose spots are copied to
-        page-locked host memory while later chunks compute; ``False`` keeps
+        phase's spots go to page-locked host memory: with
+        ``host_transfer = "copies"`` (the default) the orientations run in
+        chunks whose spots are copied while later chunks compute, with
+        ``"stores"`` the orientation kernel writes them there itself in one
+        launch (no device copy of the spots; chunked copies where the host
+        memory is not addressable by kernels); ``False`` keeps
         the spots on the device only (for device-side consumers such as
         ``get_diffraction_patterns``); the page-locked host arrays are kept
         by the generator and reused once a previous result is released.
@@ -230,10 +239,16 @@ class SimulationGenerator:
             spots = [custom_shape_spots(t, q, settings, reciprocal_radius, self._custom_shape,
                                         self.shape_factor_kwargs) for t, q in zip(tables, qs)]
         elif len(tables) == 1 and stream_to_host:
-            sp = simulate_phase_streamed(tables[0], qs[0], settings, reciprocal_radius, host_pool=self._host_pool,
-                                         timing=timing)
+            t_sim = time.perf_counter()
+            sp = None
+            if self.host_transfer == "stores":
+                sp = simulate_phase_to_host(tables[0], qs[0], settings, reciprocal_radius, host_pool=self._host_pool,
+                                            timing=timing)
+            if sp is None:
+                sp = simulate_phase_streamed(tables[0], qs[0], settings, reciprocal_radius,
+                                             host_pool=self._host_pool, timing=timing)
             sp._timing.update(table_ms=t_table * 1e3, upload_ms=t_upload * 1e3,
-                              before_stream_ms=(time.perf_counter() - t_call) * 1e3 - sp._timing["streamed_call_ms"])
+                              before_stream_ms=(t_sim - t_call) * 1e3)
             spots = [sp]
         elif len(tables) == 1:
             spots = [simulate_phase(tables[0], qs[0], settings, reciprocal_radius, buffers=SpotBuffers(dev))]

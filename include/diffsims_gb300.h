@@ -191,7 +191,9 @@ typedef struct {
     int32_t _pad;
 } ds_phase_table;
 
-/* Output spots in CSR form (device arrays). */
+/* Output spots in CSR form (device-addressable arrays: device memory, or
+ * page-locked host memory that ds_host_mapped reports as mapped, in which
+ * case the kernel's own stores carry the spots to the host). */
 typedef struct {
     int64_t *offsets;            /* n_orient + 1                                   */
     int32_t *hkl_index;          /* capacity: row of the candidate table           */
@@ -387,6 +389,16 @@ ds_status ds_set_wait_limits(int64_t lookback_polls, int64_t mbarrier_polls);
  * not completed).  scratch: >= 272 bytes (cleared here). */
 ds_status ds_probe_wait_timeout(int64_t polls, void *scratch, size_t scratch_bytes, int64_t *out,
                                 int32_t *status, void *stream);
+
+/* No counterpart in the reference.  *mapped = 1 when `ptr` is page-locked
+ * host memory that kernels address at the same value (unified addressing;
+ * cudaHostAlloc'd memory, the page-locked memory of the caching allocators),
+ * else 0 (device memory, ordinary pageable memory, null).  Such memory may
+ * be given as the output arrays of ds_simulate: the spots then go to the host
+ * in the kernel's own coalesced stores, with no separate copy.  The kernel
+ * only stores to those arrays; they must stay allocated until the stream has
+ * passed the call. */
+ds_status ds_host_mapped(const void *ptr, int32_t *mapped);
 
 /* Last host-side error message of the calling thread ("" if none). */
 const char *ds_last_error(void);

@@ -91,3 +91,87 @@ def test_calculate_diffraction2d_streamed_and_device_only_agree():
     for x, y in zip(a.coordinates[::97], b.coordinates[::97]):
         assert np.array_equal(x.data, y.data) and np.array_equal(x.intensity, y.intensity)
         assert np.array_equal(x.hkl, y.hkl)
+
+
+def test_host_mapped_query():
+    import torch
+    from diffsims_gb300 import _native as N
+    pinned = torch.empty(1024, dtype=torch.int32, pin_memory=True)
+    assert N.host_mapped(pinned.data_ptr())
+    assert N.host_mapped(pinned[100:].data_ptr())  # inside a page-locked block
+    assert not N.host_mapped(torch.empty(1024, dtype=torch.int32, device="cuda").data_ptr())
+    assert not N.host_mapped(np.zeros(1024, np.int32).ctypes.data)
+    assert not N.host_mapped(0)
+
+
+@pytest.mark.parametrize("n_orient", [5000, 777, 1])
+def test_kernel_stores_to_host_equal_one_launch(n_orient):
+    """The orientation kernel writing its spots straight into page-locked host
+    memory gives the device launch's CSR bit for bit, on the host and after
+    the upload of the device CSR."""
+    import torch
+    from diffsims_gb300.engine import SpotBuffers, simulate_phase, simulate_phase_to_host
+    table, q, settings, r = _case(torch, n_orient, model="lorentzian")
+    want = simulate_phase(table, q, settings, r, SpotBuffers(q.device))
+    got = simulate_phase_to_host(table, q, settings, r, timing=True)
+    assert got is not None
+    _check(torch, got, want)
+    t = got.timings()
+    assert t["chunks"] == 1 and t["kernel_span_ms"] > 0 and t["copy_span_ms"] == t["kernel_span_ms"]
+    assert got.nbytes() == (n_orient + 1) * 8 + got.total * 20
+
+
+def test_kernel_stores_to_host_overflow_and_pool_reuse(monkeypatch):
+    """An estimate far too small: the launch overflows the host arrays and is
+    re-run with the exact size; the pool then remembers the density, and a
+    later call reuses the released set without overflowing."""
+    import gc
+    import torch
+    from diffsims_gb300 import engine
+    table, q, settings, r = _case(torch, 2500, seed=4, model="sinc")
+    want = engine.simulate_phase(table, q, settings, r, engine.SpotBuffers(q.device))
+    pool = engine.HostSpotPool()
+    monkeypatch.setattr(engine, "estimate_spots", lambda *a: 1)
+    got = engine.simulate_phase_to_host(table, q, settings, r, host_pool=pool)
+    _check(torch, got, want)
+    assert len(pool.density) == 1 and abs(list(pool.density.values())[0] * 2500 - want.total) < 1e-6
+    n_bytes = pool.allocated_bytes
+    first_set = got._set
+    del got
+    gc.collect()
+    again = engine.simulate_phase_to_host(table, q, settings, r, host_pool=pool)
+    _check(torch, again, want)
+    assert again._set is first_set and pool.allocated_bytes == n_bytes
+    # a live result's arrays are never handed out again
+    third = engine.simulate_phase_to_host(table, q, settings, r, host_pool=pool)
+    assert third._set is not again._set
+    _check(torch, third, want)
+    _check(torch, again, want)
+
+
+def test_kernel_stores_to_host_no_orientations():
+    import torch
+    from diffsims_gb300.engine import simulate_phase_to_host
+    table, q, settings, r = _case(torch, 0)
+    assert simulate_phase_to_host(table, q, settings, r) is None
+
+
+def test_calculate_diffraction2d_host_transfers_agree():
+    import diffsims_gb300 as ds
+    from diffsims_gb300.engine import HostSpots, StreamedSpots
+    rng = np.random.default_rng(11)
+    cr = ok.Crystal((5.4, 6.0, 7.7, 90.0, 90.0, 90.0), ["Si", "O", "O"], rng.random((3, 3)), B=[0.5] * 3)
+    rot = ds.Rotation(ok.random_quaternions(3000, seed=5))
+    gen = ds.SimulationGenerator(200, shape_factor_model="linear")
+    b = gen.calculate_diffraction2d(pu.to_phase(cr), rot, reciprocal_radius=1.2, result="native")
+    assert isinstance(b.spots(0), StreamedSpots)
+    gen.host_transfer = "stores"
+    a = gen.calculate_diffraction2d(pu.to_phase(cr), rot, reciprocal_radius=1.2, result="native")
+    assert isinstance(a.spots(0), HostSpots)
+    for x, y in zip(a.coordinates[::53], b.coordinates[::53]):
+        assert np.array_equal(x.data, y.data) and np.array_equal(x.intensity, y.intensity)
+        assert np.array_equal(x.hkl, y.hkl)
+    # a device-side consumer of a host result: the device CSR is uploaded
+    img = a.get_diffraction_patterns((64, 64), sigma=1, calibration=0.02, stop=8)
+    img_b = b.get_diffraction_patterns((64, 64), sigma=1, calibration=0.02, stop=8)
+    assert bool((img == img_b).all())
