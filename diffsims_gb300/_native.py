@@ -85,7 +85,8 @@ class ds_batch_phase(C.Structure):
 
 class ds_spots(C.Structure):
     _fields_ = [("offsets", C.c_void_p), ("hkl_index", C.c_void_p), ("xyzi", C.c_void_p),
-                ("capacity", C.c_int64), ("total", C.c_void_p), ("excitation_error", C.c_void_p)]
+                ("capacity", C.c_int64), ("total", C.c_void_p), ("excitation_error", C.c_void_p),
+                ("hkl_index_bytes", C.c_int32), ("_reserved", C.c_int32)]
 
 
 class ds_raster_params(C.Structure):

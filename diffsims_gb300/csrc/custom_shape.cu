@@ -100,6 +100,8 @@ extern "C" ds_status ds_apply_shape_factors(const int64_t *offsets_in, const int
     DS_REQUIRE(out && status, "ds_apply_shape_factors: null pointer");
     DS_REQUIRE(n_patterns >= 0, "ds_apply_shape_factors: n_patterns < 0");
     DS_REQUIRE(std::isfinite(minimum_intensity), "ds_apply_shape_factors: minimum_intensity must be finite");
+    DS_REQUIRE(out->hkl_index_bytes == 0 || out->hkl_index_bytes == 4,
+               "ds_apply_shape_factors: hkl_index_bytes must be 0 or 4 (int32 rows)");
     cudaStream_t s = (cudaStream_t)stream;
     DS_REQUIRE(out->offsets && out->total, "ds_apply_shape_factors: null offsets / total");
     if (n_patterns == 0) {

@@ -498,6 +498,9 @@ extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t
         ds_status vs = validate_params(p, "ds_simulate");
         if (vs) return vs;
     }
+    DS_REQUIRE(out->hkl_index_bytes == 0 || out->hkl_index_bytes == 4 ||
+                   (out->hkl_index_bytes == 2 && t->n_hkl <= 65536),
+               "ds_simulate: hkl_index_bytes must be 0 or 4, or 2 for tables of at most 65536 rows");
     cudaStream_t s = (cudaStream_t)stream;
     if (n_orient == 0) {
         DS_CUDA_TRY(cudaMemsetAsync(out->offsets, 0, sizeof(int64_t), s));
@@ -525,6 +528,7 @@ extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t
     c.parts_log2 = refine_parts_log2(p, P.O);
     c.n_tiles = P.n_tiles;
     c.capacity = out->capacity;
+    c.idx16 = out->hkl_index_bytes == 2;
 
     unsigned char *sb = reinterpret_cast<unsigned char *>(scratch);
     TableP T;

@@ -144,6 +144,8 @@ extern "C" ds_status ds_simulate_batch(const ds_sim_params *p, const ds_batch_ph
         ds_status vs = validate_params(p, "ds_simulate_batch");
         if (vs) return vs;
     }
+    DS_REQUIRE(out->hkl_index_bytes == 0 || out->hkl_index_bytes == 4,
+               "ds_simulate_batch: hkl_index_bytes must be 0 or 4 (int32 rows)");
     DS_REQUIRE(p->orient_tile == 0 || p->orient_tile <= (p->form == DS_FORM_FP64 ? 8 : 32),
                "ds_simulate_batch: orient_tile must be <= 32 (mixed; 16 with the precession average) or 8 (FP64)");
     BatchPlan P;

@@ -68,6 +68,7 @@ struct SimConst {
     float int_tau;                  // precession average: FP32 result below this -> FP64
     int mask_on, zero_drop;         // thr > 0, thr >= 0 (the FP64 compares done once, on the host)
     int parts_log2;                 // refine / write units: 2^parts_log2 word ranges per orientation (<= 8)
+    int idx16;                      // rows written as uint16 (tables of at most 65536 rows)
     float thr_up;                   // >= thr, with margin: FP32 pre-check of I <= max * thr
     long long n_hkl, n_orient, n_tiles, capacity;
 };
@@ -1349,7 +1350,10 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
                                         fmaf(op.zb[0], e.x, fmaf(op.zb[1], e.y, op.zb[2] * e.z));
                                 const long long pos = pos0 + out_r + __popc(bal & lanemask_lt);
                                 if (pos < c.capacity) {
-                                    out_idx[pos] = jj[b];
+                                    if (c.idx16)
+                                        reinterpret_cast<uint16_t *>(out_idx)[pos] = (uint16_t)jj[b];
+                                    else
+                                        out_idx[pos] = jj[b];
                                     out_xyzi[pos] = make_float4(x, y, z, II[b]);
                                     if (out_s) {
                                         float I2, z2;
@@ -1375,7 +1379,10 @@ __device__ __forceinline__ void simulate_body(const SimConst &c, const TableP &T
                         spot_xy<FORM>(op, e, x, y);
                         const long long pos = pos0 + rank;
                         if (pos < c.capacity) {
-                            out_idx[pos] = (int32_t)j;
+                            if (c.idx16)
+                                reinterpret_cast<uint16_t *>(out_idx)[pos] = (uint16_t)j;
+                            else
+                                out_idx[pos] = (int32_t)j;
                             out_xyzi[pos] = make_float4(x, y, z, I);
                             if (out_s) out_s[pos] = sv;
                         } else {
@@ -1470,6 +1477,7 @@ inline int refine_parts_log2(const ds_sim_params *p, int O) {
 // The kernel constants of one phase; the per-launch fields (O, W, Ws,
 // n_orient, n_tiles, capacity, line_mode, parts_log2) are set by the caller.
 inline void fill_const(const ds_sim_params *p, const ds_phase_table *t, SimConst &c) {
+    c.idx16 = 0;
     c.k0 = p->k0;
     c.eps = p->max_excitation_error;
     c.width = p->shape_width;

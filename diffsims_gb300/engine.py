@@ -397,10 +397,13 @@ class HostSpotPool:
     def _free(s):
         return (s[3] is None or s[3]() is None) and all(g() is None for g in s[4])
 
-    def acquire(self, n_orient, n_spots):
+    def acquire(self, n_orient, n_spots, index_dtype=torch.int32):
         """A free set with room for ``n_orient`` orientations and ``n_spots``
-        spots (the smallest that fits), or a new one."""
-        fits = [s for s in self._sets if self._free(s) and s[0].shape[0] >= n_orient + 1 and s[1].shape[0] >= n_spots]
+        spots (the smallest that fits) whose row array has ``index_dtype``
+        (int32, or int16 holding the uint16 rows of small tables), or a new
+        one."""
+        fits = [s for s in self._sets if self._free(s) and s[0].shape[0] >= n_orient + 1 and s[1].shape[0] >= n_spots
+                and s[1].dtype == index_dtype]
         if fits:
             s = min(fits, key=lambda s: s[1].shape[0])
             s[3] = None
@@ -414,9 +417,9 @@ class HostSpotPool:
         n_o = int((n_orient + 1) * self.headroom) + 1
         n_s = max(int(n_spots * self.headroom), 1024)
         s = [torch.empty(n_o, dtype=torch.int64, pin_memory=True),
-             torch.empty(n_s, dtype=torch.int32, pin_memory=True),
+             torch.empty(n_s, dtype=index_dtype, pin_memory=True),
              torch.empty((n_s, 4), dtype=torch.float32, pin_memory=True), None, []]
-        self.allocated_bytes += n_o * 8 + n_s * 20
+        self.allocated_bytes += n_o * 8 + n_s * (16 + torch.empty(0, dtype=index_dtype).element_size())
         self._sets.append(s)
         return s
 
@@ -430,6 +433,23 @@ class HostSpotPool:
         here the tensor alias that ``Tensor.numpy()`` creates."""
         base = array.base if array.base is not None else array
         s[4].append(weakref.ref(base))
+
+
+def _row_index_dtype(table) -> torch.dtype:
+    """Storage of the spots' table rows on their way to the host: uint16 rows
+    (kept in int16 tensors) when the table has at most 65536 rows, else int32."""
+    return torch.int16 if table.n <= 65536 else torch.int32
+
+
+def _rows_int32(idx: torch.Tensor) -> torch.Tensor:
+    """Device rows as int32 (uint16 rows held in an int16 tensor widened)."""
+    return idx if idx.dtype == torch.int32 else idx.to(torch.int32) & 0xFFFF
+
+
+def _rows_numpy(idx: torch.Tensor) -> np.ndarray:
+    """Host rows as numpy: int32, or the uint16 view of int16 storage."""
+    a = idx.numpy()
+    return a.view(np.uint16) if a.dtype == np.int16 else a
 
 
 class StreamedSpots(PhaseSpots):
@@ -464,7 +484,7 @@ class StreamedSpots(PhaseSpots):
     def _device_csr(self):
         if self._dev is None:
             regs = [r for r in self._regions if r[3] > 0] or self._regions[:1]
-            idx = torch.cat([r[0][:r[3]] for r in regs])
+            idx = _rows_int32(torch.cat([r[0][:r[3]] for r in regs]))
             xyzi = torch.cat([r[1][:r[3]] for r in regs])
             s = torch.cat([r[2][:r[3]] for r in regs]) if regs[0][2] is not None else None
             self._dev = (idx, xyzi, s)
@@ -501,12 +521,17 @@ class StreamedSpots(PhaseSpots):
             for a, o, base in self._chunks:  # chunk-relative offsets made global
                 off[a:a + o.shape[0] - 1] += base
             off[self._n] = self.total
-            self._host = (off, hb[1][:self.total].numpy(), hb[2][:self.total].numpy())
+            self._host = (off, _rows_numpy(hb[1][:self.total]), hb[2][:self.total].numpy())
             for arr in self._host:
                 HostSpotPool.guard(hb, arr)
             self._timing["host_wait_ms"] = (t1 - t0) * 1e3
             self._timing["host_wrap_ms"] = (time.perf_counter() - t1) * 1e3
         return self._host
+
+    def nbytes(self):
+        """Bytes of the host CSR (what the call copied to the host)."""
+        row = self._host_bufs[1].element_size() if self._host_bufs is not None else 4
+        return (self._n + 1) * 8 + self.total * (row + 16)
 
     def timings(self):
         """Time split of the call (milliseconds), complete after ``host()``:
@@ -558,6 +583,7 @@ def simulate_phase_streamed(table: PhaseTable, quats: torch.Tensor, settings: Si
     t = table.cstruct()
     longest = max(b - a for a, b in zip(bounds[:-1], bounds[1:]))
     sbytes = lib.ds_simulate_scratch_bytes(p, t, longest)
+    idt = _row_index_dtype(table)  # uint16 rows: 18 instead of 20 bytes per spot over the link
     per = estimate_spots(table, settings, radius)
     scratch = torch.empty(max(int(sbytes), 16), dtype=torch.uint8, device=dev)
     status = torch.zeros(n_chunks, dtype=torch.int32, device=dev)
@@ -576,11 +602,11 @@ def simulate_phase_streamed(table: PhaseTable, quats: torch.Tensor, settings: Si
 
     def launch(k, cap):
         a, b = bounds[k], bounds[k + 1]
-        idx = torch.empty(cap, dtype=torch.int32, device=dev)
+        idx = torch.empty(cap, dtype=idt, device=dev)
         xyzi = torch.empty((cap, 4), dtype=torch.float32, device=dev)
         s = torch.empty(cap, dtype=torch.float64, device=dev) if with_excitation_error else None
         out = N.ds_spots(chunk_off[k].data_ptr(), idx.data_ptr(), xyzi.data_ptr(), cap, totals[k:].data_ptr(),
-                         s.data_ptr() if s is not None else None)
+                         s.data_ptr() if s is not None else None, idx.element_size(), 0)
         N.check(lib.ds_simulate(p, t, N.ptr(quats[a:b]) if b > a else N.ptr(quats), b - a, out, N.ptr(scratch),
                                 sbytes, N.ptr(status[k:]), N.stream_handle(comp)), "simulate")
         totals_h[k:k + 1].copy_(totals[k:k + 1], non_blocking=True)
@@ -619,14 +645,14 @@ def simulate_phase_streamed(table: PhaseTable, quats: torch.Tensor, settings: Si
             # host arrays sized from the first chunk's spots per orientation
             need = int(np.ceil(cnt / max(b - a, 1) * n * 1.1)) + 4096
             ta = time.perf_counter()
-            hb = host_pool.acquire(n, need)
+            hb = host_pool.acquire(n, need, idt)
             alloc_s += time.perf_counter() - ta
             h_off, h_idx, h_xyzi = hb[0], hb[1], hb[2]
         if base + cnt > h_idx.shape[0]:
             # the host arrays outgrew the estimate: a larger set (waits for the copies so far)
             copy.synchronize()
             ta = time.perf_counter()
-            nb = host_pool.acquire(n, max(base + cnt, h_idx.shape[0] * 3 // 2))
+            nb = host_pool.acquire(n, max(base + cnt, h_idx.shape[0] * 3 // 2), idt)
             alloc_s += time.perf_counter() - ta
             nb[0][:a].copy_(h_off[:a])
             nb[1][:base].copy_(h_idx[:base])
@@ -691,7 +717,8 @@ class HostSpots(PhaseSpots):
     def _device_csr(self):
         if self._dev is None:
             hb, dev = self._set, self.table.device
-            self._dev = tuple(x.to(dev) for x in (hb[0][:self._n + 1], hb[1][:self.total], hb[2][:self.total]))
+            self._dev = (hb[0][:self._n + 1].to(dev), _rows_int32(hb[1][:self.total].to(dev)),
+                         hb[2][:self.total].to(dev))
         return self._dev
 
     @property
@@ -710,14 +737,14 @@ class HostSpots(PhaseSpots):
         if self._host is None:
             t0 = time.perf_counter()
             hb = self._set
-            self._host = (hb[0][:self._n + 1].numpy(), hb[1][:self.total].numpy(), hb[2][:self.total].numpy())
+            self._host = (hb[0][:self._n + 1].numpy(), _rows_numpy(hb[1][:self.total]), hb[2][:self.total].numpy())
             for arr in self._host:
                 HostSpotPool.guard(hb, arr)
             self._timing["host_wrap_ms"] = (time.perf_counter() - t0) * 1e3
         return self._host
 
     def nbytes(self):
-        return (self._n + 1) * 8 + self.total * (4 + 16)
+        return (self._n + 1) * 8 + self.total * (self._set[1].element_size() + 16)
 
     def timings(self):
         """Time split of the call (milliseconds): host set-up before the
@@ -768,9 +795,10 @@ def simulate_phase_to_host(table: PhaseTable, quats: torch.Tensor, settings: Sim
     comp = torch.cuda.current_stream(dev)
     alloc_s = wait_s = 0.0
     events = None
+    idt = _row_index_dtype(table)
     for attempt in range(2):
         ta = time.perf_counter()
-        hb = host_pool.acquire(n, need)
+        hb = host_pool.acquire(n, need, idt)
         alloc_s += time.perf_counter() - ta
         if not host_pool.mapped(hb):
             return None
@@ -780,7 +808,7 @@ def simulate_phase_to_host(table: PhaseTable, quats: torch.Tensor, settings: Sim
             events = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
             events[0].record(comp)
         out = N.ds_spots(hb[0].data_ptr(), hb[1].data_ptr(), hb[2].data_ptr(), int(hb[1].shape[0]),
-                         total.data_ptr(), None)
+                         total.data_ptr(), None, hb[1].element_size(), 0)
         N.check(lib.ds_simulate(p, t, N.ptr(quats), n, out, N.ptr(scratch), sbytes, N.ptr(status),
                                 N.stream_handle(comp)), "simulate")
         if timing:

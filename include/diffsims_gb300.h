@@ -201,6 +201,10 @@ typedef struct {
     int64_t capacity;
     int64_t *total;              /* one int64: spots of the call (may exceed capacity) */
     double *excitation_error;    /* capacity, optional (null): s of every spot      */
+    int32_t hkl_index_bytes;     /* 0 or 4: int32 rows; 2: uint16 rows (ds_simulate
+                                    with tables of at most 65536 rows only; hkl_index
+                                    then points at capacity uint16 values)        */
+    int32_t _reserved;           /* 0 */
 } ds_spots;
 
 size_t ds_simulate_scratch_bytes(const ds_sim_params *p, const ds_phase_table *t, int64_t n_orient);
@@ -213,7 +217,9 @@ size_t ds_simulate_scratch_bytes(const ds_sim_params *p, const ds_phase_table *t
  * quats: n_orient x 4 doubles (w, x, y, z) -- active rotation of the crystal.
  * On capacity overflow *total still gets the exact size, offsets are exact,
  * rows beyond capacity are not written and DS_ERR_CAPACITY is or-ed into
- * *status: re-run with capacity >= *total. */
+ * *status: re-run with capacity >= *total.  out->hkl_index_bytes = 2 writes
+ * the rows as uint16 (tables of at most 65536 rows): 18 instead of 20 bytes
+ * per spot for results that travel to the host. */
 ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t, const double *quats,
                       int64_t n_orient, ds_spots *out, void *scratch, size_t scratch_bytes,
                       int32_t *status, void *stream);

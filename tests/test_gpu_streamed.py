@@ -118,7 +118,8 @@ def test_kernel_stores_to_host_equal_one_launch(n_orient):
     _check(torch, got, want)
     t = got.timings()
     assert t["chunks"] == 1 and t["kernel_span_ms"] > 0 and t["copy_span_ms"] == t["kernel_span_ms"]
-    assert got.nbytes() == (n_orient + 1) * 8 + got.total * 20
+    assert got.host()[1].dtype == np.uint16  # a small table: 2-byte rows
+    assert got.nbytes() == (n_orient + 1) * 8 + got.total * 18
 
 
 def test_kernel_stores_to_host_overflow_and_pool_reuse(monkeypatch):
@@ -175,3 +176,35 @@ def test_calculate_diffraction2d_host_transfers_agree():
     img = a.get_diffraction_patterns((64, 64), sigma=1, calibration=0.02, stop=8)
     img_b = b.get_diffraction_patterns((64, 64), sigma=1, calibration=0.02, stop=8)
     assert bool((img == img_b).all())
+
+
+def _large_case(torch, n_orient, cell, radius, seed=3):
+    from diffsims_gb300.engine import PhaseTable
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(seed)
+    cr = ok.Crystal((cell, cell * 1.07, cell * 0.93, 90.0, 90.0, 90.0), list(rng.choice(["O", "Si"], 6)),
+                    rng.random((6, 3)), B=rng.uniform(0.3, 1.0, 6))
+    p = ok.SimParams(accelerating_voltage=200, reciprocal_radius=radius, max_excitation_error=0.01,
+                     shape_factor_model="lorentzian")
+    settings = pu.generator_for(p).settings(p.max_excitation_error)
+    table = PhaseTable(pu.to_phase(cr), radius, True, "lobato", list(cr.B), device=dev)
+    q = torch.as_tensor(ok.random_quaternions(n_orient, seed=seed + 1)).to(dev)
+    return table, q, settings, radius
+
+
+@pytest.mark.parametrize("cell,radius,row_dtype", [(12.0, 2.0, np.uint16), (19.0, 1.6, np.int32)])
+def test_row_width_by_table_size(cell, radius, row_dtype):
+    """Rows go to the host as uint16 for tables of at most 65536 rows (here
+    ~60k, so rows above 32767 exercise the unsigned widening) and as int32
+    above that; both transfers equal the device launch."""
+    import torch
+    from diffsims_gb300.engine import SpotBuffers, simulate_phase, simulate_phase_streamed, simulate_phase_to_host
+    table, q, settings, r = _large_case(torch, 600, cell, radius)
+    assert (table.n <= 65536) == (row_dtype == np.uint16)
+    want = simulate_phase(table, q, settings, r, SpotBuffers(q.device))
+    assert want.total > 0 and (row_dtype == np.int32 or int(want.hkl_index.max()) > 32767)
+    for got in (simulate_phase_streamed(table, q, settings, r, chunk=256, first_chunk=64),
+                simulate_phase_to_host(table, q, settings, r)):
+        _check(torch, got, want)
+        assert got.host()[1].dtype == row_dtype and got.hkl_index.dtype == torch.int32
+        assert got.nbytes() == 601 * 8 + got.total * (16 + np.dtype(row_dtype).itemsize)

@@ -351,6 +351,31 @@ def test_refine_parts_is_validated(lib):
         assert lib.ds_simulate_batch(p, None, 0, out, fake, 1 << 20, fake, None) == N.DS_ERR_INVALID_ARGUMENT
 
 
+def test_row_index_width_is_validated(lib):
+    """ds_spots.hkl_index_bytes: 0 or 4 (int32 rows) everywhere, 2 (uint16
+    rows) for ds_simulate with tables of at most 65536 rows; anything else is
+    rejected with a message before any CUDA call."""
+    import ctypes as C
+    from diffsims_gb300 import _native as N
+    from diffsims_gb300.engine import SimSettings
+    p = SimSettings(39.87, 0.02, 0.02, "lorentzian").cstruct()
+    fake = C.c_void_p(16)
+    t = N.ds_phase_table()
+    for n_hkl, width in ((70000, 2), (100, 3), (100, 8), (100, -4)):
+        t.n_hkl = n_hkl
+        out = N.ds_spots(fake, fake, fake, 0, fake, None, width, 0)
+        assert lib.ds_simulate(p, t, fake, 1, out, fake, 1 << 20, fake, None) == N.DS_ERR_INVALID_ARGUMENT
+        assert "hkl_index_bytes" in lib.ds_last_error().decode()
+    out = N.ds_spots(fake, fake, fake, 0, fake, None, 2, 0)
+    phases = (N.ds_batch_phase * 1)()
+    assert lib.ds_simulate_batch(p, phases, 1, out, fake, 1 << 20, fake, None) == N.DS_ERR_INVALID_ARGUMENT
+    assert "hkl_index_bytes" in lib.ds_last_error().decode()
+    assert lib.ds_apply_shape_factors(fake, fake, fake, fake, fake, 5, 1e-20, out, fake, 1 << 20, fake,
+                                      None) == N.DS_ERR_INVALID_ARGUMENT
+    assert "hkl_index_bytes" in lib.ds_last_error().decode()
+    assert C.sizeof(N.ds_spots) == 6 * 8 + 2 * 4
+
+
 def test_phase_spots_select_and_copy():
     """PhaseSpots.select gathers whole patterns of the CSR (an index, a slice
     or an array, in the given order) and deepcopy owns its arrays; checked
