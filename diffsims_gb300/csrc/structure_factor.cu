@@ -155,11 +155,21 @@ sf_mixed_kernel(SfConst c, ds_atoms A, const int32_t *__restrict__ hkl_i, const 
     }
     const float g2f = (float)g2;
     // f_s(g) in FP64: the Lobato fits sum terms of mixed sign and size, whose
-    // cancellation costs FP32 up to ~1e-4 relative; one evaluation per
-    // (reflection, species) is cheap next to the per-atom phase work.
+    // cancellation costs FP32 up to ~1e-4 relative.  One evaluation per
+    // (reflection, species): the L lanes of a reflection take the species in
+    // turn and each value is copied to all L lanes' slots (the per-atom reads
+    // stay one slot per thread, free of bank conflicts).  Evaluated on every
+    // lane, the FP64 divisions of the fits cost more than the phase work.
     const double *cd = reinterpret_cast<const double *>(smem + Ls.coeff_d);
-    for (int s = 0; s < c.n_species; ++s)
-        fs[s * SF_THREADS + threadIdx.x] = (float)scatter_f64(cd + 10 * s, c.kind, g2);
+    {
+        const int g0 = threadIdx.x - sub;  // first lane of this reflection's group (same warp)
+        for (int s = sub; s < c.n_species; s += L) {
+            const float v = (float)scatter_f64(cd + 10 * s, c.kind, g2);
+#pragma unroll
+            for (int q = 0; q < L; ++q) fs[s * SF_THREADS + g0 + q] = v;
+        }
+        __syncwarp();
+    }
 
     dd re = {0.f, 0.f}, im = {0.f, 0.f};
     float sumsq = 0.f;
@@ -241,7 +251,25 @@ sf_fp64_kernel(SfConst c, ds_atoms A, const int32_t *__restrict__ hkl_i, const d
             if (c.g_is_spacing) g2 = g2 * g2;
         }
         double fsp[SF_MAX_SPECIES];
-        for (int s = 0; s < c.n_species; ++s) fsp[s] = scatter_f64(cd + 10 * s, c.kind, g2);
+        if constexpr (L == 1) {
+            for (int s = 0; s < c.n_species; ++s) fsp[s] = scatter_f64(cd + 10 * s, c.kind, g2);
+        } else {
+            // one evaluation per (reflection, species): lane sub of the group
+            // evaluates species sub, sub + L, ..., and the values are shuffled
+            // to the group's lanes (every lane runs every shuffle: n_species
+            // and the loop trip counts are uniform)
+            constexpr int R = (SF_MAX_SPECIES + L - 1) / L;
+            const int g0 = (threadIdx.x & 31) - sub;
+            double mine[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int s = sub + r * L;
+                mine[r] = s < c.n_species ? scatter_f64(cd + 10 * s, c.kind, g2) : 0.0;
+            }
+#pragma unroll
+            for (int s = 0; s < SF_MAX_SPECIES; ++s)
+                if (s < c.n_species) fsp[s] = __shfl_sync(FULL_MASK, mine[s / L], g0 + s % L);
+        }
         double re = 0.0, im = 0.0;
         // amplitude of the previous atom: consecutive atoms with the same
         // species, occupancy and B (the positions of one orbit) reuse it
