@@ -972,7 +972,9 @@ def run_polar(args, torch, dev, hbm_peak, spots):
     rax = np.linspace(0.0, 2.0, 256)
     aax = np.linspace(-np.pi, np.pi, 360)
     out = {}
-    for name, kw in (("unbinned", {}), ("binned", dict(radial_axes=rax, azimuthal_axes=aax))):
+    binned = dict(radial_axes=rax, azimuthal_axes=aax)
+    for name, kw in (("unbinned", {}), ("binned", binned), ("unbinned_fp32", dict(precision="fp32")),
+                     ("binned_fp32", dict(binned, precision="fp32"))):
         for _ in range(args.warmup):
             res = polar_flatten([spots], **kw)
         del res
@@ -990,6 +992,18 @@ def run_polar(args, torch, dev, hbm_peak, spots):
         nbytes = spots.total * 16 + 3 * n * m * 8
         out[name] = {"ms": t, "patterns_per_s": n / (t * 1e-3), "achieved_gbs": nbytes / (t * 1e-3) / 1e9,
                      "frac": nbytes / (t * 1e-3) / 1e9 / hbm_peak, "bytes": int(nbytes)}
+    # the FP32 mode against the FP64 one on every slot: r and theta relative
+    # error (unbinned), index mismatches (binned)
+    err = {}
+    a, b = polar_flatten([spots]), polar_flatten([spots], precision="fp32")
+    for k, name in ((0, "r"), (1, "theta")):
+        d = (a[k] - b[k]).abs() / a[k].abs().clamp_min(1e-30)
+        err[f"max_rel_{name}"] = float(torch.where(a[k] != 0, d, torch.zeros_like(d)).max().item())
+    del a, b
+    a, b = polar_flatten([spots], **binned), polar_flatten([spots], **binned, precision="fp32")
+    err["binned_slots_differing"] = int(((a[0] != b[0]) | (a[1] != b[1]) | (a[2] != b[2])).sum().item())
+    err["binned_patterns_differing"] = int(((a[0] != b[0]) | (a[1] != b[1]) | (a[2] != b[2])).any(1).sum().item())
+    del a, b
     off, _, xyzi = spots.host()
     n_cpu = 2000
     pats = [(xyzi[off[k]:off[k + 1], :3].astype(np.float64), xyzi[off[k]:off[k + 1], 3].astype(np.float64))
@@ -1001,9 +1015,12 @@ def run_polar(args, torch, dev, hbm_peak, spots):
             "unit": "patterns/s", "patterns": n, "max_spots": m, "spots": int(spots.total), **out,
             "roofline": {"bound": "hbm", "achieved": out["unbinned"]["achieved_gbs"], "peak": hbm_peak,
                          "unit": "GB/s", "frac": out["unbinned"]["frac"]},
+            "fp32_vs_fp64": err,
             "cpu_baseline": {"value": cpu_rate, "unit": "patterns/s", "cores": 1, "kind": "port",
                              "sample": f"{n_cpu} patterns of the same spots, the oracle's numpy polar_flatten"},
-            "note": "the launch plus its three float64 output allocations (the kernel writes the padding)"}
+            "note": "the launch plus its three float64 output allocations (the kernel writes the padding); "
+                    "value and roofline: the FP64 (reference-exact) unbinned mode; *_fp32: r and theta in FP32 "
+                    "(ds_polar_flatten_f32)"}
 
 
 def run_profiles(args, torch, dev):
@@ -1303,6 +1320,8 @@ def run_case(args):
                             SpotBuffers(dev))
         polar_flatten([sp])
         polar_flatten([sp], np.linspace(0.0, 2.0, 256), np.linspace(-np.pi, np.pi, 360))
+        polar_flatten([sp], precision="fp32")
+        polar_flatten([sp], np.linspace(0.0, 2.0, 256), np.linspace(-np.pi, np.pi, 360), precision="fp32")
         out.update(patterns=8192, spots=sp.total)
     elif args.case == "legacy":
         # the legacy leg's 12-atom P1 sphere table at r = 2.0 and 8192 Euler triples

@@ -52,7 +52,7 @@ EXPORTED_SYMBOLS = (
     "ds_simulate_backward_scratch_bytes", "ds_simulate_backward", "ds_structure_factors_backward_scratch_bytes",
     "ds_axis_angle_compose", "ds_axis_angle_compose_backward", "ds_polar_flatten", "ds_structure_factors_backward",
     "ds_probe_fp32_fma", "ds_set_wait_limits", "ds_probe_wait_timeout", "ds_apply_shape_factors_scratch_bytes",
-    "ds_apply_shape_factors", "ds_host_mapped", "ds_last_error", "ds_version",
+    "ds_apply_shape_factors", "ds_host_mapped", "ds_polar_flatten_f32", "ds_last_error", "ds_version",
 )
 
 
@@ -153,6 +153,7 @@ def load_library(require_cuda: bool = True):
                                                           vp, vp, vp, sz, vp]
             lib.ds_axis_angle_compose.argtypes = [vp, vp, i64, vp, vp]
             lib.ds_polar_flatten.argtypes = [vp, vp, i64, i64, vp, i64, vp, i64, vp, vp, vp, vp]
+            lib.ds_polar_flatten_f32.argtypes = [vp, vp, i64, i64, vp, i64, vp, i64, vp, vp, vp, vp]
             lib.ds_axis_angle_compose_backward.argtypes = [vp, vp, i64, vp, vp, vp]
             lib.ds_probe_fp32_fma.argtypes = [i64, i32, vp, vp]
             lib.ds_set_wait_limits.argtypes = [i64, i64]
@@ -169,7 +170,7 @@ def load_library(require_cuda: bool = True):
                          "ds_structure_factors_backward",
                          "ds_axis_angle_compose", "ds_axis_angle_compose_backward", "ds_polar_flatten",
                          "ds_probe_fp32_fma", "ds_set_wait_limits", "ds_probe_wait_timeout",
-                         "ds_apply_shape_factors", "ds_host_mapped"):
+                         "ds_apply_shape_factors", "ds_host_mapped", "ds_polar_flatten_f32"):
                 getattr(lib, name).restype = C.c_int32
             _lib = lib
     if require_cuda and not torch.cuda.is_available():

@@ -1266,14 +1266,23 @@ def simulate_batch(tables, quats, settings: SimSettings, radius: float, orient_t
     return PhaseBatch(tables, quats, settings, radius, orient_tile=orient_tile).run().spots()
 
 
-def polar_flatten(spots_list, radial_axes=None, azimuthal_axes=None):
+def polar_flatten(spots_list, radial_axes=None, azimuthal_axes=None, precision="fp64"):
     """Padded (r, theta, intensity) templates of every pattern of the given
     phases in order (``ds_polar_flatten``): three float64 device tensors of
     shape (patterns, max spots per pattern); with both axes, r and theta
-    hold closest-axis indices and out-of-range spots are dropped."""
+    hold closest-axis indices and out-of-range spots are dropped.
+    ``precision`` 'fp64' (default) computes r and theta in FP64 from the
+    float32 positions, as the reference does; 'fp32' in FP32 with float
+    axes (``ds_polar_flatten_f32``: ~2e-7 relative, bound by HBM instead of
+    the FP64 pipe)."""
     lib = N.load_library()
     if not spots_list:
         raise ValueError("no patterns")
+    if precision not in ("fp64", "fp32"):
+        raise ValueError("precision must be 'fp64' or 'fp32'")
+    f32 = precision == "fp32"
+    axis_np, axis_t = (np.float32, torch.float32) if f32 else (np.float64, torch.float64)
+    entry = lib.ds_polar_flatten_f32 if f32 else lib.ds_polar_flatten
     dev = spots_list[0].offsets.device
     counts = [int(s.n_orient) for s in spots_list]
     maxes = [int((s.offsets[1:] - s.offsets[:-1]).max().item()) if s.n_orient else 0 for s in spots_list]
@@ -1283,13 +1292,13 @@ def polar_flatten(spots_list, radial_axes=None, azimuthal_axes=None):
     t = torch.empty((n, m), dtype=torch.float64, device=dev)
     i = torch.empty((n, m), dtype=torch.float64, device=dev)
     binned = radial_axes is not None and azimuthal_axes is not None
-    rax = torch.as_tensor(np.asarray(radial_axes, dtype=np.float64)).to(dev) if binned else None
-    aax = torch.as_tensor(np.asarray(azimuthal_axes, dtype=np.float64)).to(dev) if binned else None
+    rax = torch.as_tensor(np.asarray(radial_axes, dtype=axis_np)).to(dev, axis_t) if binned else None
+    aax = torch.as_tensor(np.asarray(azimuthal_axes, dtype=axis_np)).to(dev, axis_t) if binned else None
     row = 0
     for s, c in zip(spots_list, counts):
         if c and m:
             xyzi = s.xyzi if s.total else torch.zeros((1, 4), dtype=torch.float32, device=dev)
-            N.check(lib.ds_polar_flatten(N.ptr(s.offsets), N.ptr(xyzi), c, m, N.ptr(rax),
+            N.check(entry(N.ptr(s.offsets), N.ptr(xyzi), c, m, N.ptr(rax),
                                          0 if rax is None else rax.numel(), N.ptr(aax),
                                          0 if aax is None else aax.numel(), N.ptr(r[row:]), N.ptr(t[row:]),
                                          N.ptr(i[row:]), N.stream_handle()), "polar_flatten")

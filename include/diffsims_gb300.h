@@ -334,6 +334,18 @@ ds_status ds_polar_flatten(const int64_t *offsets, const float *xyzi, int64_t n_
                            int64_t n_azimuthal, double *r_out, double *theta_out, double *intensity_out,
                            void *stream);
 
+/* ds_polar_flatten with r and theta computed in FP32 (sqrtf of x x + y y
+ * rounded in FP32, atan2f) and the axes given as float and searched in FP32;
+ * the outputs are the same float64 arrays.  r and theta agree with the FP64
+ * entry to ~2e-7 relative (the order of the float32 spot positions' own
+ * rounding); closest-axis indices can differ only for values that close to a
+ * decision boundary.  Bound by its bytes instead of the FP64 pipe.  No
+ * counterpart in the reference beyond ds_polar_flatten's. */
+ds_status ds_polar_flatten_f32(const int64_t *offsets, const float *xyzi, int64_t n_patterns, int64_t max_spots,
+                               const float *radial_axes, int64_t n_radial, const float *azimuthal_axes,
+                               int64_t n_azimuthal, double *r_out, double *theta_out, double *intensity_out,
+                               void *stream);
+
 /* ------------------------------------------------------------------------ */
 /* Adjoint of the spot intensities I = shf(s, r) |F_hkl|^2 (no counterpart in
  * the reference, which is not differentiable).  After a ds_simulate call with

@@ -66,3 +66,64 @@ def test_polar_templates_of_simulated_phases():
     np.testing.assert_array_equal(r, wr)
     np.testing.assert_array_equal(t, wt)
     np.testing.assert_array_equal(i, wi)
+
+
+def _near_boundary(v, axis, rel):
+    """Whether v lies within rel (relative, floor 1e-12) of a closest-axis
+    decision boundary: an entry (searchsorted) or a midpoint of two."""
+    mids = 0.5 * (axis[1:] + axis[:-1])
+    tol = rel * max(abs(v), 1.0) + 1e-12
+    return np.min(np.abs(axis - v)) < tol or (mids.size and np.min(np.abs(mids - v)) < tol)
+
+
+def test_polar_templates_fp32_mode():
+    """ds_polar_flatten_f32: r within 3e-7 and theta within 3e-7 relative (+1e-12)
+    of the FP64 restatement on the same float32 positions, intensities exact,
+    the same padding; binned indices equal except in patterns with a spot
+    whose FP64 value is within 1e-6 of a decision boundary."""
+    import diffsims_gb300 as ds
+    from tests.test_gpu_batch import random_cell
+    crystals = [random_cell(43, 8, edges=(4, 7)), random_cell(44, 16, edges=(7, 10))]
+    rots = [ds.Rotation(ok.random_quaternions(40, seed=9)), ds.Rotation(ok.random_quaternions(17, seed=10))]
+    gen = ds.SimulationGenerator(200, shape_factor_model="lorentzian")
+    sim = gen.calculate_diffraction2d([pu.to_phase(c) for c in crystals], rots, reciprocal_radius=1.3)
+    pats = [(v.data, v.intensity) for v in sim]
+    r, t, i = sim.polar_flatten_simulations(precision="fp32")
+    wr, wt, wi = ok.polar_flatten(pats)
+    assert r.shape == wr.shape and r.dtype == np.float64
+    np.testing.assert_allclose(r, wr, rtol=3e-7, atol=1e-12)
+    np.testing.assert_allclose(t, wt, rtol=3e-7, atol=1e-12)
+    np.testing.assert_array_equal(i, wi)
+    ra, ta = np.linspace(0, 1.3, 97), np.linspace(-np.pi, np.pi, 361)
+    r, t, i = sim.polar_flatten_simulations(radial_axes=ra, azimuthal_axes=ta, precision="fp32")
+    wr, wt, wi = ok.polar_flatten(pats, ra, ta)
+    assert r.dtype.kind == "i" and r.shape == wr.shape
+    diff = np.argwhere((r != wr) | (t != wt) | (i != wi))
+    exact_r, exact_t, _ = ok.polar_flatten(pats)
+    for p, k in diff:
+        # a differing slot: some spot of that pattern sits on a boundary
+        row_r, row_t = exact_r[p], exact_t[p]
+        assert any(_near_boundary(v, ra, 1e-6) for v in row_r) or any(_near_boundary(v, ta, 1e-6) for v in row_t)
+    with pytest.raises(ValueError):
+        sim.polar_flatten_simulations(precision="fp16")
+
+
+def test_polar_binned_nonuniform_axes():
+    """Axes that are not evenly spaced (random sorted values with repeats and
+    a geometric radial axis): the search from the uniform estimate falls back
+    to bisection and the FP64 mode still equals the oracle exactly."""
+    import diffsims_gb300 as ds
+    from tests.test_gpu_batch import random_cell
+    rng = np.random.default_rng(12)
+    cr = random_cell(45, 10, edges=(5, 8))
+    sim = ds.SimulationGenerator(200, shape_factor_model="linear").calculate_diffraction2d(
+        pu.to_phase(cr), ds.Rotation(ok.random_quaternions(25, seed=13)), reciprocal_radius=1.1)
+    pats = [(v.data, v.intensity) for v in sim]
+    axes = [(np.geomspace(0.01, 1.1, 40), np.sort(rng.uniform(-np.pi, np.pi, 50))),
+            (np.sort(np.concatenate([rng.uniform(0, 1.1, 30), [0.3] * 4])), np.linspace(-np.pi, np.pi, 7))]
+    for ra, ta in axes:
+        r, t, i = sim.polar_flatten_simulations(radial_axes=ra, azimuthal_axes=ta)
+        wr, wt, wi = ok.polar_flatten(pats, ra, ta)
+        np.testing.assert_array_equal(r, wr)
+        np.testing.assert_array_equal(t, wt)
+        np.testing.assert_array_equal(i, wi)
