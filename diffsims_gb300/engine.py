@@ -464,9 +464,12 @@ class StreamedSpots(PhaseSpots):
     from the chunks' regions on first access.  ``timings()`` gives the time
     split of the call once the copies are done."""
 
-    def __init__(self, table, chunks, regions, host_bufs, done, total, timing=None):
+    def __init__(self, table, chunks, regions, host_bufs, done, total, timing=None, status_h=None,
+                 off_stage=None):
         self.table = table
-        self._chunks = chunks        # per chunk: (first orientation, chunk offsets on the device, spot base)
+        self._status_h = status_h    # chunks' status words, complete at ``done`` (None: checked already)
+        self._off_stage = off_stage  # page-locked copy of the chunks' offsets (chunk k at a + k), at ``done``
+        self._chunks = chunks        # per chunk: (first orientation, chunk offsets on the device, spot base, k)
         self._regions = regions      # per chunk: (idx, xyzi, s, n_spots)
         self._host_bufs = host_bufs  # page-locked (offsets, hkl_index, xyzi) (pool set)
         self._done = done            # event after the last copy
@@ -481,8 +484,18 @@ class StreamedSpots(PhaseSpots):
     def n_orient(self):
         return self._n
 
+    def _check_status(self):
+        """Raise on a condition any chunk's kernel reported (waits for the
+        copies, behind which the status words travel)."""
+        if self._status_h is not None:
+            self._done.synchronize()
+            for v in self._status_h.tolist():
+                N.check_status_value(int(v), "simulate")
+            self._status_h = None
+
     def _device_csr(self):
         if self._dev is None:
+            self._check_status()
             regs = [r for r in self._regions if r[3] > 0] or self._regions[:1]
             idx = _rows_int32(torch.cat([r[0][:r[3]] for r in regs]))
             xyzi = torch.cat([r[1][:r[3]] for r in regs])
@@ -494,7 +507,8 @@ class StreamedSpots(PhaseSpots):
     @property
     def offsets(self):
         if self._off is None:
-            parts = [o[:-1] + base for _, o, base in self._chunks]
+            self._check_status()
+            parts = [o[:-1] + base for _, o, base, _ in self._chunks]
             parts.append(torch.full((1,), self.total, dtype=torch.int64, device=self._chunks[0][1].device))
             self._off = torch.cat(parts)
         return self._off
@@ -516,10 +530,13 @@ class StreamedSpots(PhaseSpots):
             t0 = time.perf_counter()
             self._done.synchronize()
             t1 = time.perf_counter()
+            self._check_status()
             hb = self._host_bufs
             off = hb[0][:self._n + 1].numpy()
-            for a, o, base in self._chunks:  # chunk-relative offsets made global
-                off[a:a + o.shape[0] - 1] += base
+            stage = self._off_stage.numpy()
+            for a, o, base, k in self._chunks:  # chunk-relative offsets made global
+                m = o.shape[0] - 1
+                np.add(stage[a + k:a + k + m], base, out=off[a:a + m])
             off[self._n] = self.total
             self._host = (off, _rows_numpy(hb[1][:self.total]), hb[2][:self.total].numpy())
             for arr in self._host:
@@ -551,15 +568,16 @@ class StreamedSpots(PhaseSpots):
 
 
 def simulate_phase_streamed(table: PhaseTable, quats: torch.Tensor, settings: SimSettings, radius: float,
-                            chunk=32768, first_chunk=2048, with_excitation_error=False,
+                            chunk=32768, first_chunk=1024, with_excitation_error=False,
                             host_pool: HostSpotPool | None = None, timing=False) -> StreamedSpots:
     """``simulate_phase`` for a result wanted on the host: the orientations
     run in chunks on the current stream, each into its own device region,
     and each chunk's spots are copied to page-locked host memory on a side
     stream as soon as its count is known, while the next chunks compute.
-    Chunk sizes double from ``first_chunk`` up to ``chunk``: the copies
-    start early, and the copy of a chunk (at about twice the kernel's time
-    per orientation) overlaps the next, twice larger, chunk.  A chunk whose
+    Chunk sizes grow by 7/4 from ``first_chunk`` up to ``chunk``: the copies
+    start early, and the copy of a chunk (at about 1.8 times the kernel's
+    time per orientation) lasts as long as the next chunk's kernel, so the
+    link does not wait for the kernel (with doubling it would).  A chunk whose
     spots overflow its region is re-run alone with the exact size.  The host
     arrays come from ``host_pool`` (reused across calls) or are allocated;
     they are sized from the first chunk's spot count.  With ``timing`` the
@@ -575,7 +593,7 @@ def simulate_phase_streamed(table: PhaseTable, quats: torch.Tensor, settings: Si
     size = max(1, min(first_chunk, chunk))
     while bounds[-1] < n:
         bounds.append(min(n, bounds[-1] + size))
-        size = min(chunk, 2 * size)
+        size = min(chunk, size * 7 // 4)
     if len(bounds) == 1:
         bounds.append(0)
     n_chunks = len(bounds) - 1
@@ -588,9 +606,19 @@ def simulate_phase_streamed(table: PhaseTable, quats: torch.Tensor, settings: Si
     scratch = torch.empty(max(int(sbytes), 16), dtype=torch.uint8, device=dev)
     status = torch.zeros(n_chunks, dtype=torch.int32, device=dev)
     totals = torch.zeros(n_chunks, dtype=torch.int64, device=dev)
-    totals_h = torch.empty(n_chunks, dtype=torch.int64, pin_memory=True)
+    totals_h = torch.zeros(n_chunks, dtype=torch.int64, pin_memory=True)
     status_h = torch.empty(n_chunks, dtype=torch.int32, pin_memory=True)
-    chunk_off = [torch.empty(b - a + 1, dtype=torch.int64, device=dev) for a, b in zip(bounds[:-1], bounds[1:])]
+    # Each chunk's spot count goes straight to page-locked host memory in the
+    # kernel's own store: a copy of it on the compute stream would queue in
+    # the copy engine behind the spot copies and hold the next chunk's kernel
+    # (and, through the host, the next copy) back.  The status words are
+    # copied once after the last chunk.
+    direct_totals = n > 0 and N.host_mapped(totals_h.data_ptr())
+    # the chunks' offsets side by side in one array (chunk k at a + k), copied
+    # to the host in one piece after the last chunk
+    all_off = torch.empty(n + n_chunks, dtype=torch.int64, device=dev)
+    off_stage = torch.empty(n + n_chunks, dtype=torch.int64, pin_memory=True)
+    chunk_off = [all_off[a + k:b + k + 1] for k, (a, b) in enumerate(zip(bounds[:-1], bounds[1:]))]
     sf_status_h = torch.empty(1, dtype=torch.int32, pin_memory=True)
     sf_status_h.copy_(table._status, non_blocking=True)  # read after the first chunk, without a stall
     k_start = k_end = c_start = None
@@ -605,40 +633,45 @@ def simulate_phase_streamed(table: PhaseTable, quats: torch.Tensor, settings: Si
         idx = torch.empty(cap, dtype=idt, device=dev)
         xyzi = torch.empty((cap, 4), dtype=torch.float32, device=dev)
         s = torch.empty(cap, dtype=torch.float64, device=dev) if with_excitation_error else None
-        out = N.ds_spots(chunk_off[k].data_ptr(), idx.data_ptr(), xyzi.data_ptr(), cap, totals[k:].data_ptr(),
+        total_ptr = totals_h[k:].data_ptr() if direct_totals else totals[k:].data_ptr()
+        out = N.ds_spots(chunk_off[k].data_ptr(), idx.data_ptr(), xyzi.data_ptr(), cap, total_ptr,
                          s.data_ptr() if s is not None else None, idx.element_size(), 0)
         N.check(lib.ds_simulate(p, t, N.ptr(quats[a:b]) if b > a else N.ptr(quats), b - a, out, N.ptr(scratch),
                                 sbytes, N.ptr(status[k:]), N.stream_handle(comp)), "simulate")
-        totals_h[k:k + 1].copy_(totals[k:k + 1], non_blocking=True)
-        status_h[k:k + 1].copy_(status[k:k + 1], non_blocking=True)
+        if not direct_totals:
+            totals_h[k:k + 1].copy_(totals[k:k + 1], non_blocking=True)
+            status_h[k:k + 1].copy_(status[k:k + 1], non_blocking=True)
         ev = torch.cuda.Event(enable_timing=timing)
         ev.record(comp)
-        return [idx, xyzi, s, ev]
+        return [idx, xyzi, s, ev, cap]
 
     caps = [max(1024, (b - a) * per * 5 // 4) for a, b in zip(bounds[:-1], bounds[1:])]
     regions = [launch(k, caps[k]) for k in range(min(2, n_chunks))]
     t_launched = time.perf_counter()
     wait_s = alloc_s = 0.0
     hb = None
-    h_off = h_idx = h_xyzi = None
+    h_idx = h_xyzi = None
     base = 0
     out_regions, chunks = [], []
     for k in range(n_chunks):
         if k + 2 < n_chunks:
             regions.append(launch(k + 2, caps[k + 2]))  # two chunks queued ahead of the copies
-        idx, xyzi, s, ev = regions[k]
+        idx, xyzi, s, ev, cap = regions[k]
         tw = time.perf_counter()
         ev.synchronize()
         wait_s += time.perf_counter() - tw
-        v = N.check_status_value(int(status_h[k]), "simulate", allow=N.DS_ERR_CAPACITY)
         if k == 0:
             N.check_status_value(int(sf_status_h[0]), "structure_factors")
+        if not direct_totals:
+            N.check_status_value(int(status_h[k]), "simulate", allow=N.DS_ERR_CAPACITY)
         cnt = int(totals_h[k])
-        if v & N.DS_ERR_CAPACITY:
+        if cnt > cap:
+            # the region overflowed (the count is exact): re-run the chunk alone
             status[k:k + 1].zero_()
-            idx, xyzi, s, ev = launch(k, cnt + 1024)
+            idx, xyzi, s, ev, cap = launch(k, cnt + 1024)
             ev.synchronize()
-            N.check_status_value(int(status_h[k]), "simulate")
+            if not direct_totals:
+                N.check_status_value(int(status_h[k]), "simulate")
             cnt = int(totals_h[k])
         a, b = bounds[k], bounds[k + 1]
         if hb is None:
@@ -647,40 +680,46 @@ def simulate_phase_streamed(table: PhaseTable, quats: torch.Tensor, settings: Si
             ta = time.perf_counter()
             hb = host_pool.acquire(n, need, idt)
             alloc_s += time.perf_counter() - ta
-            h_off, h_idx, h_xyzi = hb[0], hb[1], hb[2]
+            h_idx, h_xyzi = hb[1], hb[2]
         if base + cnt > h_idx.shape[0]:
             # the host arrays outgrew the estimate: a larger set (waits for the copies so far)
             copy.synchronize()
             ta = time.perf_counter()
             nb = host_pool.acquire(n, max(base + cnt, h_idx.shape[0] * 3 // 2), idt)
             alloc_s += time.perf_counter() - ta
-            nb[0][:a].copy_(h_off[:a])
             nb[1][:base].copy_(h_idx[:base])
             nb[2][:base].copy_(h_xyzi[:base])
             hb[3] = None
             hb[4] = []
             hb = nb
-            h_off, h_idx, h_xyzi = hb[0], hb[1], hb[2]
+            h_idx, h_xyzi = hb[1], hb[2]
         copy.wait_event(ev)
         # copies only on the side stream: a kernel there would wait for an
         # SM behind the persistent simulation kernel, and the copies behind it
         with torch.cuda.stream(copy):
             if k == 0 and c_start is not None:
                 c_start.record(copy)
-            if b > a:
-                h_off[a:b].copy_(chunk_off[k][:b - a], non_blocking=True)
             if cnt:
                 h_idx[base:base + cnt].copy_(idx[:cnt], non_blocking=True)
                 h_xyzi[base:base + cnt].copy_(xyzi[:cnt], non_blocking=True)
         out_regions.append((idx, xyzi, s, cnt))
-        chunks.append((a, chunk_off[k], base))
+        chunks.append((a, chunk_off[k], base, k))
         base += cnt
+    # the offsets and (with the counts stored directly) every chunk's status
+    # word, copied behind the spots on the copy stream; the status words are
+    # checked before the result is read (a re-run chunk's word was cleared
+    # first, so only real conditions remain)
+    copy.wait_stream(comp)
+    with torch.cuda.stream(copy):
+        off_stage.copy_(all_off, non_blocking=True)
+        if direct_totals:
+            status_h.copy_(status, non_blocking=True)
     done = torch.cuda.Event(enable_timing=timing)
     done.record(copy)
     if k_end is not None:
         k_end.record(comp)
     # the chunk buffers were read on the copy stream as well
-    for r in out_regions + [(c, None, None, 0) for c in chunk_off]:
+    for r in out_regions + [(all_off, None, None, 0)]:
         for x in r[:3]:
             if x is not None:
                 x.record_stream(copy)
@@ -688,7 +727,8 @@ def simulate_phase_streamed(table: PhaseTable, quats: torch.Tensor, settings: Si
            "streamed_call_ms": (time.perf_counter() - t_start) * 1e3, "chunks": n_chunks}
     if timing:
         rec["_events"] = (k_start, k_end, c_start)
-    res = StreamedSpots(table, chunks, out_regions, hb, done, base, rec)
+    res = StreamedSpots(table, chunks, out_regions, hb, done, base, rec, status_h if direct_totals else None,
+                        off_stage)
     host_pool.bind(hb, res)
     return res
 

@@ -219,18 +219,19 @@ class SimulationGenerator:
         settings = self.settings(max_excitation_error, shape_factor_width, form, orient_tile)
         rots, tables = [], []
         t_table = 0.0
-        t1 = time.perf_counter()
         for r in rotations:
             rots.append(r if isinstance(r, Rotation) else Rotation(quaternions_of(r)))
-        # the orientations go up first, asynchronously from page-locked staging:
-        # the copies run while the host builds the tables
-        qs = self._upload_quaternions([quaternions_of(rot) for rot in rots], dev)
-        t_upload = time.perf_counter() - t1
         for p in phases:
             t0 = time.perf_counter()
             tables.append(PhaseTable(p, reciprocal_radius, with_direct_beam, self.scattering_params,
                                      debye_waller_factors, form=form, device=dev))
             t_table += time.perf_counter() - t0
+        # the orientations go up after the tables' launches: the host fills the
+        # page-locked staging while the structure-factor kernels run, and the
+        # copies queue behind them on the same stream
+        t1 = time.perf_counter()
+        qs = self._upload_quaternions([quaternions_of(rot) for rot in rots], dev)
+        t_upload = time.perf_counter() - t1
         custom = self._custom_shape is not None and settings.precession_mode != N.DS_PRECESSION_LORENTZIAN
         if custom:
             # the caller's function on the host between the selection and the

@@ -208,3 +208,20 @@ def test_row_width_by_table_size(cell, radius, row_dtype):
         _check(torch, got, want)
         assert got.host()[1].dtype == row_dtype and got.hkl_index.dtype == torch.int32
         assert got.nbytes() == 601 * 8 + got.total * (16 + np.dtype(row_dtype).itemsize)
+
+
+def test_streamed_reports_a_later_chunks_status():
+    """A non-finite orientation in the last chunk: the kernel flags it in that
+    chunk's status word, which travels behind the spot copies; reading the
+    result (host or device) raises."""
+    import torch
+    from diffsims_gb300.engine import simulate_phase_streamed
+    table, q, settings, r = _case(torch, 3000)
+    q = q.clone()
+    q[2900] = float("nan")
+    got = simulate_phase_streamed(table, q, settings, r, chunk=1000, first_chunk=500)
+    with pytest.raises(ValueError, match="non-finite"):
+        got.host()
+    got = simulate_phase_streamed(table, q, settings, r, chunk=1000, first_chunk=500)
+    with pytest.raises(ValueError, match="non-finite"):
+        got.hkl_index
