@@ -445,6 +445,7 @@ def run_gpu(args):
     breakdown["copy_span_gbs"] = d2h / (breakdown["copy_span_ms"] * 1e-3) / 1e9 if breakdown.get(
         "copy_span_ms") else None
     breakdown["pinned_pool_bytes"] = gen._host_pool.allocated_bytes
+    breakdown["calls_ms"] = [round(x, 3) for x in e2e_ms]  # every timed call (the link is shared with the host's other load)
     breakdown["host_transfer"] = transfer
     breakdown["note"] = ("host ms per call: table (enumeration + structure factors, one count read), quaternion "
                          "upload, launch set-up, waits for the kernel (chunk_wait_ms), pinned-pool allocation (0 once "
