@@ -47,7 +47,8 @@ DS_PRECESSION_INTEGRAL = 2
 EXPORTED_SYMBOLS = (
     "ds_box_extent", "ds_enumerate_scratch_bytes", "ds_enumerate_hkl", "ds_enumerate_sphere",
     "ds_structure_factor_scratch_bytes", "ds_structure_factors", "ds_kinematical_intensities",
-    "ds_family_structure_factors", "ds_simulate_scratch_bytes", "ds_simulate", "ds_simulate_batch_scratch_bytes", "ds_simulate_batch_tile",
+    "ds_family_structure_factors", "ds_simulate_scratch_bytes", "ds_simulate", "ds_simulate_noalloc",
+    "ds_simulate_batch_scratch_bytes", "ds_simulate_batch_tile",
     "ds_simulate_batch", "ds_rasterize_scratch_bytes", "ds_rasterize",
     "ds_simulate_backward_scratch_bytes", "ds_simulate_backward", "ds_structure_factors_backward_scratch_bytes",
     "ds_axis_angle_compose", "ds_axis_angle_compose_backward", "ds_polar_flatten", "ds_structure_factors_backward",
