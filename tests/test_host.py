@@ -406,3 +406,34 @@ def test_phase_spots_select_and_copy():
     c = copy.deepcopy(sp)
     c.xyzi.zero_()
     assert np.array_equal(sp.xyzi.numpy(), xyzi) and c.total == total
+
+
+def test_row_storage_helpers_and_pool_by_index_type(monkeypatch):
+    """uint16 table rows (held in int16 tensors) widen to their unsigned
+    values on the device and read as uint16 on the host; tables above 65536
+    rows keep int32; the page-locked pool hands out a set only for the index
+    type it was made with (checked on CPU tensors)."""
+    import torch
+    from diffsims_gb300 import engine
+    rows = torch.tensor([0, 1, 32767, -32768, -1], dtype=torch.int16)
+    assert engine._rows_int32(rows).dtype == torch.int32
+    assert engine._rows_int32(rows).tolist() == [0, 1, 32767, 32768, 65535]
+    host = engine._rows_numpy(rows)
+    assert host.dtype == np.uint16 and host.tolist() == [0, 1, 32767, 32768, 65535]
+    wide = torch.tensor([5, 70000], dtype=torch.int32)
+    assert engine._rows_int32(wide) is wide and engine._rows_numpy(wide).dtype == np.int32
+
+    class Table:
+        n = 65536
+    assert engine._row_index_dtype(Table) == torch.int16
+    Table.n = 65537
+    assert engine._row_index_dtype(Table) == torch.int32
+
+    real_empty = torch.empty
+    monkeypatch.setattr(engine.torch, "empty", lambda *a, pin_memory=False, **k: real_empty(*a, **k))
+    pool = engine.HostSpotPool()
+    a = pool.acquire(10, 100, torch.int16)
+    assert a[1].dtype == torch.int16 and pool.allocated_bytes == 14 * 8 + 1024 * 18
+    b = pool.acquire(10, 100, torch.int32)  # the free int16 set is not of this type
+    assert b is not a and b[1].dtype == torch.int32
+    assert pool.acquire(10, 50, torch.int16) is a
