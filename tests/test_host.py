@@ -437,3 +437,23 @@ def test_row_storage_helpers_and_pool_by_index_type(monkeypatch):
     b = pool.acquire(10, 100, torch.int32)  # the free int16 set is not of this type
     assert b is not a and b[1].dtype == torch.int32
     assert pool.acquire(10, 50, torch.int16) is a
+
+
+def test_polar_and_pointer_query_arguments(lib):
+    """ds_polar_flatten and ds_polar_flatten_f32 reject negative sizes, one
+    axis without the other and empty axes before any CUDA call;
+    ds_host_mapped needs its output pointer and reports null as unmapped."""
+    import ctypes as C
+    from diffsims_gb300 import _native as N
+    fake = C.c_void_p(16)
+    for entry in (lib.ds_polar_flatten, lib.ds_polar_flatten_f32):
+        assert entry(fake, fake, -1, 4, None, 0, None, 0, fake, fake, fake, None) == N.DS_ERR_INVALID_ARGUMENT
+        assert "negative size" in lib.ds_last_error().decode()
+        assert entry(fake, fake, 3, 4, fake, 5, None, 0, fake, fake, fake, None) == N.DS_ERR_INVALID_ARGUMENT
+        assert "both axes" in lib.ds_last_error().decode()
+        assert entry(fake, fake, 3, 4, fake, 0, fake, 7, fake, fake, fake, None) == N.DS_ERR_INVALID_ARGUMENT
+        assert "empty axes" in lib.ds_last_error().decode()
+        assert entry(fake, fake, 0, 4, None, 0, None, 0, fake, fake, fake, None) == N.DS_OK  # nothing to do
+    assert lib.ds_host_mapped(None, None) == N.DS_ERR_INVALID_ARGUMENT
+    out = C.c_int32(7)
+    assert lib.ds_host_mapped(None, C.byref(out)) == N.DS_OK and out.value == 0
