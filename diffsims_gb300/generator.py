@@ -4,6 +4,7 @@ running on the CUDA library."""
 from __future__ import annotations
 
 import time
+from concurrent.futures import ThreadPoolExecutor
 from typing import Sequence, Union
 
 import numpy as np
@@ -112,6 +113,7 @@ class SimulationGenerator:
         self.host_transfer = "copies"
         self._qstage = None               # page-locked quaternion staging, reused across calls
         self._qstage_done = None          # event after the last uploads out of the staging
+        self._stage_pool = None           # one thread filling the staging beside the table build
 
     def __repr__(self):
         return (f"SimulationGenerator(accelerating_voltage={self.accelerating_voltage}, "
@@ -143,28 +145,43 @@ class SimulationGenerator:
                            minima_number=float(self.shape_factor_kwargs.get("minima_number", 5)), form=form,
                            orient_tile=orient_tile)
 
-    def _upload_quaternions(self, arrays, dev):
-        """Device copies of the (n, 4) quaternion arrays through one reusable
-        page-locked staging buffer: a host copy into it, then asynchronous
-        uploads on the current stream.  The next call waits for this call's
-        uploads (an event) before it overwrites the staging."""
+    def _stage_quaternions(self, arrays):
+        """Host half of the orientation upload: wait for the previous call's
+        uploads out of the reusable page-locked staging, then copy the (n, 4)
+        quaternion arrays into it.  Runs on the generator's staging thread
+        beside the table build (numpy's copy releases the GIL).  Returns the
+        staging views, one per array."""
         total = sum(int(a.shape[0]) for a in arrays)
         if self._qstage_done is not None:
             self._qstage_done.synchronize()
         if self._qstage is None or self._qstage.shape[0] < total:
             self._qstage = torch.empty((max(total, 4096), 4), dtype=torch.float64, pin_memory=True)
-        out, off = [], 0
+        views, off = [], 0
         for a in arrays:
             n = int(a.shape[0])
             st = self._qstage[off:off + n]
             st.numpy()[...] = a
-            d = torch.empty((n, 4), dtype=torch.float64, device=dev)
+            views.append(st)
+            off += n
+        return views
+
+    def _upload_staged(self, views, dev):
+        """Device half: asynchronous copies out of the page-locked staging on
+        the current stream; the next call's staging waits for them (an
+        event)."""
+        out = []
+        for st in views:
+            d = torch.empty((st.shape[0], 4), dtype=torch.float64, device=dev)
             d.copy_(st, non_blocking=True)
             out.append(d)
-            off += n
         self._qstage_done = torch.cuda.Event()
         self._qstage_done.record(torch.cuda.current_stream(dev))
         return out
+
+    def _stager(self):
+        if self._stage_pool is None:
+            self._stage_pool = ThreadPoolExecutor(max_workers=1, thread_name_prefix="diffsims-gb300-stage")
+        return self._stage_pool
 
     def calculate_diffraction2d(self, phase: Union[Phase, Sequence[Phase]],
                                 rotation: Union[Rotation, Sequence[Rotation]] = None,
@@ -221,16 +238,17 @@ class SimulationGenerator:
         t_table = 0.0
         for r in rotations:
             rots.append(r if isinstance(r, Rotation) else Rotation(quaternions_of(r)))
+        # the staging thread fills the page-locked staging with the
+        # orientations while this thread builds the tables; the uploads then
+        # queue behind the structure-factor kernels on the same stream
+        staged = self._stager().submit(self._stage_quaternions, [quaternions_of(rot) for rot in rots])
         for p in phases:
             t0 = time.perf_counter()
             tables.append(PhaseTable(p, reciprocal_radius, with_direct_beam, self.scattering_params,
                                      debye_waller_factors, form=form, device=dev))
             t_table += time.perf_counter() - t0
-        # the orientations go up after the tables' launches: the host fills the
-        # page-locked staging while the structure-factor kernels run, and the
-        # copies queue behind them on the same stream
         t1 = time.perf_counter()
-        qs = self._upload_quaternions([quaternions_of(rot) for rot in rots], dev)
+        qs = self._upload_staged(staged.result(), dev)
         t_upload = time.perf_counter() - t1
         custom = self._custom_shape is not None and settings.precession_mode != N.DS_PRECESSION_LORENTZIAN
         if custom:
