@@ -15,7 +15,8 @@ namespace ds {
 // strays from the static one at this |g|:
 //   k0 (1 - cos phi) + Pt (2 |g| + Pt) / (2 sqrt(k0^2 - (|g| + Pt)^2)).
 __global__ void sim_prep_kernel(SimConst c, const int32_t *__restrict__ hkl, const double *__restrict__ g2,
-                                float4 *__restrict__ scr, float *__restrict__ zh, float2 *__restrict__ g2dd) {
+                                const float *__restrict__ F2, float4 *__restrict__ scr, float *__restrict__ zh,
+                                float4 *__restrict__ aux) {
     long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= c.n_hkl) return;
     double gsq = g2[j];
@@ -33,7 +34,7 @@ __global__ void sim_prep_kernel(SimConst c, const int32_t *__restrict__ hkl, con
     zh[j] = (float)zhalf + c.guard;
     float hi, lo;
     split_double(gsq, hi, lo);
-    g2dd[j] = make_float2(hi, lo);
+    aux[j] = make_float4(hi, lo, F2 ? F2[j] : 0.f, 0.f);
 }
 
 __global__ void __launch_bounds__(LN_THREADS)
@@ -421,7 +422,7 @@ static ds_status make_plan(const ds_sim_params *p, const ds_phase_table *t, long
     o = align_up(o, 256);
     P.off_zh = o; o += (size_t)t->n_hkl * sizeof(float);
     o = align_up(o, 256);
-    P.off_g2 = o; o += (size_t)t->n_hkl * sizeof(float2);
+    P.off_g2 = o; o += (size_t)t->n_hkl * sizeof(float4);
     o = align_up(o, 256);
     P.off_sidx = o; o += (size_t)(2 * P.grid * P.stage_cap) * sizeof(int32_t);  // two pipeline slots per CTA
     o = align_up(o, 256);
@@ -441,10 +442,10 @@ static ds_status make_plan(const ds_sim_params *p, const ds_phase_table *t, long
     return DS_OK;
 }
 
-ds_status launch_sim_prep(const SimConst &c, const int32_t *hkl, const double *g2, float4 *scr, float *zh, float2 *g2dd,
+ds_status launch_sim_prep(const SimConst &c, const int32_t *hkl, const double *g2, const float *F2, float4 *scr, float *zh, float4 *aux,
                           long long n_hkl, cudaStream_t s) {
     if (n_hkl <= 0) return DS_OK;
-    sim_prep_kernel<<<(unsigned)((n_hkl + 255) / 256), 256, 0, s>>>(c, hkl, g2, scr, zh, g2dd);
+    sim_prep_kernel<<<(unsigned)((n_hkl + 255) / 256), 256, 0, s>>>(c, hkl, g2, F2, scr, zh, aux);
     return check_launch("sim_prep_kernel");
 }
 
@@ -534,13 +535,13 @@ extern "C" ds_status ds_simulate(const ds_sim_params *p, const ds_phase_table *t
     TableP T;
     T.scr = reinterpret_cast<float4 *>(sb + P.off_scr);
     T.zh = reinterpret_cast<float *>(sb + P.off_zh);
-    T.g2dd = reinterpret_cast<float2 *>(sb + P.off_g2);
-    T.F2 = t->F2;
+    T.aux = reinterpret_cast<float4 *>(sb + P.off_g2);
     T.F2d = t->F2d;
     DS_CUDA_TRY(cudaMemsetAsync(sb + P.off_lb, 0, lookback_scratch_bytes(P.n_tiles), s));
     if (t->n_hkl > 0) {
         sim_prep_kernel<<<(unsigned)((t->n_hkl + 255) / 256), 256, 0, s>>>(
-            c, t->hkl, t->g2, const_cast<float4 *>(T.scr), const_cast<float *>(T.zh), const_cast<float2 *>(T.g2dd));
+            c, t->hkl, t->g2, p->form == DS_FORM_MIXED ? t->F2 : nullptr, const_cast<float4 *>(T.scr),
+            const_cast<float *>(T.zh), const_cast<float4 *>(T.aux));
         ds_status st = check_launch("sim_prep_kernel");
         if (st) return st;
     }

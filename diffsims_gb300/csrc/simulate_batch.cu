@@ -40,7 +40,7 @@ struct BatchPlan {
     int Op[SIM_BATCH_MAX];
     long long n_tiles, n_orient, stage_cap;
     size_t smem, off_lb, off_sidx, off_sI, total;
-    size_t off_prep[SIM_BATCH_MAX];    // per phase: scr, zh, g2dd
+    size_t off_prep[SIM_BATCH_MAX];    // per phase: scr, zh, aux
     size_t off_bricks[SIM_BATCH_MAX];  // per phase: the brick screen's arrays
     BrickGeom bricks[SIM_BATCH_MAX];
 };
@@ -94,7 +94,7 @@ static ds_status batch_plan(const ds_sim_params *p, const ds_batch_phase *ph, in
         o = align256(o);
         P.off_prep[i] = o;
         const size_t nh = (size_t)ph[i].table.n_hkl;
-        o += align256(nh * sizeof(float4)) + align256(nh * sizeof(float)) + align256(nh * sizeof(float2));
+        o += align256(nh * sizeof(float4)) + align256(nh * sizeof(float)) + align256(nh * sizeof(float4));
     }
     P.brick_mode = (p->form == DS_FORM_MIXED && p->screen == DS_SCREEN_BRICKS) ? 1 : 0;
     for (int i = 0; i < n; ++i) {
@@ -191,11 +191,10 @@ extern "C" ds_status ds_simulate_batch(const ds_sim_params *p, const ds_batch_ph
         unsigned char *base = sb + P.off_prep[i];
         float4 *scr = reinterpret_cast<float4 *>(base);
         float *zh = reinterpret_cast<float *>(base + align256(nh * sizeof(float4)));
-        float2 *g2dd = reinterpret_cast<float2 *>(base + align256(nh * sizeof(float4)) + align256(nh * sizeof(float)));
+        float4 *aux = reinterpret_cast<float4 *>(base + align256(nh * sizeof(float4)) + align256(nh * sizeof(float)));
         d.T.scr = scr;
         d.T.zh = zh;
-        d.T.g2dd = g2dd;
-        d.T.F2 = t->F2;
+        d.T.aux = aux;
         d.T.F2d = t->F2d;
         d.T.lines = nullptr;
         d.T.line_meta = nullptr;
@@ -215,7 +214,7 @@ extern "C" ds_status ds_simulate_batch(const ds_sim_params *p, const ds_batch_ph
         d.orient0 = orient0;
         tile0 += d.n_tiles;
         orient0 += no;
-        st = launch_sim_prep(cp, t->hkl, t->g2, scr, zh, g2dd, nh, s);
+        st = launch_sim_prep(cp, t->hkl, t->g2, p->form == DS_FORM_MIXED ? t->F2 : nullptr, scr, zh, aux, nh, s);
         if (st) return st;
         if (P.brick_mode && nh > 0) {
             st = launch_brick_build(P.bricks[i], t->hkl, nh, scr, zh, sb + P.off_bricks[i], d.T, s);

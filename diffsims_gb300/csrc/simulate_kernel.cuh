@@ -434,8 +434,7 @@ __device__ inline double shape_fp64(const SimConst &c, double s, double r) {
 struct TableP {
     const float4 *scr;
     const float *zh;
-    const float2 *g2dd;
-    const float *F2;
+    const float4 *aux;    // per row: |g|^2 as an FP32 pair, |F|^2 (mixed), 0 -- one gather in the refine
     const double *F2d;
     const LineP *lines;   // line screen: per-line constants
     const int *line_meta; // [0] lines, [1] first trailing 000 row
@@ -489,8 +488,9 @@ __device__ __forceinline__ SpotIn load_spot(const TableP &T, long long j) {
     if (FORM == DS_FORM_FP64) {
         in.F2d = T.F2d[j];
     } else {
-        in.g2 = T.g2dd[j];
-        in.F2 = T.F2[j];
+        const float4 a = T.aux[j];
+        in.g2 = make_float2(a.x, a.y);
+        in.F2 = a.z;
     }
     return in;
 }
@@ -1547,7 +1547,7 @@ inline void fill_const(const ds_sim_params *p, const ds_phase_table *t, SimConst
 }
 
 // sim_prep_kernel launcher (simulate.cu): the screen arrays of one table.
-ds_status launch_sim_prep(const SimConst &c, const int32_t *hkl, const double *g2, float4 *scr, float *zh, float2 *g2dd,
+ds_status launch_sim_prep(const SimConst &c, const int32_t *hkl, const double *g2, const float *F2, float4 *scr, float *zh, float4 *aux,
                           long long n_hkl, cudaStream_t s);
 
 // Brick screen (simulate.cu).  brick_geometry picks the block shape for a
