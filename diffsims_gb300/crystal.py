@@ -214,11 +214,11 @@ def sites_of(structure):
     els, xyz, occ = [], [], []
     for site in structure:
         els.append(str(site.element))
-        xyz.append(np.asarray(site.xyz, dtype=np.float64))
-        occ.append(float(getattr(site, "occupancy", 1.0)))
+        xyz.append(site.xyz)
+        occ.append(getattr(site, "occupancy", 1.0))
     if not els:
         raise ValueError("the structure has no atoms")
-    return els, np.asarray(xyz).reshape(-1, 3), np.asarray(occ)
+    return els, np.asarray(xyz, dtype=np.float64).reshape(-1, 3), np.asarray(occ, dtype=np.float64)
 
 
 def quaternions_of(rotation) -> np.ndarray:

@@ -7,6 +7,7 @@ library (``ds_kinematical_intensities``).
 """
 from __future__ import annotations
 
+import functools
 import json
 import math
 import pathlib
@@ -45,9 +46,11 @@ def get_scattering_params_dict(scattering_params):
         "implementations.".format(scattering_params))
 
 
+@functools.lru_cache(maxsize=4096)
 def get_element(atom_type_symbol: str) -> str:
     """Alphabetic head of a CIF atom type symbol
-    (diffsims/structure_factor/atomic_scattering_parameters.py:145-164)."""
+    (diffsims/structure_factor/atomic_scattering_parameters.py:145-164);
+    remembered per symbol (a structure repeats a few symbols many times)."""
     return re.match("^(?P<element>[A-Za-z]*)", atom_type_symbol).group("element")
 
 
