@@ -446,6 +446,7 @@ def run_gpu(args):
         "copy_span_ms") else None
     breakdown["pinned_pool_bytes"] = gen._host_pool.allocated_bytes
     breakdown["calls_ms"] = [round(x, 3) for x in e2e_ms]  # every timed call (the link is shared with the host's other load)
+    breakdown["median_call_ms"] = statistics.median(e2e_ms)  # beside the mean that value and ms_per_step report
     breakdown["host_transfer"] = transfer
     breakdown["note"] = ("host ms per call: table (enumeration + structure factors, one count read), quaternion "
                          "upload, launch set-up, waits for the kernel (chunk_wait_ms), pinned-pool allocation (0 once "

@@ -654,8 +654,6 @@ def simulate_phase_streamed(table: PhaseTable, quats: torch.Tensor, settings: Si
     base = 0
     out_regions, chunks = [], []
     for k in range(n_chunks):
-        if k + 2 < n_chunks:
-            regions.append(launch(k + 2, caps[k + 2]))  # two chunks queued ahead of the copies
         idx, xyzi, s, ev, cap = regions[k]
         tw = time.perf_counter()
         ev.synchronize()
@@ -705,6 +703,10 @@ def simulate_phase_streamed(table: PhaseTable, quats: torch.Tensor, settings: Si
         out_regions.append((idx, xyzi, s, cnt))
         chunks.append((a, chunk_off[k], base, k))
         base += cnt
+        if k + 2 < n_chunks:
+            # chunk k + 1 is queued already: this launch follows the issue of
+            # chunk k's copies, so the first copy starts one launch earlier
+            regions.append(launch(k + 2, caps[k + 2]))
     # the offsets and (with the counts stored directly) every chunk's status
     # word, copied behind the spots on the copy stream; the status words are
     # checked before the result is read (a re-run chunk's word was cleared
