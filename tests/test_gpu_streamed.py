@@ -225,3 +225,20 @@ def test_streamed_reports_a_later_chunks_status():
     got = simulate_phase_streamed(table, q, settings, r, chunk=1000, first_chunk=500)
     with pytest.raises(ValueError, match="non-finite"):
         got.hkl_index
+
+
+def test_streamed_without_mapped_counts(monkeypatch):
+    """Where page-locked memory is not addressable by kernels, each chunk's
+    count and status word come back by copies instead (the same results, the
+    overflow re-run included)."""
+    import torch
+    from diffsims_gb300 import _native as N
+    from diffsims_gb300 import engine
+    table, q, settings, r = _case(torch, 2500, seed=6, model="lorentzian")
+    want = engine.simulate_phase(table, q, settings, r, engine.SpotBuffers(q.device))
+    monkeypatch.setattr(N, "host_mapped", lambda ptr: False)
+    _check(torch, engine.simulate_phase_streamed(table, q, settings, r, chunk=700, first_chunk=200), want)
+    monkeypatch.setattr(engine, "estimate_spots", lambda *a: 1)
+    _check(torch, engine.simulate_phase_streamed(table, q, settings, r, chunk=700, first_chunk=200), want)
+    # and the kernel-stores route declines, leaving the copies to the caller
+    assert engine.simulate_phase_to_host(table, q, settings, r) is None
