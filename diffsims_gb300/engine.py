@@ -577,11 +577,15 @@ def simulate_phase_streamed(table: PhaseTable, quats: torch.Tensor, settings: Si
     Chunk sizes grow by 7/4 from ``first_chunk`` up to ``chunk``: the copies
     start early, and the copy of a chunk (at about 1.8 times the kernel's
     time per orientation) lasts as long as the next chunk's kernel, so the
-    link does not wait for the kernel (with doubling it would).  A chunk whose
-    spots overflow its region is re-run alone with the exact size.  The host
-    arrays come from ``host_pool`` (reused across calls) or are allocated;
-    they are sized from the first chunk's spot count.  With ``timing`` the
-    result records CUDA events for ``StreamedSpots.timings``."""
+    link does not wait for the kernel (with doubling it would).  The kernel
+    stores each chunk's spot count into page-locked memory itself, so the
+    compute stream holds no copy; the status words follow the spots and are
+    checked when the result is read.  Table rows travel as uint16 for tables
+    of at most 65536 rows.  A chunk whose spots overflow its region is re-run
+    alone with the exact size.  The host arrays come from ``host_pool``
+    (reused across calls) or are allocated; they are sized from the first
+    chunk's spot count.  With ``timing`` the result records CUDA events for
+    ``StreamedSpots.timings``."""
     t_start = time.perf_counter()
     lib = N.load_library()
     dev = table.device
