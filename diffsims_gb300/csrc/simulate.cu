@@ -30,11 +30,13 @@ __global__ void sim_prep_kernel(SimConst c, const int32_t *__restrict__ hkl, con
     double za = (gsq + e * e - 2.0 * e * c.k0) / (2.0 * (c.k0 - e));
     double zb = (gsq + e * e + 2.0 * e * c.k0) / (2.0 * (c.k0 + e));
     double zmid = 0.5 * (za + zb), zhalf = 0.5 * (zb - za);
-    scr[j] = make_float4((float)hkl[3 * j], (float)hkl[3 * j + 1], (float)hkl[3 * j + 2], (float)(-zmid));
+    const float4 row = make_float4((float)hkl[3 * j], (float)hkl[3 * j + 1], (float)hkl[3 * j + 2], (float)(-zmid));
+    scr[j] = row;
     zh[j] = (float)zhalf + c.guard;
     float hi, lo;
     split_double(gsq, hi, lo);
-    aux[j] = make_float4(hi, lo, F2 ? F2[j] : 0.f, 0.f);
+    aux[2 * j] = row;
+    aux[2 * j + 1] = make_float4(hi, lo, F2 ? F2[j] : 0.f, 0.f);
 }
 
 __global__ void __launch_bounds__(LN_THREADS)
@@ -422,7 +424,7 @@ static ds_status make_plan(const ds_sim_params *p, const ds_phase_table *t, long
     o = align_up(o, 256);
     P.off_zh = o; o += (size_t)t->n_hkl * sizeof(float);
     o = align_up(o, 256);
-    P.off_g2 = o; o += (size_t)t->n_hkl * sizeof(float4);
+    P.off_g2 = o; o += (size_t)t->n_hkl * 2 * sizeof(float4);
     o = align_up(o, 256);
     P.off_sidx = o; o += (size_t)(2 * P.grid * P.stage_cap) * sizeof(int32_t);  // two pipeline slots per CTA
     o = align_up(o, 256);

@@ -94,7 +94,7 @@ static ds_status batch_plan(const ds_sim_params *p, const ds_batch_phase *ph, in
         o = align256(o);
         P.off_prep[i] = o;
         const size_t nh = (size_t)ph[i].table.n_hkl;
-        o += align256(nh * sizeof(float4)) + align256(nh * sizeof(float)) + align256(nh * sizeof(float4));
+        o += align256(nh * sizeof(float4)) + align256(nh * sizeof(float)) + align256(nh * 2 * sizeof(float4));
     }
     P.brick_mode = (p->form == DS_FORM_MIXED && p->screen == DS_SCREEN_BRICKS) ? 1 : 0;
     for (int i = 0; i < n; ++i) {

@@ -434,7 +434,8 @@ __device__ inline double shape_fp64(const SimConst &c, double s, double r) {
 struct TableP {
     const float4 *scr;
     const float *zh;
-    const float4 *aux;    // per row: |g|^2 as an FP32 pair, |F|^2 (mixed), 0 -- one gather in the refine
+    const float4 *aux;    // per row, 32 bytes: the screen row (h, k, l, -z_mid), then |g|^2 as an FP32
+                          // pair, |F|^2 (mixed), 0 -- one sector per candidate in the refine
     const double *F2d;
     const LineP *lines;   // line screen: per-line constants
     const int *line_meta; // [0] lines, [1] first trailing 000 row
@@ -484,11 +485,12 @@ struct SpotIn {
 template <int FORM>
 __device__ __forceinline__ SpotIn load_spot(const TableP &T, long long j) {
     SpotIn in;
-    in.e = T.scr[j];
     if (FORM == DS_FORM_FP64) {
+        in.e = T.scr[j];
         in.F2d = T.F2d[j];
     } else {
-        const float4 a = T.aux[j];
+        in.e = T.aux[2 * j];
+        const float4 a = T.aux[2 * j + 1];
         in.g2 = make_float2(a.x, a.y);
         in.F2 = a.z;
     }
