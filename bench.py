@@ -64,7 +64,7 @@ WORKLOAD = dict(workload="triclinic P1, 200 atoms, 200 kV, r=2.0, s_max=0.02, lo
 METRIC = "orientation patterns/s"
 # measured: (dram__bytes_read.sum + dram__bytes_write.sum) / spots written, one
 # simulate_kernel launch on 8192 orientations of the workload below
-DRAM_BYTES_PER_SPOT = 21.4
+DRAM_BYTES_PER_SPOT = 21.8
 UNIT = "patterns/s"
 
 
